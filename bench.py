@@ -1,0 +1,306 @@
+"""Benchmark: 3D Poisson 513^3 to 1e-10 relative residual, DOF/s.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload (one step = one full fish solve): -fsh_dim 3 -fsh_problem manupoly
+-da_refine 8 (513^3 nodes, 7-point), CG + MG V(2,2) Chebyshev/Jacobi on 9
+levels, rtol 1e-10 on the true (unpreconditioned) residual.  `value` is the
+mixed form (FP32 V-cycle and inner CG, FP64 iterative refinement) with f and g
+resident in HBM; the plain FP64 form is measured beside it.  `e2e` is the same
+solve through fishgpu_solver_solve_host with pinned host arrays: f and g
+copied in and u copied out every step.  Every vector (1.08 GB in FP64) is far
+larger than L2, so no flush is needed between steps.
+
+--impl reference times the CPU restatement of the same solve (the oracle:
+FP64 CG + MG, OpenMP on all host cores) on a bounded sample (129^3).
+Multi-GPU: replicas only (independent solves per rank, no collective on the
+data path); value = DOFs of all ranks / max time over ranks.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Poisson DOF/s to 1e-10 rel. residual, mixed vs FP64 MG, HBM %peak; p99 latency"
+BASE_ARGS = ("-fsh_dim 3 -fsh_problem manupoly -da_refine {r} -pc_type mg -mg_levels_ksp_type chebyshev "
+             "-mg_levels_pc_type jacobi -ksp_rtol 1e-10 -ksp_norm_type unpreconditioned")
+CPU_SAMPLE_REFINE = 7  # 257^3 for the CPU baseline sample
+
+
+def peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampled every 200 ms during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        self.rows = []
+        if self.p is None:
+            return
+        time.sleep(0.25)
+        self.p.terminate()
+        out, _ = self.p.communicate(timeout=10)
+        for line in out.splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) == 6:
+                self.rows.append(parts)
+
+    def summary(self):
+        if not getattr(self, "rows", None):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[q] for r in self.rows for q in range(4) if r[2 + q].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def cpu_baseline(steps=None, budget_s=12.0):
+    """Oracle (FP64 CG+MG, OpenMP) on a 129^3 sample; returns (DOF/s, info)."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import _oracle as orc
+    o = orc.options(BASE_ARGS.format(r=CPU_SAMPLE_REFINE).split())
+    dofs = o.grid.mx * o.grid.my * o.grid.mz
+    times = []
+    t_all = time.perf_counter()
+    n = 0
+    while True:
+        t0 = time.perf_counter()
+        _, rep = orc.fish_solve(o)
+        times.append(time.perf_counter() - t0)
+        n += 1
+        if steps is not None and n >= steps:
+            break
+        if steps is None and (time.perf_counter() - t_all > budget_s or n >= 5):
+            break
+    tot = sum(times)
+    return dofs * n / tot, {"cores": orc.lib().or_num_threads(), "solves": n, "its": rep["its"], "dofs": dofs,
+                            "sample": "oracle FP64 CG+MG V(2,2) Chebyshev/Jacobi, 3D %d^3 manupoly, rtol 1e-10, "
+                                      "%d solve(s), %.2f s" % (o.grid.mx, n, tot)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def run_reference(args):
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return
+    W = max(0, args.warmup)
+    K = max(1, args.steps)
+    for _ in range(min(W, 1)):
+        cpu_baseline(steps=1)
+    v, info = cpu_baseline(steps=K)
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "DOF/s", "n_gpus": args.gpus,
+            "steps": K, "warmup": W, "ms_per_step": 1e3 * info["dofs"] / v,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (manufactured manupoly problem)",
+            "config": {"workload": "3D Poisson 257^3 sample of the 513^3 solve, CPU restatement "
+                                   "(oracle) of CG+MG V(2,2) Chebyshev/Jacobi, rtol 1e-10"},
+            "cpu_baseline": {"value": v, "unit": "DOF/s", "cores": info["cores"], "kind": "port",
+                             "sample": info["sample"]},
+            "e2e": {"value": v, "unit": "DOF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def manupoly_fg(torch, o, dev):
+    """f and g of the 3D manupoly problem (c/ch6/fish.c:23-25, :60-70) at every node."""
+    mz, my, mx = o.shape
+    x = torch.linspace(0, o.ctx.Lx, mx, dtype=torch.float64, device=dev).view(1, 1, mx)
+    y = torch.linspace(0, o.ctx.Ly, my, dtype=torch.float64, device=dev).view(1, my, 1)
+    z = torch.linspace(0, o.ctx.Lz, mz, dtype=torch.float64, device=dev).view(mz, 1, 1)
+    aa, bb, cc = x * x * (1 - x * x), y * y * (y * y - 1), z * z * (z * z - 1)
+    da, db, dc = 2 * (1 - 6 * x * x), 2 * (6 * y * y - 1), 2 * (6 * z * z - 1)
+    g = (aa * bb * cc).contiguous()
+    f = (-(da * bb * cc + aa * db * cc + aa * bb * dc)).contiguous()
+    return f, g
+
+
+def run_ours(args):
+    import torch
+    import p4pdes_gb300 as fg
+
+    world, rank, local = dist_setup()
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    stream = torch.cuda.Stream(device=dev)
+    W, K = max(3, args.warmup), max(1, args.steps)
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    argv = BASE_ARGS.format(r=args.refine).split()
+    o_mx = fg.options(argv + ["-fsh_precision", "mixed"])
+    o_64 = fg.options(argv)
+    N = o_mx.dofs
+    f, g = manupoly_fg(torch, o_mx, dev)
+    for o in (o_mx, o_64):
+        o.ctx.problem, o.ctx.f, o.ctx.g = fg.USER, f.data_ptr(), g.data_ptr()
+    u = torch.empty(o_mx.shape, dtype=torch.float64, device=dev)
+    info = fg.info_for(o_mx)
+    ctx_exact = fg.Ctx.from_buffer_copy(o_mx.ctx)
+    ctx_exact.problem = fg.MANUPOLY
+
+    # ---- value: mixed form, inputs resident
+    s_mx = fg.Solver(o_mx, stream=stream.cuda_stream)
+    for _ in range(W):
+        rep = s_mx.solve(u)
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches = 0
+    with Clocks(local) as clk:
+        e0.record(stream)
+        reps = []
+        for _ in range(K):
+            reps.append(s_mx.solve(u))
+        e1.record(stream)
+        barrier()
+    ms = e0.elapsed_time(e1)
+    launches = sum(r.launches for r in reps)
+    rep_mx = reps[-1]
+    err_mx = fg.error_norms(info, u, ctx_exact)
+    ms_t = torch.tensor([ms], device=dev)
+    if world > 1:
+        import torch.distributed as dist
+        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
+    ms = ms_t.item()
+    value = world * N * K / (ms * 1e-3)
+
+    # roofline of the dominant kernel (FP32 Chebyshev step on the 513^3 level)
+    rk = args.roofline_kernel
+    kms, kbytes = s_mx.time_kernel(rk, 20)
+
+    # ---- plain FP64 form beside it
+    s_64 = fg.Solver(o_64, stream=stream.cuda_stream)
+    s_64.solve(u)
+    barrier()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    rep_64 = s_64.solve(u)
+    f1.record(stream)
+    barrier()
+    ms64 = f0.elapsed_time(f1)
+    err_64 = fg.error_norms(info, u, ctx_exact)
+    s_64.close()
+
+    # ---- e2e: host arrays through the C ABI (f, g in; u out)
+    s_mx.close()
+    o_e2e = fg.options(argv + ["-fsh_precision", "mixed"])
+    o_e2e.ctx.problem = fg.USER
+    s_e = fg.Solver(o_e2e, stream=stream.cuda_stream)
+    fh = f.cpu().pin_memory()
+    gh = g.cpu().pin_memory()
+    uh = torch.empty(o_mx.shape, dtype=torch.float64).pin_memory()
+    del f, g
+    for _ in range(1):
+        s_e.solve_host(fh, gh, uh)
+    barrier()
+    h0, h1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    h0.record(stream)
+    for _ in range(K):
+        s_e.solve_host(fh, gh, uh)
+    h1.record(stream)
+    barrier()
+    ms_e = h0.elapsed_time(h1)
+    s_e.close()
+    ms_e_t = torch.tensor([ms_e], device=dev)
+    if world > 1:
+        import torch.distributed as dist
+        dist.all_reduce(ms_e_t, op=dist.ReduceOp.MAX)
+    e2e = world * N * K / (ms_e_t.item() * 1e-3)
+
+    if rank != 0:
+        return
+    pk, pk_kind = peaks()
+    hbm = float(pk.get("hbm_gbs", 6800.0))
+    achieved = kbytes / (kms * 1e-3) / 1e9
+    traffic = None
+    try:
+        tr = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
+        traffic = tr.get(rk, {}).get("dram_bytes_per_launch")
+    except Exception:
+        pass
+    cpu_v, cpu_info = cpu_baseline()
+    line = {
+        "metric": METRIC, "value": value, "unit": "DOF/s", "n_gpus": world, "steps": K, "warmup": W,
+        "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64", "data": "synthetic (manufactured manupoly problem; f and g sampled at the nodes)",
+        "config": {
+            "workload": "3D Poisson 513^3 7-point (-da_refine 8), CG+MG V(2,2) Chebyshev/Jacobi, 9 levels, "
+                        "rtol 1e-10 true residual; mixed = FP32 V-cycle + FP32 inner CG inside FP64 "
+                        "iterative refinement",
+            "dofs": N, "levels": o_mx.mg_levels, "parallelism": "replicas" if world > 1 else "1 GPU",
+            "l2": "no flush: every vector (1.08 GB FP64) exceeds L2",
+            "mixed": {"ms": ms / K, "inner_its": rep_mx.its, "outer_its": rep_mx.outer_its,
+                      "true_rel_resid": rep_mx.true_rel_resid, "errinf": err_mx[0], "err2h": err_mx[1]},
+            "fp64": {"ms": ms64, "dof_per_s": N / (ms64 * 1e-3), "its": rep_64.its,
+                     "true_rel_resid": rep_64.true_rel_resid, "errinf": err_64[0], "err2h": err_64[1]},
+            "mixed_over_fp64": (N / (ms / K * 1e-3)) / (N / (ms64 * 1e-3)),
+            "error_ratio_mixed_over_fp64": err_mx[0] / err_64[0],
+        },
+        "e2e": {"value": e2e, "unit": "DOF/s", "h2d_bytes_per_step": 2 * 8 * N, "d2h_bytes_per_step": 8 * N},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "kernel": rk, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": traffic, "peak_kind": pk_kind,
+                     "algorithmic_bytes_per_launch": kbytes, "ms_per_launch": kms},
+        "cpu_baseline": {"value": cpu_v, "unit": "DOF/s", "cores": cpu_info["cores"], "kind": "port",
+                         "sample": cpu_info["sample"]},
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--refine", type=int, default=8, help="-da_refine (8: 513^3)")
+    ap.add_argument("--roofline-kernel", default="smooth")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

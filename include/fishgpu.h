@@ -1,0 +1,206 @@
+/*
+ * fishgpu.h -- C ABI of libfishgpu.so, a GB300 (sm_103a) structured-grid
+ * Poisson solver for the fish.c / poissonfunctions.c path of bueler/p4pdes.
+ *
+ * Conventions
+ *   - Every entry point returns an int status (FISHGPU_OK == 0).
+ *   - Device arrays are explicit (`*_dev` or documented as device pointers);
+ *     no hidden host<->device copies happen in the per-level call-backs.
+ *     Only fishgpu_solve_host() takes host arrays.
+ *   - Grid arrays are dense, x fastest: a[(k*my + j)*mx + i], indexed with
+ *     GLOBAL (i,j,k) exactly like the DMDA arrays au/aF of the reference.
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy default
+ *     stream); all work is stream-ordered.
+ *   - No PETSc types appear: DMDALocalInfo, PoissonCtx and the PETSc option
+ *     database are mirrored by fishgpu_info, fishgpu_ctx, fishgpu_opts.
+ */
+#ifndef FISHGPU_H_
+#define FISHGPU_H_
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+#define FISHGPU_OK               0
+#define FISHGPU_ERR_ARG          1  /* invalid argument / option value     */
+#define FISHGPU_ERR_CUDA         2  /* CUDA runtime error                  */
+#define FISHGPU_ERR_NOMEM        3  /* device allocation failed / budget   */
+#define FISHGPU_ERR_NOT_CONVERGED 4 /* KSP diverged or reached max_it      */
+#define FISHGPU_ERR_NONFINITE    5  /* NaN/Inf met during the solve        */
+#define FISHGPU_ERR_TIMEOUT      6  /* a device-side wait gave up          */
+#define FISHGPU_ERR_UNSUPPORTED  7  /* option the GPU library lacks        */
+#define FISHGPU_ERR_NODEVICE     8  /* no CUDA device / wrong architecture */
+
+/* ---- problem selection (replaces PoissonCtx's f_rhs/g_bdry pointers) -- */
+enum { FISHGPU_MANUPOLY = 0, FISHGPU_MANUEXP = 1, FISHGPU_ZERO = 2, FISHGPU_USER = 3 };
+
+/* Mirrors the DMDALocalInfo fields the call-backs use, plus the bounding box
+   that the reference obtains with DMGetBoundingBox(info->da, ...)
+   (c/ch6/poissonfunctions.c:34, :72). */
+typedef struct {
+  int dim;                 /* 1, 2, 3 */
+  int mx, my, mz;          /* global nodes per direction (1 when unused) */
+  int xs, ys, zs;          /* owned range start (global indices)        */
+  int xm, ym, zm;          /* owned range size                          */
+  double xmin[3], xmax[3]; /* bounding box                              */
+} fishgpu_info;
+
+/* Mirrors PoissonCtx (c/ch6/poissonfunctions.h:43-54).  The host function
+   pointers f_rhs/g_bdry become a problem enum evaluated on the device, or,
+   for FISHGPU_USER, device arrays holding f and g at every node. */
+typedef struct {
+  double Lx, Ly, Lz;
+  double cx, cy, cz;
+  int problem;             /* FISHGPU_MANUPOLY / MANUEXP / ZERO / USER   */
+  int dim;                 /* selects the 1D/2D/3D manufactured formula  */
+  const double *f;         /* FISHGPU_USER: device, f at every node      */
+  const double *g;         /* FISHGPU_USER: device, g at every node      */
+} fishgpu_ctx;
+
+/* ---- drop-in DMDA local call-backs ------------------------------------ */
+
+/* F = residual of -cx u_xx - cy u_yy - cz u_zz = f with Dirichlet rows, rows
+   scaled by the cell volume; replaces Poisson1DFunctionLocal
+   (c/ch6/poissonfunctions.c:4-26).  au, aF: device, whole grid. */
+int Poisson1DFunctionLocal_gpu(const fishgpu_info *info, const double *au, double *aF,
+                               const fishgpu_ctx *user, void *stream);
+/* replaces Poisson2DFunctionLocal (c/ch6/poissonfunctions.c:29-65) */
+int Poisson2DFunctionLocal_gpu(const fishgpu_info *info, const double *au, double *aF,
+                               const fishgpu_ctx *user, void *stream);
+/* replaces Poisson3DFunctionLocal (c/ch6/poissonfunctions.c:68-115) */
+int Poisson3DFunctionLocal_gpu(const fishgpu_info *info, const double *au, double *aF,
+                               const fishgpu_ctx *user, void *stream);
+
+/* q = J p with J the Jacobian the reference assembles (boundary rows:
+   diagonal only; interior rows: boundary columns eliminated), applied
+   matrix-free; optionally *pq_dot (device scalar) = p.q over the owned range.
+   Replaces Poisson1DJacobianLocal + MatMult (c/ch6/poissonfunctions.c:117-150). */
+int Poisson1DOperatorApply_gpu(const fishgpu_info *info, const double *p, double *q,
+                               double *pq_dot, const fishgpu_ctx *user, void *stream);
+/* replaces Poisson2DJacobianLocal + MatMult (c/ch6/poissonfunctions.c:152-193) */
+int Poisson2DOperatorApply_gpu(const fishgpu_info *info, const double *p, double *q,
+                               double *pq_dot, const fishgpu_ctx *user, void *stream);
+/* replaces Poisson3DJacobianLocal + MatMult (c/ch6/poissonfunctions.c:195-258) */
+int Poisson3DOperatorApply_gpu(const fishgpu_info *info, const double *p, double *q,
+                               double *pq_dot, const fishgpu_ctx *user, void *stream);
+
+/* u = exact solution (= g) at every owned node; replaces Form{1,2,3}DUExact
+   (c/ch6/fish.c:288-340); dimension taken from info->dim. */
+int FormUExact_gpu(const fishgpu_info *info, double *u, const fishgpu_ctx *user, void *stream);
+
+/* u = 0 (type 0) or uniform [0,1) noise from `seed` (type 1, the library's own
+   generator), then u = g on the boundary when gbdry != 0; replaces
+   InitialState (c/ch6/poissonfunctions.c:260-346). */
+int InitialState_gpu(const fishgpu_info *info, int initial_type, int gbdry,
+                     unsigned long long seed, double *u, const fishgpu_ctx *user, void *stream);
+
+/* err_inf = max|u-uexact|, err_h = ||u-uexact||_2 / sqrt(prod(m-1)) over the
+   whole grid; the report of c/ch6/fish.c:254-276.  Results to host doubles. */
+int ErrorNorms_gpu(const fishgpu_info *info, const double *u, const fishgpu_ctx *user,
+                   double *errinf, double *err2h, void *stream);
+
+/* ---- fish options (mirror c/ch6/fish.c:154-185 plus the PETSc solver
+        options fish's tests and studies use) ------------------------------ */
+enum { FISHGPU_PC_NONE = 0, FISHGPU_PC_JACOBI = 1, FISHGPU_PC_MG = 2 };
+enum { FISHGPU_SMOOTH_CHEBYSHEV = 0, FISHGPU_SMOOTH_RICHARDSON = 1 };
+enum { FISHGPU_NORM_PRECONDITIONED = 0, FISHGPU_NORM_UNPRECONDITIONED = 1 };
+enum { FISHGPU_FP64 = 0, FISHGPU_MIXED = 1 };
+enum { FISHGPU_INITIAL_ZEROS = 0, FISHGPU_INITIAL_RANDOM = 1, FISHGPU_INITIAL_GIVEN = 2 };
+
+typedef struct {
+  fishgpu_ctx ctx;          /* -fsh_problem -fsh_cx.. -fsh_Lx.. -fsh_dim     */
+  int mx, my, mz;           /* from -da_refine / -da_grid_{x,y,z}           */
+  int da_refine;
+  int initial_type;         /* -fsh_initial_type zeros|random (or GIVEN)    */
+  int initial_gonboundary;  /* -fsh_initial_gonboundary                     */
+  unsigned long long seed;  /* -fsh_seed (random initial iterate)           */
+  double rtol, atol, dtol;  /* -ksp_rtol -ksp_atol -ksp_divtol              */
+  int max_it;               /* -ksp_max_it                                  */
+  int norm_type;            /* -ksp_norm_type preconditioned|unpreconditioned */
+  int pc_type;              /* -pc_type mg|jacobi|none                      */
+  int mg_levels;            /* -pc_mg_levels (0: da_refine+1)               */
+  int mg_cycles;            /* -pc_mg_cycle_type v|w  (1|2)                 */
+  int smooth_type;          /* -mg_levels_ksp_type chebyshev|richardson     */
+  int smooth_its;           /* -mg_levels_ksp_max_it                        */
+  double esteig[4];         /* -mg_levels_ksp_chebyshev_esteig a,b,c,d      */
+  double richardson_scale;  /* -mg_levels_ksp_richardson_scale              */
+  int precision;            /* -fsh_precision fp64|mixed                    */
+  double inner_rtol;        /* -fsh_inner_rtol (mixed: FP32 inner floor)    */
+  int inner_max_it;         /* -fsh_inner_max_it                            */
+  int outer_max_it;         /* -fsh_outer_max_it                            */
+  int graph_iters;          /* -fsh_graph_iters (CG iterations per graph)   */
+  int monitor;              /* -ksp_monitor                                 */
+  int converged_reason;     /* -ksp_converged_reason                        */
+  int snes_monitor;         /* -snes_monitor[_short]                        */
+} fishgpu_opts;
+
+#define FISHGPU_MAX_HIST 512
+
+typedef struct {
+  int its;                  /* KSP iterations (mixed: inner, summed)        */
+  int reason;               /* PETSc KSPConvergedReason numbering           */
+  int outer_its;            /* mixed: refinement steps                      */
+  int nhist;                /* residual-norm history entries               */
+  double hist[FISHGPU_MAX_HIST];
+  double fnorm0, fnorm1;    /* ||F(u0)||_2, ||F(u)||_2                      */
+  double errinf, err2h;     /* vs the exact solution (manupoly/manuexp/zero) */
+  double true_rel_resid;    /* ||b - J y||_2 / ||b||_2 of the linear solve  */
+  double setup_ms, solve_ms;/* device time, CUDA events                     */
+  long long dofs;           /* mx*my*mz                                     */
+  long long launches;       /* kernels of this library launched by the solve */
+} fishgpu_report;
+
+const char *fishgpu_strerror(int code);
+/* PETSc-style reason name, e.g. "CONVERGED_RTOL" */
+const char *fishgpu_reason_name(int reason);
+
+/* defaults of fish.c + PETSc, except pc_type defaults to mg (PETSc's
+   one-rank default ILU is sequential and not offered by this library) */
+int fishgpu_opts_default(fishgpu_opts *o);
+/* parse fish's flag spellings; unknown flags are ignored as PETSc does */
+int fishgpu_opts_parse(fishgpu_opts *o, int argc, const char *const *argv);
+
+/* ---- solver: device-resident hierarchy --------------------------------- */
+typedef struct fishgpu_solver_s fishgpu_solver;
+
+int fishgpu_solver_create(const fishgpu_opts *o, void *stream, fishgpu_solver **out);
+/* Full fish flow (c/ch6/fish.c:237-280 with SNESKSPONLY): u0 from the
+   options (or u_dev itself for FISHGPU_INITIAL_GIVEN), F(u0), KSP solve of
+   J y = F(u0), u = u0 - y, errors.  u_dev: device, mx*my*mz doubles. */
+int fishgpu_solver_solve(fishgpu_solver *s, double *u_dev, fishgpu_report *rep);
+int fishgpu_solver_destroy(fishgpu_solver *s);
+/* device bytes held by the solver */
+long long fishgpu_solver_bytes(const fishgpu_solver *s);
+
+/* Same flow with HOST arrays on an existing solver (the end-to-end form):
+   for FISHGPU_USER solvers created with ctx.f == ctx.g == NULL the solver owns
+   device copies of f and g, and f_host/g_host (mx*my*mz doubles each) are
+   copied in first; u_host receives the solution (and supplies u0 for
+   FISHGPU_INITIAL_GIVEN).  All copies are stream-ordered on the solver's
+   stream and included in rep->solve_ms. */
+int fishgpu_solver_solve_host(fishgpu_solver *s, const double *f_host, const double *g_host,
+                              double *u_host, fishgpu_report *rep);
+
+/* one-shot create + solve + destroy */
+int fishgpu_solve(const fishgpu_opts *o, double *u_dev, fishgpu_report *rep);
+
+/* End-to-end form with HOST arrays: copies f_host and g_host (FISHGPU_USER
+   data, may be NULL for the built-in problems) to the device, solves, copies
+   the solution to u_host.  The copies are stream-ordered on the solver's
+   stream and included in rep->solve_ms. */
+int fishgpu_solve_host(const fishgpu_opts *o, const double *f_host, const double *g_host,
+                       double *u_host, fishgpu_report *rep);
+
+/* Times `reps` launches of one solver kernel on the finest level with the
+   solver's resident data (CUDA events on the solver's stream).  Names:
+   "apply", "cg_update", "smooth", "resid_restrict", "prolong_smooth",
+   "residual64".  Reports the mean ms per launch and the algorithmic bytes
+   one launch moves. */
+int fishgpu_solver_time_kernel(fishgpu_solver *s, const char *name, int reps,
+                               double *ms_per_launch, double *bytes_per_launch);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,316 @@
+"""p4pdes_gb300 -- GB300 (sm_103a) solver for the fish.c / poissonfunctions.c path.
+
+Python front end of libfishgpu.so (the C ABI declared in include/fishgpu.h).
+It mirrors the reference's interface for this path:
+
+  * ``Poisson{1,2,3}DFunctionLocal(info, au, aF, user)``  -- residual call-backs
+    (c/ch6/poissonfunctions.c:4-115), same argument meaning, arrays are CUDA
+    tensors indexed with global (i,j,k) like the DMDA arrays;
+  * ``Poisson{1,2,3}DOperatorApply(info, p, q, user)``   -- the Jacobian of
+    c/ch6/poissonfunctions.c:117-258 applied matrix-free, returns p.q;
+  * ``FormUExact``, ``InitialState``, ``error_norms``     -- c/ch6/fish.c:237-340,
+    c/ch6/poissonfunctions.c:260-346;
+  * ``options(argv)`` parses fish's flags (-fsh_*, -da_refine, -ksp_*, -pc_*,
+    -mg_levels_*), ``solve(opts)`` runs the fish flow on the GPU.
+
+Errors raise FishError carrying the library status (the reference returns
+PetscErrorCode).  There is no CPU fallback: if the library is missing the
+import of any entry point raises.
+"""
+import ctypes
+import os
+
+__all__ = [
+    "Info", "Ctx", "Opts", "Report", "FishError", "load", "options", "info_for", "solve",
+    "Poisson1DFunctionLocal", "Poisson2DFunctionLocal", "Poisson3DFunctionLocal",
+    "Poisson1DOperatorApply", "Poisson2DOperatorApply", "Poisson3DOperatorApply",
+    "FormUExact", "InitialState", "error_norms", "reason_name",
+]
+
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "lib", "libfishgpu.so")
+
+MANUPOLY, MANUEXP, ZERO, USER = 0, 1, 2, 3
+PROBLEMS = {"manupoly": MANUPOLY, "manuexp": MANUEXP, "zero": ZERO}
+PC_NONE, PC_JACOBI, PC_MG = 0, 1, 2
+SMOOTH_CHEBYSHEV, SMOOTH_RICHARDSON = 0, 1
+NORM_PRECONDITIONED, NORM_UNPRECONDITIONED = 0, 1
+FP64, MIXED = 0, 1
+INITIAL_ZEROS, INITIAL_RANDOM, INITIAL_GIVEN = 0, 1, 2
+MAX_HIST = 512
+
+c_int, c_double, c_void_p, c_ll, c_ull = (ctypes.c_int, ctypes.c_double, ctypes.c_void_p,
+                                          ctypes.c_longlong, ctypes.c_ulonglong)
+
+
+class Info(ctypes.Structure):
+    """fishgpu_info: the DMDALocalInfo fields plus the bounding box."""
+    _fields_ = [("dim", c_int), ("mx", c_int), ("my", c_int), ("mz", c_int),
+                ("xs", c_int), ("ys", c_int), ("zs", c_int),
+                ("xm", c_int), ("ym", c_int), ("zm", c_int),
+                ("xmin", c_double * 3), ("xmax", c_double * 3)]
+
+
+class Ctx(ctypes.Structure):
+    """fishgpu_ctx: PoissonCtx with a problem enum in place of f_rhs/g_bdry."""
+    _fields_ = [("Lx", c_double), ("Ly", c_double), ("Lz", c_double),
+                ("cx", c_double), ("cy", c_double), ("cz", c_double),
+                ("problem", c_int), ("dim", c_int), ("f", c_void_p), ("g", c_void_p)]
+
+
+class Opts(ctypes.Structure):
+    _fields_ = [("ctx", Ctx), ("mx", c_int), ("my", c_int), ("mz", c_int), ("da_refine", c_int),
+                ("initial_type", c_int), ("initial_gonboundary", c_int), ("seed", c_ull),
+                ("rtol", c_double), ("atol", c_double), ("dtol", c_double),
+                ("max_it", c_int), ("norm_type", c_int), ("pc_type", c_int), ("mg_levels", c_int),
+                ("mg_cycles", c_int), ("smooth_type", c_int), ("smooth_its", c_int),
+                ("esteig", c_double * 4), ("richardson_scale", c_double), ("precision", c_int),
+                ("inner_rtol", c_double), ("inner_max_it", c_int), ("outer_max_it", c_int),
+                ("graph_iters", c_int), ("monitor", c_int), ("converged_reason", c_int),
+                ("snes_monitor", c_int)]
+
+    @property
+    def dofs(self):
+        d = self.ctx.dim
+        return self.mx * (self.my if d >= 2 else 1) * (self.mz if d >= 3 else 1)
+
+    @property
+    def shape(self):
+        """(mz, my, mx) of the dense array, x fastest."""
+        d = self.ctx.dim
+        return (self.mz if d >= 3 else 1, self.my if d >= 2 else 1, self.mx)
+
+
+class Report(ctypes.Structure):
+    _fields_ = [("its", c_int), ("reason", c_int), ("outer_its", c_int), ("nhist", c_int),
+                ("hist", c_double * MAX_HIST), ("fnorm0", c_double), ("fnorm1", c_double),
+                ("errinf", c_double), ("err2h", c_double), ("true_rel_resid", c_double),
+                ("setup_ms", c_double), ("solve_ms", c_double), ("dofs", c_ll), ("launches", c_ll)]
+
+    def history(self):
+        return [self.hist[i] for i in range(min(self.nhist, MAX_HIST))]
+
+
+class FishError(RuntimeError):
+    def __init__(self, code, what=""):
+        self.code = code
+        msg = load().fishgpu_strerror(code).decode() if _lib is not None else str(code)
+        super().__init__("%s: %s (status %d)" % (what, msg, code) if what else msg)
+
+
+_lib = None
+_P = ctypes.POINTER
+
+
+def load():
+    """Load libfishgpu.so (built in-tree by p4pdes_gb300.build)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError("libfishgpu.so is not built (%s); run p4pdes_gb300.build.build()" % LIB_PATH)
+    lib = ctypes.CDLL(LIB_PATH)
+    for dim in (1, 2, 3):
+        f = getattr(lib, "Poisson%dDFunctionLocal_gpu" % dim)
+        f.argtypes = [_P(Info), c_void_p, c_void_p, _P(Ctx), c_void_p]
+        f.restype = c_int
+        f = getattr(lib, "Poisson%dDOperatorApply_gpu" % dim)
+        f.argtypes = [_P(Info), c_void_p, c_void_p, c_void_p, _P(Ctx), c_void_p]
+        f.restype = c_int
+    lib.FormUExact_gpu.argtypes = [_P(Info), c_void_p, _P(Ctx), c_void_p]
+    lib.InitialState_gpu.argtypes = [_P(Info), c_int, c_int, c_ull, c_void_p, _P(Ctx), c_void_p]
+    lib.ErrorNorms_gpu.argtypes = [_P(Info), c_void_p, _P(Ctx), _P(c_double), _P(c_double), c_void_p]
+    lib.fishgpu_strerror.argtypes = [c_int]
+    lib.fishgpu_strerror.restype = ctypes.c_char_p
+    lib.fishgpu_reason_name.argtypes = [c_int]
+    lib.fishgpu_reason_name.restype = ctypes.c_char_p
+    lib.fishgpu_opts_default.argtypes = [_P(Opts)]
+    lib.fishgpu_opts_parse.argtypes = [_P(Opts), c_int, _P(ctypes.c_char_p)]
+    lib.fishgpu_solver_create.argtypes = [_P(Opts), c_void_p, _P(c_void_p)]
+    lib.fishgpu_solver_solve.argtypes = [c_void_p, c_void_p, _P(Report)]
+    lib.fishgpu_solver_destroy.argtypes = [c_void_p]
+    lib.fishgpu_solver_bytes.argtypes = [c_void_p]
+    lib.fishgpu_solver_bytes.restype = c_ll
+    lib.fishgpu_solve.argtypes = [_P(Opts), c_void_p, _P(Report)]
+    lib.fishgpu_solve_host.argtypes = [_P(Opts), c_void_p, c_void_p, c_void_p, _P(Report)]
+    lib.fishgpu_solver_solve_host.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, _P(Report)]
+    lib.fishgpu_solver_solve_host.restype = c_int
+    lib.fishgpu_solver_time_kernel.argtypes = [c_void_p, ctypes.c_char_p, c_int, _P(c_double), _P(c_double)]
+    for name in ("FormUExact_gpu", "InitialState_gpu", "ErrorNorms_gpu", "fishgpu_opts_default",
+                 "fishgpu_opts_parse", "fishgpu_solver_create", "fishgpu_solver_solve",
+                 "fishgpu_solver_destroy", "fishgpu_solve", "fishgpu_solve_host",
+                 "fishgpu_solver_time_kernel"):
+        getattr(lib, name).restype = c_int
+    _lib = lib
+    return lib
+
+
+def _check(rc, what):
+    if rc != 0:
+        raise FishError(rc, what)
+
+
+def reason_name(reason):
+    return load().fishgpu_reason_name(reason).decode()
+
+
+def options(argv=()):
+    """fishgpu_opts from fish's command-line flags (a list or a string)."""
+    if isinstance(argv, str):
+        argv = argv.split()
+    o = Opts()
+    lib = load()
+    _check(lib.fishgpu_opts_default(ctypes.byref(o)), "fishgpu_opts_default")
+    arr = (ctypes.c_char_p * max(1, len(argv)))(*[a.encode() for a in argv])
+    _check(lib.fishgpu_opts_parse(ctypes.byref(o), len(argv), arr), "fishgpu_opts_parse")
+    return o
+
+
+def info_for(opts):
+    """The whole-grid local info of one GPU holding the whole DMDA."""
+    d = opts.ctx.dim
+    inf = Info()
+    inf.dim = d
+    inf.mx = opts.mx
+    inf.my = opts.my if d >= 2 else 1
+    inf.mz = opts.mz if d >= 3 else 1
+    inf.xm, inf.ym, inf.zm = inf.mx, inf.my, inf.mz
+    inf.xmax[0], inf.xmax[1], inf.xmax[2] = opts.ctx.Lx, opts.ctx.Ly, opts.ctx.Lz
+    return inf
+
+
+def _ptr(t):
+    if t is None:
+        return None
+    if not t.is_cuda or not t.is_contiguous():
+        raise ValueError("expected a contiguous CUDA tensor")
+    return t.data_ptr()
+
+
+def _stream(stream):
+    if stream is None:
+        import torch
+        return torch.cuda.current_stream().cuda_stream
+    return int(stream)
+
+
+def _fl(dim, info, au, aF, user, stream):
+    fn = getattr(load(), "Poisson%dDFunctionLocal_gpu" % dim)
+    _check(fn(ctypes.byref(info), _ptr(au), _ptr(aF), ctypes.byref(user), _stream(stream)),
+           "Poisson%dDFunctionLocal" % dim)
+
+
+def Poisson1DFunctionLocal(info, au, aF, user, stream=None):
+    _fl(1, info, au, aF, user, stream)
+
+
+def Poisson2DFunctionLocal(info, au, aF, user, stream=None):
+    _fl(2, info, au, aF, user, stream)
+
+
+def Poisson3DFunctionLocal(info, au, aF, user, stream=None):
+    _fl(3, info, au, aF, user, stream)
+
+
+def _apply(dim, info, p, q, user, stream, dot):
+    import torch
+    fn = getattr(load(), "Poisson%dDOperatorApply_gpu" % dim)
+    d = torch.zeros(1, dtype=torch.float64, device=p.device) if dot else None
+    _check(fn(ctypes.byref(info), _ptr(p), _ptr(q), _ptr(d), ctypes.byref(user), _stream(stream)),
+           "Poisson%dDOperatorApply" % dim)
+    return d
+
+
+def Poisson1DOperatorApply(info, p, q, user, stream=None, dot=True):
+    return _apply(1, info, p, q, user, stream, dot)
+
+
+def Poisson2DOperatorApply(info, p, q, user, stream=None, dot=True):
+    return _apply(2, info, p, q, user, stream, dot)
+
+
+def Poisson3DOperatorApply(info, p, q, user, stream=None, dot=True):
+    return _apply(3, info, p, q, user, stream, dot)
+
+
+def FormUExact(info, u, user, stream=None):
+    _check(load().FormUExact_gpu(ctypes.byref(info), _ptr(u), ctypes.byref(user), _stream(stream)),
+           "FormUExact")
+
+
+def InitialState(info, initial_type, gbdry, u, user, seed=0, stream=None):
+    _check(load().InitialState_gpu(ctypes.byref(info), initial_type, int(bool(gbdry)), seed, _ptr(u),
+                                   ctypes.byref(user), _stream(stream)), "InitialState")
+
+
+def error_norms(info, u, user, stream=None):
+    a, b = c_double(), c_double()
+    _check(load().ErrorNorms_gpu(ctypes.byref(info), _ptr(u), ctypes.byref(user), ctypes.byref(a),
+                                 ctypes.byref(b), _stream(stream)), "ErrorNorms")
+    return a.value, b.value
+
+
+class Solver:
+    """Device-resident hierarchy; solve() runs the fish flow (u0, F(u0), KSP, u)."""
+
+    def __init__(self, opts, stream=None):
+        self.opts = opts
+        self._h = c_void_p()
+        st = None if stream is None else int(stream)
+        _check(load().fishgpu_solver_create(ctypes.byref(opts), st, ctypes.byref(self._h)),
+               "fishgpu_solver_create")
+
+    def solve(self, u):
+        rep = Report()
+        rc = load().fishgpu_solver_solve(self._h, _ptr(u), ctypes.byref(rep))
+        if rc not in (0, 4):
+            raise FishError(rc, "fishgpu_solver_solve")
+        return rep
+
+    def solve_host(self, f=None, g=None, u=None):
+        """Host-array solve (numpy or pinned torch CPU tensors, float64)."""
+        def addr(a):
+            if a is None:
+                return None
+            return a.data_ptr() if hasattr(a, "data_ptr") else a.ctypes.data
+        rep = Report()
+        rc = load().fishgpu_solver_solve_host(self._h, addr(f), addr(g), addr(u), ctypes.byref(rep))
+        if rc not in (0, 4):
+            raise FishError(rc, "fishgpu_solver_solve_host")
+        return rep
+
+    def time_kernel(self, name, reps):
+        ms, by = c_double(), c_double()
+        _check(load().fishgpu_solver_time_kernel(self._h, name.encode(), reps, ctypes.byref(ms),
+                                                 ctypes.byref(by)), "time_kernel")
+        return ms.value, by.value
+
+    @property
+    def device_bytes(self):
+        return load().fishgpu_solver_bytes(self._h)
+
+    def close(self):
+        if self._h:
+            load().fishgpu_solver_destroy(self._h)
+            self._h = c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def solve(opts, u=None):
+    """Run the fish flow; returns (u, report).  u: CUDA float64 tensor (mz,my,mx)."""
+    import torch
+    if u is None:
+        u = torch.empty(opts.shape, dtype=torch.float64, device="cuda")
+    with Solver(opts) as s:
+        rep = s.solve(u)
+    return u, rep

@@ -1,0 +1,349 @@
+// kernels.cuh -- stencil, smoother, grid-transfer and Krylov-vector kernels.
+//
+// All kernels are templated on the dimension DIM (1,2,3) and on the storage
+// and arithmetic type T (double for the FP64 path, float for the FP32
+// V-cycle of the mixed form).  A thread owns one (i,j) column and marches
+// `zc` consecutive k-planes; blocks are (32,8) threads over (i,j) (256 x 1
+// in 1D).  Kernels that belong to a CG iteration take the device KspState
+// and return at once when it is marked done, so surplus iterations of a
+// captured graph cost only empty launches.
+//
+// The operator is the Jacobian the reference assembles
+// (c/ch6/poissonfunctions.c:117-258), applied matrix-free: boundary rows
+// are scdiag*p; interior rows are scdiag*p - sum_d sc_d * (neighbours along d
+// that are NOT boundary nodes).  The FP64 instruction count is kept minimal
+// (GB300's FP64 pipe, not HBM, bounds the FP64 form): 1 + 2*DIM per apply.
+#pragma once
+
+#include "fishgpu_internal.cuh"
+
+namespace fg {
+
+struct Range {   // owned box [xs,xe) x [ys,ye) x [zs,ze)
+  int xs, ys, zs, xe, ye, ze;
+};
+
+__host__ __device__ inline Range full_range(const Geom &g) { return Range{0, 0, 0, g.mx, g.my, g.mz}; }
+
+template <typename T>
+struct Wt {
+  T sx, sy, sz, sd;
+  __device__ __forceinline__ explicit Wt(const Geom &g)
+      : sx((T)g.sc[0]), sy((T)g.sc[1]), sz((T)g.sc[2]), sd((T)g.scdiag) {}
+};
+
+template <int DIM>
+__device__ __forceinline__ bool on_bdry(const Geom &g, int i, int j, int k) {
+  bool b = (i == 0) | (i == g.mx - 1);
+  if (DIM >= 2) b |= (j == 0) | (j == g.my - 1);
+  if (DIM >= 3) b |= (k == 0) | (k == g.mz - 1);
+  return b;
+}
+
+// s0 + sum_d sc_d * (interior neighbours of n along d); n must be interior.
+template <int DIM, typename T>
+__device__ __forceinline__ T nbr_sum(const T *__restrict__ p, long long n, int i, int j, int k,
+                                     const Geom &g, const Wt<T> &w, T s0) {
+  T a = (i - 1 > 0 ? p[n - 1] : T(0)) + (i + 1 < g.mx - 1 ? p[n + 1] : T(0));
+  T s = fma(w.sx, a, s0);
+  if (DIM >= 2) {
+    T b = (j - 1 > 0 ? p[n - g.pitch] : T(0)) + (j + 1 < g.my - 1 ? p[n + g.pitch] : T(0));
+    s = fma(w.sy, b, s);
+  }
+  if (DIM >= 3) {
+    T c = (k - 1 > 0 ? p[n - g.plane] : T(0)) + (k + 1 < g.mz - 1 ? p[n + g.plane] : T(0));
+    s = fma(w.sz, c, s);
+  }
+  return s;
+}
+
+// (A p)_n
+template <int DIM, typename T>
+__device__ __forceinline__ T apply_at(const T *__restrict__ p, long long n, int i, int j, int k,
+                                      const Geom &g, const Wt<T> &w) {
+  T pn = p[n];
+  if (on_bdry<DIM>(g, i, j, k)) return w.sd * pn;
+  return fma(w.sd, pn, -nbr_sum<DIM, T>(p, n, i, j, k, g, w, T(0)));
+}
+
+// (b - A x)_n
+template <int DIM, typename T>
+__device__ __forceinline__ T resid_at(const T *__restrict__ b, const T *__restrict__ x, long long n,
+                                      int i, int j, int k, const Geom &g, const Wt<T> &w) {
+  T xn = x[n], bn = b[n];
+  if (on_bdry<DIM>(g, i, j, k)) return fma(-w.sd, xn, bn);
+  return fma(-w.sd, xn, nbr_sum<DIM, T>(x, n, i, j, k, g, w, bn));
+}
+
+__device__ __forceinline__ bool ksp_done(const KspState *st) {
+  return st && __ldcg(&st->done);
+}
+
+// Grid-stride loop over tiles of blockDim.x x blockDim.y columns x tm.zc
+// planes (x fastest); a thread marches k through its tile's planes.
+#define FG_POINT_LOOP_BEGIN(R)                                                  \
+  for (int t_ = blockIdx.x; t_ < tm.tx * tm.ty * tm.tz; t_ += gridDim.x) {      \
+    const int i = (R).xs + (t_ % tm.tx) * blockDim.x + threadIdx.x;             \
+    const int j = (R).ys + ((t_ / tm.tx) % tm.ty) * blockDim.y + threadIdx.y;   \
+    const int kbeg = (R).zs + (t_ / (tm.tx * tm.ty)) * tm.zc;                   \
+    const int kend = min(kbeg + tm.zc, (R).ze);                                 \
+    if (i < (R).xe && j < (R).ye) {                                             \
+      for (int k = kbeg; k < kend; k++) {                                       \
+        const long long n = gidx(g, i, j, k);
+
+#define FG_POINT_LOOP_END \
+  }                       \
+  }                       \
+  }
+
+// ------------------------------------------------------------------ apply
+// q = A p on the range; DOT: p.q reduced, finalised by `fin`.
+template <int DIM, typename T, bool DOT>
+__global__ void __launch_bounds__(256) k_apply(Geom g, Range R, Tiles tm, KspState *st,
+                                               const T *__restrict__ p, T *__restrict__ q,
+                                               Reducer red, int slot, Fin fin, double *out) {
+  if (ksp_done(st)) return;
+  const Wt<T> w(g);
+  T acc = T(0);
+  FG_POINT_LOOP_BEGIN(R)
+  T v = apply_at<DIM, T>(p, n, i, j, k, g, w);
+  q[n] = v;
+  if (DOT) acc = fma(p[n], v, acc);
+  FG_POINT_LOOP_END
+  if (DOT) {
+    double v1[1] = {(double)acc};
+    reduce_and_finalize<1>(v1, red, slot, st, fin, out);
+  }
+}
+
+// ------------------------------------------------------------------ CG vectors
+// p = z + (beta/betaold) p; p = z on the first iteration (PETSc VecAYPX / VecCopy)
+template <int DIM, typename T>
+__global__ void __launch_bounds__(256) k_cg_p(Geom g, Range R, Tiles tm, KspState *st,
+                                              const T *__restrict__ z, T *__restrict__ p) {
+  if (ksp_done(st)) return;
+  const bool first = st->i == 0;
+  const T bb = first ? T(0) : (T)(st->beta / st->betaold);
+  FG_POINT_LOOP_BEGIN(R)
+  p[n] = first ? z[n] : fma(bb, p[n], z[n]);
+  FG_POINT_LOOP_END
+}
+
+// y += alpha p; r -= alpha w; RR: r.r reduced (unpreconditioned norm test)
+template <int DIM, typename T, bool RR>
+__global__ void __launch_bounds__(256) k_cg_xr(Geom g, Range R, Tiles tm, KspState *st,
+                                               const T *__restrict__ p, const T *__restrict__ w,
+                                               T *__restrict__ y, T *__restrict__ r, Reducer red,
+                                               int slot) {
+  if (ksp_done(st)) return;
+  const T a = (T)st->alpha;
+  T acc = T(0);
+  FG_POINT_LOOP_BEGIN(R)
+  y[n] = fma(a, p[n], y[n]);
+  T rn = fma(-a, w[n], r[n]);
+  r[n] = rn;
+  if (RR) acc = fma(rn, rn, acc);
+  FG_POINT_LOOP_END
+  if (RR) {
+    double v1[1] = {(double)acc};
+    reduce_and_finalize<1>(v1, red, slot, st, FIN_RR, nullptr);
+  }
+}
+
+// z.z and z.r reduced together
+template <int DIM, typename T>
+__global__ void __launch_bounds__(256) k_dots_zr(Geom g, Range R, Tiles tm, KspState *st,
+                                                 const T *__restrict__ z, const T *__restrict__ r,
+                                                 Reducer red, int slot, Fin fin, double *out) {
+  if (ksp_done(st)) return;
+  T zz = T(0), zr = T(0);
+  FG_POINT_LOOP_BEGIN(R)
+  T zn = z[n];
+  zz = fma(zn, zn, zz);
+  zr = fma(zn, r[n], zr);
+  FG_POINT_LOOP_END
+  double v2[2] = {(double)zz, (double)zr};
+  reduce_and_finalize<2>(v2, red, slot, st, fin, out);
+}
+
+// ------------------------------------------------------------------ smoothers
+// One Chebyshev (or Richardson) step preconditioned by Jacobi:
+//   out = ckm1*xkm1 + ck*xk + crd*(b - A xk),   crd = c_r / scdiag.
+// HAS_XK=false means xk = 0 (first step from a zero iterate);
+// HAS_KM1=false drops the xkm1 term.  out may alias xkm1 (read at n only).
+template <int DIM, typename T, bool HAS_XK, bool HAS_KM1>
+__global__ void __launch_bounds__(256) k_cheb(Geom g, Tiles tm, KspState *st, const T *__restrict__ b,
+                                              const T *xkm1, const T *__restrict__ xk, T *out,
+                                              T ckm1, T ck, T crd) {
+  if (ksp_done(st)) return;
+  const Wt<T> w(g);
+  const Range R = full_range(g);
+  FG_POINT_LOOP_BEGIN(R)
+  T v;
+  if (HAS_XK) {
+    T t = resid_at<DIM, T>(b, xk, n, i, j, k, g, w);
+    T base = ck * xk[n];
+    if (HAS_KM1) base = fma(ckm1, xkm1[n], base);
+    v = fma(crd, t, base);
+  } else {
+    v = crd * b[n];
+    if (HAS_KM1) v = fma(ckm1, xkm1[n], v);
+  }
+  out[n] = v;
+  FG_POINT_LOOP_END
+}
+
+// r = b - A x
+template <int DIM, typename T>
+__global__ void __launch_bounds__(256) k_resid(Geom g, Tiles tm, KspState *st, const T *__restrict__ b,
+                                               const T *__restrict__ x, T *__restrict__ r) {
+  if (ksp_done(st)) return;
+  const Wt<T> w(g);
+  const Range R = full_range(g);
+  FG_POINT_LOOP_BEGIN(R)
+  r[n] = resid_at<DIM, T>(b, x, n, i, j, k, g, w);
+  FG_POINT_LOOP_END
+}
+
+// ------------------------------------------------------------------ grid transfers
+// b_c = P^T r_f : full weighting with weights prod_d (1 - |delta_d|/2), the
+// transpose of DMDA's Q1 interpolation, over every coarse node.
+template <int DIM, typename T>
+__global__ void __launch_bounds__(256) k_restrict(Geom gf, Geom g, Tiles tm, KspState *st,
+                                                  const T *__restrict__ rf, T *__restrict__ bc) {
+  if (ksp_done(st)) return;
+  const Range R = full_range(g);
+  FG_POINT_LOOP_BEGIN(R)
+  const int fi = 2 * i;
+  const bool hw = fi - 1 >= 0, he = fi + 1 < gf.mx;
+  T acc = T(0);
+  const int dk = DIM >= 3 ? 1 : 0, dj = DIM >= 2 ? 1 : 0;
+  for (int a = -dk; a <= dk; a++) {
+    const int fk = 2 * k + a;
+    if (fk < 0 || fk >= gf.mz) continue;
+    T accy = T(0);
+    for (int bb = -dj; bb <= dj; bb++) {
+      const int fj = 2 * j + bb;
+      if (fj < 0 || fj >= gf.my) continue;
+      const long long m = gidx(gf, fi, fj, fk);
+      T side = (hw ? rf[m - 1] : T(0)) + (he ? rf[m + 1] : T(0));
+      T row = fma(T(0.5), side, rf[m]);
+      accy = bb ? fma(T(0.5), row, accy) : accy + row;
+    }
+    acc = a ? fma(T(0.5), accy, acc) : acc + accy;
+  }
+  bc[n] = acc;
+  FG_POINT_LOOP_END
+}
+
+// x_f += P x_c : DMDA Q1 interpolation, vertex-centred, ratio 2
+template <int DIM, typename T>
+__global__ void __launch_bounds__(256) k_prolong(Geom g, Geom gc, Tiles tm, KspState *st,
+                                                 const T *__restrict__ xc, T *__restrict__ xf) {
+  if (ksp_done(st)) return;
+  const Range R = full_range(g);
+  FG_POINT_LOOP_BEGIN(R)
+  const int I = i >> 1, J = j >> 1, K = k >> 1;
+  const bool oi = i & 1, oj = DIM >= 2 && (j & 1), ok = DIM >= 3 && (k & 1);
+  const long long m = gidx(gc, I, J, K);
+  T s = xc[m];
+  if (oi) s += xc[m + 1];
+  if (oj) {
+    T t = xc[m + gc.pitch];
+    if (oi) t += xc[m + gc.pitch + 1];
+    s += t;
+  }
+  if (ok) {
+    const long long m2 = m + gc.plane;
+    T t = xc[m2];
+    if (oi) t += xc[m2 + 1];
+    if (oj) {
+      T u = xc[m2 + gc.pitch];
+      if (oi) u += xc[m2 + gc.pitch + 1];
+      t += u;
+    }
+    s += t;
+  }
+  const int nodd = (int)oi + (int)oj + (int)ok;
+  const T wgt = nodd == 0 ? T(1) : nodd == 1 ? T(0.5) : nodd == 2 ? T(0.25) : T(0.125);
+  xf[n] = fma(wgt, s, xf[n]);
+  FG_POINT_LOOP_END
+}
+
+// ------------------------------------------------------------------ coarse solve
+// Exact solve on the coarsest level in ONE block: boundary rows x = b/scdiag;
+// interior by sine-transform diagonalisation x = S (Lambda^{-1} (S b)) with
+// S_d[i][k] = sqrt(2/(n+1)) sin(ik pi/(n+1)) (symmetric, orthogonal) and
+// Lambda = sum_d sc_d (2 - 2cos(k_d pi/(n_d+1))).  S and 1/Lambda come from
+// the host (setup); work holds 2 * prod(n_d) entries.
+template <int DIM, typename T>
+__global__ void __launch_bounds__(1024) k_coarse(Geom g, KspState *st, const T *__restrict__ b,
+                                                 T *__restrict__ x, const T *__restrict__ S0,
+                                                 const T *__restrict__ S1, const T *__restrict__ S2,
+                                                 const T *__restrict__ ilam, T *work, int n0, int n1,
+                                                 int n2) {
+  if (ksp_done(st)) return;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const long long N = (long long)g.mx * g.my * g.mz;
+  const T dinv = (T)(1.0 / g.scdiag);
+  for (long long q = tid; q < N; q += nt) {
+    int i = (int)(q % g.mx), j = (int)((q / g.mx) % g.my), k = (int)(q / ((long long)g.mx * g.my));
+    long long n = gidx(g, i, j, k);
+    x[n] = b[n] * dinv;
+  }
+  const int ni = n0 * n1 * n2;
+  if (ni <= 0) return;
+  T *A = work, *B = work + ni;
+  const int oj = DIM >= 2 ? 1 : 0, ok = DIM >= 3 ? 1 : 0;
+  __syncthreads();
+  for (int q = tid; q < ni; q += nt) {
+    int i = q % n0, j = (q / n0) % n1, k = q / (n0 * n1);
+    A[q] = b[gidx(g, i + 1, j + oj, k + ok)];
+  }
+  __syncthreads();
+  for (int pass = 0; pass < 2; pass++) {
+    for (int d = 0; d < DIM; d++) {
+      const T *S = d == 0 ? S0 : d == 1 ? S1 : S2;
+      const int nd = d == 0 ? n0 : d == 1 ? n1 : n2;
+      const int st_d = d == 0 ? 1 : d == 1 ? n0 : n0 * n1;
+      for (int q = tid; q < ni; q += nt) {
+        int c = d == 0 ? q % n0 : d == 1 ? (q / n0) % n1 : q / (n0 * n1);
+        int base = q - c * st_d;
+        T s = T(0);
+        for (int kk = 0; kk < nd; kk++) s = fma(S[c * nd + kk], A[base + kk * st_d], s);
+        B[q] = s;
+      }
+      __syncthreads();
+      T *t = A; A = B; B = t;
+    }
+    if (pass == 0) {
+      for (int q = tid; q < ni; q += nt) A[q] *= ilam[q];
+      __syncthreads();
+    }
+  }
+  for (int q = tid; q < ni; q += nt) {
+    int i = q % n0, j = (q / n0) % n1, k = q / (n0 * n1);
+    x[gidx(g, i + 1, j + oj, k + ok)] = A[q];
+  }
+}
+
+// ------------------------------------------------------------------ misc
+template <int DIM, typename T>
+__global__ void __launch_bounds__(256) k_zero(Geom g, Tiles tm, T *__restrict__ a) {
+  const Range R = full_range(g);
+  FG_POINT_LOOP_BEGIN(R)
+  a[n] = T(0);
+  FG_POINT_LOOP_END
+}
+
+template <int DIM, typename T>
+__global__ void __launch_bounds__(256) k_copy(Geom g, Tiles tm, KspState *st, const T *__restrict__ a,
+                                              T *__restrict__ b) {
+  if (ksp_done(st)) return;
+  const Range R = full_range(g);
+  FG_POINT_LOOP_BEGIN(R)
+  b[n] = a[n];
+  FG_POINT_LOOP_END
+}
+
+}  // namespace fg

@@ -1,0 +1,904 @@
+// solver.cu -- device-resident CG + geometric multigrid for the fish solve.
+//
+// Replaces the PETSc stack fish selects (c/ch6/fish.c:223-239: SNESKSPONLY,
+// KSPCG, -pc_type mg) with project code:
+//   * KSP: CG with PETSc's cg.c semantics (preconditioned or unpreconditioned
+//     norm, KSPConvergedDefault test), all scalars on the device;
+//   * PC: multiplicative V/W cycles over the DMDA hierarchy
+//     (m_c = (m_f-1)/2+1), rediscretised level operators (fish.c:7),
+//     Q1 interpolation P and restriction P^T, Chebyshev/Jacobi or
+//     Richardson/Jacobi smoothing with a nonzero initial guess, exact
+//     coarse solve (single block);
+//   * the KSP set-up and one CG iteration are captured once as CUDA graphs.
+// Forms: FISHGPU_FP64 (everything FP64; the twin of the CPU oracle) and
+// FISHGPU_MIXED (FP64 iterative refinement: FP64 true residual, norms and
+// solution update; FP32 inner CG with an FP32 V-cycle).
+//
+// Internal vectors use the padded layout of vkernels.cuh (row pitch a
+// multiple of 4, zero padding); the caller's u is dense and is packed /
+// unpacked at the ends of a solve.
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <vector>
+
+#include "common.cuh"
+#include "vkernels.cuh"
+
+namespace fg {
+
+constexpr int MAX_LEVELS = 24;
+constexpr int ZC = 32;            // k-planes per block in the 3D stencil kernels
+constexpr int FLAT_BLOCKS = 4096; // grid cap of the pointwise kernels
+
+template <typename T>
+struct Level {
+  Geom g;      // padded pitch
+  Slots sl;
+  T *b = nullptr, *r = nullptr;
+  T *X[3] = {nullptr, nullptr, nullptr};  // rotating iterate buffers
+  int cur = 0;                            // buffer holding the iterate (enqueue time)
+  double emin = 0.0, emax = 0.0;
+  // coarsest level only
+  T *S[3] = {nullptr, nullptr, nullptr};
+  T *ilam = nullptr, *work = nullptr;
+  int n[3] = {1, 1, 1};
+};
+
+template <typename T>
+struct Hier {
+  int nlev = 0;
+  Level<T> lev[MAX_LEVELS];
+  T *zbuf = nullptr;  // z for the Jacobi / none preconditioners
+  T *z = nullptr;     // where the preconditioner leaves z (fixed per option set)
+};
+
+static Geom padded(Geom g) {
+  g.pitch = (g.mx + 3) / 4 * 4;
+  g.plane = (long long)g.pitch * g.my;
+  return g;
+}
+
+// Exact spectrum ends of D^{-1}A for the constant-diagonal stencil:
+// 1 -+ sum_d (2 sc_d / scdiag) cos(pi/(m_d-1)); boundary rows give 1.
+static void spectrum(const Geom &g, double *lmin, double *lmax) {
+  const int m[3] = {g.mx, g.my, g.mz};
+  bool interior = true;
+  for (int d = 0; d < g.dim; d++)
+    if (m[d] < 3) interior = false;
+  double s = 0.0;
+  if (interior)
+    for (int d = 0; d < g.dim; d++) s += 2.0 * g.sc[d] / g.scdiag * cos(M_PI / (m[d] - 1));
+  *lmax = fmax(1.0, 1.0 + s);
+  *lmin = fmin(1.0, 1.0 - s);
+}
+
+static Geom coarsen(const Geom &f, const fishgpu_ctx &c) {
+  return padded(make_geom(f.dim, (f.mx - 1) / 2 + 1, f.dim >= 2 ? (f.my - 1) / 2 + 1 : 1,
+                          f.dim >= 3 ? (f.mz - 1) / 2 + 1 : 1, c.Lx, c.Ly, c.Lz, c.cx, c.cy, c.cz));
+}
+
+static size_t nelem(const Geom &g) { return (size_t)g.plane * g.mz; }
+
+static unsigned flat_grid(long long tot4) {
+  long long b = (tot4 + 255) / 256;
+  if (b > FLAT_BLOCKS) b = FLAT_BLOCKS;
+  return (unsigned)(b < 1 ? 1 : b);
+}
+
+}  // namespace fg
+
+using namespace fg;
+
+struct fishgpu_solver_s {
+  fishgpu_opts o;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  Geom fine;       // padded
+  Geom dense;      // the caller's layout (pitch = mx)
+  Slots sf;        // slots of the fine level
+  Launch Lf;       // scalar launch over the fine grid
+  unsigned gfl = 1;  // grid of the pointwise kernels on the fine level
+  Prob prob;
+  KspState *st = nullptr;    // device
+  KspState *st_h = nullptr;  // pinned host mirror
+  Reducer red;
+  double *dval = nullptr;    // device scalars for FIN_STORE results
+  double *hval = nullptr;    // pinned host copy
+  Hier<double> h64;
+  Hier<float> h32;
+  // FP64 vectors (padded): u, KSP vectors (FP64 form) / outer vectors (mixed)
+  double *u64 = nullptr, *r64 = nullptr, *p64 = nullptr, *w64 = nullptr, *y64 = nullptr, *b64 = nullptr;
+  // FP32 inner KSP vectors (mixed form)
+  float *r32 = nullptr, *p32 = nullptr, *w32 = nullptr, *y32 = nullptr;
+  cudaGraphExec_t gexec = nullptr;       // giters CG iterations
+  cudaGraphExec_t gexec_init = nullptr;  // the KSP set-up sequence
+  long long n_init = 0, n_iter = 0;      // kernel nodes of the two graphs
+  long long launches = 0;                // kernels launched by the current solve
+  int giters = 1;
+  double *f_own = nullptr, *g_own = nullptr, *u_own = nullptr;  // FISHGPU_USER, host-array form
+  std::vector<void *> allocs;
+  long long bytes = 0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+namespace fg {
+
+template <typename T>
+static int dalloc(fishgpu_solver *S, T **p, size_t n) {
+  void *q = nullptr;
+  const size_t bytes = (sizeof(T) * (n ? n : 1) + 255) / 256 * 256;
+  if (cudaMalloc(&q, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return FISHGPU_ERR_NOMEM;
+  }
+  S->allocs.push_back(q);
+  S->bytes += (long long)bytes;
+  if (cudaMemsetAsync(q, 0, bytes, S->stream) != cudaSuccess) return FISHGPU_ERR_CUDA;
+  *p = (T *)q;
+  return FISHGPU_OK;
+}
+
+template <typename T>
+static int build_hier(fishgpu_solver *S, Hier<T> &H) {
+  const fishgpu_opts &o = S->o;
+  int rc;
+  if (o.pc_type != FISHGPU_PC_MG) {  // Jacobi / none: z has its own buffer
+    H.nlev = 1;
+    H.lev[0].g = S->fine;
+    H.lev[0].sl = S->sf;
+    return dalloc(S, &H.zbuf, nelem(S->fine));
+  }
+  const int L = o.mg_levels;
+  if (L < 1 || L > MAX_LEVELS) return FISHGPU_ERR_ARG;
+  H.nlev = L;
+  Geom g = S->fine;
+  for (int l = L - 1; l >= 0; l--) {
+    Level<T> &lv = H.lev[l];
+    lv.g = g;
+    lv.sl = make_slots(g, ZC);
+    double lmin, lmax;
+    spectrum(g, &lmin, &lmax);
+    lv.emin = o.esteig[0] * lmin + o.esteig[1] * lmax;
+    lv.emax = o.esteig[2] * lmin + o.esteig[3] * lmax;
+    const size_t N = nelem(g);
+    if (l < L - 1 && (rc = dalloc(S, &lv.b, N))) return rc;
+    for (int q = 0; q < 3; q++)
+      if ((rc = dalloc(S, &lv.X[q], N))) return rc;
+    if (l > 0 && (rc = dalloc(S, &lv.r, N))) return rc;
+    if (l > 0) {
+      const int m[3] = {g.mx, g.my, g.mz};
+      for (int d = 0; d < g.dim; d++)
+        if (m[d] < 3 || (m[d] - 1) % 2 != 0) return FISHGPU_ERR_ARG;  // cannot coarsen
+      g = coarsen(g, o.ctx);
+    }
+  }
+  // coarsest level: sine-transform data for the exact solve
+  Level<T> &c = H.lev[0];
+  const int m[3] = {c.g.mx, c.g.my, c.g.mz};
+  long long ni = 1;
+  for (int d = 0; d < 3; d++) {
+    c.n[d] = d < c.g.dim ? m[d] - 2 : 1;
+    ni *= c.n[d] > 0 ? c.n[d] : 0;
+  }
+  if (ni > 300000) return FISHGPU_ERR_UNSUPPORTED;  // single-block exact solve only for small grids
+  if (ni > 0) {
+    std::vector<T> hS, hl((size_t)ni);
+    for (int d = 0; d < c.g.dim; d++) {
+      const int n = c.n[d];
+      hS.assign((size_t)n * n, T(0));
+      const double a = sqrt(2.0 / (n + 1));
+      for (int i = 1; i <= n; i++)
+        for (int k = 1; k <= n; k++) hS[(size_t)(i - 1) * n + (k - 1)] = (T)(a * sin(M_PI * (double)i * k / (n + 1)));
+      if ((rc = dalloc(S, &c.S[d], (size_t)n * n))) return rc;
+      if (cudaMemcpy(c.S[d], hS.data(), sizeof(T) * n * n, cudaMemcpyHostToDevice) != cudaSuccess)
+        return FISHGPU_ERR_CUDA;
+    }
+    for (int k = 0; k < c.n[2]; k++)
+      for (int j = 0; j < c.n[1]; j++)
+        for (int i = 0; i < c.n[0]; i++) {
+          const int q[3] = {i, j, k};
+          double lam = 0.0;
+          for (int d = 0; d < c.g.dim; d++) lam += c.g.sc[d] * (2.0 - 2.0 * cos(M_PI * (q[d] + 1) / (c.n[d] + 1)));
+          hl[((size_t)k * c.n[1] + j) * c.n[0] + i] = (T)(1.0 / lam);
+        }
+    if ((rc = dalloc(S, &c.ilam, (size_t)ni)) || (rc = dalloc(S, &c.work, 2 * (size_t)ni))) return rc;
+    if (cudaMemcpy(c.ilam, hl.data(), sizeof(T) * ni, cudaMemcpyHostToDevice) != cudaSuccess)
+      return FISHGPU_ERR_CUDA;
+    for (int d = c.g.dim; d < 3; d++) c.S[d] = c.S[0];  // unused
+  }
+  return FISHGPU_OK;
+}
+
+// ------------------------------------------------------------------ enqueue
+static inline int third(int a, int b) { return 3 - a - b; }
+
+// Level smoother, PETSc KSPCHEBYSHEV / KSPRICHARDSON with PCJACOBI, `its`
+// iterations, nonzero initial guess; from_zero: the iterate is known to be 0
+// (the arithmetic is identical).  Rotates the level's three buffers.
+template <int DIM, typename T>
+static void enq_smooth(fishgpu_solver *S, Level<T> &lv, bool from_zero) {
+  const fishgpu_opts &o = S->o;
+  const double dinv = 1.0 / lv.g.scdiag;
+  cudaStream_t s = S->stream;
+  KspState *st = S->st;
+  const unsigned gb = slot_blocks(lv.sl);
+  const unsigned gf = flat_grid(lv.sl.tot4);
+  if (o.smooth_type == FISHGPU_SMOOTH_RICHARDSON) {
+    const T crd = (T)(o.richardson_scale * dinv);
+    int cur = lv.cur;
+    for (int it = 0; it < o.smooth_its; it++) {
+      const int nxt = (cur + 1) % 3;
+      if (from_zero && it == 0)
+        v_scale<T><<<gf, 256, 0, s>>>(lv.sl.tot4, st, lv.b, crd, lv.X[nxt]);
+      else
+        v_cheb<DIM, T, false><<<gb, 256, 0, s>>>(lv.g, lv.sl, st, lv.b, nullptr, lv.X[cur], lv.X[nxt], T(0), T(1), crd);
+      cur = nxt;
+    }
+    lv.cur = cur;
+    return;
+  }
+  // Chebyshev (first kind) on [emin, emax]
+  const double scale = 2.0 / (lv.emax + lv.emin);
+  const double alpha = 1.0 - scale * lv.emin;
+  const double mu = 1.0 / alpha, omegaprod = 2.0 / alpha;
+  const double c1 = scale * dinv;
+  if (from_zero && o.smooth_its == 2) {
+    // x1 = c1 b; x2 = omega x1 + omega c1 (b - A x1) = 2 omega c1 b - omega c1^2 (A b)
+    const double ckp1 = 2.0 * mu * mu - 1.0, omega = omegaprod * mu / ckp1;
+    const int nxt = (lv.cur + 1) % 3;
+    v_cheb2_zero<DIM, T><<<gb, 256, 0, s>>>(lv.g, lv.sl, st, lv.b, lv.X[nxt], (T)(2.0 * omega * c1),
+                                            (T)(omega * c1 * c1));
+    lv.cur = nxt;
+    return;
+  }
+  int km1 = -1, kk;  // -1: the zero iterate
+  if (from_zero) {
+    kk = (lv.cur + 1) % 3;
+    v_scale<T><<<gf, 256, 0, s>>>(lv.sl.tot4, st, lv.b, (T)c1, lv.X[kk]);
+  } else {
+    km1 = lv.cur;
+    kk = (lv.cur + 1) % 3;
+    v_cheb<DIM, T, false><<<gb, 256, 0, s>>>(lv.g, lv.sl, st, lv.b, nullptr, lv.X[km1], lv.X[kk], T(0), T(1), (T)c1);
+  }
+  double ckm1 = 1.0, ck = mu;
+  for (int it = 1; it < o.smooth_its; it++) {
+    const double ckp1 = 2.0 * mu * ck - ckm1;
+    const double omega = omegaprod * ck / ckp1;
+    // x_{k+1} = (1-omega) x_{k-1} + omega x_k + omega scale D^{-1}(b - A x_k)
+    const int out = km1 < 0 ? (kk + 1) % 3 : third(km1, kk);
+    if (km1 < 0)
+      v_cheb<DIM, T, false><<<gb, 256, 0, s>>>(lv.g, lv.sl, st, lv.b, nullptr, lv.X[kk], lv.X[out], T(0), (T)omega,
+                                               (T)(omega * c1));
+    else
+      v_cheb<DIM, T, true><<<gb, 256, 0, s>>>(lv.g, lv.sl, st, lv.b, lv.X[km1], lv.X[kk], lv.X[out],
+                                              (T)(1.0 - omega), (T)omega, (T)(omega * c1));
+    km1 = kk;
+    kk = out;
+    ckm1 = ck;
+    ck = ckp1;
+  }
+  lv.cur = kk;
+}
+
+template <int DIM, typename T>
+static void enq_vcycle(fishgpu_solver *S, Hier<T> &H, int l, bool from_zero) {
+  Level<T> &lv = H.lev[l];
+  cudaStream_t s = S->stream;
+  KspState *st = S->st;
+  if (l == 0) {
+    lv.cur = 0;
+    k_coarse<DIM, T><<<1, 1024, 0, s>>>(lv.g, st, lv.b, lv.X[0], lv.S[0], lv.S[1], lv.S[2], lv.ilam, lv.work,
+                                        lv.n[0], lv.n[1], lv.n[2]);
+    return;
+  }
+  Level<T> &lc = H.lev[l - 1];
+  enq_smooth<DIM, T>(S, lv, from_zero);
+  v_resid<DIM, T><<<slot_blocks(lv.sl), 256, 0, s>>>(lv.g, lv.sl, st, lv.b, lv.X[lv.cur], lv.r);
+  v_restrict<DIM, T><<<slot_blocks(lc.sl), 256, 0, s>>>(lv.g, lc.g, lc.sl, st, lv.r, lc.b);
+  for (int c = 0; c < S->o.mg_cycles; c++) enq_vcycle<DIM, T>(S, H, l - 1, c == 0);
+  v_prolong<DIM, T><<<slot_blocks(lc.sl), 256, 0, s>>>(lv.g, lc.g, lc.sl, st, lc.X[lc.cur], lv.X[lv.cur]);
+  enq_smooth<DIM, T>(S, lv, false);
+}
+
+// z = B r; H.z is where z lands (the same buffer at every application).
+template <int DIM, typename T>
+static void enq_pc(fishgpu_solver *S, Hier<T> &H, const T *r) {
+  const fishgpu_opts &o = S->o;
+  const long long tot4 = S->sf.tot4;
+  if (o.pc_type == FISHGPU_PC_NONE) {
+    v_scale<T><<<S->gfl, 256, 0, S->stream>>>(tot4, S->st, r, T(1), H.zbuf);
+    H.z = H.zbuf;
+    return;
+  }
+  if (o.pc_type == FISHGPU_PC_JACOBI) {  // z = D^{-1} r
+    v_scale<T><<<S->gfl, 256, 0, S->stream>>>(tot4, S->st, r, (T)(1.0 / S->fine.scdiag), H.zbuf);
+    H.z = H.zbuf;
+    return;
+  }
+  for (int l = 0; l < H.nlev; l++) H.lev[l].cur = 0;
+  Level<T> &top = H.lev[H.nlev - 1];
+  top.b = const_cast<T *>(r);
+  enq_vcycle<DIM, T>(S, H, H.nlev - 1, true);
+  H.z = top.X[top.cur];
+}
+
+template <typename T>
+struct KspVecs {
+  T *r, *p, *w, *y;
+};
+
+template <int DIM, typename T>
+static void enq_cg_init(fishgpu_solver *S, Hier<T> &H, KspVecs<T> v) {
+  cudaStream_t s = S->stream;
+  const long long tot4 = S->sf.tot4;
+  v_zero<T><<<S->gfl, 256, 0, s>>>(tot4, v.y);
+  if (S->o.norm_type == FISHGPU_NORM_UNPRECONDITIONED)
+    v_dots<T><<<S->gfl, 256, 0, s>>>(tot4, S->st, v.r, v.r, S->red, 0, FIN_INIT_RR, nullptr);
+  enq_pc<DIM, T>(S, H, v.r);
+  v_dots<T><<<S->gfl, 256, 0, s>>>(tot4, S->st, H.z, v.r, S->red, 0, FIN_INIT_ZZZR, nullptr);
+}
+
+template <int DIM, typename T>
+static void enq_cg_iter(fishgpu_solver *S, Hier<T> &H, KspVecs<T> v) {
+  cudaStream_t s = S->stream;
+  KspState *st = S->st;
+  const long long tot4 = S->sf.tot4;
+  const unsigned gf = S->gfl;
+  v_cg_p<T><<<gf, 256, 0, s>>>(tot4, st, H.z, v.p);  // z of the previous application
+  v_apply_dot<DIM, T><<<slot_blocks(S->sf), 256, 0, s>>>(S->fine, S->sf, st, v.p, v.w, S->red, 0, FIN_PW, nullptr);
+  if (S->o.norm_type == FISHGPU_NORM_UNPRECONDITIONED)
+    v_cg_xr<T, true><<<gf, 256, 0, s>>>(tot4, st, v.p, v.w, v.y, v.r, S->red, 0);
+  else
+    v_cg_xr<T, false><<<gf, 256, 0, s>>>(tot4, st, v.p, v.w, v.y, v.r, S->red, 0);
+  enq_pc<DIM, T>(S, H, v.r);
+  v_dots<T><<<gf, 256, 0, s>>>(tot4, st, H.z, v.r, S->red, 0, FIN_ZZZR, nullptr);
+}
+
+static long long kernel_nodes(cudaGraph_t g) {
+  size_t n = 0;
+  if (cudaGraphGetNodes(g, nullptr, &n) != cudaSuccess || n == 0) return 0;
+  std::vector<cudaGraphNode_t> nodes(n);
+  if (cudaGraphGetNodes(g, nodes.data(), &n) != cudaSuccess) return 0;
+  long long k = 0;
+  for (size_t q = 0; q < n; q++) {
+    cudaGraphNodeType t;
+    if (cudaGraphNodeGetType(nodes[q], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) k++;
+  }
+  return k;
+}
+
+// Capture what `enq` enqueues on the solver's stream into an executable graph.
+template <typename F>
+static int capture(fishgpu_solver *S, F enq, cudaGraphExec_t *exec, long long *nkern) {
+  cudaGraph_t graph;
+  FG_CUDA(cudaStreamBeginCapture(S->stream, cudaStreamCaptureModeThreadLocal));
+  enq();
+  cudaError_t e = cudaStreamEndCapture(S->stream, &graph);
+  if (e != cudaSuccess) return FISHGPU_ERR_CUDA;
+  *nkern = kernel_nodes(graph);
+  e = cudaGraphInstantiate(exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) {
+    *exec = nullptr;
+    return FISHGPU_ERR_CUDA;
+  }
+  return FISHGPU_OK;
+}
+
+static void reset_state(fishgpu_solver *S, double rtol, double atol, double dtol, int max_it, int norm) {
+  KspState *h = S->st_h;
+  memset(h, 0, sizeof(*h));
+  h->rtol = rtol;
+  h->atol = atol;
+  h->dtol = dtol;
+  h->max_it = max_it;
+  h->norm_type = norm;
+  h->betaold = 1.0;
+}
+
+// CG solve of J y = r from y = 0 (r is overwritten), on the solver's stream.
+// The caller reads S->st_h for its, reason and the history.
+template <int DIM, typename T>
+static int run_ksp(fishgpu_solver *S, Hier<T> &H, KspVecs<T> v, double rtol, int max_it, int norm) {
+  cudaStream_t s = S->stream;
+  int rc;
+  if (!S->gexec_init &&
+      (rc = capture(S, [&] { enq_cg_init<DIM, T>(S, H, v); }, &S->gexec_init, &S->n_init)))
+    return rc;
+  if (!S->gexec &&
+      (rc = capture(S, [&] { for (int g = 0; g < S->giters; g++) enq_cg_iter<DIM, T>(S, H, v); }, &S->gexec,
+                    &S->n_iter)))
+    return rc;
+  reset_state(S, rtol, S->o.atol, S->o.dtol, max_it, norm);
+  FG_CUDA(cudaMemcpyAsync(S->st, S->st_h, sizeof(KspState), cudaMemcpyHostToDevice, s));
+  FG_CUDA(cudaGraphLaunch(S->gexec_init, s));
+  S->launches += S->n_init;
+  const long long guard = (long long)max_it / S->giters + 4;
+  for (long long launch = 0;; launch++) {
+    FG_CUDA(cudaMemcpyAsync(&S->st_h->done, &S->st->done, sizeof(int), cudaMemcpyDeviceToHost, s));
+    FG_CUDA(cudaStreamSynchronize(s));
+    if (S->st_h->done) break;
+    if (launch > guard) return FISHGPU_ERR_TIMEOUT;
+    FG_CUDA(cudaGraphLaunch(S->gexec, s));
+    S->launches += S->n_iter;
+  }
+  FG_CUDA(cudaMemcpyAsync(S->st_h, S->st, sizeof(KspState), cudaMemcpyDeviceToHost, s));
+  FG_CUDA(cudaStreamSynchronize(s));
+  return FISHGPU_OK;
+}
+
+// ------------------------------------------------------------------ FP64 helpers
+// F(u) of c/ch6/poissonfunctions.c:29-115 on the whole (padded) grid
+template <int DIM>
+__global__ void __launch_bounds__(256) k_residual64(Geom g, Tiles tm, Prob pb, const double *__restrict__ u,
+                                                    double *__restrict__ F) {
+  const Range R = full_range(g);
+  FG_POINT_LOOP_BEGIN(R)
+  const double uc = u[n];
+  if (on_bdry<DIM>(g, i, j, k)) {
+    F[n] = (uc - g_at(pb, g, i, j, k)) * g.scdiag;
+  } else {
+    const double ue = (i + 1 == g.mx - 1) ? g_at(pb, g, i + 1, j, k) : u[n + 1];
+    const double uw = (i - 1 == 0) ? g_at(pb, g, i - 1, j, k) : u[n - 1];
+    if (DIM == 1) {
+      F[n] = pb.cx * (2.0 * uc - uw - ue) / g.h[0] - g.h[0] * f_at(pb, g, i, j, k);
+    } else {
+      const double un = (j + 1 == g.my - 1) ? g_at(pb, g, i, j + 1, k) : u[n + g.pitch];
+      const double us = (j - 1 == 0) ? g_at(pb, g, i, j - 1, k) : u[n - g.pitch];
+      if (DIM == 2) {
+        F[n] = g.scdiag * uc - g.sc[0] * (uw + ue) - g.sc[1] * (us + un) - g.vol * f_at(pb, g, i, j, k);
+      } else {
+        const double uu = (k + 1 == g.mz - 1) ? g_at(pb, g, i, j, k + 1) : u[n + g.plane];
+        const double ud = (k - 1 == 0) ? g_at(pb, g, i, j, k - 1) : u[n - g.plane];
+        F[n] = g.scdiag * uc - g.sc[0] * (uw + ue) - g.sc[1] * (us + un) - g.sc[2] * (uu + ud) -
+               g.vol * f_at(pb, g, i, j, k);
+      }
+    }
+  }
+  FG_POINT_LOOP_END
+}
+
+// u0 into the padded u (InitialState, poissonfunctions.c:260-346); GIVEN packs
+// the caller's dense array
+template <int DIM>
+__global__ void __launch_bounds__(256) k_initial64(Geom g, Geom gd, Tiles tm, Prob pb, int type, int gbdry,
+                                                   unsigned long long seed, const double *__restrict__ given,
+                                                   double *__restrict__ u) {
+  const Range R = full_range(g);
+  FG_POINT_LOOP_BEGIN(R)
+  double v;
+  if (type == FISHGPU_INITIAL_GIVEN) {
+    v = given[gidx(gd, i, j, k)];
+  } else if (type == FISHGPU_INITIAL_RANDOM) {
+    unsigned long long x = (seed ^ (((unsigned long long)k * g.my + j) * g.mx + i)) + 0x9E3779B97F4A7C15ULL;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBULL;
+    x ^= x >> 31;
+    v = (double)(x >> 11) * 0x1.0p-53;
+  } else {
+    v = 0.0;
+  }
+  if (gbdry && on_bdry<DIM>(g, i, j, k)) v = g_at(pb, g, i, j, k);
+  u[n] = v;
+  FG_POINT_LOOP_END
+}
+
+// the caller's dense u from the padded one
+template <int DIM>
+__global__ void __launch_bounds__(256) k_unpack64(Geom g, Geom gd, Tiles tm, const double *__restrict__ up,
+                                                  double *__restrict__ ud) {
+  const Range R = full_range(g);
+  FG_POINT_LOOP_BEGIN(R)
+  ud[gidx(gd, i, j, k)] = up[n];
+  FG_POINT_LOOP_END
+}
+
+static int read_vals(fishgpu_solver *S, int n) {
+  FG_CUDA(cudaMemcpyAsync(S->hval, S->dval, sizeof(double) * n, cudaMemcpyDeviceToHost, S->stream));
+  FG_CUDA(cudaStreamSynchronize(S->stream));
+  return FISHGPU_OK;
+}
+
+static void fill_from_state(const KspState *h, fishgpu_report *rep) {
+  rep->its = h->its;
+  rep->reason = h->reason;
+  rep->nhist = h->nhist;
+  const int n = h->nhist < FISHGPU_MAX_HIST ? h->nhist : FISHGPU_MAX_HIST;
+  for (int q = 0; q < n; q++) rep->hist[q] = h->hist[q];
+}
+
+// sum of squares of the padded FP64 vector a into dval[slot]
+static void enq_norm2(fishgpu_solver *S, const double *a, int slot) {
+  v_dots<double><<<S->gfl, 256, 0, S->stream>>>(S->sf.tot4, nullptr, a, a, S->red, 1, FIN_STORE, S->dval + slot);
+}
+
+template <int DIM>
+static int solve_dim(fishgpu_solver *S, double *u, fishgpu_report *rep) {
+  const fishgpu_opts &o = S->o;
+  cudaStream_t s = S->stream;
+  const Launch &L = S->Lf;
+  const Geom &g = S->fine;
+  const long long tot4 = S->sf.tot4;
+  const unsigned gfl = S->gfl;
+  FG_CUDA(cudaEventRecord(S->ev0, s));
+  S->launches = 3;  // initial state, F(u0), ||F(u0)||
+  k_initial64<DIM><<<L.grid, L.block, 0, s>>>(g, S->dense, L.tm, S->prob, o.initial_type, o.initial_gonboundary,
+                                               o.seed, u, S->u64);
+  double *F = o.precision == FISHGPU_MIXED ? S->b64 : S->r64;
+  k_residual64<DIM><<<L.grid, L.block, 0, s>>>(g, L.tm, S->prob, S->u64, F);
+  enq_norm2(S, F, 0);
+  FG_CUDA(cudaGetLastError());
+  int rc = read_vals(S, 1);
+  if (rc) return rc;
+  const double bn = sqrt(S->hval[0]);
+  rep->fnorm0 = bn;
+  if (o.precision == FISHGPU_FP64) {
+    KspVecs<double> v{S->r64, S->p64, S->w64, S->y64};
+    if ((rc = run_ksp<DIM, double>(S, S->h64, v, o.rtol, o.max_it, o.norm_type))) return rc;
+    fill_from_state(S->st_h, rep);
+    rep->outer_its = 0;
+  } else {
+    // FP64 iterative refinement around an FP32 CG + FP32 V-cycle
+    const double ttol = fmax(o.rtol * bn, o.atol);
+    double rn = bn;
+    int reason = 0, its = 0, outer = 0, nh = 0;
+    v_zero<double><<<gfl, 256, 0, s>>>(tot4, S->y64);
+    S->launches += 1;
+    rep->hist[nh++] = rn;
+    KspVecs<float> v{S->r32, S->p32, S->w32, S->y32};
+    while (true) {
+      if (isnan(rn) || isinf(rn)) { reason = R_DIVERGED_NANORINF; break; }
+      if (rn <= ttol) { reason = rn < o.atol ? R_CONVERGED_ATOL : R_CONVERGED_RTOL; break; }
+      if (outer >= o.outer_max_it || its >= o.max_it) { reason = R_DIVERGED_ITS; break; }
+      const double *rsrc = outer == 0 ? S->b64 : S->r64;
+      v_demote<<<gfl, 256, 0, s>>>(tot4, rsrc, 1.0 / rn, S->r32);
+      S->launches += 4;  // demote, promote-add, FP64 residual, its norm
+      // inner tolerance: what is still needed, never below the FP32 floor
+      double irtol = fmax(o.inner_rtol, 0.5 * ttol / rn);
+      if (irtol > 0.5) irtol = 0.5;
+      if ((rc = run_ksp<DIM, float>(S, S->h32, v, irtol, o.inner_max_it, FISHGPU_NORM_UNPRECONDITIONED))) return rc;
+      const KspState *h = S->st_h;
+      its += h->its;
+      if (h->reason == R_DIVERGED_NANORINF || h->reason == R_DIVERGED_INDEFINITE_MAT ||
+          h->reason == R_DIVERGED_INDEFINITE_PC) {
+        reason = h->reason;
+        break;
+      }
+      v_promote_add<<<gfl, 256, 0, s>>>(tot4, S->y32, rn, S->y64);
+      // FP64 true residual r = b - J y and its norm
+      v_resid<DIM, double><<<slot_blocks(S->sf), 256, 0, s>>>(g, S->sf, nullptr, S->b64, S->y64, S->r64);
+      enq_norm2(S, S->r64, 0);
+      FG_CUDA(cudaGetLastError());
+      if ((rc = read_vals(S, 1))) return rc;
+      rn = sqrt(S->hval[0]);
+      outer++;
+      if (nh < FISHGPU_MAX_HIST) rep->hist[nh] = rn;
+      nh++;
+    }
+    rep->its = its;
+    rep->reason = reason;
+    rep->outer_its = outer;
+    rep->nhist = nh;
+  }
+  // u = u0 - y, then the caller's dense copy
+  v_sub<<<gfl, 256, 0, s>>>(tot4, S->y64, S->u64);
+  k_unpack64<DIM><<<L.grid, L.block, 0, s>>>(g, S->dense, L.tm, S->u64, u);
+  S->launches += 4;  // update, unpack, F(u), ||F(u)||
+  FG_CUDA(cudaEventRecord(S->ev1, s));
+  // F(u) for the final SNES norm (r64 is free now)
+  k_residual64<DIM><<<L.grid, L.block, 0, s>>>(g, L.tm, S->prob, S->u64, S->r64);
+  enq_norm2(S, S->r64, 1);
+  FG_CUDA(cudaGetLastError());
+  if ((rc = read_vals(S, 2))) return rc;
+  rep->fnorm1 = sqrt(S->hval[1]);
+  rep->true_rel_resid = bn > 0.0 ? rep->fnorm1 / bn : 0.0;
+  float ms = 0.f;
+  FG_CUDA(cudaEventElapsedTime(&ms, S->ev0, S->ev1));
+  rep->solve_ms = ms;
+  return FISHGPU_OK;
+}
+
+// Largest grid of a reduction kernel on the fine level.
+static int reduction_blocks(const fishgpu_solver *S) {
+  int a = (int)slot_blocks(S->sf), b = (int)S->gfl;
+  return a > b ? a : b;
+}
+
+template <int DIM>
+static int time_kernel_dim(fishgpu_solver *S, const char *name, int reps, double *ms, double *bytes) {
+  const bool mixed = S->o.precision == FISHGPU_MIXED;
+  const double N = (double)S->fine.mx * S->fine.my * S->fine.mz;
+  cudaStream_t s = S->stream;
+  const Geom &g = S->fine;
+  const Slots &sl = S->sf;
+  const unsigned gb = slot_blocks(sl);
+  if (S->o.pc_type != FISHGPU_PC_MG) return FISHGPU_ERR_UNSUPPORTED;
+  Level<float> &lf = S->h32.lev[S->h32.nlev > 0 ? S->h32.nlev - 1 : 0];
+  Level<double> &ld = S->h64.lev[S->h64.nlev > 0 ? S->h64.nlev - 1 : 0];
+  Level<float> &cf = S->h32.lev[S->h32.nlev > 1 ? S->h32.nlev - 2 : 0];
+  Level<double> &cd = S->h64.lev[S->h64.nlev > 1 ? S->h64.nlev - 2 : 0];
+  const double sz = mixed ? 4.0 : 8.0;
+  float t = 0.f;
+  FG_CUDA(cudaEventRecord(S->ev0, s));
+  for (int q = 0; q < reps; q++) {
+    if (!strcmp(name, "smooth")) {  // one Chebyshev step with x_{k-1}: reads b, x_{k-1}, x_k, writes x_{k+1}
+      if (mixed)
+        v_cheb<DIM, float, true><<<gb, 256, 0, s>>>(g, sl, nullptr, S->r32, lf.X[0], lf.X[1], lf.X[2], 0.5f, 0.5f, 0.1f);
+      else
+        v_cheb<DIM, double, true><<<gb, 256, 0, s>>>(g, sl, nullptr, S->r64, ld.X[0], ld.X[1], ld.X[2], 0.5, 0.5, 0.1);
+      *bytes = 4.0 * sz * N;
+    } else if (!strcmp(name, "smooth_zero")) {  // two steps from zero: reads b, writes x
+      if (mixed)
+        v_cheb2_zero<DIM, float><<<gb, 256, 0, s>>>(g, sl, nullptr, S->r32, lf.X[0], 0.5f, 0.1f);
+      else
+        v_cheb2_zero<DIM, double><<<gb, 256, 0, s>>>(g, sl, nullptr, S->r64, ld.X[0], 0.5, 0.1);
+      *bytes = 2.0 * sz * N;
+    } else if (!strcmp(name, "resid")) {
+      if (mixed)
+        v_resid<DIM, float><<<gb, 256, 0, s>>>(g, sl, nullptr, S->r32, lf.X[0], lf.X[1]);
+      else
+        v_resid<DIM, double><<<gb, 256, 0, s>>>(g, sl, nullptr, S->r64, ld.X[0], ld.X[1]);
+      *bytes = 3.0 * sz * N;
+    } else if (!strcmp(name, "apply")) {
+      if (mixed)
+        v_apply_dot<DIM, float><<<gb, 256, 0, s>>>(g, sl, nullptr, S->p32, S->w32, S->red, 1, FIN_STORE, S->dval + 2);
+      else
+        v_apply_dot<DIM, double><<<gb, 256, 0, s>>>(g, sl, nullptr, S->p64, S->w64, S->red, 1, FIN_STORE, S->dval + 2);
+      *bytes = 2.0 * sz * N;
+    } else if (!strcmp(name, "cg_update")) {
+      if (mixed)
+        v_cg_xr<float, false><<<S->gfl, 256, 0, s>>>(sl.tot4, nullptr, S->p32, S->w32, S->y32, S->r32, S->red, 1);
+      else
+        v_cg_xr<double, false><<<S->gfl, 256, 0, s>>>(sl.tot4, nullptr, S->p64, S->w64, S->y64, S->r64, S->red, 1);
+      *bytes = 6.0 * sz * N;
+    } else if (!strcmp(name, "restrict")) {
+      if (mixed)
+        v_restrict<DIM, float><<<slot_blocks(cf.sl), 256, 0, s>>>(g, cf.g, cf.sl, nullptr, lf.X[0], cf.b);
+      else
+        v_restrict<DIM, double><<<slot_blocks(cd.sl), 256, 0, s>>>(g, cd.g, cd.sl, nullptr, ld.X[0], cd.b);
+      *bytes = sz * N * (1.0 + 1.0 / (1 << DIM));
+    } else if (!strcmp(name, "prolong")) {
+      if (mixed)
+        v_prolong<DIM, float><<<slot_blocks(cf.sl), 256, 0, s>>>(g, cf.g, cf.sl, nullptr, cf.X[0], lf.X[0]);
+      else
+        v_prolong<DIM, double><<<slot_blocks(cd.sl), 256, 0, s>>>(g, cd.g, cd.sl, nullptr, cd.X[0], ld.X[0]);
+      *bytes = sz * N * (2.0 + 1.0 / (1 << DIM));
+    } else if (!strcmp(name, "residual64")) {
+      v_resid<DIM, double><<<gb, 256, 0, s>>>(g, sl, nullptr, S->r64, S->y64, S->u64);
+      *bytes = 3.0 * 8.0 * N;
+    } else {
+      return FISHGPU_ERR_ARG;
+    }
+  }
+  FG_CUDA(cudaEventRecord(S->ev1, s));
+  FG_CUDA(cudaEventSynchronize(S->ev1));
+  FG_CUDA(cudaGetLastError());
+  FG_CUDA(cudaEventElapsedTime(&t, S->ev0, S->ev1));
+  *ms = (double)t / reps;
+  return FISHGPU_OK;
+}
+
+}  // namespace fg
+
+// ------------------------------------------------------------------ C ABI
+extern "C" int fishgpu_solver_destroy(fishgpu_solver *S) {
+  if (!S) return FISHGPU_OK;
+  if (S->stream) cudaStreamSynchronize(S->stream);
+  if (S->gexec) cudaGraphExecDestroy(S->gexec);
+  if (S->gexec_init) cudaGraphExecDestroy(S->gexec_init);
+  for (void *p : S->allocs) cudaFree(p);
+  if (S->st_h) cudaFreeHost(S->st_h);
+  if (S->hval) cudaFreeHost(S->hval);
+  if (S->ev0) cudaEventDestroy(S->ev0);
+  if (S->ev1) cudaEventDestroy(S->ev1);
+  if (S->own_stream && S->stream) cudaStreamDestroy(S->stream);
+  delete S;
+  return FISHGPU_OK;
+}
+
+static int validate_opts(const fishgpu_opts *o) {
+  if (!o) return FISHGPU_ERR_ARG;
+  const int dim = o->ctx.dim;
+  if (dim < 1 || dim > 3) return FISHGPU_ERR_ARG;
+  if (o->mx < 3 || (dim >= 2 && o->my < 3) || (dim >= 3 && o->mz < 3)) return FISHGPU_ERR_ARG;
+  if (!(o->ctx.cx > 0) || !(o->ctx.cy > 0) || !(o->ctx.cz > 0)) return FISHGPU_ERR_ARG;
+  if (!(o->ctx.Lx > 0) || !(o->ctx.Ly > 0) || !(o->ctx.Lz > 0)) return FISHGPU_ERR_ARG;
+  if (o->ctx.problem < 0 || o->ctx.problem > FISHGPU_USER) return FISHGPU_ERR_ARG;
+  if (o->ctx.problem == FISHGPU_USER && (!o->ctx.f) != (!o->ctx.g)) return FISHGPU_ERR_ARG;
+  if (o->pc_type < 0 || o->pc_type > FISHGPU_PC_MG) return FISHGPU_ERR_UNSUPPORTED;
+  if (o->smooth_its < 1 || o->max_it < 0 || o->mg_cycles < 1 || o->mg_cycles > 2) return FISHGPU_ERR_ARG;
+  if (o->precision != FISHGPU_FP64 && o->precision != FISHGPU_MIXED) return FISHGPU_ERR_ARG;
+  if (o->precision == FISHGPU_MIXED && o->pc_type != FISHGPU_PC_MG) return FISHGPU_ERR_UNSUPPORTED;
+  if (o->initial_type < 0 || o->initial_type > FISHGPU_INITIAL_GIVEN) return FISHGPU_ERR_ARG;
+  if (!(o->rtol >= 0) || !(o->atol >= 0) || !(o->dtol > 0)) return FISHGPU_ERR_ARG;
+  const long long N = (long long)o->mx * (dim >= 2 ? o->my : 1) * (dim >= 3 ? o->mz : 1);
+  if (N > (1LL << 40)) return FISHGPU_ERR_ARG;
+  return FISHGPU_OK;
+}
+
+extern "C" int fishgpu_solver_create(const fishgpu_opts *o, void *stream, fishgpu_solver **out) {
+  if (!out) return FISHGPU_ERR_ARG;
+  *out = nullptr;
+  int rc = validate_opts(o);
+  if (rc) return rc;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return FISHGPU_ERR_NODEVICE;
+  }
+  fishgpu_solver *S = new fishgpu_solver();
+  S->o = *o;
+  const int dim = o->ctx.dim;
+  if (stream) {
+    S->stream = (cudaStream_t)stream;
+  } else {
+    if (cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking) != cudaSuccess) {
+      delete S;
+      return FISHGPU_ERR_CUDA;
+    }
+    S->own_stream = true;
+  }
+  S->dense = make_geom(dim, o->mx, dim >= 2 ? o->my : 1, dim >= 3 ? o->mz : 1, o->ctx.Lx, o->ctx.Ly, o->ctx.Lz,
+                       o->ctx.cx, o->ctx.cy, o->ctx.cz);
+  S->fine = padded(S->dense);
+  S->sf = make_slots(S->fine, ZC);
+  S->Lf = launch_for(S->fine);
+  S->gfl = flat_grid(S->sf.tot4);
+  S->prob = Prob{o->ctx.problem, dim, o->ctx.cx, o->ctx.cy, o->ctx.cz, o->ctx.f, o->ctx.g, S->dense.pitch,
+                 S->dense.plane};
+  const size_t N = nelem(S->fine);
+  const long long dofs = (long long)S->dense.plane * S->dense.mz;
+  S->giters = o->graph_iters > 0 ? o->graph_iters : (dofs >= (1LL << 20) ? 1 : 4);
+#define CK(x)                            \
+  do {                                   \
+    if ((rc = (x)) != FISHGPU_OK) {      \
+      fishgpu_solver_destroy(S);         \
+      return rc;                         \
+    }                                    \
+  } while (0)
+  if (cudaMallocHost((void **)&S->st_h, sizeof(KspState)) != cudaSuccess ||
+      cudaMallocHost((void **)&S->hval, sizeof(double) * 8) != cudaSuccess ||
+      cudaEventCreate(&S->ev0) != cudaSuccess || cudaEventCreate(&S->ev1) != cudaSuccess) {
+    fishgpu_solver_destroy(S);
+    return FISHGPU_ERR_CUDA;
+  }
+  const int cap = reduction_blocks(S);
+  CK(dalloc(S, &S->st, 1));
+  CK(dalloc(S, &S->dval, 8));
+  CK(dalloc(S, &S->red.partials, (size_t)2 * 2 * cap));  // two slots of up to two values
+  CK(dalloc(S, &S->red.tickets, 4));
+  S->red.cap = cap;
+  CK(dalloc(S, &S->u64, N));
+  CK(dalloc(S, &S->y64, N));
+  CK(dalloc(S, &S->r64, N));
+  if (o->ctx.problem == FISHGPU_USER && !o->ctx.f) {  // the solver owns f and g (dense)
+    const size_t Nd = (size_t)dofs;
+    CK(dalloc(S, &S->f_own, Nd));
+    CK(dalloc(S, &S->g_own, Nd));
+    S->prob.f = S->f_own;
+    S->prob.g = S->g_own;
+    S->o.ctx.f = S->f_own;
+    S->o.ctx.g = S->g_own;
+  }
+  if (o->precision == FISHGPU_FP64) {
+    CK(dalloc(S, &S->p64, N));
+    CK(dalloc(S, &S->w64, N));
+    CK(build_hier<double>(S, S->h64));
+  } else {
+    CK(dalloc(S, &S->b64, N));
+    CK(dalloc(S, &S->r32, N));
+    CK(dalloc(S, &S->p32, N));
+    CK(dalloc(S, &S->w32, N));
+    CK(dalloc(S, &S->y32, N));
+    CK(build_hier<float>(S, S->h32));
+  }
+#undef CK
+  if (cudaStreamSynchronize(S->stream) != cudaSuccess) {
+    fishgpu_solver_destroy(S);
+    return FISHGPU_ERR_CUDA;
+  }
+  *out = S;
+  return FISHGPU_OK;
+}
+
+extern "C" long long fishgpu_solver_bytes(const fishgpu_solver *S) { return S ? S->bytes : 0; }
+
+extern "C" int fishgpu_solver_solve(fishgpu_solver *S, double *u_dev, fishgpu_report *rep) {
+  if (!S || !u_dev || !rep) return FISHGPU_ERR_ARG;
+  memset(rep, 0, sizeof(*rep));
+  rep->dofs = (long long)S->dense.plane * S->dense.mz;
+  int rc;
+  switch (S->o.ctx.dim) {
+  case 1: rc = solve_dim<1>(S, u_dev, rep); break;
+  case 2: rc = solve_dim<2>(S, u_dev, rep); break;
+  default: rc = solve_dim<3>(S, u_dev, rep); break;
+  }
+  if (rc) return rc;
+  // error report against the exact solution (fish.c:250-276)
+  if (S->o.ctx.problem != FISHGPU_USER) {
+    fishgpu_info info;
+    memset(&info, 0, sizeof(info));
+    info.dim = S->o.ctx.dim;
+    info.mx = S->dense.mx; info.my = S->dense.my; info.mz = S->dense.mz;
+    info.xm = info.mx; info.ym = info.my; info.zm = info.mz;
+    info.xmax[0] = S->o.ctx.Lx; info.xmax[1] = S->o.ctx.Ly; info.xmax[2] = S->o.ctx.Lz;
+    fishgpu_ctx c = S->o.ctx;
+    rc = ErrorNorms_gpu(&info, u_dev, &c, &rep->errinf, &rep->err2h, (void *)S->stream);
+    if (rc) return rc;
+    S->launches += 1;
+  }
+  rep->launches = S->launches;
+  if (rep->reason == R_DIVERGED_NANORINF) return FISHGPU_ERR_NONFINITE;
+  if (rep->reason < 0) return FISHGPU_ERR_NOT_CONVERGED;
+  return FISHGPU_OK;
+}
+
+extern "C" int fishgpu_solve(const fishgpu_opts *o, double *u_dev, fishgpu_report *rep) {
+  fishgpu_solver *S = nullptr;
+  int rc = fishgpu_solver_create(o, nullptr, &S);
+  if (rc) return rc;
+  rc = fishgpu_solver_solve(S, u_dev, rep);
+  fishgpu_solver_destroy(S);
+  return rc;
+}
+
+extern "C" int fishgpu_solver_solve_host(fishgpu_solver *S, const double *f_host, const double *g_host,
+                                         double *u_host, fishgpu_report *rep) {
+  if (!S || !u_host || !rep) return FISHGPU_ERR_ARG;
+  const bool user = S->o.ctx.problem == FISHGPU_USER;
+  if (user && (!S->f_own || !f_host || !g_host)) return FISHGPU_ERR_ARG;
+  const size_t N = (size_t)S->dense.plane * S->dense.mz;
+  cudaStream_t s = S->stream;
+  if (!S->u_own) {
+    int rc = dalloc(S, &S->u_own, N);
+    if (rc) return rc;
+  }
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return FISHGPU_ERR_CUDA;
+  int rc = FISHGPU_OK;
+  cudaEventRecord(e0, s);
+  if (user && (cudaMemcpyAsync(S->f_own, f_host, sizeof(double) * N, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+               cudaMemcpyAsync(S->g_own, g_host, sizeof(double) * N, cudaMemcpyHostToDevice, s) != cudaSuccess))
+    rc = FISHGPU_ERR_CUDA;
+  if (!rc && S->o.initial_type == FISHGPU_INITIAL_GIVEN &&
+      cudaMemcpyAsync(S->u_own, u_host, sizeof(double) * N, cudaMemcpyHostToDevice, s) != cudaSuccess)
+    rc = FISHGPU_ERR_CUDA;
+  const int src = rc ? rc : fishgpu_solver_solve(S, S->u_own, rep);
+  if (!rc && src != FISHGPU_OK && src != FISHGPU_ERR_NOT_CONVERGED) rc = src;
+  if (!rc && cudaMemcpyAsync(u_host, S->u_own, sizeof(double) * N, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+    rc = FISHGPU_ERR_CUDA;
+  cudaEventRecord(e1, s);
+  if (cudaStreamSynchronize(s) != cudaSuccess) rc = FISHGPU_ERR_CUDA;
+  float ms = 0.f;
+  if (!rc && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess) rep->solve_ms = ms;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return rc ? rc : src;
+}
+
+extern "C" int fishgpu_solve_host(const fishgpu_opts *o, const double *f_host, const double *g_host,
+                                  double *u_host, fishgpu_report *rep) {
+  if (!o || !u_host || !rep) return FISHGPU_ERR_ARG;
+  fishgpu_opts oo = *o;
+  oo.ctx.f = nullptr;
+  oo.ctx.g = nullptr;
+  fishgpu_solver *S = nullptr;
+  int rc = fishgpu_solver_create(&oo, nullptr, &S);
+  if (rc) return rc;
+  rc = fishgpu_solver_solve_host(S, f_host, g_host, u_host, rep);
+  fishgpu_solver_destroy(S);
+  return rc;
+}
+
+extern "C" int fishgpu_solver_time_kernel(fishgpu_solver *S, const char *name, int reps,
+                                          double *ms_per_launch, double *bytes_per_launch) {
+  if (!S || !name || reps < 1 || !ms_per_launch || !bytes_per_launch) return FISHGPU_ERR_ARG;
+  switch (S->o.ctx.dim) {
+  case 1: return time_kernel_dim<1>(S, name, reps, ms_per_launch, bytes_per_launch);
+  case 2: return time_kernel_dim<2>(S, name, reps, ms_per_launch, bytes_per_launch);
+  default: return time_kernel_dim<3>(S, name, reps, ms_per_launch, bytes_per_launch);
+  }
+}

@@ -1,0 +1,535 @@
+// vkernels.cuh -- the solver's hot kernels on the padded, vectorised layout.
+//
+// Layout of every solver vector (all levels, both precisions): row pitch a
+// multiple of 4 points, base aligned to 16 B (FP32) / 32 B (FP64); the padding
+// points i >= mx are kept at zero by every kernel that writes a vector, so
+// pointwise kernels and dot products may run over the flat padded array.
+//
+// Work decomposition: a thread owns a "slot" of 4 consecutive x-points
+// (one float4, or two double2).  The slots of one k-plane are numbered
+// row-major; a block of 256 threads takes 256 consecutive slots (crossing
+// rows, so its loads per plane are one contiguous run of 4 KB (FP32)) and
+// marches `zc` planes in k with the k-1/k/k+1 values of its slot in
+// registers.  x-neighbours across slots come from warp shuffles (the warp's
+// edge lanes load one scalar); y-neighbours are two vector loads (L1/L2
+// hits); z-neighbours are the register window.  Grid = chunks x z-chunks,
+// one block per (chunk, z-chunk): no grid-stride tail.
+#pragma once
+
+#include "fishgpu_internal.cuh"
+
+namespace fg {
+
+template <typename T>
+struct V4 {
+  T x, y, z, w;
+};
+
+__device__ __forceinline__ V4<float> ld4(const float *p) {
+  float4 v = *reinterpret_cast<const float4 *>(p);
+  return V4<float>{v.x, v.y, v.z, v.w};
+}
+__device__ __forceinline__ V4<double> ld4(const double *p) {
+  double2 a = *reinterpret_cast<const double2 *>(p);
+  double2 b = *reinterpret_cast<const double2 *>(p + 2);
+  return V4<double>{a.x, a.y, b.x, b.y};
+}
+__device__ __forceinline__ void st4(float *p, const V4<float> &v) {
+  *reinterpret_cast<float4 *>(p) = make_float4(v.x, v.y, v.z, v.w);
+}
+__device__ __forceinline__ void st4(double *p, const V4<double> &v) {
+  *reinterpret_cast<double2 *>(p) = make_double2(v.x, v.y);
+  *reinterpret_cast<double2 *>(p + 2) = make_double2(v.z, v.w);
+}
+template <typename T>
+__device__ __forceinline__ V4<T> zero4() {
+  return V4<T>{T(0), T(0), T(0), T(0)};
+}
+template <typename T>
+__device__ __forceinline__ V4<T> add4(const V4<T> &a, const V4<T> &b) {
+  return V4<T>{a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w};
+}
+template <typename T>
+__device__ __forceinline__ T el(const V4<T> &v, int e) {
+  return e == 0 ? v.x : e == 1 ? v.y : e == 2 ? v.z : v.w;
+}
+template <typename T>
+__device__ __forceinline__ void set_el(V4<T> &v, int e, T a) {
+  if (e == 0) v.x = a; else if (e == 1) v.y = a; else if (e == 2) v.z = a; else v.w = a;
+}
+
+// Launch shape of the slot decomposition of one level.
+struct Slots {
+  int P4;         // slots per row (pitch / 4)
+  int per_plane;  // slots per k-plane (P4 * my)
+  int nchunk;     // 256-slot chunks per plane
+  int zc, nz;     // planes per block, z-chunks
+  long long tot4; // slots in the whole array
+};
+
+inline Slots make_slots(const Geom &g, int zc_want) {
+  Slots s;
+  s.P4 = g.pitch / 4;
+  s.per_plane = s.P4 * g.my;
+  s.nchunk = (s.per_plane + 255) / 256;
+  s.zc = g.dim == 3 ? (zc_want < g.mz ? zc_want : g.mz) : 1;
+  s.nz = (g.mz + s.zc - 1) / s.zc;
+  s.tot4 = (long long)s.per_plane * g.mz;
+  return s;
+}
+inline unsigned slot_blocks(const Slots &s) { return (unsigned)s.nchunk * (unsigned)s.nz; }
+
+// Per-thread slot coordinates.
+struct SlotPos {
+  int i4, j, k0, k1;
+  bool in;   // slot exists (within the plane)
+  long long col;
+};
+
+__device__ __forceinline__ SlotPos slot_pos(const Geom &g, const Slots &s) {
+  SlotPos p;
+  const int c = blockIdx.x % s.nchunk, kz = blockIdx.x / s.nchunk;
+  const int f = c * 256 + threadIdx.x;
+  p.in = f < s.per_plane;
+  p.j = p.in ? f / s.P4 : 0;
+  p.i4 = p.in ? (f - p.j * s.P4) * 4 : 0;
+  p.k0 = kz * s.zc;
+  p.k1 = min(p.k0 + s.zc, g.mz);
+  p.col = (long long)p.j * g.pitch + p.i4;
+  return p;
+}
+
+template <typename T>
+struct Wv {
+  T sx, sy, sz, sd;
+  __device__ __forceinline__ explicit Wv(const Geom &g)
+      : sx((T)g.sc[0]), sy((T)g.sc[1]), sz((T)g.sc[2]), sd((T)g.scdiag) {}
+};
+
+// Neighbour data of a slot at plane k.
+template <typename T>
+struct Nb {
+  V4<T> c;   // centre values
+  T l, r;    // x-neighbours of element 0 (i4-1) and element 3 (i4+4)
+  V4<T> ys;  // sum of the y-neighbours that are interior nodes
+  V4<T> zs;  // sum of the z-neighbours that are interior nodes
+};
+
+// Loads everything but the z-window for plane k; shuffles need all lanes.
+template <int DIM, typename T>
+__device__ __forceinline__ void load_xy(const Geom &g, const SlotPos &p, const T *__restrict__ x, long long n,
+                                        const V4<T> &c, Nb<T> &nb) {
+  const int lane = threadIdx.x & 31;
+  T l = __shfl_up_sync(0xffffffffu, c.w, 1);
+  T r = __shfl_down_sync(0xffffffffu, c.x, 1);
+  if (lane == 0) l = (p.in && p.i4 > 0) ? x[n - 1] : T(0);
+  if (lane == 31) r = (p.in && p.i4 + 4 < g.mx) ? x[n + 4] : T(0);
+  nb.c = c;
+  nb.l = l;
+  nb.r = r;
+  if (DIM >= 2) {
+    const bool hs = p.j - 1 > 0, hn = p.j + 1 < g.my - 1;
+    V4<T> s4 = (p.in && hs) ? ld4(x + n - g.pitch) : zero4<T>();
+    V4<T> n4 = (p.in && hn) ? ld4(x + n + g.pitch) : zero4<T>();
+    nb.ys = add4(s4, n4);
+  } else {
+    nb.ys = zero4<T>();
+  }
+}
+
+// b - A x at element e (A: the Jacobian, boundary rows diagonal, boundary
+// columns eliminated); `bd` true for a boundary node.  Padding points are
+// not evaluated by the callers.
+template <int DIM, typename T>
+__device__ __forceinline__ T resid_el(const Geom &g, const Wv<T> &w, const Nb<T> &nb, int e, int i, bool jkb, T bv) {
+  const T xc = el(nb.c, e);
+  const bool bd = jkb || i == 0 || i == g.mx - 1;
+  if (bd) return fma(-w.sd, xc, bv);
+  const T xl = e == 0 ? nb.l : el(nb.c, e - 1);
+  const T xr = e == 3 ? nb.r : el(nb.c, e + 1);
+  const T a = (i - 1 > 0 ? xl : T(0)) + (i + 1 < g.mx - 1 ? xr : T(0));
+  T s = fma(w.sx, a, bv);
+  if (DIM >= 2) s = fma(w.sy, el(nb.ys, e), s);
+  if (DIM >= 3) s = fma(w.sz, el(nb.zs, e), s);
+  return fma(-w.sd, xc, s);
+}
+
+__device__ __forceinline__ bool ksp_done_v(const KspState *st) { return st && __ldcg(&st->done); }
+
+// Generic z-march over the slot's planes.  `Op` is called once per plane
+// with (k, n, nb) after the neighbour data is assembled; it performs its own
+// loads/stores of other arrays at n.  `x` is the stencil input.
+template <int DIM, typename T, class Op>
+__device__ __forceinline__ void march(const Geom &g, const Slots &s, const SlotPos &p, const T *__restrict__ x,
+                                      Op &op) {
+  V4<T> zd = zero4<T>(), zc = zero4<T>();
+  if (p.in) {
+    if (DIM >= 3 && p.k0 > 0) zd = ld4(x + (long long)(p.k0 - 1) * g.plane + p.col);
+    zc = ld4(x + (long long)p.k0 * g.plane + p.col);
+  }
+  for (int k = p.k0; k < p.k1; k++) {
+    const long long n = (long long)k * g.plane + p.col;
+    V4<T> zu = zero4<T>();
+    if (DIM >= 3 && p.in && k + 1 < g.mz) zu = ld4(x + n + g.plane);
+    Nb<T> nb;
+    load_xy<DIM, T>(g, p, x, n, zc, nb);
+    if (DIM >= 3) {
+      const bool hd = k - 1 > 0, hu = k + 1 < g.mz - 1;
+      nb.zs = add4(hd ? zd : zero4<T>(), hu ? zu : zero4<T>());
+    } else {
+      nb.zs = zero4<T>();
+    }
+    if (p.in) op(k, n, nb);
+    zd = zc;
+    zc = zu;
+  }
+}
+
+__device__ __forceinline__ bool jk_bdry(const Geom &g, int dim, int j, int k) {
+  return (dim >= 2 && (j == 0 || j == g.my - 1)) || (dim >= 3 && (k == 0 || k == g.mz - 1));
+}
+
+// ------------------------------------------------------------------ stencil ops
+// out = ckm1*xkm1 + ck*xk + crd*(b - A xk)   (Chebyshev / Richardson step)
+// HAS_KM1=false drops the xkm1 term.  out must not alias any input (the
+// smoother rotates three buffers per level).
+template <int DIM, typename T, bool HAS_KM1>
+__global__ void __launch_bounds__(256) v_cheb(Geom g, Slots s, KspState *st, const T *__restrict__ b,
+                                              const T *__restrict__ xkm1, const T *__restrict__ xk,
+                                              T *__restrict__ out, T ckm1, T ck, T crd) {
+  if (ksp_done_v(st)) return;
+  const SlotPos p = slot_pos(g, s);
+  const Wv<T> w(g);
+  auto op = [&](int k, long long n, const Nb<T> &nb) {
+    const V4<T> bv = ld4(b + n);
+    V4<T> km = HAS_KM1 ? ld4(xkm1 + n) : zero4<T>();
+    const bool jkb = jk_bdry(g, DIM, p.j, k);
+    V4<T> o;
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+      const int i = p.i4 + e;
+      T v = T(0);
+      if (i < g.mx) {
+        const T r = resid_el<DIM, T>(g, w, nb, e, i, jkb, el(bv, e));
+        T base = ck * el(nb.c, e);
+        if (HAS_KM1) base = fma(ckm1, el(km, e), base);
+        v = fma(crd, r, base);
+      }
+      set_el(o, e, v);
+    }
+    st4(out + n, o);
+  };
+  march<DIM, T>(g, s, p, xk, op);
+}
+
+// Two Chebyshev steps from a zero iterate in one pass over b:
+//   x1 = c1 b,  x2 = omega x1 + omega c1 (b - A x1) = a0 b - a1 (A b)
+// with a0 = 2 omega c1, a1 = omega c1^2 (c1 = scale/scdiag).
+template <int DIM, typename T>
+__global__ void __launch_bounds__(256) v_cheb2_zero(Geom g, Slots s, KspState *st, const T *__restrict__ b,
+                                                    T *__restrict__ out, T a0, T a1) {
+  if (ksp_done_v(st)) return;
+  const SlotPos p = slot_pos(g, s);
+  const Wv<T> w(g);
+  auto op = [&](int k, long long n, const Nb<T> &nb) {
+    const bool jkb = jk_bdry(g, DIM, p.j, k);
+    V4<T> o;
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+      const int i = p.i4 + e;
+      T v = T(0);
+      if (i < g.mx) {
+        // -(A b) = (0 - A b): resid_el with bv = 0
+        const T mab = resid_el<DIM, T>(g, w, nb, e, i, jkb, T(0));
+        v = fma(a1, mab, a0 * el(nb.c, e));
+      }
+      set_el(o, e, v);
+    }
+    st4(out + n, o);
+  };
+  march<DIM, T>(g, s, p, b, op);
+}
+
+// r = b - A x
+template <int DIM, typename T>
+__global__ void __launch_bounds__(256) v_resid(Geom g, Slots s, KspState *st, const T *__restrict__ b,
+                                               const T *__restrict__ x, T *__restrict__ r) {
+  if (ksp_done_v(st)) return;
+  const SlotPos p = slot_pos(g, s);
+  const Wv<T> w(g);
+  auto op = [&](int k, long long n, const Nb<T> &nb) {
+    const V4<T> bv = ld4(b + n);
+    const bool jkb = jk_bdry(g, DIM, p.j, k);
+    V4<T> o;
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+      const int i = p.i4 + e;
+      set_el(o, e, i < g.mx ? resid_el<DIM, T>(g, w, nb, e, i, jkb, el(bv, e)) : T(0));
+    }
+    st4(r + n, o);
+  };
+  march<DIM, T>(g, s, p, x, op);
+}
+
+// w = A p; p.w reduced (per-thread partials in T, blocks in FP64)
+template <int DIM, typename T>
+__global__ void __launch_bounds__(256) v_apply_dot(Geom g, Slots s, KspState *st, const T *__restrict__ pv,
+                                                   T *__restrict__ wv, Reducer red, int slot, Fin fin,
+                                                   double *out) {
+  if (ksp_done_v(st)) return;
+  const SlotPos p = slot_pos(g, s);
+  const Wv<T> w(g);
+  T acc = T(0);
+  auto op = [&](int k, long long n, const Nb<T> &nb) {
+    const bool jkb = jk_bdry(g, DIM, p.j, k);
+    V4<T> o;
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+      const int i = p.i4 + e;
+      T v = T(0);
+      if (i < g.mx) {
+        v = -resid_el<DIM, T>(g, w, nb, e, i, jkb, T(0));
+        acc = fma(el(nb.c, e), v, acc);
+      }
+      set_el(o, e, v);
+    }
+    st4(wv + n, o);
+  };
+  march<DIM, T>(g, s, p, pv, op);
+  double v1[1] = {(double)acc};
+  reduce_and_finalize<1>(v1, red, slot, st, fin, out);
+}
+
+// ------------------------------------------------------------------ grid transfers
+// b_c = P^T r_f (full weighting; weights 1, 1/2 per offset and dimension).
+// A thread owns a coarse slot (I4..I4+3) and marches coarse planes; the fine
+// x-values 2I4-1 .. 2I4+7 come from two fine slots and a shuffle.
+template <int DIM, typename T>
+__device__ __forceinline__ V4<T> restrict_row(const Geom &gf, const T *__restrict__ rf, long long m, int I4, bool ok) {
+  // fine row values at 2I-1, 2I, 2I+1 weighted (1/2, 1, 1/2) for I = I4..I4+3
+  const int lane = threadIdx.x & 31;
+  const int fi = 2 * I4;
+  V4<T> A = zero4<T>(), B = zero4<T>();
+  if (ok) {
+    A = ld4(rf + m);
+    if (fi + 4 < gf.pitch) B = ld4(rf + m + 4);
+  }
+  T L = __shfl_up_sync(0xffffffffu, B.w, 1);
+  if (lane == 0) L = (ok && fi > 0) ? rf[m - 1] : T(0);
+  if (fi == 0) L = T(0);
+  const T h = T(0.5);
+  return V4<T>{fma(h, L + A.y, A.x), fma(h, A.y + A.w, A.z), fma(h, A.w + B.y, B.x), fma(h, B.y + B.w, B.z)};
+}
+
+template <int DIM, typename T>
+__global__ void __launch_bounds__(256) v_restrict(Geom gf, Geom g, Slots s, KspState *st, const T *__restrict__ rf,
+                                                  T *__restrict__ bc) {
+  if (ksp_done_v(st)) return;
+  const SlotPos p = slot_pos(g, s);
+  const T h = T(0.5);
+  // fine row offset of fine row fj, plane fk
+  auto rowsum = [&](int fk) -> V4<T> {  // sum over fj = 2J-1..2J+1 with weights (1/2,1,1/2)
+    const long long base = (long long)fk * gf.plane + 2LL * p.i4;
+    const int fj = 2 * p.j;
+    V4<T> c = restrict_row<DIM, T>(gf, rf, base + (long long)fj * gf.pitch, p.i4, p.in);
+    if (DIM < 2) return c;
+    const bool hs = fj - 1 >= 0, hn = fj + 1 < gf.my;
+    V4<T> sr = restrict_row<DIM, T>(gf, rf, base + (long long)(fj - 1) * gf.pitch, p.i4, p.in && hs);
+    V4<T> nr = restrict_row<DIM, T>(gf, rf, base + (long long)(fj + 1) * gf.pitch, p.i4, p.in && hn);
+    return V4<T>{fma(h, sr.x + nr.x, c.x), fma(h, sr.y + nr.y, c.y), fma(h, sr.z + nr.z, c.z),
+                 fma(h, sr.w + nr.w, c.w)};
+  };
+  V4<T> below = zero4<T>();  // row sums of fine plane 2K-1
+  if (DIM >= 3 && p.k0 > 0) below = rowsum(2 * p.k0 - 1);
+  for (int k = p.k0; k < p.k1; k++) {
+    V4<T> mid = rowsum(DIM >= 3 ? 2 * k : 0);
+    V4<T> above = zero4<T>();
+    if (DIM >= 3 && 2 * k + 1 < gf.mz) above = rowsum(2 * k + 1);
+    V4<T> o = mid;
+    if (DIM >= 3)
+      o = V4<T>{fma(h, below.x + above.x, mid.x), fma(h, below.y + above.y, mid.y),
+                fma(h, below.z + above.z, mid.z), fma(h, below.w + above.w, mid.w)};
+    if (p.in) {
+#pragma unroll
+      for (int e = 0; e < 4; e++)
+        if (p.i4 + e >= g.mx) set_el(o, e, T(0));
+      st4(bc + (long long)k * g.plane + p.col, o);
+    }
+    below = above;
+  }
+}
+
+// x_f += P x_c (Q1 interpolation).  A thread owns a coarse slot I4..I4+3 and
+// writes the 8 fine x-points 2I4 .. 2I4+7 of fine rows 2J, 2J+1 and planes
+// 2K, 2K+1 (those inside the fine grid).
+template <int DIM, typename T>
+__global__ void __launch_bounds__(256) v_prolong(Geom gf, Geom g, Slots s, KspState *st, const T *__restrict__ xc,
+                                                 T *__restrict__ xf) {
+  if (ksp_done_v(st)) return;
+  const SlotPos p = slot_pos(g, s);
+  const int lane = threadIdx.x & 31;
+  const T h = T(0.5);
+  // coarse row values C (4) and the next coarse value, x-interpolated to 8 fine values
+  auto xinterp = [&](long long m, bool ok, V4<T> &lo, V4<T> &hi) {
+    V4<T> C = ok ? ld4(xc + m) : zero4<T>();
+    T nx = __shfl_down_sync(0xffffffffu, C.x, 1);
+    if (lane == 31) nx = (ok && p.i4 + 4 < g.mx) ? xc[m + 4] : T(0);
+    lo = V4<T>{C.x, h * (C.x + C.y), C.y, h * (C.y + C.z)};
+    hi = V4<T>{C.z, h * (C.z + C.w), C.w, h * (C.w + nx)};
+  };
+  const int fi = 2 * p.i4;
+  // a fine slot is written only where it lies inside the fine row; points past
+  // mx_f are padding and keep their zero
+  auto addrow = [&](long long fm, const V4<T> &lo, const V4<T> &hi, T wgt) {
+    if (fi < gf.mx) {
+      V4<T> a = ld4(xf + fm);
+#pragma unroll
+      for (int e = 0; e < 4; e++)
+        if (fi + e < gf.mx) set_el(a, e, fma(wgt, el(lo, e), el(a, e)));
+      st4(xf + fm, a);
+    }
+    if (fi + 4 < gf.mx) {
+      V4<T> a = ld4(xf + fm + 4);
+#pragma unroll
+      for (int e = 0; e < 4; e++)
+        if (fi + 4 + e < gf.mx) set_el(a, e, fma(wgt, el(hi, e), el(a, e)));
+      st4(xf + fm + 4, a);
+    }
+  };
+  // fine planes 2k (coarse plane k) and 2k+1 (mean of planes k, k+1); fine
+  // rows 2J (row J) and 2J+1 (mean of rows J, J+1).  Loop bounds are uniform
+  // across the warp (the shuffles in xinterp need every lane); validity is
+  // carried by masks.
+  for (int k = p.k0; k < p.k1; k++) {
+    const int nfk = DIM >= 3 ? 2 : 1;
+    for (int dk = 0; dk < nfk; dk++) {
+      const int fk = DIM >= 3 ? 2 * k + dk : 0;
+      if (fk >= gf.mz) break;  // uniform: k is the same in the whole block
+      const int nfj = DIM >= 2 ? 2 : 1;
+      for (int dj = 0; dj < nfj; dj++) {
+        const int fj = DIM >= 2 ? 2 * p.j + dj : 0;
+        const bool rowok = p.in && fj < gf.my;
+        V4<T> lo = zero4<T>(), hi = zero4<T>();
+        for (int ck = 0; ck <= dk; ck++)
+          for (int cj = 0; cj <= dj; cj++) {
+            V4<T> l1, h1;
+            const long long m = (long long)(k + ck) * g.plane + (long long)(p.j + cj) * g.pitch + p.i4;
+            xinterp(m, rowok, l1, h1);
+            lo = add4(lo, l1);
+            hi = add4(hi, h1);
+          }
+        const T wgt = (dj && dk) ? T(0.25) : (dj || dk) ? T(0.5) : T(1);
+        if (rowok) addrow((long long)fk * gf.plane + (long long)fj * gf.pitch + fi, lo, hi, wgt);
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------------ pointwise
+// Flat over all slots of the padded array (padding stays zero).
+#define FG_FLAT_BEGIN(tot4)                                                              \
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < (tot4);      \
+       q += (long long)gridDim.x * blockDim.x) {                                         \
+    const long long n = q * 4;
+#define FG_FLAT_END }
+
+// p = z + (beta/betaold) p ; p = z on the first iteration
+template <typename T>
+__global__ void __launch_bounds__(256) v_cg_p(long long tot4, KspState *st, const T *__restrict__ z, T *__restrict__ pv) {
+  if (ksp_done_v(st)) return;
+  const bool first = st->i == 0;
+  const T bb = first ? T(0) : (T)(st->beta / st->betaold);
+  FG_FLAT_BEGIN(tot4)
+  const V4<T> zv = ld4(z + n);
+  if (first) {
+    st4(pv + n, zv);
+  } else {
+    const V4<T> pp = ld4(pv + n);
+    st4(pv + n, V4<T>{fma(bb, pp.x, zv.x), fma(bb, pp.y, zv.y), fma(bb, pp.z, zv.z), fma(bb, pp.w, zv.w)});
+  }
+  FG_FLAT_END
+}
+
+// y += alpha p; r -= alpha w; RR: r.r reduced
+template <typename T, bool RR>
+__global__ void __launch_bounds__(256) v_cg_xr(long long tot4, KspState *st, const T *__restrict__ pv,
+                                               const T *__restrict__ wv, T *__restrict__ y, T *__restrict__ r,
+                                               Reducer red, int slot) {
+  if (ksp_done_v(st)) return;
+  const T a = (T)st->alpha;
+  T acc = T(0);
+  FG_FLAT_BEGIN(tot4)
+  const V4<T> pp = ld4(pv + n), ww = ld4(wv + n), yy = ld4(y + n), rr = ld4(r + n);
+  st4(y + n, V4<T>{fma(a, pp.x, yy.x), fma(a, pp.y, yy.y), fma(a, pp.z, yy.z), fma(a, pp.w, yy.w)});
+  const V4<T> rn{fma(-a, ww.x, rr.x), fma(-a, ww.y, rr.y), fma(-a, ww.z, rr.z), fma(-a, ww.w, rr.w)};
+  st4(r + n, rn);
+  if (RR) acc = fma(rn.x, rn.x, fma(rn.y, rn.y, fma(rn.z, rn.z, fma(rn.w, rn.w, acc))));
+  FG_FLAT_END
+  if (RR) {
+    double v1[1] = {(double)acc};
+    reduce_and_finalize<1>(v1, red, slot, st, FIN_RR, nullptr);
+  }
+}
+
+// z.z and z.r reduced together
+template <typename T>
+__global__ void __launch_bounds__(256) v_dots(long long tot4, KspState *st, const T *__restrict__ z,
+                                              const T *__restrict__ r, Reducer red, int slot, Fin fin, double *out) {
+  if (ksp_done_v(st)) return;
+  T zz = T(0), zr = T(0);
+  FG_FLAT_BEGIN(tot4)
+  const V4<T> a = ld4(z + n), b = ld4(r + n);
+  zz = fma(a.x, a.x, fma(a.y, a.y, fma(a.z, a.z, fma(a.w, a.w, zz))));
+  zr = fma(a.x, b.x, fma(a.y, b.y, fma(a.z, b.z, fma(a.w, b.w, zr))));
+  FG_FLAT_END
+  double v2[2] = {(double)zz, (double)zr};
+  reduce_and_finalize<2>(v2, red, slot, st, fin, out);
+}
+
+// out = c * in (Jacobi apply, or scaled copy)
+template <typename T>
+__global__ void __launch_bounds__(256) v_scale(long long tot4, KspState *st, const T *__restrict__ in, T c,
+                                               T *__restrict__ out) {
+  if (ksp_done_v(st)) return;
+  FG_FLAT_BEGIN(tot4)
+  const V4<T> a = ld4(in + n);
+  st4(out + n, V4<T>{c * a.x, c * a.y, c * a.z, c * a.w});
+  FG_FLAT_END
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) v_zero(long long tot4, T *__restrict__ a) {
+  FG_FLAT_BEGIN(tot4)
+  st4(a + n, zero4<T>());
+  FG_FLAT_END
+}
+
+// r32 = (float)(r64 * inv_s)
+__global__ void __launch_bounds__(256) v_demote(long long tot4, const double *__restrict__ r, double inv_s,
+                                                float *__restrict__ r32) {
+  FG_FLAT_BEGIN(tot4)
+  const V4<double> a = ld4(r + n);
+  st4(r32 + n, V4<float>{(float)(a.x * inv_s), (float)(a.y * inv_s), (float)(a.z * inv_s), (float)(a.w * inv_s)});
+  FG_FLAT_END
+}
+
+// y64 += s * (double)e32
+__global__ void __launch_bounds__(256) v_promote_add(long long tot4, const float *__restrict__ e, double s,
+                                                     double *__restrict__ y) {
+  FG_FLAT_BEGIN(tot4)
+  const V4<float> a = ld4(e + n);
+  const V4<double> b = ld4(y + n);
+  st4(y + n, V4<double>{fma(s, (double)a.x, b.x), fma(s, (double)a.y, b.y), fma(s, (double)a.z, b.z),
+                        fma(s, (double)a.w, b.w)});
+  FG_FLAT_END
+}
+
+// a -= b
+__global__ void __launch_bounds__(256) v_sub(long long tot4, const double *__restrict__ b, double *__restrict__ a) {
+  FG_FLAT_BEGIN(tot4)
+  const V4<double> x = ld4(a + n), y = ld4(b + n);
+  st4(a + n, V4<double>{x.x - y.x, x.y - y.y, x.z - y.z, x.w - y.w});
+  FG_FLAT_END
+}
+
+}  // namespace fg

@@ -1,0 +1,304 @@
+"""GPU parity tests: libfishgpu.so (through its C ABI) against the CPU oracle.
+
+Tolerances (FP64 form): call-back outputs agree to 1e-13 relative (same
+formulas, different FMA contraction and exp() implementation); the CG residual
+history agrees to 1e-8 relative per iteration and the iteration count and
+reason agree exactly; discretisation errors agree to 1e-9 relative.
+Mixed form: final error within 1.01x of the FP64 error, true relative residual
+below rtol.
+"""
+import json
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+import _oracle as orc
+
+pytestmark = pytest.mark.gpu
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLDEN = json.load(open(os.path.join(ROOT, "tests", "golden", "fish_goldens.json")))
+
+
+def fgmod():
+    import p4pdes_gb300 as fg
+    return fg
+
+
+def info_ctx(g, xs=None, xm=None):
+    fg = fgmod()
+    inf = fg.Info()
+    inf.dim, inf.mx, inf.my, inf.mz = g.dim, g.mx, g.my, g.mz
+    s = xs or (0, 0, 0)
+    w = xm or (g.mx, g.my, g.mz)
+    inf.xs, inf.ys, inf.zs = s
+    inf.xm, inf.ym, inf.zm = w
+    inf.xmax[0], inf.xmax[1], inf.xmax[2] = g.Lx, g.Ly, g.Lz
+    c = fg.Ctx()
+    c.Lx, c.Ly, c.Lz, c.cx, c.cy, c.cz = g.Lx, g.Ly, g.Lz, g.cx, g.cy, g.cz
+    c.problem, c.dim = g.problem, g.dim
+    return inf, c
+
+
+def tcuda(a):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+GRIDS = [
+    (1, (17, 1, 1), orc.MANUPOLY, (1.0, 1.0, 1.0), (1.0, 1.0, 1.0)),
+    (1, (9, 1, 1), orc.MANUEXP, (1.0, 1.0, 1.0), (2.0, 1.0, 1.0)),
+    (2, (33, 17, 1), orc.MANUPOLY, (0.3, 2.0, 1.0), (1.0, 1.0, 1.0)),
+    (2, (65, 65, 1), orc.MANUEXP, (1.0, 1.0, 1.0), (1.0, 2.0, 1.0)),
+    (2, (37, 3, 1), orc.MANUPOLY, (1.0, 1.0, 1.0), (1.0, 1.0, 1.0)),
+    (3, (9, 9, 9), orc.MANUPOLY, (0.01, 2.0, 100.0), (1.0, 1.0, 1.0)),
+    (3, (33, 17, 65), orc.MANUEXP, (1.0, 1.0, 1.0), (1.0, 1.0, 1.0)),
+    (3, (35, 6, 5), orc.MANUPOLY, (1.0, 1.5, 0.5), (1.0, 0.5, 3.0)),
+]
+
+
+@pytest.mark.parametrize("case", GRIDS)
+def test_residual_callback_matches_oracle(cuda, case):
+    import torch
+    fg = fgmod()
+    dim, m, prob, c, L = case
+    g = orc.grid(dim, *m, problem=prob, c=c, L=L)
+    u = np.random.default_rng(11).standard_normal(orc.shape(g))
+    ref = orc.residual(g, u)
+    inf, ctx = info_ctx(g)
+    F = torch.full(orc.shape(g), np.nan, dtype=torch.float64, device=cuda)
+    getattr(fg, "Poisson%dDFunctionLocal" % dim)(inf, tcuda(u), F, ctx)
+    torch.cuda.synchronize()
+    got = F.cpu().numpy()
+    assert np.max(np.abs(got - ref)) <= 1e-13 * np.max(np.abs(ref))
+
+
+@pytest.mark.parametrize("case", GRIDS)
+def test_apply_and_dot_match_oracle(cuda, case):
+    import torch
+    fg = fgmod()
+    dim, m, prob, c, L = case
+    g = orc.grid(dim, *m, problem=prob, c=c, L=L)
+    p = np.random.default_rng(5).standard_normal(orc.shape(g))
+    ref = orc.apply(g, p)
+    inf, ctx = info_ctx(g)
+    q = torch.empty(orc.shape(g), dtype=torch.float64, device=cuda)
+    d = getattr(fg, "Poisson%dDOperatorApply" % dim)(inf, tcuda(p), q, ctx)
+    torch.cuda.synchronize()
+    assert np.max(np.abs(q.cpu().numpy() - ref)) <= 1e-13 * np.max(np.abs(ref))
+    dref = float(np.vdot(p, ref))
+    assert abs(d.item() - dref) <= 1e-12 * abs(dref)
+
+
+def test_callbacks_respect_the_owned_range(cuda):
+    import torch
+    fg = fgmod()
+    g = orc.grid(3, 17, 13, 11, problem=orc.MANUPOLY, c=(1.0, 2.0, 3.0))
+    u = np.random.default_rng(2).standard_normal(orc.shape(g))
+    ref = orc.residual(g, u)
+    inf, ctx = info_ctx(g, xs=(3, 1, 4), xm=(9, 10, 5))
+    F = torch.full(orc.shape(g), -7.0, dtype=torch.float64, device=cuda)
+    fg.Poisson3DFunctionLocal(inf, tcuda(u), F, ctx)
+    got = F.cpu().numpy()
+    box = (slice(4, 9), slice(1, 11), slice(3, 12))
+    assert np.max(np.abs(got[box] - ref[box])) <= 1e-13 * np.max(np.abs(ref))
+    mask = np.ones_like(got, dtype=bool)
+    mask[box] = False
+    assert np.all(got[mask] == -7.0)
+    # empty owned range is a no-op
+    inf.xm = 0
+    fg.Poisson3DFunctionLocal(inf, tcuda(u), F, ctx)
+    assert np.all(F.cpu().numpy()[mask] == -7.0)
+
+
+def test_user_arrays_match_builtin_problem(cuda):
+    """FISHGPU_USER with f and g sampled from manupoly gives the built-in result."""
+    import torch
+    fg = fgmod()
+    g = orc.grid(2, 33, 17, problem=orc.MANUPOLY)
+    h = [g.Lx / (g.mx - 1), g.Ly / (g.my - 1)]
+    jj, ii = np.meshgrid(np.arange(g.my), np.arange(g.mx), indexing="ij")
+    x, y = ii * h[0], jj * h[1]
+    gv = (x * x * (1 - x * x) * y * y * (y * y - 1))[None]
+    fv = -((2 * (1 - 6 * x * x)) * (y * y * (y * y - 1)) + (x * x * (1 - x * x)) * (2 * (6 * y * y - 1)))[None]
+    u = np.random.default_rng(9).standard_normal(orc.shape(g))
+    inf, ctx = info_ctx(g)
+    F1 = torch.empty(orc.shape(g), dtype=torch.float64, device=cuda)
+    fg.Poisson2DFunctionLocal(inf, tcuda(u), F1, ctx)
+    ft, gt = tcuda(fv), tcuda(gv)
+    ctx.problem, ctx.f, ctx.g = fg.USER, ft.data_ptr(), gt.data_ptr()
+    F2 = torch.empty_like(F1)
+    fg.Poisson2DFunctionLocal(inf, tcuda(u), F2, ctx)
+    assert torch.allclose(F1, F2, rtol=1e-12, atol=1e-14)
+
+
+@pytest.mark.parametrize("dim,m", [(1, (33, 1, 1)), (2, (17, 9, 1)), (3, (9, 17, 5))])
+@pytest.mark.parametrize("itype,gb", [(0, True), (0, False), (1, True), (1, False)])
+def test_initial_state_and_exact_match_oracle(cuda, dim, m, itype, gb):
+    import torch
+    fg = fgmod()
+    g = orc.grid(dim, *m, problem=orc.MANUEXP)
+    inf, ctx = info_ctx(g)
+    u = torch.empty(orc.shape(g), dtype=torch.float64, device=cuda)
+    fg.InitialState(inf, itype, gb, u, ctx, seed=1234)
+    ref = orc.initial(g, itype, gb, seed=1234)
+    got = u.cpu().numpy()
+    # same generator (splitmix64 of the dense index) on both sides
+    assert np.max(np.abs(got - ref)) <= 1e-14 * max(1.0, np.max(np.abs(ref)))
+    fg.FormUExact(inf, u, ctx)
+    assert np.max(np.abs(u.cpu().numpy() - orc.exact(g))) <= 1e-14 * np.max(np.abs(orc.exact(g)))
+    e = fg.error_norms(inf, tcuda(ref), ctx)
+    eref = orc.errnorms(g, ref)
+    assert abs(e[0] - eref[0]) <= 1e-14 * eref[0] and abs(e[1] - eref[1]) <= 1e-12 * eref[1]
+
+
+# ---------------------------------------------------------------- solver parity
+SOLVES = [r["args"] + ["-pc_type", "mg"] for r in GOLDEN] + [
+    "-fsh_dim 2 -fsh_problem manupoly -da_refine 7 -pc_type mg -mg_levels_ksp_type chebyshev "
+    "-mg_levels_pc_type jacobi -ksp_rtol 1e-10".split(),
+    "-fsh_dim 3 -fsh_problem manupoly -da_refine 5 -pc_type mg -ksp_rtol 1e-10".split(),
+    "-fsh_dim 3 -fsh_problem manuexp -da_refine 4 -pc_type mg -ksp_rtol 1e-10 -ksp_norm_type unpreconditioned".split(),
+    "-fsh_dim 2 -fsh_problem manupoly -da_refine 5 -pc_type mg -pc_mg_levels 3 -ksp_rtol 1e-10".split(),
+    "-fsh_dim 3 -fsh_problem manupoly -da_refine 4 -pc_type mg -pc_mg_levels 2 -ksp_rtol 1e-9".split(),
+    "-fsh_dim 2 -fsh_problem manupoly -da_refine 5 -pc_type mg -mg_levels_ksp_max_it 3 -ksp_rtol 1e-10".split(),
+    "-fsh_dim 2 -fsh_problem manupoly -da_refine 4 -pc_type mg -pc_mg_cycle_type w -ksp_rtol 1e-10".split(),
+    "-fsh_dim 2 -fsh_problem manupoly -da_refine 4 -pc_type mg -mg_levels_ksp_type richardson "
+    "-mg_levels_ksp_richardson_scale 0.6 -mg_levels_ksp_max_it 2 -ksp_rtol 1e-8".split(),
+    "-fsh_dim 2 -fsh_problem manupoly -da_refine 4 -pc_type jacobi -ksp_rtol 1e-8".split(),
+    "-fsh_dim 2 -fsh_problem manupoly -da_refine 3 -pc_type none -ksp_rtol 1e-8".split(),
+    "-fsh_dim 3 -fsh_problem manupoly -da_refine 3 -pc_type mg -fsh_initial_type random -fsh_seed 77 -ksp_rtol 1e-10".split(),
+    "-fsh_dim 2 -fsh_problem manupoly -da_grid_x 5 -da_grid_y 3 -da_refine 4 -fsh_Lx 2 -fsh_cy 3 -pc_type mg -ksp_rtol 1e-10".split(),
+    "-fsh_dim 3 -fsh_problem manupoly -da_refine 3 -pc_type mg -mg_levels_ksp_chebyshev_esteig 0,0.2,0,1.2 -ksp_rtol 1e-10".split(),
+]
+
+
+def compare_runs(args, fg_rep, ref):
+    assert fg_rep.reason == ref["reason"], args
+    assert fg_rep.its == ref["its"], (fg_rep.its, ref["its"], args)
+    h = fg_rep.history()
+    assert len(h) == len(ref["hist"])
+    # 1e-8 relative per iteration; entries at round-off level (below 1e-13 of
+    # the initial norm, e.g. after an exact coarse solve) are rounding noise
+    floor = 1e-13 * ref["hist"][0]
+    for a, b in zip(h, ref["hist"]):
+        assert abs(a - b) <= 1e-8 * abs(b) + floor, (a, b, args)
+    assert abs(fg_rep.fnorm0 - ref["fnorm0"]) <= 1e-12 * ref["fnorm0"]
+    for key in ("errinf", "err2h"):
+        assert abs(getattr(fg_rep, key) - ref[key]) <= 1e-9 * ref[key] + 1e-15, (key, args)
+
+
+@pytest.mark.parametrize("args", SOLVES, ids=lambda a: " ".join(a)[:90])
+def test_fp64_solve_matches_oracle(cuda, args):
+    fg = fgmod()
+    o = fg.options(args)
+    u, rep = fg.solve(o)
+    oo = orc.options(args)
+    uref, ref = orc.fish_solve(oo)
+    compare_runs(args, rep, ref)
+    diff = np.max(np.abs(u.cpu().numpy() - uref))
+    assert diff <= 1e-9 * max(1e-300, np.max(np.abs(uref)))
+
+
+def test_fp64_solve_reaches_the_exact_discrete_solution(cuda):
+    fg = fgmod()
+    args = "-fsh_dim 3 -fsh_problem manupoly -da_refine 6 -pc_type mg -ksp_rtol 1e-13"
+    u, rep = fg.solve(fg.options(args))
+    g = orc.options(args).grid
+    u0 = orc.initial(g, 0, True)
+    ustar = u0 - orc.exact_solve(g, orc.residual(g, u0))
+    assert np.max(np.abs(u.cpu().numpy() - ustar)) <= 1e-11 * np.max(np.abs(ustar))
+    e = orc.errnorms(g, ustar)
+    assert abs(rep.errinf - e[0]) <= 1e-8 * e[0]
+
+
+@pytest.mark.parametrize("args", [
+    "-fsh_dim 2 -fsh_problem manupoly -da_refine 7 -pc_type mg -ksp_rtol 1e-10",
+    "-fsh_dim 3 -fsh_problem manupoly -da_refine 5 -pc_type mg -ksp_rtol 1e-10",
+    "-fsh_dim 3 -fsh_problem manuexp -da_refine 4 -pc_type mg -ksp_rtol 1e-10",
+])
+def test_mixed_form_matches_fp64_error(cuda, args):
+    fg = fgmod()
+    _, r64 = fg.solve(fg.options(args + " -ksp_norm_type unpreconditioned"))
+    _, rmx = fg.solve(fg.options(args + " -fsh_precision mixed"))
+    assert rmx.reason == 2 and rmx.outer_its >= 1
+    assert rmx.true_rel_resid <= 1e-10
+    assert rmx.errinf <= 1.01 * r64.errinf and rmx.err2h <= 1.01 * r64.err2h
+    # the FP64 outer history is the true residual and decreases
+    h = rmx.history()
+    assert all(b < a for a, b in zip(h, h[1:]))
+
+
+def test_zero_problem_converges_at_iteration_zero(cuda):
+    fg = fgmod()
+    u, rep = fg.solve(fg.options("-fsh_dim 2 -fsh_problem zero -da_refine 3 -pc_type mg"))
+    assert rep.its == 0 and rep.reason == 3 and rep.errinf == 0.0
+
+
+def test_iteration_cap_reports_not_converged(cuda):
+    import torch
+    fg = fgmod()
+    o = fg.options("-fsh_dim 2 -fsh_problem manupoly -da_refine 5 -pc_type jacobi -ksp_max_it 3 -ksp_rtol 1e-12")
+    u = torch.empty(o.shape, dtype=torch.float64, device=cuda)
+    with fg.Solver(o) as s:
+        rep = s.solve(u)
+    assert rep.reason == -3 and rep.its == 3
+    oo = orc.options("-fsh_dim 2 -fsh_problem manupoly -da_refine 5 -pc_type jacobi -ksp_max_it 3 -ksp_rtol 1e-12")
+    assert orc.fish_solve(oo)[1]["its"] == 3
+
+
+def test_nonfinite_user_data_is_reported(cuda):
+    import torch
+    fg = fgmod()
+    o = fg.options("-fsh_dim 2 -da_refine 3 -pc_type mg")
+    f = torch.zeros(o.shape, dtype=torch.float64, device=cuda)
+    g = torch.zeros_like(f)
+    f[0, 5, 5] = float("nan")
+    o.ctx.problem, o.ctx.f, o.ctx.g = fg.USER, f.data_ptr(), g.data_ptr()
+    u = torch.empty_like(f)
+    with fg.Solver(o) as s:
+        with pytest.raises(fg.FishError) as e:
+            s.solve(u)
+    assert e.value.code == 5
+
+
+def test_solver_is_reusable_and_deterministic(cuda):
+    import torch
+    fg = fgmod()
+    o = fg.options("-fsh_dim 3 -fsh_problem manupoly -da_refine 4 -pc_type mg -ksp_rtol 1e-10")
+    with fg.Solver(o) as s:
+        u1 = torch.empty(o.shape, dtype=torch.float64, device=cuda)
+        u2 = torch.empty_like(u1)
+        r1 = s.solve(u1)
+        r2 = s.solve(u2)
+    assert torch.equal(u1, u2) and r1.history() == r2.history()
+
+
+def test_host_array_entry_point(cuda):
+    import ctypes
+    fg = fgmod()
+    o = fg.options("-fsh_dim 2 -fsh_problem manupoly -da_refine 5 -pc_type mg -ksp_rtol 1e-10")
+    u = np.empty(o.shape)
+    rep = fg.Report()
+    rc = fg.load().fishgpu_solve_host(ctypes.byref(o), None, None, u.ctypes.data, ctypes.byref(rep))
+    assert rc == 0
+    uref, ref = orc.fish_solve(orc.options("-fsh_dim 2 -fsh_problem manupoly -da_refine 5 -pc_type mg -ksp_rtol 1e-10"))
+    assert np.max(np.abs(u - uref)) <= 1e-9 * np.max(np.abs(uref))
+
+
+@pytest.mark.parametrize("rec", [r for r in GOLDEN if r["test"] in (1, 7)],
+                         ids=lambda r: "fish.test%d" % r["test"])
+def test_fish_driver_replays_golden(cuda, rec):
+    """The C driver with the reference's flags prints the reference's error
+    line and SNES norm lines for the runs solved to rtol 1e-12 (runs that
+    stop at rtol 1e-5 depend on PETSc's default ILU preconditioner, which the
+    GPU library replaces by multigrid; the oracle pins those)."""
+    exe = os.path.join(ROOT, "p4pdes_gb300", "bin", "fish")
+    p = subprocess.run([exe] + rec["args"], stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True)
+    assert p.returncode == 0, p.stderr
+    want = [l for l in rec["stdout"].splitlines() if "error |u-uexact|" in l or "SNES Function norm" in l
+            or l.startswith("problem ")]
+    got = [l for l in p.stdout.splitlines() if "error |u-uexact|" in l or "SNES Function norm" in l
+           or l.startswith("problem ")]
+    assert got == want
