@@ -85,6 +85,19 @@ int Poisson2DOperatorApply_gpu(const fishgpu_info *info, const double *p, double
 int Poisson3DOperatorApply_gpu(const fishgpu_info *info, const double *p, double *q,
                                double *pq_dot, const fishgpu_ctx *user, void *stream);
 
+/* Same result as Poisson{1,2,3}DOperatorApply_gpu (dimension from info->dim)
+   for callers that may not allocate device memory once running (a serving
+   loop working inside a fixed HBM budget, a host framework whose own pool owns
+   the device): it allocates nothing and keeps the dot product's partial sums
+   in a static device array of 4096 doubles + 256 B held by every GPU that
+   loads the library.  Launches that would need more partial sums are rejected
+   with FISHGPU_ERR_ARG.  All calls on a device share the array, so calls that
+   overlap on the GPU race; the first call on a device looks up the array's
+   address and should come before any stream capture.  This entry point has
+   no counterpart in the reference. */
+int PoissonOperatorApplyNoAlloc_gpu(const fishgpu_info *info, const double *p, double *q,
+                                    double *pq_dot, const fishgpu_ctx *user, void *stream);
+
 /* u = exact solution (= g) at every owned node; replaces Form{1,2,3}DUExact
    (c/ch6/fish.c:288-340); dimension taken from info->dim. */
 int FormUExact_gpu(const fishgpu_info *info, double *u, const fishgpu_ctx *user, void *stream);

@@ -116,6 +116,8 @@ def load():
         f = getattr(lib, "Poisson%dDOperatorApply_gpu" % dim)
         f.argtypes = [_P(Info), c_void_p, c_void_p, c_void_p, _P(Ctx), c_void_p]
         f.restype = c_int
+    lib.PoissonOperatorApplyNoAlloc_gpu.argtypes = [_P(Info), c_void_p, c_void_p, c_void_p, _P(Ctx), c_void_p]
+    lib.PoissonOperatorApplyNoAlloc_gpu.restype = c_int
     lib.FormUExact_gpu.argtypes = [_P(Info), c_void_p, _P(Ctx), c_void_p]
     lib.InitialState_gpu.argtypes = [_P(Info), c_int, c_int, c_ull, c_void_p, _P(Ctx), c_void_p]
     lib.ErrorNorms_gpu.argtypes = [_P(Info), c_void_p, _P(Ctx), _P(c_double), _P(c_double), c_void_p]
