@@ -269,6 +269,8 @@ def run_ours(args):
             "dofs": N, "levels": o_mx.mg_levels, "parallelism": "replicas" if world > 1 else "1 GPU",
             "l2": "no flush: every vector (1.08 GB FP64) exceeds L2",
             "mixed": {"ms": ms / K, "inner_its": rep_mx.its, "outer_its": rep_mx.outer_its,
+                      "inner_its_per_outer": [rep_mx.inner_its[i] for i in range(min(rep_mx.outer_its, 32))],
+                      "outer_true_residuals": rep_mx.history(),
                       "true_rel_resid": rep_mx.true_rel_resid, "errinf": err_mx[0], "err2h": err_mx[1]},
             "fp64": {"ms": ms64, "dof_per_s": N / (ms64 * 1e-3), "its": rep_64.its,
                      "true_rel_resid": rep_64.true_rel_resid, "errinf": err_64[0], "err2h": err_64[1]},

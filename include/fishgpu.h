@@ -149,6 +149,7 @@ typedef struct {
 } fishgpu_opts;
 
 #define FISHGPU_MAX_HIST 512
+#define FISHGPU_MAX_OUTER 32
 
 typedef struct {
   int its;                  /* KSP iterations (mixed: inner, summed)        */
@@ -162,6 +163,7 @@ typedef struct {
   double setup_ms, solve_ms;/* device time, CUDA events                     */
   long long dofs;           /* mx*my*mz                                     */
   long long launches;       /* kernels of this library launched by the solve */
+  int inner_its[FISHGPU_MAX_OUTER]; /* mixed: inner CG iterations per refinement step */
 } fishgpu_report;
 
 const char *fishgpu_strerror(int code);

@@ -37,6 +37,7 @@ NORM_PRECONDITIONED, NORM_UNPRECONDITIONED = 0, 1
 FP64, MIXED = 0, 1
 INITIAL_ZEROS, INITIAL_RANDOM, INITIAL_GIVEN = 0, 1, 2
 MAX_HIST = 512
+MAX_OUTER = 32
 
 c_int, c_double, c_void_p, c_ll, c_ull = (ctypes.c_int, ctypes.c_double, ctypes.c_void_p,
                                           ctypes.c_longlong, ctypes.c_ulonglong)
@@ -84,7 +85,8 @@ class Report(ctypes.Structure):
     _fields_ = [("its", c_int), ("reason", c_int), ("outer_its", c_int), ("nhist", c_int),
                 ("hist", c_double * MAX_HIST), ("fnorm0", c_double), ("fnorm1", c_double),
                 ("errinf", c_double), ("err2h", c_double), ("true_rel_resid", c_double),
-                ("setup_ms", c_double), ("solve_ms", c_double), ("dofs", c_ll), ("launches", c_ll)]
+                ("setup_ms", c_double), ("solve_ms", c_double), ("dofs", c_ll), ("launches", c_ll),
+                ("inner_its", c_int * MAX_OUTER)]
 
     def history(self):
         return [self.hist[i] for i in range(min(self.nhist, MAX_HIST))]

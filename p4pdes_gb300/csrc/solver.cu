@@ -111,6 +111,8 @@ struct fishgpu_solver_s {
   Hier<float> h32;
   // FP64 vectors (padded): u, KSP vectors (FP64 form) / outer vectors (mixed)
   double *u64 = nullptr, *r64 = nullptr, *p64 = nullptr, *w64 = nullptr, *y64 = nullptr, *b64 = nullptr;
+  double *beff = nullptr;    // F(u) = A u - beff (vol*f plus the boundary data of the eliminated columns)
+  bool beff_ready = false;   // built-in problems: computed once
   // FP32 inner KSP vectors (mixed form)
   float *r32 = nullptr, *p32 = nullptr, *w32 = nullptr, *y32 = nullptr;
   cudaGraphExec_t gexec = nullptr;       // giters CG iterations
@@ -431,32 +433,29 @@ static int run_ksp(fishgpu_solver *S, Hier<T> &H, KspVecs<T> v, double rtol, int
 }
 
 // ------------------------------------------------------------------ FP64 helpers
-// F(u) of c/ch6/poissonfunctions.c:29-115 on the whole (padded) grid
+// F(u) = A u - beff with A the Jacobian (boundary rows scdiag, boundary
+// columns eliminated): beff = scdiag*g on boundary rows; on interior rows
+// vol*f plus sc_d*g at each neighbour on the boundary -- the reference's
+// residual (poissonfunctions.c:10-19, :43-59, :86-106) rearranged.
 template <int DIM>
-__global__ void __launch_bounds__(256) k_residual64(Geom g, Tiles tm, Prob pb, const double *__restrict__ u,
-                                                    double *__restrict__ F) {
+__global__ void __launch_bounds__(256) k_beff64(Geom g, Tiles tm, Prob pb, double *__restrict__ be) {
   const Range R = full_range(g);
   FG_POINT_LOOP_BEGIN(R)
-  const double uc = u[n];
   if (on_bdry<DIM>(g, i, j, k)) {
-    F[n] = (uc - g_at(pb, g, i, j, k)) * g.scdiag;
+    be[n] = g.scdiag * g_at(pb, g, i, j, k);
   } else {
-    const double ue = (i + 1 == g.mx - 1) ? g_at(pb, g, i + 1, j, k) : u[n + 1];
-    const double uw = (i - 1 == 0) ? g_at(pb, g, i - 1, j, k) : u[n - 1];
-    if (DIM == 1) {
-      F[n] = pb.cx * (2.0 * uc - uw - ue) / g.h[0] - g.h[0] * f_at(pb, g, i, j, k);
-    } else {
-      const double un = (j + 1 == g.my - 1) ? g_at(pb, g, i, j + 1, k) : u[n + g.pitch];
-      const double us = (j - 1 == 0) ? g_at(pb, g, i, j - 1, k) : u[n - g.pitch];
-      if (DIM == 2) {
-        F[n] = g.scdiag * uc - g.sc[0] * (uw + ue) - g.sc[1] * (us + un) - g.vol * f_at(pb, g, i, j, k);
-      } else {
-        const double uu = (k + 1 == g.mz - 1) ? g_at(pb, g, i, j, k + 1) : u[n + g.plane];
-        const double ud = (k - 1 == 0) ? g_at(pb, g, i, j, k - 1) : u[n - g.plane];
-        F[n] = g.scdiag * uc - g.sc[0] * (uw + ue) - g.sc[1] * (us + un) - g.sc[2] * (uu + ud) -
-               g.vol * f_at(pb, g, i, j, k);
-      }
+    double v = g.vol * f_at(pb, g, i, j, k);
+    if (i - 1 == 0) v = fma(g.sc[0], g_at(pb, g, i - 1, j, k), v);
+    if (i + 1 == g.mx - 1) v = fma(g.sc[0], g_at(pb, g, i + 1, j, k), v);
+    if (DIM >= 2) {
+      if (j - 1 == 0) v = fma(g.sc[1], g_at(pb, g, i, j - 1, k), v);
+      if (j + 1 == g.my - 1) v = fma(g.sc[1], g_at(pb, g, i, j + 1, k), v);
     }
+    if (DIM >= 3) {
+      if (k - 1 == 0) v = fma(g.sc[2], g_at(pb, g, i, j, k - 1), v);
+      if (k + 1 == g.mz - 1) v = fma(g.sc[2], g_at(pb, g, i, j, k + 1), v);
+    }
+    be[n] = v;
   }
   FG_POINT_LOOP_END
 }
@@ -524,11 +523,17 @@ static int solve_dim(fishgpu_solver *S, double *u, fishgpu_report *rep) {
   const long long tot4 = S->sf.tot4;
   const unsigned gfl = S->gfl;
   FG_CUDA(cudaEventRecord(S->ev0, s));
-  S->launches = 3;  // initial state, F(u0), ||F(u0)||
+  S->launches = 3;  // initial state, -F(u0), ||F(u0)||
   k_initial64<DIM><<<L.grid, L.block, 0, s>>>(g, S->dense, L.tm, S->prob, o.initial_type, o.initial_gonboundary,
                                                o.seed, u, S->u64);
+  if (!S->beff_ready) {
+    k_beff64<DIM><<<L.grid, L.block, 0, s>>>(g, L.tm, S->prob, S->beff);
+    S->launches += 1;
+    S->beff_ready = S->o.ctx.problem != FISHGPU_USER;  // user data may change between solves
+  }
+  // the KSP right-hand side is -F(u0) = beff - A u0; it solves for -y and u = u0 + (-y)
   double *F = o.precision == FISHGPU_MIXED ? S->b64 : S->r64;
-  k_residual64<DIM><<<L.grid, L.block, 0, s>>>(g, L.tm, S->prob, S->u64, F);
+  v_resid<DIM, double><<<slot_blocks(S->sf), 256, 0, s>>>(g, S->sf, nullptr, S->beff, S->u64, F);
   enq_norm2(S, F, 0);
   FG_CUDA(cudaGetLastError());
   int rc = read_vals(S, 1);
@@ -562,6 +567,7 @@ static int solve_dim(fishgpu_solver *S, double *u, fishgpu_report *rep) {
       if ((rc = run_ksp<DIM, float>(S, S->h32, v, irtol, o.inner_max_it, FISHGPU_NORM_UNPRECONDITIONED))) return rc;
       const KspState *h = S->st_h;
       its += h->its;
+      if (outer < FISHGPU_MAX_OUTER) rep->inner_its[outer] = h->its;
       if (h->reason == R_DIVERGED_NANORINF || h->reason == R_DIVERGED_INDEFINITE_MAT ||
           h->reason == R_DIVERGED_INDEFINITE_PC) {
         reason = h->reason;
@@ -583,19 +589,27 @@ static int solve_dim(fishgpu_solver *S, double *u, fishgpu_report *rep) {
     rep->outer_its = outer;
     rep->nhist = nh;
   }
-  // u = u0 - y, then the caller's dense copy
-  v_sub<<<gfl, 256, 0, s>>>(tot4, S->y64, S->u64);
+  // u = u0 + (-y), then the caller's dense copy
+  v_add<<<gfl, 256, 0, s>>>(tot4, S->y64, S->u64);
   k_unpack64<DIM><<<L.grid, L.block, 0, s>>>(g, S->dense, L.tm, S->u64, u);
-  S->launches += 4;  // update, unpack, F(u), ||F(u)||
-  FG_CUDA(cudaEventRecord(S->ev1, s));
-  // F(u) for the final SNES norm (r64 is free now)
-  k_residual64<DIM><<<L.grid, L.block, 0, s>>>(g, L.tm, S->prob, S->u64, S->r64);
-  enq_norm2(S, S->r64, 1);
-  FG_CUDA(cudaGetLastError());
-  if ((rc = read_vals(S, 2))) return rc;
-  rep->fnorm1 = sqrt(S->hval[1]);
+  S->launches += 2;  // update, unpack
+  if (o.precision == FISHGPU_MIXED) {
+    // the last refinement step computed the FP64 residual beff - A(u0 + y) = -F(u)
+    FG_CUDA(cudaEventRecord(S->ev1, s));
+    rep->fnorm1 = rep->nhist > 0 ? rep->hist[(rep->nhist < FISHGPU_MAX_HIST ? rep->nhist : FISHGPU_MAX_HIST) - 1] : bn;
+  } else {
+    // F(u) for the final SNES norm (r64 is free now)
+    v_resid<DIM, double><<<slot_blocks(S->sf), 256, 0, s>>>(g, S->sf, nullptr, S->beff, S->u64, S->r64);
+    enq_norm2(S, S->r64, 1);
+    S->launches += 2;
+    FG_CUDA(cudaEventRecord(S->ev1, s));
+    FG_CUDA(cudaGetLastError());
+    if ((rc = read_vals(S, 2))) return rc;
+    rep->fnorm1 = sqrt(S->hval[1]);
+  }
   rep->true_rel_resid = bn > 0.0 ? rep->fnorm1 / bn : 0.0;
   float ms = 0.f;
+  FG_CUDA(cudaEventSynchronize(S->ev1));
   FG_CUDA(cudaEventElapsedTime(&ms, S->ev0, S->ev1));
   rep->solve_ms = ms;
   return FISHGPU_OK;
@@ -772,6 +786,7 @@ extern "C" int fishgpu_solver_create(const fishgpu_opts *o, void *stream, fishgp
   CK(dalloc(S, &S->red.tickets, 4));
   S->red.cap = cap;
   CK(dalloc(S, &S->u64, N));
+  CK(dalloc(S, &S->beff, N));
   CK(dalloc(S, &S->y64, N));
   CK(dalloc(S, &S->r64, N));
   if (o->ctx.problem == FISHGPU_USER && !o->ctx.f) {  // the solver owns f and g (dense)

@@ -67,12 +67,21 @@ struct Slots {
   long long tot4; // slots in the whole array
 };
 
-inline Slots make_slots(const Geom &g, int zc_want) {
+// zc_max planes per block at most, fewer when needed to keep at least
+// `min_blocks` blocks (small levels, and the coarse-grid launches of the
+// grid transfers, would otherwise leave SMs idle).
+inline Slots make_slots(const Geom &g, int zc_max, int min_blocks = 2432) {
   Slots s;
   s.P4 = g.pitch / 4;
   s.per_plane = s.P4 * g.my;
   s.nchunk = (s.per_plane + 255) / 256;
-  s.zc = g.dim == 3 ? (zc_want < g.mz ? zc_want : g.mz) : 1;
+  int zc = 1;
+  if (g.dim == 3) {
+    const long long want = ((long long)s.nchunk * g.mz) / (min_blocks > 0 ? min_blocks : 1);
+    zc = (int)(want < 1 ? 1 : want > zc_max ? zc_max : want);
+    if (zc > g.mz) zc = g.mz;
+  }
+  s.zc = zc;
   s.nz = (g.mz + s.zc - 1) / s.zc;
   s.tot4 = (long long)s.per_plane * g.mz;
   return s;
@@ -361,7 +370,8 @@ __global__ void __launch_bounds__(256) v_restrict(Geom gf, Geom g, Slots s, KspS
 
 // x_f += P x_c (Q1 interpolation).  A thread owns a coarse slot I4..I4+3 and
 // writes the 8 fine x-points 2I4 .. 2I4+7 of fine rows 2J, 2J+1 and planes
-// 2K, 2K+1 (those inside the fine grid).
+// 2K, 2K+1 (those inside the fine grid).  The x-interpolated coarse rows J and
+// J+1 of plane K+1 are kept for the next plane (one plane window).
 template <int DIM, typename T>
 __global__ void __launch_bounds__(256) v_prolong(Geom gf, Geom g, Slots s, KspState *st, const T *__restrict__ xc,
                                                  T *__restrict__ xf) {
@@ -369,18 +379,21 @@ __global__ void __launch_bounds__(256) v_prolong(Geom gf, Geom g, Slots s, KspSt
   const SlotPos p = slot_pos(g, s);
   const int lane = threadIdx.x & 31;
   const T h = T(0.5);
-  // coarse row values C (4) and the next coarse value, x-interpolated to 8 fine values
-  auto xinterp = [&](long long m, bool ok, V4<T> &lo, V4<T> &hi) {
+  const int fi = 2 * p.i4;
+  const bool ok0 = p.in;
+  const bool ok1 = p.in && DIM >= 2 && p.j + 1 < g.my;  // coarse row J+1 (fine row 2J+1) exists
+  // coarse row (k, jj) x-interpolated to 8 fine values; every lane calls it
+  auto xrow = [&](int k, int jj, bool ok, V4<T> &lo, V4<T> &hi) {
+    const long long m = (long long)k * g.plane + (long long)jj * g.pitch + p.i4;
     V4<T> C = ok ? ld4(xc + m) : zero4<T>();
     T nx = __shfl_down_sync(0xffffffffu, C.x, 1);
     if (lane == 31) nx = (ok && p.i4 + 4 < g.mx) ? xc[m + 4] : T(0);
     lo = V4<T>{C.x, h * (C.x + C.y), C.y, h * (C.y + C.z)};
     hi = V4<T>{C.z, h * (C.z + C.w), C.w, h * (C.w + nx)};
   };
-  const int fi = 2 * p.i4;
-  // a fine slot is written only where it lies inside the fine row; points past
-  // mx_f are padding and keep their zero
-  auto addrow = [&](long long fm, const V4<T> &lo, const V4<T> &hi, T wgt) {
+  // x_f[fk][fj][fi..fi+7] += wgt * (lo, hi); points past mx_f are padding
+  auto addrow = [&](int fk, int fj, const V4<T> &lo, const V4<T> &hi, T wgt) {
+    const long long fm = (long long)fk * gf.plane + (long long)fj * gf.pitch + fi;
     if (fi < gf.mx) {
       V4<T> a = ld4(xf + fm);
 #pragma unroll
@@ -396,32 +409,25 @@ __global__ void __launch_bounds__(256) v_prolong(Geom gf, Geom g, Slots s, KspSt
       st4(xf + fm + 4, a);
     }
   };
-  // fine planes 2k (coarse plane k) and 2k+1 (mean of planes k, k+1); fine
-  // rows 2J (row J) and 2J+1 (mean of rows J, J+1).  Loop bounds are uniform
-  // across the warp (the shuffles in xinterp need every lane); validity is
-  // carried by masks.
+  V4<T> a0l, a0h, a1l, a1h;  // plane k: rows J, J+1
+  xrow(p.k0, p.j, ok0, a0l, a0h);
+  xrow(p.k0, p.j + (ok1 ? 1 : 0), ok1, a1l, a1h);
   for (int k = p.k0; k < p.k1; k++) {
-    const int nfk = DIM >= 3 ? 2 : 1;
-    for (int dk = 0; dk < nfk; dk++) {
-      const int fk = DIM >= 3 ? 2 * k + dk : 0;
-      if (fk >= gf.mz) break;  // uniform: k is the same in the whole block
-      const int nfj = DIM >= 2 ? 2 : 1;
-      for (int dj = 0; dj < nfj; dj++) {
-        const int fj = DIM >= 2 ? 2 * p.j + dj : 0;
-        const bool rowok = p.in && fj < gf.my;
-        V4<T> lo = zero4<T>(), hi = zero4<T>();
-        for (int ck = 0; ck <= dk; ck++)
-          for (int cj = 0; cj <= dj; cj++) {
-            V4<T> l1, h1;
-            const long long m = (long long)(k + ck) * g.plane + (long long)(p.j + cj) * g.pitch + p.i4;
-            xinterp(m, rowok, l1, h1);
-            lo = add4(lo, l1);
-            hi = add4(hi, h1);
-          }
-        const T wgt = (dj && dk) ? T(0.25) : (dj || dk) ? T(0.5) : T(1);
-        if (rowok) addrow((long long)fk * gf.plane + (long long)fj * gf.pitch + fi, lo, hi, wgt);
-      }
+    const bool up = DIM >= 3 && k + 1 < g.mz;  // fine plane 2k+1 exists (uniform in the block)
+    V4<T> b0l = zero4<T>(), b0h = zero4<T>(), b1l = zero4<T>(), b1h = zero4<T>();
+    if (up) {
+      xrow(k + 1, p.j, ok0, b0l, b0h);
+      xrow(k + 1, p.j + (ok1 ? 1 : 0), ok1, b1l, b1h);
     }
+    const int fk = DIM >= 3 ? 2 * k : 0, fj = DIM >= 2 ? 2 * p.j : 0;
+    if (ok0) addrow(fk, fj, a0l, a0h, T(1));
+    if (ok1) addrow(fk, fj + 1, add4(a0l, a1l), add4(a0h, a1h), h);
+    if (up) {
+      if (ok0) addrow(fk + 1, fj, add4(a0l, b0l), add4(a0h, b0h), h);
+      if (ok1) addrow(fk + 1, fj + 1, add4(add4(a0l, a1l), add4(b0l, b1l)), add4(add4(a0h, a1h), add4(b0h, b1h)),
+                      T(0.25));
+    }
+    a0l = b0l; a0h = b0h; a1l = b1l; a1h = b1h;
   }
 }
 
@@ -524,11 +530,11 @@ __global__ void __launch_bounds__(256) v_promote_add(long long tot4, const float
   FG_FLAT_END
 }
 
-// a -= b
-__global__ void __launch_bounds__(256) v_sub(long long tot4, const double *__restrict__ b, double *__restrict__ a) {
+// a += b
+__global__ void __launch_bounds__(256) v_add(long long tot4, const double *__restrict__ b, double *__restrict__ a) {
   FG_FLAT_BEGIN(tot4)
   const V4<double> x = ld4(a + n), y = ld4(b + n);
-  st4(a + n, V4<double>{x.x - y.x, x.y - y.y, x.z - y.z, x.w - y.w});
+  st4(a + n, V4<double>{x.x + y.x, x.y + y.y, x.z + y.z, x.w + y.w});
   FG_FLAT_END
 }
 

@@ -49,7 +49,12 @@ int main(int argc, char **argv) {
   if (o.snes_monitor) print_snes_norm(0, rep.fnorm0);
   if (o.monitor) {
     int n = rep.nhist < FISHGPU_MAX_HIST ? rep.nhist : FISHGPU_MAX_HIST;
-    for (int i = 0; i < n; i++) printf("    %d KSP Residual norm %g\n", i, rep.hist[i]);
+    if (o.precision == FISHGPU_MIXED) /* refinement steps: FP64 true residual and inner CG iterations */
+      for (int i = 0; i < n; i++)
+        printf("    %d refinement residual norm %g (inner iterations %d)\n", i, rep.hist[i],
+               i > 0 && i - 1 < FISHGPU_MAX_OUTER ? rep.inner_its[i - 1] : 0);
+    else
+      for (int i = 0; i < n; i++) printf("    %d KSP Residual norm %g\n", i, rep.hist[i]);
   }
   if (o.converged_reason) {
     if (rep.reason > 0)
