@@ -110,11 +110,12 @@ struct fishgpu_solver_s {
   Hier<double> h64;
   Hier<float> h32;
   // FP64 vectors (padded): u, KSP vectors (FP64 form) / outer vectors (mixed)
-  double *u64 = nullptr, *r64 = nullptr, *p64 = nullptr, *w64 = nullptr, *y64 = nullptr, *b64 = nullptr;
+  double *u64 = nullptr, *r64 = nullptr, *p64 = nullptr, *q64 = nullptr, *w64 = nullptr, *y64 = nullptr;
+  double *b64 = nullptr;
   double *beff = nullptr;    // F(u) = A u - beff (vol*f plus the boundary data of the eliminated columns)
   bool beff_ready = false;   // built-in problems: computed once
   // FP32 inner KSP vectors (mixed form)
-  float *r32 = nullptr, *p32 = nullptr, *w32 = nullptr, *y32 = nullptr;
+  float *r32 = nullptr, *p32 = nullptr, *q32 = nullptr, *w32 = nullptr, *y32 = nullptr;
   cudaGraphExec_t gexec = nullptr;       // giters CG iterations
   cudaGraphExec_t gexec_init = nullptr;  // the KSP set-up sequence
   long long n_init = 0, n_iter = 0;      // kernel nodes of the two graphs
@@ -220,9 +221,12 @@ static inline int third(int a, int b) { return 3 - a - b; }
 // Level smoother, PETSc KSPCHEBYSHEV / KSPRICHARDSON with PCJACOBI, `its`
 // iterations, nonzero initial guess; from_zero: the iterate is known to be 0
 // (the arithmetic is identical).  Rotates the level's three buffers.
+// dots: when >= 0, the last step also reduces z.z and z.b and runs Fin(dots)
+// (the CG scalar update), so the separate dot kernel is not needed.
 template <int DIM, typename T>
-static void enq_smooth(fishgpu_solver *S, Level<T> &lv, bool from_zero) {
+static void enq_smooth(fishgpu_solver *S, Level<T> &lv, bool from_zero, int dots = -1) {
   const fishgpu_opts &o = S->o;
+  const Fin fin = (Fin)(dots < 0 ? 0 : dots);
   const double dinv = 1.0 / lv.g.scdiag;
   cudaStream_t s = S->stream;
   KspState *st = S->st;
@@ -233,8 +237,12 @@ static void enq_smooth(fishgpu_solver *S, Level<T> &lv, bool from_zero) {
     int cur = lv.cur;
     for (int it = 0; it < o.smooth_its; it++) {
       const int nxt = (cur + 1) % 3;
+      const bool last = it == o.smooth_its - 1 && dots >= 0;
       if (from_zero && it == 0)
         v_scale<T><<<gf, 256, 0, s>>>(lv.sl.tot4, st, lv.b, crd, lv.X[nxt]);
+      else if (last)
+        v_cheb<DIM, T, false, true><<<gb, 256, 0, s>>>(lv.g, lv.sl, st, lv.b, nullptr, lv.X[cur], lv.X[nxt], T(0), T(1),
+                                                       crd, S->red, 0, fin);
       else
         v_cheb<DIM, T, false><<<gb, 256, 0, s>>>(lv.g, lv.sl, st, lv.b, nullptr, lv.X[cur], lv.X[nxt], T(0), T(1), crd);
       cur = nxt;
@@ -263,7 +271,11 @@ static void enq_smooth(fishgpu_solver *S, Level<T> &lv, bool from_zero) {
   } else {
     km1 = lv.cur;
     kk = (lv.cur + 1) % 3;
-    v_cheb<DIM, T, false><<<gb, 256, 0, s>>>(lv.g, lv.sl, st, lv.b, nullptr, lv.X[km1], lv.X[kk], T(0), T(1), (T)c1);
+    if (o.smooth_its == 1 && dots >= 0)
+      v_cheb<DIM, T, false, true><<<gb, 256, 0, s>>>(lv.g, lv.sl, st, lv.b, nullptr, lv.X[km1], lv.X[kk], T(0), T(1),
+                                                     (T)c1, S->red, 0, fin);
+    else
+      v_cheb<DIM, T, false><<<gb, 256, 0, s>>>(lv.g, lv.sl, st, lv.b, nullptr, lv.X[km1], lv.X[kk], T(0), T(1), (T)c1);
   }
   double ckm1 = 1.0, ck = mu;
   for (int it = 1; it < o.smooth_its; it++) {
@@ -271,9 +283,13 @@ static void enq_smooth(fishgpu_solver *S, Level<T> &lv, bool from_zero) {
     const double omega = omegaprod * ck / ckp1;
     // x_{k+1} = (1-omega) x_{k-1} + omega x_k + omega scale D^{-1}(b - A x_k)
     const int out = km1 < 0 ? (kk + 1) % 3 : third(km1, kk);
+    const bool last = it == o.smooth_its - 1 && dots >= 0;
     if (km1 < 0)
       v_cheb<DIM, T, false><<<gb, 256, 0, s>>>(lv.g, lv.sl, st, lv.b, nullptr, lv.X[kk], lv.X[out], T(0), (T)omega,
                                                (T)(omega * c1));
+    else if (last)
+      v_cheb<DIM, T, true, true><<<gb, 256, 0, s>>>(lv.g, lv.sl, st, lv.b, lv.X[km1], lv.X[kk], lv.X[out],
+                                                    (T)(1.0 - omega), (T)omega, (T)(omega * c1), S->red, 0, fin);
     else
       v_cheb<DIM, T, true><<<gb, 256, 0, s>>>(lv.g, lv.sl, st, lv.b, lv.X[km1], lv.X[kk], lv.X[out],
                                               (T)(1.0 - omega), (T)omega, (T)(omega * c1));
@@ -286,7 +302,7 @@ static void enq_smooth(fishgpu_solver *S, Level<T> &lv, bool from_zero) {
 }
 
 template <int DIM, typename T>
-static void enq_vcycle(fishgpu_solver *S, Hier<T> &H, int l, bool from_zero) {
+static void enq_vcycle(fishgpu_solver *S, Hier<T> &H, int l, bool from_zero, int dots = -1) {
   Level<T> &lv = H.lev[l];
   cudaStream_t s = S->stream;
   KspState *st = S->st;
@@ -302,34 +318,38 @@ static void enq_vcycle(fishgpu_solver *S, Hier<T> &H, int l, bool from_zero) {
   v_restrict<DIM, T><<<slot_blocks(lc.sl), 256, 0, s>>>(lv.g, lc.g, lc.sl, st, lv.r, lc.b);
   for (int c = 0; c < S->o.mg_cycles; c++) enq_vcycle<DIM, T>(S, H, l - 1, c == 0);
   v_prolong<DIM, T><<<slot_blocks(lc.sl), 256, 0, s>>>(lv.g, lc.g, lc.sl, st, lc.X[lc.cur], lv.X[lv.cur]);
-  enq_smooth<DIM, T>(S, lv, false);
+  enq_smooth<DIM, T>(S, lv, false, dots);
 }
 
 // z = B r; H.z is where z lands (the same buffer at every application).
+// Returns true when z.z and z.r were reduced (and Fin(dots) run) by the last
+// smoothing step, false when the caller still has to reduce them.
 template <int DIM, typename T>
-static void enq_pc(fishgpu_solver *S, Hier<T> &H, const T *r) {
+static bool enq_pc(fishgpu_solver *S, Hier<T> &H, const T *r, int dots) {
   const fishgpu_opts &o = S->o;
   const long long tot4 = S->sf.tot4;
   if (o.pc_type == FISHGPU_PC_NONE) {
     v_scale<T><<<S->gfl, 256, 0, S->stream>>>(tot4, S->st, r, T(1), H.zbuf);
     H.z = H.zbuf;
-    return;
+    return false;
   }
   if (o.pc_type == FISHGPU_PC_JACOBI) {  // z = D^{-1} r
     v_scale<T><<<S->gfl, 256, 0, S->stream>>>(tot4, S->st, r, (T)(1.0 / S->fine.scdiag), H.zbuf);
     H.z = H.zbuf;
-    return;
+    return false;
   }
   for (int l = 0; l < H.nlev; l++) H.lev[l].cur = 0;
   Level<T> &top = H.lev[H.nlev - 1];
   top.b = const_cast<T *>(r);
-  enq_vcycle<DIM, T>(S, H, H.nlev - 1, true);
+  const bool fused = H.nlev > 1;  // a single level ends with the coarse solve, no smoother
+  enq_vcycle<DIM, T>(S, H, H.nlev - 1, true, fused ? dots : -1);
   H.z = top.X[top.cur];
+  return fused;
 }
 
 template <typename T>
 struct KspVecs {
-  T *r, *p, *w, *y;
+  T *r, *p[2], *w, *y;  // p: two buffers, the direction update reads one and writes the other
 };
 
 template <int DIM, typename T>
@@ -339,24 +359,26 @@ static void enq_cg_init(fishgpu_solver *S, Hier<T> &H, KspVecs<T> v) {
   v_zero<T><<<S->gfl, 256, 0, s>>>(tot4, v.y);
   if (S->o.norm_type == FISHGPU_NORM_UNPRECONDITIONED)
     v_dots<T><<<S->gfl, 256, 0, s>>>(tot4, S->st, v.r, v.r, S->red, 0, FIN_INIT_RR, nullptr);
-  enq_pc<DIM, T>(S, H, v.r);
-  v_dots<T><<<S->gfl, 256, 0, s>>>(tot4, S->st, H.z, v.r, S->red, 0, FIN_INIT_ZZZR, nullptr);
+  if (!enq_pc<DIM, T>(S, H, v.r, FIN_INIT_ZZZR))
+    v_dots<T><<<S->gfl, 256, 0, s>>>(tot4, S->st, H.z, v.r, S->red, 0, FIN_INIT_ZZZR, nullptr);
 }
 
+// One CG iteration; `par` selects which p buffer holds the previous direction.
 template <int DIM, typename T>
-static void enq_cg_iter(fishgpu_solver *S, Hier<T> &H, KspVecs<T> v) {
+static void enq_cg_iter(fishgpu_solver *S, Hier<T> &H, KspVecs<T> v, int par) {
   cudaStream_t s = S->stream;
   KspState *st = S->st;
   const long long tot4 = S->sf.tot4;
   const unsigned gf = S->gfl;
-  v_cg_p<T><<<gf, 256, 0, s>>>(tot4, st, H.z, v.p);  // z of the previous application
-  v_apply_dot<DIM, T><<<slot_blocks(S->sf), 256, 0, s>>>(S->fine, S->sf, st, v.p, v.w, S->red, 0, FIN_PW, nullptr);
+  T *pold = v.p[par], *pnew = v.p[1 - par];
+  // p = z + beta/betaold p (z of the previous application), w = A p, p.w
+  v_cgp_apply<DIM, T><<<slot_blocks(S->sf), 256, 0, s>>>(S->fine, S->sf, st, H.z, pold, pnew, v.w, S->red, 0);
   if (S->o.norm_type == FISHGPU_NORM_UNPRECONDITIONED)
-    v_cg_xr<T, true><<<gf, 256, 0, s>>>(tot4, st, v.p, v.w, v.y, v.r, S->red, 0);
+    v_cg_xr<T, true><<<gf, 256, 0, s>>>(tot4, st, pnew, v.w, v.y, v.r, S->red, 0);
   else
-    v_cg_xr<T, false><<<gf, 256, 0, s>>>(tot4, st, v.p, v.w, v.y, v.r, S->red, 0);
-  enq_pc<DIM, T>(S, H, v.r);
-  v_dots<T><<<gf, 256, 0, s>>>(tot4, st, H.z, v.r, S->red, 0, FIN_ZZZR, nullptr);
+    v_cg_xr<T, false><<<gf, 256, 0, s>>>(tot4, st, pnew, v.w, v.y, v.r, S->red, 0);
+  if (!enq_pc<DIM, T>(S, H, v.r, FIN_ZZZR))
+    v_dots<T><<<gf, 256, 0, s>>>(tot4, st, H.z, v.r, S->red, 0, FIN_ZZZR, nullptr);
 }
 
 static long long kernel_nodes(cudaGraph_t g) {
@@ -411,8 +433,8 @@ static int run_ksp(fishgpu_solver *S, Hier<T> &H, KspVecs<T> v, double rtol, int
       (rc = capture(S, [&] { enq_cg_init<DIM, T>(S, H, v); }, &S->gexec_init, &S->n_init)))
     return rc;
   if (!S->gexec &&
-      (rc = capture(S, [&] { for (int g = 0; g < S->giters; g++) enq_cg_iter<DIM, T>(S, H, v); }, &S->gexec,
-                    &S->n_iter)))
+      (rc = capture(S, [&] { for (int g = 0; g < S->giters; g++) enq_cg_iter<DIM, T>(S, H, v, g & 1); },
+                    &S->gexec, &S->n_iter)))
     return rc;
   reset_state(S, rtol, S->o.atol, S->o.dtol, max_it, norm);
   FG_CUDA(cudaMemcpyAsync(S->st, S->st_h, sizeof(KspState), cudaMemcpyHostToDevice, s));
@@ -541,7 +563,7 @@ static int solve_dim(fishgpu_solver *S, double *u, fishgpu_report *rep) {
   const double bn = sqrt(S->hval[0]);
   rep->fnorm0 = bn;
   if (o.precision == FISHGPU_FP64) {
-    KspVecs<double> v{S->r64, S->p64, S->w64, S->y64};
+    KspVecs<double> v{S->r64, {S->p64, S->q64}, S->w64, S->y64};
     if ((rc = run_ksp<DIM, double>(S, S->h64, v, o.rtol, o.max_it, o.norm_type))) return rc;
     fill_from_state(S->st_h, rep);
     rep->outer_its = 0;
@@ -553,7 +575,15 @@ static int solve_dim(fishgpu_solver *S, double *u, fishgpu_report *rep) {
     v_zero<double><<<gfl, 256, 0, s>>>(tot4, S->y64);
     S->launches += 1;
     rep->hist[nh++] = rn;
-    KspVecs<float> v{S->r32, S->p32, S->w32, S->y32};
+    KspVecs<float> v{S->r32, {S->p32, S->q32}, S->w32, S->y32};
+    // The first correction is smooth and carries the FP32 rounding of its
+    // storage, which J amplifies by up to its condition number: the true
+    // residual cannot drop below ~kappa * 2^-24 of ||b|| in that step, so the
+    // first inner solve stops there.  kappa is the exact ratio of the extreme
+    // eigenvalues of D^{-1}J on the fine grid.
+    double lmin, lmax;
+    spectrum(g, &lmin, &lmax);
+    const double first_floor = fmin(0.5, 0.3 * (lmax / fmax(lmin, 1e-300)) * 0x1.0p-24);
     while (true) {
       if (isnan(rn) || isinf(rn)) { reason = R_DIVERGED_NANORINF; break; }
       if (rn <= ttol) { reason = rn < o.atol ? R_CONVERGED_ATOL : R_CONVERGED_RTOL; break; }
@@ -563,6 +593,7 @@ static int solve_dim(fishgpu_solver *S, double *u, fishgpu_report *rep) {
       S->launches += 4;  // demote, promote-add, FP64 residual, its norm
       // inner tolerance: what is still needed, never below the FP32 floor
       double irtol = fmax(o.inner_rtol, 0.5 * ttol / rn);
+      if (outer == 0) irtol = fmax(irtol, first_floor);
       if (irtol > 0.5) irtol = 0.5;
       if ((rc = run_ksp<DIM, float>(S, S->h32, v, irtol, o.inner_max_it, FISHGPU_NORM_UNPRECONDITIONED))) return rc;
       const KspState *h = S->st_h;
@@ -765,7 +796,9 @@ extern "C" int fishgpu_solver_create(const fishgpu_opts *o, void *stream, fishgp
                  S->dense.plane};
   const size_t N = nelem(S->fine);
   const long long dofs = (long long)S->dense.plane * S->dense.mz;
-  S->giters = o->graph_iters > 0 ? o->graph_iters : (dofs >= (1LL << 20) ? 1 : 4);
+  // iterations per graph launch: even, since consecutive iterations alternate the two p buffers
+  S->giters = o->graph_iters > 0 ? o->graph_iters : (dofs >= (1LL << 20) ? 2 : 4);
+  S->giters += S->giters & 1;
 #define CK(x)                            \
   do {                                   \
     if ((rc = (x)) != FISHGPU_OK) {      \
@@ -800,12 +833,14 @@ extern "C" int fishgpu_solver_create(const fishgpu_opts *o, void *stream, fishgp
   }
   if (o->precision == FISHGPU_FP64) {
     CK(dalloc(S, &S->p64, N));
+    CK(dalloc(S, &S->q64, N));
     CK(dalloc(S, &S->w64, N));
     CK(build_hier<double>(S, S->h64));
   } else {
     CK(dalloc(S, &S->b64, N));
     CK(dalloc(S, &S->r32, N));
     CK(dalloc(S, &S->p32, N));
+    CK(dalloc(S, &S->q32, N));
     CK(dalloc(S, &S->w32, N));
     CK(dalloc(S, &S->y32, N));
     CK(build_hier<float>(S, S->h32));

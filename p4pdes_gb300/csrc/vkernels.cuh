@@ -108,6 +108,14 @@ __device__ __forceinline__ SlotPos slot_pos(const Geom &g, const Slots &s) {
   return p;
 }
 
+// Resident blocks per SM the compiler is asked to fit: 5 x 256 threads for
+// FP32 stencils (48 registers, no spills) to cover HBM latency; FP64 stencils
+// are FP64-pipe-bound and keep their registers.
+template <typename T>
+struct MinBlocks {
+  static constexpr int value = sizeof(T) == 4 ? 5 : 1;
+};
+
 template <typename T>
 struct Wv {
   T sx, sy, sz, sd;
@@ -124,22 +132,46 @@ struct Nb {
   V4<T> zs;  // sum of the z-neighbours that are interior nodes
 };
 
+// Stencil input read from one array.
+template <typename T>
+struct ArraySrc {
+  const T *__restrict__ x;
+  __device__ __forceinline__ V4<T> v4(long long n) const { return ld4(x + n); }
+  __device__ __forceinline__ T s(long long n) const { return x[n]; }
+};
+
+// Stencil input p = z + bb * q formed on the fly (p = z when first).
+template <typename T>
+struct AxpySrc {
+  const T *__restrict__ z;
+  const T *__restrict__ q;
+  T bb;
+  bool first;
+  __device__ __forceinline__ V4<T> v4(long long n) const {
+    const V4<T> a = ld4(z + n);
+    if (first) return a;
+    const V4<T> b = ld4(q + n);
+    return V4<T>{fma(bb, b.x, a.x), fma(bb, b.y, a.y), fma(bb, b.z, a.z), fma(bb, b.w, a.w)};
+  }
+  __device__ __forceinline__ T s(long long n) const { return first ? z[n] : fma(bb, q[n], z[n]); }
+};
+
 // Loads everything but the z-window for plane k; shuffles need all lanes.
-template <int DIM, typename T>
-__device__ __forceinline__ void load_xy(const Geom &g, const SlotPos &p, const T *__restrict__ x, long long n,
-                                        const V4<T> &c, Nb<T> &nb) {
+template <int DIM, typename T, class Src>
+__device__ __forceinline__ void load_xy(const Geom &g, const SlotPos &p, const Src &x, long long n, const V4<T> &c,
+                                        Nb<T> &nb) {
   const int lane = threadIdx.x & 31;
   T l = __shfl_up_sync(0xffffffffu, c.w, 1);
   T r = __shfl_down_sync(0xffffffffu, c.x, 1);
-  if (lane == 0) l = (p.in && p.i4 > 0) ? x[n - 1] : T(0);
-  if (lane == 31) r = (p.in && p.i4 + 4 < g.mx) ? x[n + 4] : T(0);
+  if (lane == 0) l = (p.in && p.i4 > 0) ? x.s(n - 1) : T(0);
+  if (lane == 31) r = (p.in && p.i4 + 4 < g.mx) ? x.s(n + 4) : T(0);
   nb.c = c;
   nb.l = l;
   nb.r = r;
   if (DIM >= 2) {
     const bool hs = p.j - 1 > 0, hn = p.j + 1 < g.my - 1;
-    V4<T> s4 = (p.in && hs) ? ld4(x + n - g.pitch) : zero4<T>();
-    V4<T> n4 = (p.in && hn) ? ld4(x + n + g.pitch) : zero4<T>();
+    V4<T> s4 = (p.in && hs) ? x.v4(n - g.pitch) : zero4<T>();
+    V4<T> n4 = (p.in && hn) ? x.v4(n + g.pitch) : zero4<T>();
     nb.ys = add4(s4, n4);
   } else {
     nb.ys = zero4<T>();
@@ -168,18 +200,17 @@ __device__ __forceinline__ bool ksp_done_v(const KspState *st) { return st && __
 // Generic z-march over the slot's planes.  `Op` is called once per plane
 // with (k, n, nb) after the neighbour data is assembled; it performs its own
 // loads/stores of other arrays at n.  `x` is the stencil input.
-template <int DIM, typename T, class Op>
-__device__ __forceinline__ void march(const Geom &g, const Slots &s, const SlotPos &p, const T *__restrict__ x,
-                                      Op &op) {
+template <int DIM, typename T, class Op, class Src>
+__device__ __forceinline__ void march_src(const Geom &g, const Slots &s, const SlotPos &p, const Src &x, Op &op) {
   V4<T> zd = zero4<T>(), zc = zero4<T>();
   if (p.in) {
-    if (DIM >= 3 && p.k0 > 0) zd = ld4(x + (long long)(p.k0 - 1) * g.plane + p.col);
-    zc = ld4(x + (long long)p.k0 * g.plane + p.col);
+    if (DIM >= 3 && p.k0 > 0) zd = x.v4((long long)(p.k0 - 1) * g.plane + p.col);
+    zc = x.v4((long long)p.k0 * g.plane + p.col);
   }
   for (int k = p.k0; k < p.k1; k++) {
     const long long n = (long long)k * g.plane + p.col;
     V4<T> zu = zero4<T>();
-    if (DIM >= 3 && p.in && k + 1 < g.mz) zu = ld4(x + n + g.plane);
+    if (DIM >= 3 && p.in && k + 1 < g.mz) zu = x.v4(n + g.plane);
     Nb<T> nb;
     load_xy<DIM, T>(g, p, x, n, zc, nb);
     if (DIM >= 3) {
@@ -194,6 +225,12 @@ __device__ __forceinline__ void march(const Geom &g, const Slots &s, const SlotP
   }
 }
 
+template <int DIM, typename T, class Op>
+__device__ __forceinline__ void march(const Geom &g, const Slots &s, const SlotPos &p, const T *__restrict__ x,
+                                      Op &op) {
+  march_src<DIM, T>(g, s, p, ArraySrc<T>{x}, op);
+}
+
 __device__ __forceinline__ bool jk_bdry(const Geom &g, int dim, int j, int k) {
   return (dim >= 2 && (j == 0 || j == g.my - 1)) || (dim >= 3 && (k == 0 || k == g.mz - 1));
 }
@@ -202,13 +239,17 @@ __device__ __forceinline__ bool jk_bdry(const Geom &g, int dim, int j, int k) {
 // out = ckm1*xkm1 + ck*xk + crd*(b - A xk)   (Chebyshev / Richardson step)
 // HAS_KM1=false drops the xkm1 term.  out must not alias any input (the
 // smoother rotates three buffers per level).
-template <int DIM, typename T, bool HAS_KM1>
-__global__ void __launch_bounds__(256) v_cheb(Geom g, Slots s, KspState *st, const T *__restrict__ b,
+// DOTS: also reduces out.out and out.b (the preconditioned residual's z.z and
+// z.r when this is the last smoothing step on the finest level) and runs `fin`.
+template <int DIM, typename T, bool HAS_KM1, bool DOTS = false>
+__global__ void __launch_bounds__(256, MinBlocks<T>::value) v_cheb(Geom g, Slots s, KspState *st, const T *__restrict__ b,
                                               const T *__restrict__ xkm1, const T *__restrict__ xk,
-                                              T *__restrict__ out, T ckm1, T ck, T crd) {
+                                              T *__restrict__ out, T ckm1, T ck, T crd, Reducer red = Reducer{},
+                                              int slot = 0, Fin fin = FIN_STORE) {
   if (ksp_done_v(st)) return;
   const SlotPos p = slot_pos(g, s);
   const Wv<T> w(g);
+  T zz = T(0), zr = T(0);
   auto op = [&](int k, long long n, const Nb<T> &nb) {
     const V4<T> bv = ld4(b + n);
     V4<T> km = HAS_KM1 ? ld4(xkm1 + n) : zero4<T>();
@@ -223,19 +264,27 @@ __global__ void __launch_bounds__(256) v_cheb(Geom g, Slots s, KspState *st, con
         T base = ck * el(nb.c, e);
         if (HAS_KM1) base = fma(ckm1, el(km, e), base);
         v = fma(crd, r, base);
+        if (DOTS) {
+          zz = fma(v, v, zz);
+          zr = fma(v, el(bv, e), zr);
+        }
       }
       set_el(o, e, v);
     }
     st4(out + n, o);
   };
   march<DIM, T>(g, s, p, xk, op);
+  if (DOTS) {
+    double v2[2] = {(double)zz, (double)zr};
+    reduce_and_finalize<2>(v2, red, slot, st, fin, nullptr);
+  }
 }
 
 // Two Chebyshev steps from a zero iterate in one pass over b:
 //   x1 = c1 b,  x2 = omega x1 + omega c1 (b - A x1) = a0 b - a1 (A b)
 // with a0 = 2 omega c1, a1 = omega c1^2 (c1 = scale/scdiag).
 template <int DIM, typename T>
-__global__ void __launch_bounds__(256) v_cheb2_zero(Geom g, Slots s, KspState *st, const T *__restrict__ b,
+__global__ void __launch_bounds__(256, MinBlocks<T>::value) v_cheb2_zero(Geom g, Slots s, KspState *st, const T *__restrict__ b,
                                                     T *__restrict__ out, T a0, T a1) {
   if (ksp_done_v(st)) return;
   const SlotPos p = slot_pos(g, s);
@@ -261,7 +310,7 @@ __global__ void __launch_bounds__(256) v_cheb2_zero(Geom g, Slots s, KspState *s
 
 // r = b - A x
 template <int DIM, typename T>
-__global__ void __launch_bounds__(256) v_resid(Geom g, Slots s, KspState *st, const T *__restrict__ b,
+__global__ void __launch_bounds__(256, MinBlocks<T>::value) v_resid(Geom g, Slots s, KspState *st, const T *__restrict__ b,
                                                const T *__restrict__ x, T *__restrict__ r) {
   if (ksp_done_v(st)) return;
   const SlotPos p = slot_pos(g, s);
@@ -282,7 +331,7 @@ __global__ void __launch_bounds__(256) v_resid(Geom g, Slots s, KspState *st, co
 
 // w = A p; p.w reduced (per-thread partials in T, blocks in FP64)
 template <int DIM, typename T>
-__global__ void __launch_bounds__(256) v_apply_dot(Geom g, Slots s, KspState *st, const T *__restrict__ pv,
+__global__ void __launch_bounds__(256, MinBlocks<T>::value) v_apply_dot(Geom g, Slots s, KspState *st, const T *__restrict__ pv,
                                                    T *__restrict__ wv, Reducer red, int slot, Fin fin,
                                                    double *out) {
   if (ksp_done_v(st)) return;
@@ -307,6 +356,40 @@ __global__ void __launch_bounds__(256) v_apply_dot(Geom g, Slots s, KspState *st
   march<DIM, T>(g, s, p, pv, op);
   double v1[1] = {(double)acc};
   reduce_and_finalize<1>(v1, red, slot, st, fin, out);
+}
+
+// p_new = z + (beta/betaold) p_old (p_new = z on the first CG iteration),
+// w = A p_new, p_new.w reduced: the CG direction update fused into the apply.
+// p_old and p_new are different buffers (neighbours read p_old).
+template <int DIM, typename T>
+__global__ void __launch_bounds__(256, MinBlocks<T>::value) v_cgp_apply(Geom g, Slots s, KspState *st, const T *__restrict__ z,
+                                                   const T *__restrict__ pold, T *__restrict__ pnew,
+                                                   T *__restrict__ wv, Reducer red, int slot) {
+  if (ksp_done_v(st)) return;
+  const SlotPos p = slot_pos(g, s);
+  const Wv<T> w(g);
+  const bool first = st->i == 0;
+  const AxpySrc<T> src{z, pold, first ? T(0) : (T)(st->beta / st->betaold), first};
+  T acc = T(0);
+  auto op = [&](int k, long long n, const Nb<T> &nb) {
+    const bool jkb = jk_bdry(g, DIM, p.j, k);
+    V4<T> o;
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+      const int i = p.i4 + e;
+      T v = T(0);
+      if (i < g.mx) {
+        v = -resid_el<DIM, T>(g, w, nb, e, i, jkb, T(0));
+        acc = fma(el(nb.c, e), v, acc);
+      }
+      set_el(o, e, v);
+    }
+    st4(pnew + n, nb.c);
+    st4(wv + n, o);
+  };
+  march_src<DIM, T>(g, s, p, src, op);
+  double v1[1] = {(double)acc};
+  reduce_and_finalize<1>(v1, red, slot, st, FIN_PW, nullptr);
 }
 
 // ------------------------------------------------------------------ grid transfers
@@ -373,7 +456,7 @@ __global__ void __launch_bounds__(256) v_restrict(Geom gf, Geom g, Slots s, KspS
 // 2K, 2K+1 (those inside the fine grid).  The x-interpolated coarse rows J and
 // J+1 of plane K+1 are kept for the next plane (one plane window).
 template <int DIM, typename T>
-__global__ void __launch_bounds__(256) v_prolong(Geom gf, Geom g, Slots s, KspState *st, const T *__restrict__ xc,
+__global__ void __launch_bounds__(256, 4) v_prolong(Geom gf, Geom g, Slots s, KspState *st, const T *__restrict__ xc,
                                                  T *__restrict__ xf) {
   if (ksp_done_v(st)) return;
   const SlotPos p = slot_pos(g, s);
