@@ -215,6 +215,40 @@ int fishgpu_solve_host(const fishgpu_opts *o, const double *f_host, const double
 int fishgpu_solver_time_kernel(fishgpu_solver *s, const char *name, int reps,
                                double *ms_per_launch, double *bytes_per_launch);
 
+/* ---- batches: many independent 2D problems of uneven sizes -------------
+   -Laplace(u) = f on the unit square, u = 0 on the boundary, fish's 5-point
+   discretisation (cx = cy = 1), n x n nodes with n = 2^k + 1.  Solved with
+   the mixed form (FP64 refinement around FP32 CG + FP32 V-cycle, levels down
+   to 3 x 3).  Instances of one size run together: one launch per multigrid
+   phase covers all of them; size groups run concurrently. */
+typedef struct {
+  double rtol, atol;      /* on the FP64 true residual, per instance      */
+  double inner_rtol;      /* FP32 inner CG floor                          */
+  int inner_max_it;       /* per refinement step                          */
+  int outer_max_it;
+  int smooth_its;         /* Chebyshev/Jacobi steps per level (2: V(2,2)) */
+  int mg_cycles;          /* 1 = V, 2 = W                                 */
+  double esteig[4];
+  int tune;               /* pick each level's block size by timing       */
+} fishgpu_batch_opts;
+
+typedef struct {
+  int ninst, groups, converged, max_outer, max_inner;
+  long long total_inner_its, dofs, launches;
+  double solve_ms;
+} fishgpu_batch_report;
+
+typedef struct fishgpu_batch_s fishgpu_batch;
+
+int fishgpu_batch_opts_default(fishgpu_batch_opts *o);
+/* n[q]: nodes per side of instance q (2^k + 1); allocates every hierarchy */
+int fishgpu_batch_create(const fishgpu_batch_opts *o, int ninst, const int *n, fishgpu_batch **out);
+/* f[q], u[q]: device pointers to dense n[q] x n[q] arrays (x fastest) */
+int fishgpu_batch_solve(fishgpu_batch *b, const double *const *f, double *const *u, fishgpu_batch_report *rep);
+/* per-instance results of the last solve (host arrays of ninst, any may be NULL) */
+int fishgpu_batch_results(const fishgpu_batch *b, int *inner_its, int *outer_its, double *rel_resid, int *reason);
+int fishgpu_batch_destroy(fishgpu_batch *b);
+
 #ifdef __cplusplus
 }
 #endif

@@ -92,6 +92,18 @@ class Report(ctypes.Structure):
         return [self.hist[i] for i in range(min(self.nhist, MAX_HIST))]
 
 
+class BatchOpts(ctypes.Structure):
+    _fields_ = [("rtol", c_double), ("atol", c_double), ("inner_rtol", c_double), ("inner_max_it", c_int),
+                ("outer_max_it", c_int), ("smooth_its", c_int), ("mg_cycles", c_int), ("esteig", c_double * 4),
+                ("tune", c_int)]
+
+
+class BatchReport(ctypes.Structure):
+    _fields_ = [("ninst", c_int), ("groups", c_int), ("converged", c_int), ("max_outer", c_int),
+                ("max_inner", c_int), ("total_inner_its", c_ll), ("dofs", c_ll), ("launches", c_ll),
+                ("solve_ms", c_double)]
+
+
 class FishError(RuntimeError):
     def __init__(self, code, what=""):
         self.code = code
@@ -138,6 +150,14 @@ def load():
     lib.fishgpu_solve_host.argtypes = [_P(Opts), c_void_p, c_void_p, c_void_p, _P(Report)]
     lib.fishgpu_solver_solve_host.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, _P(Report)]
     lib.fishgpu_solver_solve_host.restype = c_int
+    lib.fishgpu_batch_opts_default.argtypes = [_P(BatchOpts)]
+    lib.fishgpu_batch_create.argtypes = [_P(BatchOpts), c_int, _P(c_int), _P(c_void_p)]
+    lib.fishgpu_batch_solve.argtypes = [c_void_p, _P(c_void_p), _P(c_void_p), _P(BatchReport)]
+    lib.fishgpu_batch_results.argtypes = [c_void_p, _P(c_int), _P(c_int), _P(c_double), _P(c_int)]
+    lib.fishgpu_batch_destroy.argtypes = [c_void_p]
+    for name in ("fishgpu_batch_opts_default", "fishgpu_batch_create", "fishgpu_batch_solve",
+                 "fishgpu_batch_results", "fishgpu_batch_destroy"):
+        getattr(lib, name).restype = c_int
     lib.fishgpu_solver_time_kernel.argtypes = [c_void_p, ctypes.c_char_p, c_int, _P(c_double), _P(c_double)]
     for name in ("FormUExact_gpu", "InitialState_gpu", "ErrorNorms_gpu", "fishgpu_opts_default",
                  "fishgpu_opts_parse", "fishgpu_solver_create", "fishgpu_solver_solve",
@@ -295,6 +315,58 @@ class Solver:
     def close(self):
         if self._h:
             load().fishgpu_solver_destroy(self._h)
+            self._h = c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Many independent 2D problems -Laplace(u) = f, u = 0 on the boundary of the
+    unit square, n x n nodes (n = 2^k + 1), solved together (mixed form)."""
+
+    def __init__(self, sizes, rtol=1e-8, tune=True, **kw):
+        o = BatchOpts()
+        _check(load().fishgpu_batch_opts_default(ctypes.byref(o)), "fishgpu_batch_opts_default")
+        o.rtol = rtol
+        o.tune = int(bool(tune))
+        for k, v in kw.items():
+            setattr(o, k, v)
+        self.sizes = [int(n) for n in sizes]
+        arr = (c_int * len(self.sizes))(*self.sizes)
+        self._h = c_void_p()
+        _check(load().fishgpu_batch_create(ctypes.byref(o), len(self.sizes), arr, ctypes.byref(self._h)),
+               "fishgpu_batch_create")
+
+    def solve(self, fs, us):
+        """fs, us: lists of contiguous CUDA float64 tensors (n, n)."""
+        n = len(self.sizes)
+        fa = (c_void_p * n)(*[_ptr(f) for f in fs])
+        ua = (c_void_p * n)(*[_ptr(u) for u in us])
+        rep = BatchReport()
+        rc = load().fishgpu_batch_solve(self._h, fa, ua, ctypes.byref(rep))
+        if rc not in (0, 4):
+            raise FishError(rc, "fishgpu_batch_solve")
+        return rep
+
+    def results(self):
+        n = len(self.sizes)
+        a, b, c, d = (c_int * n)(), (c_int * n)(), (c_double * n)(), (c_int * n)()
+        _check(load().fishgpu_batch_results(self._h, a, b, c, d), "fishgpu_batch_results")
+        return list(a), list(b), list(c), list(d)
+
+    def close(self):
+        if self._h:
+            load().fishgpu_batch_destroy(self._h)
             self._h = c_void_p()
 
     def __enter__(self):

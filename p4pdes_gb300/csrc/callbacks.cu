@@ -171,6 +171,7 @@ static int scratch_alloc(cudaStream_t s, int nblocks, int nv, Reducer *red, doub
   red->partials = (double *)p;
   red->tickets = (unsigned int *)(p + part);
   red->cap = nblocks;
+  red->tcap = 1;
   if (extra) *extra = (double *)(p + part + 64);
   if (cudaMemsetAsync(p + part, 0, 64 + sizeof(double) * (size_t)nextra, s) != cudaSuccess)
     return FISHGPU_ERR_CUDA;

@@ -67,6 +67,7 @@ struct KspState {
   int pad_;
   double dp, rnorm0, ttol, beta, betaold, dpi, dpiold, alpha;
   double acc[4];
+  unsigned int *ndone;  // batches: incremented once when this instance stops
   double hist[FISHGPU_MAX_HIST];
 };
 
@@ -75,6 +76,7 @@ struct Reducer {
   double *partials;
   unsigned int *tickets;
   int cap;   // capacity per value
+  int tcap;  // tickets per slot (batched reductions: one per plane)
 };
 
 // ---------------------------------------------------------------- problems
@@ -194,6 +196,7 @@ __device__ inline void ksp_push(KspState *st, double dp) {
 __device__ inline void ksp_stop(KspState *st, int reason) {
   st->reason = reason;
   st->done = 1;
+  if (st->ndone) atomicAdd(st->ndone, 1u);
 }
 
 // Scalar part of one KSPCG step (the PETSc cg.c algorithm), run by one thread
@@ -280,7 +283,7 @@ __device__ __forceinline__ void reduce_and_finalize(double (&v)[NV], Reducer red
 #pragma unroll
     for (int q = 0; q < NV; q++) red.partials[(slot * NV + q) * red.cap + bid] = v[q];
     __threadfence();
-    unsigned int t = atomicAdd(&red.tickets[slot], 1u);
+    unsigned int t = atomicAdd(&red.tickets[(size_t)slot * (red.tcap > 1 ? red.tcap : 1)], 1u);
     am_last = (t == (unsigned)(nb - 1));
   }
   __syncthreads();
@@ -294,7 +297,7 @@ __device__ __forceinline__ void reduce_and_finalize(double (&v)[NV], Reducer red
   }
   block_sum<NV>(s);
   if (tid == 0) {
-    red.tickets[slot] = 0u;
+    red.tickets[(size_t)slot * (red.tcap > 1 ? red.tcap : 1)] = 0u;
     if (st || fin == FIN_STORE) ksp_finalize(st, fin, s, NV, out);
   }
 }

@@ -277,14 +277,22 @@ __global__ void __launch_bounds__(256) k_prolong(Geom g, Geom gc, Tiles tm, KspS
 // Lambda = sum_d sc_d (2 - 2cos(k_d pi/(n_d+1))).  S and 1/Lambda come from
 // the host (setup); work holds 2 * prod(n_d) entries.
 template <int DIM, typename T>
-__global__ void __launch_bounds__(1024) k_coarse(Geom g, KspState *st, const T *__restrict__ b,
+__global__ void __launch_bounds__(1024) k_coarse(Geom g, KspState *st, int batch, const T *__restrict__ b,
                                                  T *__restrict__ x, const T *__restrict__ S0,
                                                  const T *__restrict__ S1, const T *__restrict__ S2,
-                                                 const T *__restrict__ ilam, T *work, int n0, int n1,
-                                                 int n2) {
+                                                 const T *__restrict__ ilam, T *work, int n0, int n1, int n2) {
+  // 3D: one block for the grid; 1D/2D: block q solves k-plane q (a batch of
+  // independent instances when batch != 0, else the single plane)
+  const int plane = DIM < 3 ? (int)blockIdx.x : 0;
+  if (batch && st) st += plane;
   if (ksp_done(st)) return;
+  if (DIM < 3) {
+    b += (long long)plane * g.plane;
+    x += (long long)plane * g.plane;
+  }
   const int tid = threadIdx.x, nt = blockDim.x;
-  const long long N = (long long)g.mx * g.my * g.mz;
+  const int mzl = DIM < 3 ? 1 : g.mz;
+  const long long N = (long long)g.mx * g.my * mzl;
   const T dinv = (T)(1.0 / g.scdiag);
   for (long long q = tid; q < N; q += nt) {
     int i = (int)(q % g.mx), j = (int)((q / g.mx) % g.my), k = (int)(q / ((long long)g.mx * g.my));
@@ -293,7 +301,7 @@ __global__ void __launch_bounds__(1024) k_coarse(Geom g, KspState *st, const T *
   }
   const int ni = n0 * n1 * n2;
   if (ni <= 0) return;
-  T *A = work, *B = work + ni;
+  T *A = work + (size_t)blockIdx.x * 2 * ni, *B = A + ni;
   const int oj = DIM >= 2 ? 1 : 0, ok = DIM >= 3 ? 1 : 0;
   __syncthreads();
   for (int q = tid; q < ni; q += nt) {

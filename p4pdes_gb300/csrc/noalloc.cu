@@ -91,6 +91,7 @@ static int apply_noalloc(const fishgpu_info *info, const double *p, double *q, d
   red.partials = (double *)base;
   red.tickets = (unsigned int *)(base + sizeof(double) * NOALLOC_MAX_BLOCKS);
   red.cap = (int)L.grid.x;
+  red.tcap = 1;
   if (cudaMemsetAsync(red.tickets, 0, NOALLOC_TICKET_BYTES, s) != cudaSuccess) return FISHGPU_ERR_CUDA;
   k_apply<DIM, double, true><<<L.grid, L.block, 0, s>>>(g, R, L.tm, nullptr, p, q, red, 0, FIN_STORE, pq_dot);
   return cudaGetLastError() == cudaSuccess ? FISHGPU_OK : FISHGPU_ERR_CUDA;

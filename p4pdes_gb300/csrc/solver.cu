@@ -22,6 +22,10 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
+#include <map>
+#include <mutex>
+#include <thread>
 #include <vector>
 
 #include "common.cuh"
@@ -121,7 +125,12 @@ struct fishgpu_solver_s {
   long long n_init = 0, n_iter = 0;      // kernel nodes of the two graphs
   long long launches = 0;                // kernels launched by the current solve
   int giters = 1;
+  int ksp_norm = FISHGPU_NORM_PRECONDITIONED;  // norm of the CG loop the graphs are built for
   double *f_own = nullptr, *g_own = nullptr, *u_own = nullptr;  // FISHGPU_USER, host-array form
+  // batch groups: 2D instances of one size stacked as k-planes
+  int batch = 0, nplanes = 1;
+  unsigned int *ndone = nullptr;
+  double *scl = nullptr, *iscl = nullptr;    // per-plane refinement scales (device)
   std::vector<void *> allocs;
   long long bytes = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -160,8 +169,9 @@ static int build_hier(fishgpu_solver *S, Hier<T> &H) {
   Geom g = S->fine;
   for (int l = L - 1; l >= 0; l--) {
     Level<T> &lv = H.lev[l];
+    if (S->batch) g.mz = S->nplanes;  // a batch keeps its instances as planes on every level
     lv.g = g;
-    lv.sl = make_slots(g, ZC);
+    lv.sl = make_slots(g, ZC, 2432, 256, S->batch);
     double lmin, lmax;
     spectrum(g, &lmin, &lmax);
     lv.emin = o.esteig[0] * lmin + o.esteig[1] * lmax;
@@ -207,7 +217,8 @@ static int build_hier(fishgpu_solver *S, Hier<T> &H) {
           for (int d = 0; d < c.g.dim; d++) lam += c.g.sc[d] * (2.0 - 2.0 * cos(M_PI * (q[d] + 1) / (c.n[d] + 1)));
           hl[((size_t)k * c.n[1] + j) * c.n[0] + i] = (T)(1.0 / lam);
         }
-    if ((rc = dalloc(S, &c.ilam, (size_t)ni)) || (rc = dalloc(S, &c.work, 2 * (size_t)ni))) return rc;
+    const size_t nwork = 2 * (size_t)ni * (c.g.dim < 3 ? (size_t)c.g.mz : 1);  // one work area per block
+    if ((rc = dalloc(S, &c.ilam, (size_t)ni)) || (rc = dalloc(S, &c.work, nwork))) return rc;
     if (cudaMemcpy(c.ilam, hl.data(), sizeof(T) * ni, cudaMemcpyHostToDevice) != cudaSuccess)
       return FISHGPU_ERR_CUDA;
     for (int d = c.g.dim; d < 3; d++) c.S[d] = c.S[0];  // unused
@@ -239,12 +250,12 @@ static void enq_smooth(fishgpu_solver *S, Level<T> &lv, bool from_zero, int dots
       const int nxt = (cur + 1) % 3;
       const bool last = it == o.smooth_its - 1 && dots >= 0;
       if (from_zero && it == 0)
-        v_scale<T><<<gf, 256, 0, s>>>(lv.sl.tot4, st, lv.b, crd, lv.X[nxt]);
+        v_scale<T><<<gb, lv.sl.chunk, 0, s>>>(lv.g, lv.sl, st, lv.b, crd, lv.X[nxt]);
       else if (last)
-        v_cheb<DIM, T, false, true><<<gb, 256, 0, s>>>(lv.g, lv.sl, st, lv.b, nullptr, lv.X[cur], lv.X[nxt], T(0), T(1),
+        v_cheb<DIM, T, false, true><<<gb, lv.sl.chunk, 0, s>>>(lv.g, lv.sl, st, lv.b, nullptr, lv.X[cur], lv.X[nxt], T(0), T(1),
                                                        crd, S->red, 0, fin);
       else
-        v_cheb<DIM, T, false><<<gb, 256, 0, s>>>(lv.g, lv.sl, st, lv.b, nullptr, lv.X[cur], lv.X[nxt], T(0), T(1), crd);
+        v_cheb<DIM, T, false><<<gb, lv.sl.chunk, 0, s>>>(lv.g, lv.sl, st, lv.b, nullptr, lv.X[cur], lv.X[nxt], T(0), T(1), crd);
       cur = nxt;
     }
     lv.cur = cur;
@@ -259,7 +270,7 @@ static void enq_smooth(fishgpu_solver *S, Level<T> &lv, bool from_zero, int dots
     // x1 = c1 b; x2 = omega x1 + omega c1 (b - A x1) = 2 omega c1 b - omega c1^2 (A b)
     const double ckp1 = 2.0 * mu * mu - 1.0, omega = omegaprod * mu / ckp1;
     const int nxt = (lv.cur + 1) % 3;
-    v_cheb2_zero<DIM, T><<<gb, 256, 0, s>>>(lv.g, lv.sl, st, lv.b, lv.X[nxt], (T)(2.0 * omega * c1),
+    v_cheb2_zero<DIM, T><<<gb, lv.sl.chunk, 0, s>>>(lv.g, lv.sl, st, lv.b, lv.X[nxt], (T)(2.0 * omega * c1),
                                             (T)(omega * c1 * c1));
     lv.cur = nxt;
     return;
@@ -267,15 +278,15 @@ static void enq_smooth(fishgpu_solver *S, Level<T> &lv, bool from_zero, int dots
   int km1 = -1, kk;  // -1: the zero iterate
   if (from_zero) {
     kk = (lv.cur + 1) % 3;
-    v_scale<T><<<gf, 256, 0, s>>>(lv.sl.tot4, st, lv.b, (T)c1, lv.X[kk]);
+    v_scale<T><<<gb, lv.sl.chunk, 0, s>>>(lv.g, lv.sl, st, lv.b, (T)c1, lv.X[kk]);
   } else {
     km1 = lv.cur;
     kk = (lv.cur + 1) % 3;
     if (o.smooth_its == 1 && dots >= 0)
-      v_cheb<DIM, T, false, true><<<gb, 256, 0, s>>>(lv.g, lv.sl, st, lv.b, nullptr, lv.X[km1], lv.X[kk], T(0), T(1),
+      v_cheb<DIM, T, false, true><<<gb, lv.sl.chunk, 0, s>>>(lv.g, lv.sl, st, lv.b, nullptr, lv.X[km1], lv.X[kk], T(0), T(1),
                                                      (T)c1, S->red, 0, fin);
     else
-      v_cheb<DIM, T, false><<<gb, 256, 0, s>>>(lv.g, lv.sl, st, lv.b, nullptr, lv.X[km1], lv.X[kk], T(0), T(1), (T)c1);
+      v_cheb<DIM, T, false><<<gb, lv.sl.chunk, 0, s>>>(lv.g, lv.sl, st, lv.b, nullptr, lv.X[km1], lv.X[kk], T(0), T(1), (T)c1);
   }
   double ckm1 = 1.0, ck = mu;
   for (int it = 1; it < o.smooth_its; it++) {
@@ -285,13 +296,13 @@ static void enq_smooth(fishgpu_solver *S, Level<T> &lv, bool from_zero, int dots
     const int out = km1 < 0 ? (kk + 1) % 3 : third(km1, kk);
     const bool last = it == o.smooth_its - 1 && dots >= 0;
     if (km1 < 0)
-      v_cheb<DIM, T, false><<<gb, 256, 0, s>>>(lv.g, lv.sl, st, lv.b, nullptr, lv.X[kk], lv.X[out], T(0), (T)omega,
+      v_cheb<DIM, T, false><<<gb, lv.sl.chunk, 0, s>>>(lv.g, lv.sl, st, lv.b, nullptr, lv.X[kk], lv.X[out], T(0), (T)omega,
                                                (T)(omega * c1));
     else if (last)
-      v_cheb<DIM, T, true, true><<<gb, 256, 0, s>>>(lv.g, lv.sl, st, lv.b, lv.X[km1], lv.X[kk], lv.X[out],
+      v_cheb<DIM, T, true, true><<<gb, lv.sl.chunk, 0, s>>>(lv.g, lv.sl, st, lv.b, lv.X[km1], lv.X[kk], lv.X[out],
                                                     (T)(1.0 - omega), (T)omega, (T)(omega * c1), S->red, 0, fin);
     else
-      v_cheb<DIM, T, true><<<gb, 256, 0, s>>>(lv.g, lv.sl, st, lv.b, lv.X[km1], lv.X[kk], lv.X[out],
+      v_cheb<DIM, T, true><<<gb, lv.sl.chunk, 0, s>>>(lv.g, lv.sl, st, lv.b, lv.X[km1], lv.X[kk], lv.X[out],
                                               (T)(1.0 - omega), (T)omega, (T)(omega * c1));
     km1 = kk;
     kk = out;
@@ -308,16 +319,16 @@ static void enq_vcycle(fishgpu_solver *S, Hier<T> &H, int l, bool from_zero, int
   KspState *st = S->st;
   if (l == 0) {
     lv.cur = 0;
-    k_coarse<DIM, T><<<1, 1024, 0, s>>>(lv.g, st, lv.b, lv.X[0], lv.S[0], lv.S[1], lv.S[2], lv.ilam, lv.work,
+    k_coarse<DIM, T><<<DIM < 3 ? lv.g.mz : 1, 1024, 0, s>>>(lv.g, st, lv.sl.batch, lv.b, lv.X[0], lv.S[0], lv.S[1], lv.S[2], lv.ilam, lv.work,
                                         lv.n[0], lv.n[1], lv.n[2]);
     return;
   }
   Level<T> &lc = H.lev[l - 1];
   enq_smooth<DIM, T>(S, lv, from_zero);
-  v_resid<DIM, T><<<slot_blocks(lv.sl), 256, 0, s>>>(lv.g, lv.sl, st, lv.b, lv.X[lv.cur], lv.r);
-  v_restrict<DIM, T><<<slot_blocks(lc.sl), 256, 0, s>>>(lv.g, lc.g, lc.sl, st, lv.r, lc.b);
+  v_resid<DIM, T><<<slot_blocks(lv.sl), lv.sl.chunk, 0, s>>>(lv.g, lv.sl, st, lv.b, lv.X[lv.cur], lv.r);
+  v_restrict<DIM, T><<<slot_blocks(lc.sl), lc.sl.chunk, 0, s>>>(lv.g, lc.g, lc.sl, st, lv.r, lc.b);
   for (int c = 0; c < S->o.mg_cycles; c++) enq_vcycle<DIM, T>(S, H, l - 1, c == 0);
-  v_prolong<DIM, T><<<slot_blocks(lc.sl), 256, 0, s>>>(lv.g, lc.g, lc.sl, st, lc.X[lc.cur], lv.X[lv.cur]);
+  v_prolong<DIM, T><<<slot_blocks(lc.sl), lc.sl.chunk, 0, s>>>(lv.g, lc.g, lc.sl, st, lc.X[lc.cur], lv.X[lv.cur]);
   enq_smooth<DIM, T>(S, lv, false, dots);
 }
 
@@ -329,12 +340,12 @@ static bool enq_pc(fishgpu_solver *S, Hier<T> &H, const T *r, int dots) {
   const fishgpu_opts &o = S->o;
   const long long tot4 = S->sf.tot4;
   if (o.pc_type == FISHGPU_PC_NONE) {
-    v_scale<T><<<S->gfl, 256, 0, S->stream>>>(tot4, S->st, r, T(1), H.zbuf);
+    v_scale<T><<<slot_blocks(S->sf), S->sf.chunk, 0, S->stream>>>(S->fine, S->sf, S->st, r, T(1), H.zbuf);
     H.z = H.zbuf;
     return false;
   }
   if (o.pc_type == FISHGPU_PC_JACOBI) {  // z = D^{-1} r
-    v_scale<T><<<S->gfl, 256, 0, S->stream>>>(tot4, S->st, r, (T)(1.0 / S->fine.scdiag), H.zbuf);
+    v_scale<T><<<slot_blocks(S->sf), S->sf.chunk, 0, S->stream>>>(S->fine, S->sf, S->st, r, (T)(1.0 / S->fine.scdiag), H.zbuf);
     H.z = H.zbuf;
     return false;
   }
@@ -356,11 +367,11 @@ template <int DIM, typename T>
 static void enq_cg_init(fishgpu_solver *S, Hier<T> &H, KspVecs<T> v) {
   cudaStream_t s = S->stream;
   const long long tot4 = S->sf.tot4;
-  v_zero<T><<<S->gfl, 256, 0, s>>>(tot4, v.y);
-  if (S->o.norm_type == FISHGPU_NORM_UNPRECONDITIONED)
-    v_dots<T><<<S->gfl, 256, 0, s>>>(tot4, S->st, v.r, v.r, S->red, 0, FIN_INIT_RR, nullptr);
+  v_zero<T><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(S->fine, S->sf, v.y);
+  if (S->ksp_norm == FISHGPU_NORM_UNPRECONDITIONED)
+    v_dots<T><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(S->fine, S->sf, S->st, v.r, v.r, S->red, 0, FIN_INIT_RR, nullptr);
   if (!enq_pc<DIM, T>(S, H, v.r, FIN_INIT_ZZZR))
-    v_dots<T><<<S->gfl, 256, 0, s>>>(tot4, S->st, H.z, v.r, S->red, 0, FIN_INIT_ZZZR, nullptr);
+    v_dots<T><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(S->fine, S->sf, S->st, H.z, v.r, S->red, 0, FIN_INIT_ZZZR, nullptr);
 }
 
 // One CG iteration; `par` selects which p buffer holds the previous direction.
@@ -372,13 +383,13 @@ static void enq_cg_iter(fishgpu_solver *S, Hier<T> &H, KspVecs<T> v, int par) {
   const unsigned gf = S->gfl;
   T *pold = v.p[par], *pnew = v.p[1 - par];
   // p = z + beta/betaold p (z of the previous application), w = A p, p.w
-  v_cgp_apply<DIM, T><<<slot_blocks(S->sf), 256, 0, s>>>(S->fine, S->sf, st, H.z, pold, pnew, v.w, S->red, 0);
-  if (S->o.norm_type == FISHGPU_NORM_UNPRECONDITIONED)
-    v_cg_xr<T, true><<<gf, 256, 0, s>>>(tot4, st, pnew, v.w, v.y, v.r, S->red, 0);
+  v_cgp_apply<DIM, T><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(S->fine, S->sf, st, H.z, pold, pnew, v.w, S->red, 0);
+  if (S->ksp_norm == FISHGPU_NORM_UNPRECONDITIONED)
+    v_cg_xr<T, true><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(S->fine, S->sf, st, pnew, v.w, v.y, v.r, S->red, 0);
   else
-    v_cg_xr<T, false><<<gf, 256, 0, s>>>(tot4, st, pnew, v.w, v.y, v.r, S->red, 0);
+    v_cg_xr<T, false><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(S->fine, S->sf, st, pnew, v.w, v.y, v.r, S->red, 0);
   if (!enq_pc<DIM, T>(S, H, v.r, FIN_ZZZR))
-    v_dots<T><<<gf, 256, 0, s>>>(tot4, st, H.z, v.r, S->red, 0, FIN_ZZZR, nullptr);
+    v_dots<T><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(S->fine, S->sf, st, H.z, v.r, S->red, 0, FIN_ZZZR, nullptr);
 }
 
 static long long kernel_nodes(cudaGraph_t g) {
@@ -426,8 +437,9 @@ static void reset_state(fishgpu_solver *S, double rtol, double atol, double dtol
 // CG solve of J y = r from y = 0 (r is overwritten), on the solver's stream.
 // The caller reads S->st_h for its, reason and the history.
 template <int DIM, typename T>
-static int run_ksp(fishgpu_solver *S, Hier<T> &H, KspVecs<T> v, double rtol, int max_it, int norm) {
+static int run_ksp(fishgpu_solver *S, Hier<T> &H, KspVecs<T> v, double rtol, int max_it) {
   cudaStream_t s = S->stream;
+  const int norm = S->ksp_norm;  // the captured graphs compute this norm
   int rc;
   if (!S->gexec_init &&
       (rc = capture(S, [&] { enq_cg_init<DIM, T>(S, H, v); }, &S->gexec_init, &S->n_init)))
@@ -533,7 +545,7 @@ static void fill_from_state(const KspState *h, fishgpu_report *rep) {
 
 // sum of squares of the padded FP64 vector a into dval[slot]
 static void enq_norm2(fishgpu_solver *S, const double *a, int slot) {
-  v_dots<double><<<S->gfl, 256, 0, S->stream>>>(S->sf.tot4, nullptr, a, a, S->red, 1, FIN_STORE, S->dval + slot);
+  v_dots<double><<<slot_blocks(S->sf), S->sf.chunk, 0, S->stream>>>(S->fine, S->sf, nullptr, a, a, S->red, 1, FIN_STORE, S->dval + slot);
 }
 
 template <int DIM>
@@ -555,7 +567,7 @@ static int solve_dim(fishgpu_solver *S, double *u, fishgpu_report *rep) {
   }
   // the KSP right-hand side is -F(u0) = beff - A u0; it solves for -y and u = u0 + (-y)
   double *F = o.precision == FISHGPU_MIXED ? S->b64 : S->r64;
-  v_resid<DIM, double><<<slot_blocks(S->sf), 256, 0, s>>>(g, S->sf, nullptr, S->beff, S->u64, F);
+  v_resid<DIM, double><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(g, S->sf, nullptr, S->beff, S->u64, F);
   enq_norm2(S, F, 0);
   FG_CUDA(cudaGetLastError());
   int rc = read_vals(S, 1);
@@ -564,7 +576,7 @@ static int solve_dim(fishgpu_solver *S, double *u, fishgpu_report *rep) {
   rep->fnorm0 = bn;
   if (o.precision == FISHGPU_FP64) {
     KspVecs<double> v{S->r64, {S->p64, S->q64}, S->w64, S->y64};
-    if ((rc = run_ksp<DIM, double>(S, S->h64, v, o.rtol, o.max_it, o.norm_type))) return rc;
+    if ((rc = run_ksp<DIM, double>(S, S->h64, v, o.rtol, o.max_it))) return rc;
     fill_from_state(S->st_h, rep);
     rep->outer_its = 0;
   } else {
@@ -572,7 +584,7 @@ static int solve_dim(fishgpu_solver *S, double *u, fishgpu_report *rep) {
     const double ttol = fmax(o.rtol * bn, o.atol);
     double rn = bn;
     int reason = 0, its = 0, outer = 0, nh = 0;
-    v_zero<double><<<gfl, 256, 0, s>>>(tot4, S->y64);
+    v_zero<double><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(g, S->sf, S->y64);
     S->launches += 1;
     rep->hist[nh++] = rn;
     KspVecs<float> v{S->r32, {S->p32, S->q32}, S->w32, S->y32};
@@ -589,13 +601,13 @@ static int solve_dim(fishgpu_solver *S, double *u, fishgpu_report *rep) {
       if (rn <= ttol) { reason = rn < o.atol ? R_CONVERGED_ATOL : R_CONVERGED_RTOL; break; }
       if (outer >= o.outer_max_it || its >= o.max_it) { reason = R_DIVERGED_ITS; break; }
       const double *rsrc = outer == 0 ? S->b64 : S->r64;
-      v_demote<<<gfl, 256, 0, s>>>(tot4, rsrc, 1.0 / rn, S->r32);
+      v_demote<<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(g, S->sf, rsrc, nullptr, 1.0 / rn, S->r32);
       S->launches += 4;  // demote, promote-add, FP64 residual, its norm
       // inner tolerance: what is still needed, never below the FP32 floor
       double irtol = fmax(o.inner_rtol, 0.5 * ttol / rn);
       if (outer == 0) irtol = fmax(irtol, first_floor);
       if (irtol > 0.5) irtol = 0.5;
-      if ((rc = run_ksp<DIM, float>(S, S->h32, v, irtol, o.inner_max_it, FISHGPU_NORM_UNPRECONDITIONED))) return rc;
+      if ((rc = run_ksp<DIM, float>(S, S->h32, v, irtol, o.inner_max_it))) return rc;
       const KspState *h = S->st_h;
       its += h->its;
       if (outer < FISHGPU_MAX_OUTER) rep->inner_its[outer] = h->its;
@@ -604,9 +616,9 @@ static int solve_dim(fishgpu_solver *S, double *u, fishgpu_report *rep) {
         reason = h->reason;
         break;
       }
-      v_promote_add<<<gfl, 256, 0, s>>>(tot4, S->y32, rn, S->y64);
+      v_promote_add<<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(g, S->sf, S->y32, nullptr, rn, S->y64);
       // FP64 true residual r = b - J y and its norm
-      v_resid<DIM, double><<<slot_blocks(S->sf), 256, 0, s>>>(g, S->sf, nullptr, S->b64, S->y64, S->r64);
+      v_resid<DIM, double><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(g, S->sf, nullptr, S->b64, S->y64, S->r64);
       enq_norm2(S, S->r64, 0);
       FG_CUDA(cudaGetLastError());
       if ((rc = read_vals(S, 1))) return rc;
@@ -621,7 +633,7 @@ static int solve_dim(fishgpu_solver *S, double *u, fishgpu_report *rep) {
     rep->nhist = nh;
   }
   // u = u0 + (-y), then the caller's dense copy
-  v_add<<<gfl, 256, 0, s>>>(tot4, S->y64, S->u64);
+  v_add<<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(g, S->sf, S->y64, S->u64);
   k_unpack64<DIM><<<L.grid, L.block, 0, s>>>(g, S->dense, L.tm, S->u64, u);
   S->launches += 2;  // update, unpack
   if (o.precision == FISHGPU_MIXED) {
@@ -630,7 +642,7 @@ static int solve_dim(fishgpu_solver *S, double *u, fishgpu_report *rep) {
     rep->fnorm1 = rep->nhist > 0 ? rep->hist[(rep->nhist < FISHGPU_MAX_HIST ? rep->nhist : FISHGPU_MAX_HIST) - 1] : bn;
   } else {
     // F(u) for the final SNES norm (r64 is free now)
-    v_resid<DIM, double><<<slot_blocks(S->sf), 256, 0, s>>>(g, S->sf, nullptr, S->beff, S->u64, S->r64);
+    v_resid<DIM, double><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(g, S->sf, nullptr, S->beff, S->u64, S->r64);
     enq_norm2(S, S->r64, 1);
     S->launches += 2;
     FG_CUDA(cudaEventRecord(S->ev1, s));
@@ -647,10 +659,7 @@ static int solve_dim(fishgpu_solver *S, double *u, fishgpu_report *rep) {
 }
 
 // Largest grid of a reduction kernel on the fine level.
-static int reduction_blocks(const fishgpu_solver *S) {
-  int a = (int)slot_blocks(S->sf), b = (int)S->gfl;
-  return a > b ? a : b;
-}
+static int reduction_blocks(const fishgpu_solver *S) { return (int)slot_blocks(S->sf); }
 
 template <int DIM>
 static int time_kernel_dim(fishgpu_solver *S, const char *name, int reps, double *ms, double *bytes) {
@@ -671,48 +680,48 @@ static int time_kernel_dim(fishgpu_solver *S, const char *name, int reps, double
   for (int q = 0; q < reps; q++) {
     if (!strcmp(name, "smooth")) {  // one Chebyshev step with x_{k-1}: reads b, x_{k-1}, x_k, writes x_{k+1}
       if (mixed)
-        v_cheb<DIM, float, true><<<gb, 256, 0, s>>>(g, sl, nullptr, S->r32, lf.X[0], lf.X[1], lf.X[2], 0.5f, 0.5f, 0.1f);
+        v_cheb<DIM, float, true><<<gb, sl.chunk, 0, s>>>(g, sl, nullptr, S->r32, lf.X[0], lf.X[1], lf.X[2], 0.5f, 0.5f, 0.1f);
       else
-        v_cheb<DIM, double, true><<<gb, 256, 0, s>>>(g, sl, nullptr, S->r64, ld.X[0], ld.X[1], ld.X[2], 0.5, 0.5, 0.1);
+        v_cheb<DIM, double, true><<<gb, sl.chunk, 0, s>>>(g, sl, nullptr, S->r64, ld.X[0], ld.X[1], ld.X[2], 0.5, 0.5, 0.1);
       *bytes = 4.0 * sz * N;
     } else if (!strcmp(name, "smooth_zero")) {  // two steps from zero: reads b, writes x
       if (mixed)
-        v_cheb2_zero<DIM, float><<<gb, 256, 0, s>>>(g, sl, nullptr, S->r32, lf.X[0], 0.5f, 0.1f);
+        v_cheb2_zero<DIM, float><<<gb, sl.chunk, 0, s>>>(g, sl, nullptr, S->r32, lf.X[0], 0.5f, 0.1f);
       else
-        v_cheb2_zero<DIM, double><<<gb, 256, 0, s>>>(g, sl, nullptr, S->r64, ld.X[0], 0.5, 0.1);
+        v_cheb2_zero<DIM, double><<<gb, sl.chunk, 0, s>>>(g, sl, nullptr, S->r64, ld.X[0], 0.5, 0.1);
       *bytes = 2.0 * sz * N;
     } else if (!strcmp(name, "resid")) {
       if (mixed)
-        v_resid<DIM, float><<<gb, 256, 0, s>>>(g, sl, nullptr, S->r32, lf.X[0], lf.X[1]);
+        v_resid<DIM, float><<<gb, sl.chunk, 0, s>>>(g, sl, nullptr, S->r32, lf.X[0], lf.X[1]);
       else
-        v_resid<DIM, double><<<gb, 256, 0, s>>>(g, sl, nullptr, S->r64, ld.X[0], ld.X[1]);
+        v_resid<DIM, double><<<gb, sl.chunk, 0, s>>>(g, sl, nullptr, S->r64, ld.X[0], ld.X[1]);
       *bytes = 3.0 * sz * N;
     } else if (!strcmp(name, "apply")) {
       if (mixed)
-        v_apply_dot<DIM, float><<<gb, 256, 0, s>>>(g, sl, nullptr, S->p32, S->w32, S->red, 1, FIN_STORE, S->dval + 2);
+        v_apply_dot<DIM, float><<<gb, sl.chunk, 0, s>>>(g, sl, nullptr, S->p32, S->w32, S->red, 1, FIN_STORE, S->dval + 2);
       else
-        v_apply_dot<DIM, double><<<gb, 256, 0, s>>>(g, sl, nullptr, S->p64, S->w64, S->red, 1, FIN_STORE, S->dval + 2);
+        v_apply_dot<DIM, double><<<gb, sl.chunk, 0, s>>>(g, sl, nullptr, S->p64, S->w64, S->red, 1, FIN_STORE, S->dval + 2);
       *bytes = 2.0 * sz * N;
     } else if (!strcmp(name, "cg_update")) {
       if (mixed)
-        v_cg_xr<float, false><<<S->gfl, 256, 0, s>>>(sl.tot4, nullptr, S->p32, S->w32, S->y32, S->r32, S->red, 1);
+        v_cg_xr<float, false><<<gb, sl.chunk, 0, s>>>(g, sl, nullptr, S->p32, S->w32, S->y32, S->r32, S->red, 1);
       else
-        v_cg_xr<double, false><<<S->gfl, 256, 0, s>>>(sl.tot4, nullptr, S->p64, S->w64, S->y64, S->r64, S->red, 1);
+        v_cg_xr<double, false><<<gb, sl.chunk, 0, s>>>(g, sl, nullptr, S->p64, S->w64, S->y64, S->r64, S->red, 1);
       *bytes = 6.0 * sz * N;
     } else if (!strcmp(name, "restrict")) {
       if (mixed)
-        v_restrict<DIM, float><<<slot_blocks(cf.sl), 256, 0, s>>>(g, cf.g, cf.sl, nullptr, lf.X[0], cf.b);
+        v_restrict<DIM, float><<<slot_blocks(cf.sl), cf.sl.chunk, 0, s>>>(g, cf.g, cf.sl, nullptr, lf.X[0], cf.b);
       else
-        v_restrict<DIM, double><<<slot_blocks(cd.sl), 256, 0, s>>>(g, cd.g, cd.sl, nullptr, ld.X[0], cd.b);
+        v_restrict<DIM, double><<<slot_blocks(cd.sl), cd.sl.chunk, 0, s>>>(g, cd.g, cd.sl, nullptr, ld.X[0], cd.b);
       *bytes = sz * N * (1.0 + 1.0 / (1 << DIM));
     } else if (!strcmp(name, "prolong")) {
       if (mixed)
-        v_prolong<DIM, float><<<slot_blocks(cf.sl), 256, 0, s>>>(g, cf.g, cf.sl, nullptr, cf.X[0], lf.X[0]);
+        v_prolong<DIM, float><<<slot_blocks(cf.sl), cf.sl.chunk, 0, s>>>(g, cf.g, cf.sl, nullptr, cf.X[0], lf.X[0]);
       else
-        v_prolong<DIM, double><<<slot_blocks(cd.sl), 256, 0, s>>>(g, cd.g, cd.sl, nullptr, cd.X[0], ld.X[0]);
+        v_prolong<DIM, double><<<slot_blocks(cd.sl), cd.sl.chunk, 0, s>>>(g, cd.g, cd.sl, nullptr, cd.X[0], ld.X[0]);
       *bytes = sz * N * (2.0 + 1.0 / (1 << DIM));
     } else if (!strcmp(name, "residual64")) {
-      v_resid<DIM, double><<<gb, 256, 0, s>>>(g, sl, nullptr, S->r64, S->y64, S->u64);
+      v_resid<DIM, double><<<gb, sl.chunk, 0, s>>>(g, sl, nullptr, S->r64, S->y64, S->u64);
       *bytes = 3.0 * 8.0 * N;
     } else {
       return FISHGPU_ERR_ARG;
@@ -799,6 +808,9 @@ extern "C" int fishgpu_solver_create(const fishgpu_opts *o, void *stream, fishgp
   // iterations per graph launch: even, since consecutive iterations alternate the two p buffers
   S->giters = o->graph_iters > 0 ? o->graph_iters : (dofs >= (1LL << 20) ? 2 : 4);
   S->giters += S->giters & 1;
+  // FP64 form: the user's norm; mixed form: the inner CG stops on its own
+  // (unpreconditioned) residual, which the refinement loop relates to the true one
+  S->ksp_norm = o->precision == FISHGPU_MIXED ? FISHGPU_NORM_UNPRECONDITIONED : o->norm_type;
 #define CK(x)                            \
   do {                                   \
     if ((rc = (x)) != FISHGPU_OK) {      \
@@ -818,6 +830,7 @@ extern "C" int fishgpu_solver_create(const fishgpu_opts *o, void *stream, fishgp
   CK(dalloc(S, &S->red.partials, (size_t)2 * 2 * cap));  // two slots of up to two values
   CK(dalloc(S, &S->red.tickets, 4));
   S->red.cap = cap;
+  S->red.tcap = 1;
   CK(dalloc(S, &S->u64, N));
   CK(dalloc(S, &S->beff, N));
   CK(dalloc(S, &S->y64, N));
@@ -951,4 +964,484 @@ extern "C" int fishgpu_solver_time_kernel(fishgpu_solver *S, const char *name, i
   case 2: return time_kernel_dim<2>(S, name, reps, ms_per_launch, bytes_per_launch);
   default: return time_kernel_dim<3>(S, name, reps, ms_per_launch, bytes_per_launch);
   }
+}
+
+// ====================================================================== batches
+// Thousands of independent 2D problems -Laplace(u) = f on the unit square with
+// u = 0 on the boundary (fish's operator with cx = cy = 1), of uneven sizes
+// n = 2^k + 1.  Instances of one size form a group: a 2D grid whose k-planes
+// are the instances, solved by one set of launches per multigrid phase (every
+// kernel works per plane: own CG state, own reductions, own refinement
+// scale), with the mixed form (FP64 refinement around FP32 CG + V-cycle).
+// Groups run concurrently, each on its own stream and host thread.
+namespace fg {
+
+// f of instance q (dense n x n) -> b = h^2 f on interior nodes, 0 on the boundary
+__global__ void __launch_bounds__(256) k_pack_rhs(Geom g, const double *const *f, double *__restrict__ b) {
+  const long long per = (long long)g.mx * g.my;
+  const int q = blockIdx.y;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < per; t += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(t % g.mx), j = (int)(t / g.mx);
+    const bool bd = i == 0 || j == 0 || i == g.mx - 1 || j == g.my - 1;
+    b[(long long)q * g.plane + (long long)j * g.pitch + i] = bd ? 0.0 : g.vol * f[q][t];
+  }
+}
+
+// u of instance q (dense) from plane q of y
+__global__ void __launch_bounds__(256) k_unpack_planes(Geom g, const double *__restrict__ y, double *const *u) {
+  const long long per = (long long)g.mx * g.my;
+  const int q = blockIdx.y;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < per; t += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(t % g.mx), j = (int)(t / g.mx);
+    u[q][t] = y[(long long)q * g.plane + (long long)j * g.pitch + i];
+  }
+}
+
+// ---------------------------------------------------------------- autotuner
+// Picks the block size (slots per block) of each level of a group by timing
+// one Chebyshev step with each candidate; results are cached per (n, planes).
+static std::mutex g_tune_mu;
+static std::map<std::pair<int, int>, int> g_tune_cache;
+
+static int tune_chunk(fishgpu_solver *S, Level<float> &lv) {
+  const std::pair<int, int> key(lv.g.mx, lv.g.mz);
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune_cache.find(key);
+    if (it != g_tune_cache.end()) return it->second;
+  }
+  static const int cand[3] = {64, 128, 256};
+  int best = 256;
+  float best_ms = 1e30f;
+  cudaStream_t s = S->stream;
+  for (int c = 0; c < 3; c++) {
+    const Slots sl = make_slots(lv.g, ZC, 2432, cand[c], 1);
+    const unsigned gb = slot_blocks(sl);
+    // b = the level's residual buffer, x_{k-1}, x_k, out: its three iterate buffers
+    for (int w = 0; w < 2; w++)
+      v_cheb<2, float, true><<<gb, sl.chunk, 0, s>>>(lv.g, sl, nullptr, lv.r, lv.X[0], lv.X[1], lv.X[2], 0.5f, 0.5f,
+                                                      0.1f);
+    cudaEventRecord(S->ev0, s);
+    for (int r = 0; r < 5; r++)
+      v_cheb<2, float, true><<<gb, sl.chunk, 0, s>>>(lv.g, sl, nullptr, lv.r, lv.X[0], lv.X[1], lv.X[2], 0.5f, 0.5f,
+                                                      0.1f);
+    cudaEventRecord(S->ev1, s);
+    if (cudaEventSynchronize(S->ev1) != cudaSuccess) return 256;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, S->ev0, S->ev1);
+    if (ms < best_ms) { best_ms = ms; best = cand[c]; }
+  }
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune_cache[key] = best;
+  return best;
+}
+
+}  // namespace fg
+
+struct fishgpu_batch_s {
+  fishgpu_batch_opts o;
+  int ninst = 0;
+  std::vector<int> n;                     // nodes per side, per instance
+  std::vector<fishgpu_solver *> groups;   // one per distinct size
+  std::vector<std::vector<int>> members;  // instances of each group, plane order
+  std::vector<int> inner_its, outer_its;
+  std::vector<double> rel_resid;
+  std::vector<int> reason;
+  cudaStream_t user_stream = nullptr;
+};
+
+namespace fg {
+
+static int group_create(const fishgpu_batch_opts &bo, int n, int count, fishgpu_solver **out) {
+  fishgpu_opts o;
+  fishgpu_opts_default(&o);
+  o.ctx.dim = 2;
+  o.ctx.problem = FISHGPU_ZERO;
+  o.mx = o.my = n;
+  o.mz = 1;
+  int levels = 1;
+  for (int m = n; m > 3 && (m - 1) % 2 == 0; m = (m - 1) / 2 + 1) levels++;
+  o.mg_levels = levels;
+  o.pc_type = FISHGPU_PC_MG;
+  o.precision = FISHGPU_MIXED;
+  o.rtol = bo.rtol;
+  o.atol = bo.atol;
+  o.max_it = bo.inner_max_it;
+  o.inner_max_it = bo.inner_max_it;
+  o.outer_max_it = bo.outer_max_it;
+  o.inner_rtol = bo.inner_rtol;
+  o.smooth_its = bo.smooth_its;
+  o.mg_cycles = bo.mg_cycles;
+  for (int q = 0; q < 4; q++) o.esteig[q] = bo.esteig[q];
+  o.graph_iters = 2;
+  o.norm_type = FISHGPU_NORM_UNPRECONDITIONED;
+  fishgpu_solver *S = new fishgpu_solver();
+  S->o = o;
+  S->ksp_norm = FISHGPU_NORM_UNPRECONDITIONED;
+  S->batch = 1;
+  S->nplanes = count;
+  int rc = FISHGPU_OK;
+  if (cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete S;
+    return FISHGPU_ERR_CUDA;
+  }
+  S->own_stream = true;
+  S->dense = make_geom(2, n, n, 1, 1.0, 1.0, 1.0, 1.0, 1.0, 1.0);
+  S->fine = padded(S->dense);
+  S->fine.mz = count;
+  S->sf = make_slots(S->fine, 1, 0, 256, 1);
+  S->Lf = launch_for(S->fine);
+  S->prob = Prob{FISHGPU_ZERO, 2, 1.0, 1.0, 1.0, nullptr, nullptr, S->dense.pitch, S->dense.plane};
+  S->giters = 2;
+  const size_t N = nelem(S->fine);
+#define CK(x)                         \
+  do {                                \
+    if ((rc = (x)) != FISHGPU_OK) {   \
+      fishgpu_solver_destroy(S);      \
+      return rc;                      \
+    }                                 \
+  } while (0)
+  if (cudaMallocHost((void **)&S->st_h, sizeof(KspState) * count) != cudaSuccess ||
+      cudaMallocHost((void **)&S->hval, sizeof(double) * 2 * count) != cudaSuccess ||
+      cudaEventCreate(&S->ev0) != cudaSuccess || cudaEventCreate(&S->ev1) != cudaSuccess) {
+    fishgpu_solver_destroy(S);
+    return FISHGPU_ERR_CUDA;
+  }
+  CK(dalloc(S, &S->st, (size_t)count));
+  CK(dalloc(S, &S->dval, 2 * (size_t)count));
+  CK(dalloc(S, &S->ndone, 1));
+  CK(dalloc(S, &S->scl, (size_t)count));
+  CK(dalloc(S, &S->iscl, (size_t)count));
+  CK(dalloc(S, &S->b64, N));
+  CK(dalloc(S, &S->y64, N));
+  CK(dalloc(S, &S->r64, N));
+  CK(dalloc(S, &S->r32, N));
+  CK(dalloc(S, &S->p32, N));
+  CK(dalloc(S, &S->q32, N));
+  CK(dalloc(S, &S->w32, N));
+  CK(dalloc(S, &S->y32, N));
+  CK(build_hier<float>(S, S->h32));
+  // tune block sizes per level before anything is captured
+  if (bo.tune) {
+    if (cudaStreamSynchronize(S->stream) != cudaSuccess) {
+      fishgpu_solver_destroy(S);
+      return FISHGPU_ERR_CUDA;
+    }
+    for (int l = S->h32.nlev - 1; l >= 1; l--) {
+      Level<float> &lv = S->h32.lev[l];
+      lv.sl = make_slots(lv.g, ZC, 2432, tune_chunk(S, lv), 1);
+    }
+    S->sf = S->h32.lev[S->h32.nlev - 1].sl;
+  }
+  // reductions are over the fine level's blocks, tickets per plane
+  const int cap = (int)slot_blocks(S->sf);
+  CK(dalloc(S, &S->red.partials, (size_t)2 * 2 * cap));
+  CK(dalloc(S, &S->red.tickets, (size_t)2 * count));
+  S->red.cap = cap;
+  S->red.tcap = count;
+#undef CK
+  if (cudaStreamSynchronize(S->stream) != cudaSuccess) {
+    fishgpu_solver_destroy(S);
+    return FISHGPU_ERR_CUDA;
+  }
+  *out = S;
+  return FISHGPU_OK;
+}
+
+// per-plane FP64 norms^2 of a into hval[0..count)
+static int plane_norms(fishgpu_solver *S, const double *a) {
+  v_dots<double><<<slot_blocks(S->sf), S->sf.chunk, 0, S->stream>>>(S->fine, S->sf, nullptr, a, a, S->red, 1,
+                                                                    FIN_STORE, S->dval);
+  FG_CUDA(cudaGetLastError());
+  FG_CUDA(cudaMemcpyAsync(S->hval, S->dval, sizeof(double) * 2 * S->nplanes, cudaMemcpyDeviceToHost, S->stream));
+  FG_CUDA(cudaStreamSynchronize(S->stream));
+  return FISHGPU_OK;
+}
+
+// Batched refinement solve of one group; f, u: device arrays of `count`
+// device pointers.  Results per plane into its/outer/relres/reason.
+static int group_solve(fishgpu_solver *S, const double *const *f, double *const *u, int *its_out, int *outer_out,
+                       double *relres_out, int *reason_out) {
+  const fishgpu_opts &o = S->o;
+  const int count = S->nplanes;
+  cudaStream_t s = S->stream;
+  const Geom &g = S->fine;
+  const unsigned gb = slot_blocks(S->sf);
+  S->launches = 0;
+  {
+    dim3 grid((unsigned)std::min<long long>(((long long)g.mx * g.my + 255) / 256, 64), (unsigned)count);
+    k_pack_rhs<<<grid, 256, 0, s>>>(g, f, S->b64);
+  }
+  v_zero<double><<<gb, S->sf.chunk, 0, s>>>(g, S->sf, S->y64);
+  int rc = plane_norms(S, S->b64);
+  if (rc) return rc;
+  std::vector<double> bn(count), rn(count), ttol(count);
+  std::vector<int> active(count), its(count, 0), outer(count, 0), reason(count, 0);
+  for (int q = 0; q < count; q++) {
+    bn[q] = rn[q] = sqrt(S->hval[2 * q]);
+    ttol[q] = fmax(o.rtol * bn[q], o.atol);
+  }
+  double lmin, lmax;
+  spectrum(g, &lmin, &lmax);
+  const double first_floor = fmin(0.5, 0.3 * (lmax / fmax(lmin, 1e-300)) * 0x1.0p-24);
+  std::vector<double> hs(count), his(count);
+  KspVecs<float> v{S->r32, {S->p32, S->q32}, S->w32, S->y32};
+  for (int step = 0;; step++) {
+    int nact = 0;
+    for (int q = 0; q < count; q++) {
+      active[q] = 0;
+      if (reason[q]) continue;
+      if (isnan(rn[q]) || isinf(rn[q])) reason[q] = R_DIVERGED_NANORINF;
+      else if (rn[q] <= ttol[q]) reason[q] = rn[q] < o.atol ? R_CONVERGED_ATOL : R_CONVERGED_RTOL;
+      else if (step >= o.outer_max_it) reason[q] = R_DIVERGED_ITS;
+      else active[q] = 1;
+      nact += active[q];
+    }
+    if (!nact) break;
+    // per-plane scales and fresh inner KSP states (inactive planes: done)
+    unsigned int ninact = 0;
+    for (int q = 0; q < count; q++) {
+      KspState *h = &S->st_h[q];
+      memset(h, 0, sizeof(*h));
+      h->betaold = 1.0;
+      h->atol = o.atol;
+      h->dtol = o.dtol;
+      h->max_it = o.inner_max_it;
+      h->norm_type = FISHGPU_NORM_UNPRECONDITIONED;
+      h->ndone = S->ndone;
+      if (active[q]) {
+        double irtol = fmax(o.inner_rtol, 0.5 * ttol[q] / rn[q]);
+        if (step == 0) irtol = fmax(irtol, first_floor);
+        h->rtol = fmin(irtol, 0.5);
+        hs[q] = rn[q];
+        his[q] = 1.0 / rn[q];
+      } else {
+        h->done = 1;
+        ninact++;
+        hs[q] = 0.0;
+        his[q] = 0.0;
+      }
+    }
+    FG_CUDA(cudaMemcpyAsync(S->scl, hs.data(), sizeof(double) * count, cudaMemcpyHostToDevice, s));
+    FG_CUDA(cudaMemcpyAsync(S->iscl, his.data(), sizeof(double) * count, cudaMemcpyHostToDevice, s));
+    FG_CUDA(cudaMemcpyAsync(S->st, S->st_h, sizeof(KspState) * count, cudaMemcpyHostToDevice, s));
+    FG_CUDA(cudaMemcpyAsync(S->ndone, &ninact, sizeof(unsigned int), cudaMemcpyHostToDevice, s));
+    v_demote<<<gb, S->sf.chunk, 0, s>>>(g, S->sf, step == 0 ? S->b64 : S->r64, S->iscl, 0.0, S->r32);
+    if (!S->gexec_init &&
+        (rc = capture(S, [&] { enq_cg_init<2, float>(S, S->h32, v); }, &S->gexec_init, &S->n_init)))
+      return rc;
+    if (!S->gexec &&
+        (rc = capture(S, [&] { for (int q = 0; q < S->giters; q++) enq_cg_iter<2, float>(S, S->h32, v, q & 1); },
+                      &S->gexec, &S->n_iter)))
+      return rc;
+    FG_CUDA(cudaGraphLaunch(S->gexec_init, s));
+    S->launches += S->n_init + 2;
+    unsigned int *hdone = (unsigned int *)S->hval;  // reuse pinned scratch for the counter
+    const long long guard = (long long)o.inner_max_it / S->giters + 4;
+    for (long long l = 0;; l++) {
+      FG_CUDA(cudaMemcpyAsync(hdone, S->ndone, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
+      FG_CUDA(cudaStreamSynchronize(s));
+      if (*hdone >= (unsigned)count) break;
+      if (l > guard) return FISHGPU_ERR_TIMEOUT;
+      FG_CUDA(cudaGraphLaunch(S->gexec, s));
+      S->launches += S->n_iter;
+    }
+    FG_CUDA(cudaMemcpyAsync(S->st_h, S->st, sizeof(KspState) * count, cudaMemcpyDeviceToHost, s));
+    v_promote_add<<<gb, S->sf.chunk, 0, s>>>(g, S->sf, S->y32, S->scl, 0.0, S->y64);
+    v_resid<2, double><<<gb, S->sf.chunk, 0, s>>>(g, S->sf, nullptr, S->b64, S->y64, S->r64);
+    S->launches += 3;
+    if ((rc = plane_norms(S, S->r64))) return rc;
+    for (int q = 0; q < count; q++) {
+      if (!active[q]) continue;
+      const KspState *h = &S->st_h[q];
+      its[q] += h->its;
+      outer[q]++;
+      rn[q] = sqrt(S->hval[2 * q]);
+      if (h->reason == R_DIVERGED_NANORINF || h->reason == R_DIVERGED_INDEFINITE_MAT ||
+          h->reason == R_DIVERGED_INDEFINITE_PC)
+        reason[q] = h->reason;
+    }
+  }
+  {
+    dim3 grid((unsigned)std::min<long long>(((long long)g.mx * g.my + 255) / 256, 64), (unsigned)count);
+    k_unpack_planes<<<grid, 256, 0, s>>>(g, S->y64, u);
+    S->launches += 1;
+  }
+  FG_CUDA(cudaGetLastError());
+  FG_CUDA(cudaStreamSynchronize(s));
+  for (int q = 0; q < count; q++) {
+    its_out[q] = its[q];
+    outer_out[q] = outer[q];
+    relres_out[q] = bn[q] > 0 ? rn[q] / bn[q] : 0.0;
+    reason_out[q] = reason[q];
+  }
+  return FISHGPU_OK;
+}
+
+}  // namespace fg
+
+extern "C" int fishgpu_batch_opts_default(fishgpu_batch_opts *o) {
+  if (!o) return FISHGPU_ERR_ARG;
+  memset(o, 0, sizeof(*o));
+  o->rtol = 1e-8;
+  o->atol = 1e-50;
+  o->inner_rtol = 1e-6;
+  o->inner_max_it = 100;
+  o->outer_max_it = 30;
+  o->smooth_its = 2;
+  o->mg_cycles = 1;
+  o->esteig[0] = 0.0;
+  o->esteig[1] = 0.1;
+  o->esteig[2] = 0.0;
+  o->esteig[3] = 1.1;
+  o->tune = 1;
+  return FISHGPU_OK;
+}
+
+extern "C" int fishgpu_batch_destroy(fishgpu_batch *B) {
+  if (!B) return FISHGPU_OK;
+  for (fishgpu_solver *S : B->groups) fishgpu_solver_destroy(S);
+  delete B;
+  return FISHGPU_OK;
+}
+
+extern "C" int fishgpu_batch_create(const fishgpu_batch_opts *o, int ninst, const int *n, fishgpu_batch **out) {
+  if (!o || ninst < 1 || !n || !out) return FISHGPU_ERR_ARG;
+  *out = nullptr;
+  if (!(o->rtol >= 0) || o->inner_max_it < 1 || o->smooth_its < 1 || o->mg_cycles < 1 || o->mg_cycles > 2)
+    return FISHGPU_ERR_ARG;
+  std::map<int, std::vector<int>> bysize;
+  for (int q = 0; q < ninst; q++) {
+    const int m = n[q];
+    // 2^k + 1 nodes, k >= 1: coarsens down to 3 x 3
+    if (m < 3 || m > (1 << 15) + 1 || ((m - 1) & (m - 2)) != 0) return FISHGPU_ERR_ARG;
+    bysize[m].push_back(q);
+  }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return FISHGPU_ERR_NODEVICE;
+  }
+  fishgpu_batch *B = new fishgpu_batch();
+  B->o = *o;
+  B->ninst = ninst;
+  B->n.assign(n, n + ninst);
+  for (auto it = bysize.rbegin(); it != bysize.rend(); ++it) {  // largest first
+    fishgpu_solver *S = nullptr;
+    int rc = group_create(*o, it->first, (int)it->second.size(), &S);
+    if (rc) {
+      fishgpu_batch_destroy(B);
+      return rc;
+    }
+    B->groups.push_back(S);
+    B->members.push_back(it->second);
+  }
+  B->inner_its.assign(ninst, 0);
+  B->outer_its.assign(ninst, 0);
+  B->rel_resid.assign(ninst, 0.0);
+  B->reason.assign(ninst, 0);
+  *out = B;
+  return FISHGPU_OK;
+}
+
+extern "C" int fishgpu_batch_solve(fishgpu_batch *B, const double *const *f, double *const *u,
+                                   fishgpu_batch_report *rep) {
+  if (!B || !f || !u || !rep) return FISHGPU_ERR_ARG;
+  memset(rep, 0, sizeof(*rep));
+  const int G = (int)B->groups.size();
+  // per group: device arrays of the members' f and u pointers
+  std::vector<const double **> fdev(G, nullptr);
+  std::vector<double **> udev(G, nullptr);
+  std::vector<int> grc(G, FISHGPU_OK);
+  std::vector<std::vector<int>> its(G), outer(G), reason(G);
+  std::vector<std::vector<double>> rel(G);
+  cudaEvent_t e0, e1;
+  cudaStream_t s0;
+  if (cudaStreamCreateWithFlags(&s0, cudaStreamNonBlocking) != cudaSuccess) return FISHGPU_ERR_CUDA;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  int rc = FISHGPU_OK;
+  for (int gi = 0; gi < G && !rc; gi++) {
+    const std::vector<int> &mem = B->members[gi];
+    std::vector<const double *> hf(mem.size());
+    std::vector<double *> hu(mem.size());
+    for (size_t q = 0; q < mem.size(); q++) {
+      hf[q] = f[mem[q]];
+      hu[q] = u[mem[q]];
+      if (!hf[q] || !hu[q]) rc = FISHGPU_ERR_ARG;
+    }
+    if (rc) break;
+    if (cudaMalloc((void **)&fdev[gi], sizeof(double *) * mem.size()) != cudaSuccess ||
+        cudaMalloc((void **)&udev[gi], sizeof(double *) * mem.size()) != cudaSuccess) {
+      rc = FISHGPU_ERR_NOMEM;
+      break;
+    }
+    cudaMemcpy(fdev[gi], hf.data(), sizeof(double *) * mem.size(), cudaMemcpyHostToDevice);
+    cudaMemcpy(udev[gi], hu.data(), sizeof(double *) * mem.size(), cudaMemcpyHostToDevice);
+    its[gi].resize(mem.size());
+    outer[gi].resize(mem.size());
+    reason[gi].resize(mem.size());
+    rel[gi].resize(mem.size());
+  }
+  if (!rc) {
+    cudaDeviceSynchronize();
+    cudaEventRecord(e0, s0);
+    std::vector<std::thread> th;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    for (int gi = 0; gi < G; gi++)
+      th.emplace_back([&, gi, dev] {
+        cudaSetDevice(dev);
+        grc[gi] = group_solve(B->groups[gi], fdev[gi], udev[gi], its[gi].data(), outer[gi].data(), rel[gi].data(),
+                              reason[gi].data());
+      });
+    for (auto &t : th) t.join();
+    cudaDeviceSynchronize();
+    cudaEventRecord(e1, s0);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    rep->solve_ms = ms;
+    for (int gi = 0; gi < G; gi++)
+      if (grc[gi] && !rc) rc = grc[gi];
+  }
+  for (int gi = 0; gi < G; gi++) {
+    if (fdev[gi]) cudaFree(fdev[gi]);
+    if (udev[gi]) cudaFree(udev[gi]);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaStreamDestroy(s0);
+  if (rc) return rc;
+  rep->ninst = B->ninst;
+  rep->groups = G;
+  for (int gi = 0; gi < G; gi++) {
+    const std::vector<int> &mem = B->members[gi];
+    rep->launches += B->groups[gi]->launches;
+    for (size_t q = 0; q < mem.size(); q++) {
+      const int id = mem[q];
+      B->inner_its[id] = its[gi][q];
+      B->outer_its[id] = outer[gi][q];
+      B->rel_resid[id] = rel[gi][q];
+      B->reason[id] = reason[gi][q];
+      rep->total_inner_its += its[gi][q];
+      if (reason[gi][q] > 0) rep->converged++;
+      if (outer[gi][q] > rep->max_outer) rep->max_outer = outer[gi][q];
+      if (its[gi][q] > rep->max_inner) rep->max_inner = its[gi][q];
+      rep->dofs += (long long)B->n[id] * B->n[id];
+    }
+  }
+  return rep->converged == B->ninst ? FISHGPU_OK : FISHGPU_ERR_NOT_CONVERGED;
+}
+
+extern "C" int fishgpu_batch_results(const fishgpu_batch *B, int *inner_its, int *outer_its, double *rel_resid,
+                                     int *reason) {
+  if (!B) return FISHGPU_ERR_ARG;
+  for (int q = 0; q < B->ninst; q++) {
+    if (inner_its) inner_its[q] = B->inner_its[q];
+    if (outer_its) outer_its[q] = B->outer_its[q];
+    if (rel_resid) rel_resid[q] = B->rel_resid[q];
+    if (reason) reason[q] = B->reason[q];
+  }
+  return FISHGPU_OK;
 }

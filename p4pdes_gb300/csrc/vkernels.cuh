@@ -7,7 +7,7 @@
 //
 // Work decomposition: a thread owns a "slot" of 4 consecutive x-points
 // (one float4, or two double2).  The slots of one k-plane are numbered
-// row-major; a block of 256 threads takes 256 consecutive slots (crossing
+// row-major; a block of `chunk` threads (256 by default) takes that many consecutive slots (crossing
 // rows, so its loads per plane are one contiguous run of 4 KB (FP32)) and
 // marches `zc` planes in k with the k-1/k/k+1 values of its slot in
 // registers.  x-neighbours across slots come from warp shuffles (the warp's
@@ -58,25 +58,31 @@ __device__ __forceinline__ void set_el(V4<T> &v, int e, T a) {
   if (e == 0) v.x = a; else if (e == 1) v.y = a; else if (e == 2) v.z = a; else v.w = a;
 }
 
-// Launch shape of the slot decomposition of one level.
+// Launch shape of the slot decomposition of one level.  Batched grids
+// (batch = 1) are 2D instances stacked as k-planes: one block covers part of
+// one plane, the KSP state, early exit and reductions are per plane.
 struct Slots {
   int P4;         // slots per row (pitch / 4)
   int per_plane;  // slots per k-plane (P4 * my)
-  int nchunk;     // 256-slot chunks per plane
+  int chunk;      // slots per block = threads per block (multiple of 32, <= 256)
+  int nchunk;     // chunks per plane
   int zc, nz;     // planes per block, z-chunks
+  int batch;      // 1: planes are independent instances
   long long tot4; // slots in the whole array
 };
 
 // zc_max planes per block at most, fewer when needed to keep at least
 // `min_blocks` blocks (small levels, and the coarse-grid launches of the
 // grid transfers, would otherwise leave SMs idle).
-inline Slots make_slots(const Geom &g, int zc_max, int min_blocks = 2432) {
+inline Slots make_slots(const Geom &g, int zc_max, int min_blocks = 2432, int chunk = 256, int batch = 0) {
   Slots s;
   s.P4 = g.pitch / 4;
   s.per_plane = s.P4 * g.my;
-  s.nchunk = (s.per_plane + 255) / 256;
+  s.chunk = chunk;
+  s.batch = batch;
+  s.nchunk = (s.per_plane + chunk - 1) / chunk;
   int zc = 1;
-  if (g.dim == 3) {
+  if (g.dim == 3 && !batch) {
     const long long want = ((long long)s.nchunk * g.mz) / (min_blocks > 0 ? min_blocks : 1);
     zc = (int)(want < 1 ? 1 : want > zc_max ? zc_max : want);
     if (zc > g.mz) zc = g.mz;
@@ -98,7 +104,7 @@ struct SlotPos {
 __device__ __forceinline__ SlotPos slot_pos(const Geom &g, const Slots &s) {
   SlotPos p;
   const int c = blockIdx.x % s.nchunk, kz = blockIdx.x / s.nchunk;
-  const int f = c * 256 + threadIdx.x;
+  const int f = c * s.chunk + threadIdx.x;
   p.in = f < s.per_plane;
   p.j = p.in ? f / s.P4 : 0;
   p.i4 = p.in ? (f - p.j * s.P4) * 4 : 0;
@@ -197,6 +203,50 @@ __device__ __forceinline__ T resid_el(const Geom &g, const Wv<T> &w, const Nb<T>
 
 __device__ __forceinline__ bool ksp_done_v(const KspState *st) { return st && __ldcg(&st->done); }
 
+// The KSP state a block works for: the whole grid's, or its plane's in a batch.
+__device__ __forceinline__ KspState *block_state(KspState *st, const Slots &s) {
+  if (!st || !s.batch) return st;
+  return st + blockIdx.x / s.nchunk;
+}
+
+// Sum over the blocks of a launch (or, for a batch, over the blocks of one
+// plane: tickets and the finaliser are per plane) and run `fin`.
+template <int NV>
+__device__ __forceinline__ void reduce_slots(double (&v)[NV], Reducer red, int slot, KspState *st, Fin fin,
+                                             double *out, const Slots &s) {
+  if (!s.batch) {
+    reduce_and_finalize<NV>(v, red, slot, st, fin, out);
+    return;
+  }
+  __shared__ bool am_last;
+  const int tid = threadIdx.x;
+  const int nt = blockDim.x;
+  const int plane = blockIdx.x / s.nchunk, first = plane * s.nchunk, nb = s.nchunk;
+  block_sum<NV>(v);
+  unsigned int *ticket = red.tickets + (size_t)slot * red.tcap + plane;
+  if (tid == 0) {
+#pragma unroll
+    for (int q = 0; q < NV; q++) red.partials[(slot * NV + q) * red.cap + blockIdx.x] = v[q];
+    __threadfence();
+    unsigned int t = atomicAdd(ticket, 1u);
+    am_last = (t == (unsigned)(nb - 1));
+  }
+  __syncthreads();
+  if (!am_last) return;
+  __threadfence();
+  double sum[NV];
+#pragma unroll
+  for (int q = 0; q < NV; q++) {
+    sum[q] = 0.0;
+    for (int b = tid; b < nb; b += nt) sum[q] += __ldcg(&red.partials[(slot * NV + q) * red.cap + first + b]);
+  }
+  block_sum<NV>(sum);
+  if (tid == 0) {
+    *ticket = 0u;
+    if (st || fin == FIN_STORE) ksp_finalize(st, fin, sum, NV, out ? out + plane * NV : nullptr);
+  }
+}
+
 // Generic z-march over the slot's planes.  `Op` is called once per plane
 // with (k, n, nb) after the neighbour data is assembled; it performs its own
 // loads/stores of other arrays at n.  `x` is the stencil input.
@@ -246,6 +296,7 @@ __global__ void __launch_bounds__(256, MinBlocks<T>::value) v_cheb(Geom g, Slots
                                               const T *__restrict__ xkm1, const T *__restrict__ xk,
                                               T *__restrict__ out, T ckm1, T ck, T crd, Reducer red = Reducer{},
                                               int slot = 0, Fin fin = FIN_STORE) {
+  st = block_state(st, s);
   if (ksp_done_v(st)) return;
   const SlotPos p = slot_pos(g, s);
   const Wv<T> w(g);
@@ -276,7 +327,7 @@ __global__ void __launch_bounds__(256, MinBlocks<T>::value) v_cheb(Geom g, Slots
   march<DIM, T>(g, s, p, xk, op);
   if (DOTS) {
     double v2[2] = {(double)zz, (double)zr};
-    reduce_and_finalize<2>(v2, red, slot, st, fin, nullptr);
+    reduce_slots<2>(v2, red, slot, st, fin, nullptr, s);
   }
 }
 
@@ -286,6 +337,7 @@ __global__ void __launch_bounds__(256, MinBlocks<T>::value) v_cheb(Geom g, Slots
 template <int DIM, typename T>
 __global__ void __launch_bounds__(256, MinBlocks<T>::value) v_cheb2_zero(Geom g, Slots s, KspState *st, const T *__restrict__ b,
                                                     T *__restrict__ out, T a0, T a1) {
+  st = block_state(st, s);
   if (ksp_done_v(st)) return;
   const SlotPos p = slot_pos(g, s);
   const Wv<T> w(g);
@@ -312,6 +364,7 @@ __global__ void __launch_bounds__(256, MinBlocks<T>::value) v_cheb2_zero(Geom g,
 template <int DIM, typename T>
 __global__ void __launch_bounds__(256, MinBlocks<T>::value) v_resid(Geom g, Slots s, KspState *st, const T *__restrict__ b,
                                                const T *__restrict__ x, T *__restrict__ r) {
+  st = block_state(st, s);
   if (ksp_done_v(st)) return;
   const SlotPos p = slot_pos(g, s);
   const Wv<T> w(g);
@@ -334,6 +387,7 @@ template <int DIM, typename T>
 __global__ void __launch_bounds__(256, MinBlocks<T>::value) v_apply_dot(Geom g, Slots s, KspState *st, const T *__restrict__ pv,
                                                    T *__restrict__ wv, Reducer red, int slot, Fin fin,
                                                    double *out) {
+  st = block_state(st, s);
   if (ksp_done_v(st)) return;
   const SlotPos p = slot_pos(g, s);
   const Wv<T> w(g);
@@ -355,7 +409,7 @@ __global__ void __launch_bounds__(256, MinBlocks<T>::value) v_apply_dot(Geom g, 
   };
   march<DIM, T>(g, s, p, pv, op);
   double v1[1] = {(double)acc};
-  reduce_and_finalize<1>(v1, red, slot, st, fin, out);
+  reduce_slots<1>(v1, red, slot, st, fin, out, s);
 }
 
 // p_new = z + (beta/betaold) p_old (p_new = z on the first CG iteration),
@@ -365,6 +419,7 @@ template <int DIM, typename T>
 __global__ void __launch_bounds__(256, MinBlocks<T>::value) v_cgp_apply(Geom g, Slots s, KspState *st, const T *__restrict__ z,
                                                    const T *__restrict__ pold, T *__restrict__ pnew,
                                                    T *__restrict__ wv, Reducer red, int slot) {
+  st = block_state(st, s);
   if (ksp_done_v(st)) return;
   const SlotPos p = slot_pos(g, s);
   const Wv<T> w(g);
@@ -389,7 +444,7 @@ __global__ void __launch_bounds__(256, MinBlocks<T>::value) v_cgp_apply(Geom g, 
   };
   march_src<DIM, T>(g, s, p, src, op);
   double v1[1] = {(double)acc};
-  reduce_and_finalize<1>(v1, red, slot, st, FIN_PW, nullptr);
+  reduce_slots<1>(v1, red, slot, st, FIN_PW, nullptr, s);
 }
 
 // ------------------------------------------------------------------ grid transfers
@@ -416,6 +471,7 @@ __device__ __forceinline__ V4<T> restrict_row(const Geom &gf, const T *__restric
 template <int DIM, typename T>
 __global__ void __launch_bounds__(256) v_restrict(Geom gf, Geom g, Slots s, KspState *st, const T *__restrict__ rf,
                                                   T *__restrict__ bc) {
+  st = block_state(st, s);
   if (ksp_done_v(st)) return;
   const SlotPos p = slot_pos(g, s);
   const T h = T(0.5);
@@ -434,7 +490,7 @@ __global__ void __launch_bounds__(256) v_restrict(Geom gf, Geom g, Slots s, KspS
   V4<T> below = zero4<T>();  // row sums of fine plane 2K-1
   if (DIM >= 3 && p.k0 > 0) below = rowsum(2 * p.k0 - 1);
   for (int k = p.k0; k < p.k1; k++) {
-    V4<T> mid = rowsum(DIM >= 3 ? 2 * k : 0);
+    V4<T> mid = rowsum(DIM >= 3 ? 2 * k : k);  // 2D: k is the instance of a batch
     V4<T> above = zero4<T>();
     if (DIM >= 3 && 2 * k + 1 < gf.mz) above = rowsum(2 * k + 1);
     V4<T> o = mid;
@@ -458,6 +514,7 @@ __global__ void __launch_bounds__(256) v_restrict(Geom gf, Geom g, Slots s, KspS
 template <int DIM, typename T>
 __global__ void __launch_bounds__(256, 4) v_prolong(Geom gf, Geom g, Slots s, KspState *st, const T *__restrict__ xc,
                                                  T *__restrict__ xf) {
+  st = block_state(st, s);
   if (ksp_done_v(st)) return;
   const SlotPos p = slot_pos(g, s);
   const int lane = threadIdx.x & 31;
@@ -502,7 +559,7 @@ __global__ void __launch_bounds__(256, 4) v_prolong(Geom gf, Geom g, Slots s, Ks
       xrow(k + 1, p.j, ok0, b0l, b0h);
       xrow(k + 1, p.j + (ok1 ? 1 : 0), ok1, b1l, b1h);
     }
-    const int fk = DIM >= 3 ? 2 * k : 0, fj = DIM >= 2 ? 2 * p.j : 0;
+    const int fk = DIM >= 3 ? 2 * k : k, fj = DIM >= 2 ? 2 * p.j : 0;
     if (ok0) addrow(fk, fj, a0l, a0h, T(1));
     if (ok1) addrow(fk, fj + 1, add4(a0l, a1l), add4(a0h, a1h), h);
     if (up) {
@@ -515,110 +572,100 @@ __global__ void __launch_bounds__(256, 4) v_prolong(Geom gf, Geom g, Slots s, Ks
 }
 
 // ------------------------------------------------------------------ pointwise
-// Flat over all slots of the padded array (padding stays zero).
-#define FG_FLAT_BEGIN(tot4)                                                              \
-  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < (tot4);      \
-       q += (long long)gridDim.x * blockDim.x) {                                         \
-    const long long n = q * 4;
-#define FG_FLAT_END }
+// Slot decomposition as the stencils (one vec4 of points per thread per
+// plane); padding points stay zero because every input's padding is zero.
+#define FG_PW_BEGIN                                        \
+  const SlotPos p = slot_pos(g, s);                        \
+  if (p.in)                                                \
+    for (int k = p.k0; k < p.k1; k++) {                    \
+      const long long n = (long long)k * g.plane + p.col;
+#define FG_PW_END }
 
-// p = z + (beta/betaold) p ; p = z on the first iteration
-template <typename T>
-__global__ void __launch_bounds__(256) v_cg_p(long long tot4, KspState *st, const T *__restrict__ z, T *__restrict__ pv) {
-  if (ksp_done_v(st)) return;
-  const bool first = st->i == 0;
-  const T bb = first ? T(0) : (T)(st->beta / st->betaold);
-  FG_FLAT_BEGIN(tot4)
-  const V4<T> zv = ld4(z + n);
-  if (first) {
-    st4(pv + n, zv);
-  } else {
-    const V4<T> pp = ld4(pv + n);
-    st4(pv + n, V4<T>{fma(bb, pp.x, zv.x), fma(bb, pp.y, zv.y), fma(bb, pp.z, zv.z), fma(bb, pp.w, zv.w)});
-  }
-  FG_FLAT_END
-}
-
-// y += alpha p; r -= alpha w; RR: r.r reduced
+// y += alpha p; r -= alpha w; RR: r.r reduced (unpreconditioned norm test)
 template <typename T, bool RR>
-__global__ void __launch_bounds__(256) v_cg_xr(long long tot4, KspState *st, const T *__restrict__ pv,
+__global__ void __launch_bounds__(256) v_cg_xr(Geom g, Slots s, KspState *st, const T *__restrict__ pv,
                                                const T *__restrict__ wv, T *__restrict__ y, T *__restrict__ r,
                                                Reducer red, int slot) {
+  st = block_state(st, s);
   if (ksp_done_v(st)) return;
   const T a = (T)st->alpha;
   T acc = T(0);
-  FG_FLAT_BEGIN(tot4)
+  FG_PW_BEGIN
   const V4<T> pp = ld4(pv + n), ww = ld4(wv + n), yy = ld4(y + n), rr = ld4(r + n);
   st4(y + n, V4<T>{fma(a, pp.x, yy.x), fma(a, pp.y, yy.y), fma(a, pp.z, yy.z), fma(a, pp.w, yy.w)});
   const V4<T> rn{fma(-a, ww.x, rr.x), fma(-a, ww.y, rr.y), fma(-a, ww.z, rr.z), fma(-a, ww.w, rr.w)};
   st4(r + n, rn);
   if (RR) acc = fma(rn.x, rn.x, fma(rn.y, rn.y, fma(rn.z, rn.z, fma(rn.w, rn.w, acc))));
-  FG_FLAT_END
+  FG_PW_END
   if (RR) {
     double v1[1] = {(double)acc};
-    reduce_and_finalize<1>(v1, red, slot, st, FIN_RR, nullptr);
+    reduce_slots<1>(v1, red, slot, st, FIN_RR, nullptr, s);
   }
 }
 
-// z.z and z.r reduced together
+// z.z and z.r reduced together (out: per plane for a batch)
 template <typename T>
-__global__ void __launch_bounds__(256) v_dots(long long tot4, KspState *st, const T *__restrict__ z,
+__global__ void __launch_bounds__(256) v_dots(Geom g, Slots s, KspState *st, const T *__restrict__ z,
                                               const T *__restrict__ r, Reducer red, int slot, Fin fin, double *out) {
+  st = block_state(st, s);
   if (ksp_done_v(st)) return;
   T zz = T(0), zr = T(0);
-  FG_FLAT_BEGIN(tot4)
+  FG_PW_BEGIN
   const V4<T> a = ld4(z + n), b = ld4(r + n);
   zz = fma(a.x, a.x, fma(a.y, a.y, fma(a.z, a.z, fma(a.w, a.w, zz))));
   zr = fma(a.x, b.x, fma(a.y, b.y, fma(a.z, b.z, fma(a.w, b.w, zr))));
-  FG_FLAT_END
+  FG_PW_END
   double v2[2] = {(double)zz, (double)zr};
-  reduce_and_finalize<2>(v2, red, slot, st, fin, out);
+  reduce_slots<2>(v2, red, slot, st, fin, out, s);
 }
 
 // out = c * in (Jacobi apply, or scaled copy)
 template <typename T>
-__global__ void __launch_bounds__(256) v_scale(long long tot4, KspState *st, const T *__restrict__ in, T c,
+__global__ void __launch_bounds__(256) v_scale(Geom g, Slots s, KspState *st, const T *__restrict__ in, T c,
                                                T *__restrict__ out) {
+  st = block_state(st, s);
   if (ksp_done_v(st)) return;
-  FG_FLAT_BEGIN(tot4)
+  FG_PW_BEGIN
   const V4<T> a = ld4(in + n);
   st4(out + n, V4<T>{c * a.x, c * a.y, c * a.z, c * a.w});
-  FG_FLAT_END
+  FG_PW_END
 }
 
 template <typename T>
-__global__ void __launch_bounds__(256) v_zero(long long tot4, T *__restrict__ a) {
-  FG_FLAT_BEGIN(tot4)
+__global__ void __launch_bounds__(256) v_zero(Geom g, Slots s, T *__restrict__ a) {
+  FG_PW_BEGIN
   st4(a + n, zero4<T>());
-  FG_FLAT_END
+  FG_PW_END
 }
 
-// r32 = (float)(r64 * inv_s)
-__global__ void __launch_bounds__(256) v_demote(long long tot4, const double *__restrict__ r, double inv_s,
-                                                float *__restrict__ r32) {
-  FG_FLAT_BEGIN(tot4)
+// r32 = (float)(r64 * inv_s); inv_s per plane for a batch (scale[plane])
+__global__ void __launch_bounds__(256) v_demote(Geom g, Slots s, const double *__restrict__ r, const double *scale,
+                                                double inv_s, float *__restrict__ r32) {
+  FG_PW_BEGIN
+  const double is = scale ? scale[k] : inv_s;
   const V4<double> a = ld4(r + n);
-  st4(r32 + n, V4<float>{(float)(a.x * inv_s), (float)(a.y * inv_s), (float)(a.z * inv_s), (float)(a.w * inv_s)});
-  FG_FLAT_END
+  st4(r32 + n, V4<float>{(float)(a.x * is), (float)(a.y * is), (float)(a.z * is), (float)(a.w * is)});
+  FG_PW_END
 }
 
-// y64 += s * (double)e32
-__global__ void __launch_bounds__(256) v_promote_add(long long tot4, const float *__restrict__ e, double s,
-                                                     double *__restrict__ y) {
-  FG_FLAT_BEGIN(tot4)
+// y64 += s * (double)e32; s per plane for a batch (scale[plane])
+__global__ void __launch_bounds__(256) v_promote_add(Geom g, Slots s, const float *__restrict__ e, const double *scale,
+                                                     double sc, double *__restrict__ y) {
+  FG_PW_BEGIN
+  const double f = scale ? scale[k] : sc;
   const V4<float> a = ld4(e + n);
   const V4<double> b = ld4(y + n);
-  st4(y + n, V4<double>{fma(s, (double)a.x, b.x), fma(s, (double)a.y, b.y), fma(s, (double)a.z, b.z),
-                        fma(s, (double)a.w, b.w)});
-  FG_FLAT_END
+  st4(y + n, V4<double>{fma(f, (double)a.x, b.x), fma(f, (double)a.y, b.y), fma(f, (double)a.z, b.z),
+                        fma(f, (double)a.w, b.w)});
+  FG_PW_END
 }
 
 // a += b
-__global__ void __launch_bounds__(256) v_add(long long tot4, const double *__restrict__ b, double *__restrict__ a) {
-  FG_FLAT_BEGIN(tot4)
+__global__ void __launch_bounds__(256) v_add(Geom g, Slots s, const double *__restrict__ b, double *__restrict__ a) {
+  FG_PW_BEGIN
   const V4<double> x = ld4(a + n), y = ld4(b + n);
   st4(a + n, V4<double>{x.x + y.x, x.y + y.y, x.z + y.z, x.w + y.w});
-  FG_FLAT_END
+  FG_PW_END
 }
 
 }  // namespace fg

@@ -230,6 +230,17 @@ def test_mixed_form_matches_fp64_error(cuda, args):
     assert all(b < a for a, b in zip(h, h[1:]))
 
 
+def test_mixed_form_inner_iterations_do_not_depend_on_the_outer_norm_option(cuda):
+    """The inner FP32 CG always stops on its own unpreconditioned residual,
+    whatever -ksp_norm_type says (that option governs the FP64 form)."""
+    fg = fgmod()
+    base = "-fsh_dim 3 -fsh_problem manupoly -da_refine 5 -pc_type mg -ksp_rtol 1e-10 -fsh_precision mixed"
+    _, a = fg.solve(fg.options(base))
+    _, b = fg.solve(fg.options(base + " -ksp_norm_type unpreconditioned"))
+    assert a.its == b.its and a.outer_its == b.outer_its and a.its <= 30
+    assert a.history() == b.history()
+
+
 def test_zero_problem_converges_at_iteration_zero(cuda):
     fg = fgmod()
     u, rep = fg.solve(fg.options("-fsh_dim 2 -fsh_problem zero -da_refine 3 -pc_type mg"))
