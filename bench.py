@@ -147,6 +147,57 @@ def manupoly_fg(torch, o, dev):
     return f, g
 
 
+def batch_leg(torch, fg, n_inst, reps=3):
+    """4096 independent 2D instances, n = 2^k + 1 with k ~ U{5..9} from
+    default_rng(0), f ~ N(0,1) per node from default_rng(1), u = 0 on the
+    boundary, rtol 1e-8, mixed form; inputs resident on the device."""
+    import numpy as np
+    ks = np.random.default_rng(0).integers(5, 10, size=n_inst)
+    sizes = [int(2 ** k + 1) for k in ks]
+    frng = np.random.default_rng(1)
+    fs = [torch.from_numpy(frng.standard_normal((n, n))).cuda() for n in sizes]
+    us = [torch.empty_like(f) for f in fs]
+    t0 = time.perf_counter()
+    b = fg.Batch(sizes, rtol=1e-8, tune=True)
+    b.solve(fs, us)  # warm-up (graphs, tuned chunk sizes)
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t0
+    best = None
+    for _ in range(reps):
+        rep = b.solve(fs, us)
+        if best is None or rep.solve_ms < best.solve_ms:
+            best = rep
+    inner, outer, rel, reason = b.results()
+    b.close()
+    return {
+        "workload": "%d 2D Poisson instances, n = 2^k+1, k ~ U{5..9} (seed 0), f ~ N(0,1) (seed 1), rtol 1e-8, "
+                    "mixed form, inputs resident" % n_inst,
+        "solve_ms": best.solve_ms, "solves_per_s": n_inst / (best.solve_ms * 1e-3),
+        "dofs": best.dofs, "dof_per_s": best.dofs / (best.solve_ms * 1e-3), "groups": best.groups,
+        "converged": best.converged, "max_outer": best.max_outer, "max_inner": best.max_inner,
+        "max_rel_resid": max(rel), "launches": best.launches, "setup_s": setup_s,
+        "timing": "CUDA events around one batched solve, best of %d" % reps,
+    }
+
+
+def serve_leg(fg, n_req, rate=2000.0, workers=16):
+    """Mixed 2D/3D serving stream through the continuous-batching server."""
+    from p4pdes_gb300 import serve
+    stream = serve.make_stream(n_req, rate=rate, seed=2)
+    with fg.Server(hbm_budget_bytes=120 << 30, workers=workers, rtol=1e-8) as srv:
+        # pre-warm the pool: `workers` resident solvers of every size in the stream
+        keys = sorted({(d, n) for _, d, n in stream})
+        wstream = [(0.0, d, n) for d, n in keys for _ in range(workers)]
+        serve.run_stream(srv, wstream, distinct_rhs=1)
+        out = serve.run_stream(srv, stream)
+        out["pool"] = srv.stats()
+    out["workload"] = ("Poisson arrivals %.0f req/s (seed 2), 2D n in [65,1025] / 3D n in [33,257] log-uniform "
+                       "rounded to 2^k+1, f ~ N(0,1), rtol 1e-8 mixed, HBM budget 120 GB, %d workers, "
+                       "pinned host arrays" % (rate, workers))
+    out["latency"] = "host clock, submit -> solution copied back to the host"
+    return out
+
+
 def run_ours(args):
     import torch
     import p4pdes_gb300 as fg
@@ -206,6 +257,14 @@ def run_ours(args):
     # roofline of the dominant kernel (FP32 Chebyshev step on the 513^3 level)
     rk = args.roofline_kernel
     kms, kbytes = s_mx.time_kernel(rk, 20)
+    kernel_table = {}
+    for name in ("smooth", "smooth_dots", "smooth_zero", "cgp_apply", "cg_update", "resid", "restrict", "prolong",
+                 "residual64"):
+        try:
+            t, b = s_mx.time_kernel(name, 10)
+        except fg.FishError:
+            continue
+        kernel_table[name] = {"ms": t, "algorithmic_bytes": b, "gbs": b / (t * 1e-3) / 1e9}
 
     # ---- plain FP64 form beside it
     s_64 = fg.Solver(o_64, stream=stream.cuda_stream)
@@ -258,6 +317,8 @@ def run_ours(args):
     except Exception:
         pass
     cpu_v, cpu_info = cpu_baseline()
+    batch = batch_leg(torch, fg, args.batch_instances) if args.batch_instances > 0 else None
+    serving = serve_leg(fg, args.serve_requests) if args.serve_requests > 0 else None
     line = {
         "metric": METRIC, "value": value, "unit": "DOF/s", "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -276,12 +337,15 @@ def run_ours(args):
                      "true_rel_resid": rep_64.true_rel_resid, "errinf": err_64[0], "err2h": err_64[1]},
             "mixed_over_fp64": (N / (ms / K * 1e-3)) / (N / (ms64 * 1e-3)),
             "error_ratio_mixed_over_fp64": err_mx[0] / err_64[0],
+            "batch": batch,
+            "serving": serving,
         },
         "e2e": {"value": e2e, "unit": "DOF/s", "h2d_bytes_per_step": 2 * 8 * N, "d2h_bytes_per_step": 8 * N},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "kernel": rk, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": traffic, "peak_kind": pk_kind,
-                     "algorithmic_bytes_per_launch": kbytes, "ms_per_launch": kms},
+                     "algorithmic_bytes_per_launch": kbytes, "ms_per_launch": kms,
+                     "fine_level_kernels": {k: dict(v, frac=v["gbs"] / hbm) for k, v in kernel_table.items()}},
         "cpu_baseline": {"value": cpu_v, "unit": "DOF/s", "cores": cpu_info["cores"], "kind": "port",
                          "sample": cpu_info["sample"]},
         "clocks": clk.summary(),
@@ -297,6 +361,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--refine", type=int, default=8, help="-da_refine (8: 513^3)")
     ap.add_argument("--roofline-kernel", default="smooth")
+    ap.add_argument("--batch-instances", type=int, default=4096, help="batched 2D leg (0: skip)")
+    ap.add_argument("--serve-requests", type=int, default=1000, help="serving-stream leg (0: skip)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -28,7 +28,7 @@ extern "C" {
 #define FISHGPU_ERR_NOMEM        3  /* device allocation failed / budget   */
 #define FISHGPU_ERR_NOT_CONVERGED 4 /* KSP diverged or reached max_it      */
 #define FISHGPU_ERR_NONFINITE    5  /* NaN/Inf met during the solve        */
-#define FISHGPU_ERR_TIMEOUT      6  /* a device-side wait gave up          */
+#define FISHGPU_ERR_TIMEOUT      6  /* a wait gave up (device or server)    */
 #define FISHGPU_ERR_UNSUPPORTED  7  /* option the GPU library lacks        */
 #define FISHGPU_ERR_NODEVICE     8  /* no CUDA device / wrong architecture */
 
@@ -197,6 +197,10 @@ long long fishgpu_solver_bytes(const fishgpu_solver *s);
 int fishgpu_solver_solve_host(fishgpu_solver *s, const double *f_host, const double *g_host,
                               double *u_host, fishgpu_report *rep);
 
+/* device bytes fishgpu_solver_create would allocate (plus the host-array
+   buffers of fishgpu_solver_solve_host for FISHGPU_USER); -1 if invalid */
+long long fishgpu_solver_estimate_bytes(const fishgpu_opts *o);
+
 /* one-shot create + solve + destroy */
 int fishgpu_solve(const fishgpu_opts *o, double *u_dev, fishgpu_report *rep);
 
@@ -248,6 +252,42 @@ int fishgpu_batch_solve(fishgpu_batch *b, const double *const *f, double *const 
 /* per-instance results of the last solve (host arrays of ninst, any may be NULL) */
 int fishgpu_batch_results(const fishgpu_batch *b, int *inner_its, int *outer_its, double *rel_resid, int *reason);
 int fishgpu_batch_destroy(fishgpu_batch *b);
+
+/* ---- server: continuous batching of independent solves ----------------
+   Each request is -Laplace(u) = f (fish's operator, cx = cy = cz = 1) on the
+   unit square/cube with u = 0 on the boundary, n nodes per side (2^k + 1),
+   f and u host arrays (n^dim doubles, x fastest) that stay valid until the
+   request is waited for.  A request starts as soon as a worker is free and
+   a solver for its size fits in the HBM budget; solvers stay device-resident
+   in a pool keyed by size (idle ones of other sizes are evicted LRU-first
+   when room is needed).  Workers run on their own streams, so solves
+   overlap on the device. */
+typedef struct {
+  long long hbm_budget_bytes; /* device bytes the pooled solvers may hold    */
+  int workers;                /* concurrent solves                           */
+  double rtol;                /* true relative residual per request          */
+  int precision;              /* FISHGPU_MIXED (default) or FISHGPU_FP64     */
+  int fifo;                   /* 1: a request waits for every earlier one    */
+} fishgpu_server_opts;
+
+typedef struct {
+  int status;                 /* library status of the solve                */
+  int its, outer_its;
+  double rel_resid;
+  double queue_ms, service_ms, latency_ms; /* host clock, submit -> done    */
+} fishgpu_server_result;
+
+typedef struct fishgpu_server_s fishgpu_server;
+
+int fishgpu_server_opts_default(fishgpu_server_opts *o);
+int fishgpu_server_create(const fishgpu_server_opts *o, fishgpu_server **out);
+int fishgpu_server_submit(fishgpu_server *s, int dim, int n, const double *f_host, double *u_host,
+                          long long *ticket);
+/* timeout_ms < 0: wait without limit; FISHGPU_ERR_TIMEOUT when not finished */
+int fishgpu_server_wait(fishgpu_server *s, long long ticket, double timeout_ms, fishgpu_server_result *res);
+int fishgpu_server_stats(fishgpu_server *s, long long *pooled_bytes, int *pooled_solvers, long long *created,
+                         long long *evicted);
+int fishgpu_server_destroy(fishgpu_server *s);
 
 #ifdef __cplusplus
 }

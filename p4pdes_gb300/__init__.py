@@ -11,7 +11,9 @@ It mirrors the reference's interface for this path:
   * ``FormUExact``, ``InitialState``, ``error_norms``     -- c/ch6/fish.c:237-340,
     c/ch6/poissonfunctions.c:260-346;
   * ``options(argv)`` parses fish's flags (-fsh_*, -da_refine, -ksp_*, -pc_*,
-    -mg_levels_*), ``solve(opts)`` runs the fish flow on the GPU.
+    -mg_levels_*), ``solve(opts)`` runs the fish flow on the GPU;
+  * ``Solver`` keeps one hierarchy device-resident, ``Batch`` solves many 2D
+    instances together, ``Server`` admits a stream of solves by HBM budget.
 
 Errors raise FishError carrying the library status (the reference returns
 PetscErrorCode).  There is no CPU fallback: if the library is missing the
@@ -25,6 +27,7 @@ __all__ = [
     "Poisson1DFunctionLocal", "Poisson2DFunctionLocal", "Poisson3DFunctionLocal",
     "Poisson1DOperatorApply", "Poisson2DOperatorApply", "Poisson3DOperatorApply",
     "FormUExact", "InitialState", "error_norms", "reason_name",
+    "Solver", "Batch", "Server", "estimate_bytes", "server_request_opts",
 ]
 
 LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "lib", "libfishgpu.so")
@@ -104,6 +107,16 @@ class BatchReport(ctypes.Structure):
                 ("solve_ms", c_double)]
 
 
+class ServerOpts(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", c_ll), ("workers", c_int), ("rtol", c_double), ("precision", c_int),
+                ("fifo", c_int)]
+
+
+class ServerResult(ctypes.Structure):
+    _fields_ = [("status", c_int), ("its", c_int), ("outer_its", c_int), ("rel_resid", c_double),
+                ("queue_ms", c_double), ("service_ms", c_double), ("latency_ms", c_double)]
+
+
 class FishError(RuntimeError):
     def __init__(self, code, what=""):
         self.code = code
@@ -159,6 +172,17 @@ def load():
                  "fishgpu_batch_results", "fishgpu_batch_destroy"):
         getattr(lib, name).restype = c_int
     lib.fishgpu_solver_time_kernel.argtypes = [c_void_p, ctypes.c_char_p, c_int, _P(c_double), _P(c_double)]
+    lib.fishgpu_solver_estimate_bytes.argtypes = [_P(Opts)]
+    lib.fishgpu_solver_estimate_bytes.restype = c_ll
+    lib.fishgpu_server_opts_default.argtypes = [_P(ServerOpts)]
+    lib.fishgpu_server_create.argtypes = [_P(ServerOpts), _P(c_void_p)]
+    lib.fishgpu_server_submit.argtypes = [c_void_p, c_int, c_int, c_void_p, c_void_p, _P(c_ll)]
+    lib.fishgpu_server_wait.argtypes = [c_void_p, c_ll, c_double, _P(ServerResult)]
+    lib.fishgpu_server_stats.argtypes = [c_void_p, _P(c_ll), _P(c_int), _P(c_ll), _P(c_ll)]
+    lib.fishgpu_server_destroy.argtypes = [c_void_p]
+    for name in ("fishgpu_server_opts_default", "fishgpu_server_create", "fishgpu_server_submit",
+                 "fishgpu_server_wait", "fishgpu_server_stats", "fishgpu_server_destroy"):
+        getattr(lib, name).restype = c_int
     for name in ("FormUExact_gpu", "InitialState_gpu", "ErrorNorms_gpu", "fishgpu_opts_default",
                  "fishgpu_opts_parse", "fishgpu_solver_create", "fishgpu_solver_solve",
                  "fishgpu_solver_destroy", "fishgpu_solve", "fishgpu_solve_host",
@@ -380,6 +404,92 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+def estimate_bytes(opts):
+    """Device bytes a Solver for these options holds (-1: invalid options)."""
+    return load().fishgpu_solver_estimate_bytes(ctypes.byref(opts))
+
+
+def _host_addr(a):
+    return a.data_ptr() if hasattr(a, "data_ptr") else a.ctypes.data
+
+
+class Server:
+    """Solve server with continuous batching: requests -Laplace(u) = f on the
+    unit square/cube, u = 0 on the boundary, n nodes per side (2^k + 1), are
+    admitted as worker slots and HBM budget free up and overlap on the device.
+    f and u are host float64 arrays (numpy or CPU tensors, pinned for speed)
+    that must stay alive until wait() returns."""
+
+    def __init__(self, hbm_budget_bytes=120 << 30, workers=8, rtol=1e-8, precision=MIXED, fifo=False):
+        o = ServerOpts()
+        _check(load().fishgpu_server_opts_default(ctypes.byref(o)), "fishgpu_server_opts_default")
+        o.hbm_budget_bytes = int(hbm_budget_bytes)
+        o.workers = int(workers)
+        o.rtol = rtol
+        o.precision = precision
+        o.fifo = int(bool(fifo))
+        self._h = c_void_p()
+        self._keep = {}
+        _check(load().fishgpu_server_create(ctypes.byref(o), ctypes.byref(self._h)), "fishgpu_server_create")
+
+    def submit(self, dim, n, f, u):
+        t = c_ll()
+        _check(load().fishgpu_server_submit(self._h, dim, n, _host_addr(f), _host_addr(u), ctypes.byref(t)),
+               "fishgpu_server_submit")
+        self._keep[t.value] = (f, u)
+        return t.value
+
+    def wait(self, ticket, timeout_ms=-1.0):
+        r = ServerResult()
+        _check(load().fishgpu_server_wait(self._h, ticket, timeout_ms, ctypes.byref(r)), "fishgpu_server_wait")
+        self._keep.pop(ticket, None)
+        return r
+
+    def stats(self):
+        b, n, c, e = c_ll(), c_int(), c_ll(), c_ll()
+        _check(load().fishgpu_server_stats(self._h, ctypes.byref(b), ctypes.byref(n), ctypes.byref(c),
+                                           ctypes.byref(e)), "fishgpu_server_stats")
+        return {"pooled_bytes": b.value, "pooled_solvers": n.value, "created": c.value, "evicted": e.value}
+
+    def close(self):
+        if self._h:
+            load().fishgpu_server_destroy(self._h)
+            self._h = c_void_p()
+            self._keep.clear()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def server_request_opts(dim, n, rtol=1e-8, precision=MIXED):
+    """The solver options the server uses for a (dim, n) request."""
+    o = options([])
+    o.ctx.dim = dim
+    o.ctx.problem = USER
+    o.mx = n
+    o.my = n if dim >= 2 else 1
+    o.mz = n if dim >= 3 else 1
+    levels, m = 1, n
+    while m > 3 and (m - 1) % 2 == 0:
+        m = (m - 1) // 2 + 1
+        levels += 1
+    o.mg_levels = levels
+    o.pc_type = PC_MG
+    o.precision = precision
+    o.rtol = rtol
+    o.norm_type = NORM_UNPRECONDITIONED
+    return o
 
 
 def solve(opts, u=None):

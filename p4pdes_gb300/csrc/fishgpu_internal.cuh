@@ -201,9 +201,12 @@ __device__ inline void ksp_stop(KspState *st, int reason) {
 
 // Scalar part of one KSPCG step (the PETSc cg.c algorithm), run by one thread
 // of the last block of the reduction that produced `tot`.
-__device__ inline void ksp_finalize(KspState *st, Fin fin, const double *tot, int nv, double *out) {
+// Not inlined: one thread runs it once per launch, and keeping its switch out
+// of the stencil kernels leaves their registers to the z-march.
+static __device__ __noinline__ void ksp_finalize(KspState *st, Fin fin, const double *tot, int nv, double *out) {
   if (fin == FIN_STORE) {
-    for (int q = 0; q < nv; q++) out[q] = tot[q];
+    if (out)
+      for (int q = 0; q < nv; q++) out[q] = tot[q];
     return;
   }
   const bool precond = st->norm_type == FISHGPU_NORM_PRECONDITIONED;

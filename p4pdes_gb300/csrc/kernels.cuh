@@ -1,12 +1,11 @@
-// kernels.cuh -- stencil, smoother, grid-transfer and Krylov-vector kernels.
+// kernels.cuh -- the point-wise operator kernels of the call-back entry
+// points (any owned sub-box, global indexing) and the exact coarse solve.
 //
-// All kernels are templated on the dimension DIM (1,2,3) and on the storage
-// and arithmetic type T (double for the FP64 path, float for the FP32
-// V-cycle of the mixed form).  A thread owns one (i,j) column and marches
-// `zc` consecutive k-planes; blocks are (32,8) threads over (i,j) (256 x 1
-// in 1D).  Kernels that belong to a CG iteration take the device KspState
-// and return at once when it is marked done, so surplus iterations of a
-// captured graph cost only empty launches.
+// Templated on the dimension DIM (1,2,3) and on the storage and arithmetic
+// type T.  A thread owns one (i,j) column and marches `zc` consecutive
+// k-planes; blocks are (32,8) threads over (i,j) (256 x 1 in 1D).  The
+// solver's own whole-grid kernels (vectorised, padded layout) live in
+// vkernels.cuh.
 //
 // The operator is the Jacobian the reference assembles
 // (c/ch6/poissonfunctions.c:117-258), applied matrix-free: boundary rows
@@ -116,160 +115,6 @@ __global__ void __launch_bounds__(256) k_apply(Geom g, Range R, Tiles tm, KspSta
   }
 }
 
-// ------------------------------------------------------------------ CG vectors
-// p = z + (beta/betaold) p; p = z on the first iteration (PETSc VecAYPX / VecCopy)
-template <int DIM, typename T>
-__global__ void __launch_bounds__(256) k_cg_p(Geom g, Range R, Tiles tm, KspState *st,
-                                              const T *__restrict__ z, T *__restrict__ p) {
-  if (ksp_done(st)) return;
-  const bool first = st->i == 0;
-  const T bb = first ? T(0) : (T)(st->beta / st->betaold);
-  FG_POINT_LOOP_BEGIN(R)
-  p[n] = first ? z[n] : fma(bb, p[n], z[n]);
-  FG_POINT_LOOP_END
-}
-
-// y += alpha p; r -= alpha w; RR: r.r reduced (unpreconditioned norm test)
-template <int DIM, typename T, bool RR>
-__global__ void __launch_bounds__(256) k_cg_xr(Geom g, Range R, Tiles tm, KspState *st,
-                                               const T *__restrict__ p, const T *__restrict__ w,
-                                               T *__restrict__ y, T *__restrict__ r, Reducer red,
-                                               int slot) {
-  if (ksp_done(st)) return;
-  const T a = (T)st->alpha;
-  T acc = T(0);
-  FG_POINT_LOOP_BEGIN(R)
-  y[n] = fma(a, p[n], y[n]);
-  T rn = fma(-a, w[n], r[n]);
-  r[n] = rn;
-  if (RR) acc = fma(rn, rn, acc);
-  FG_POINT_LOOP_END
-  if (RR) {
-    double v1[1] = {(double)acc};
-    reduce_and_finalize<1>(v1, red, slot, st, FIN_RR, nullptr);
-  }
-}
-
-// z.z and z.r reduced together
-template <int DIM, typename T>
-__global__ void __launch_bounds__(256) k_dots_zr(Geom g, Range R, Tiles tm, KspState *st,
-                                                 const T *__restrict__ z, const T *__restrict__ r,
-                                                 Reducer red, int slot, Fin fin, double *out) {
-  if (ksp_done(st)) return;
-  T zz = T(0), zr = T(0);
-  FG_POINT_LOOP_BEGIN(R)
-  T zn = z[n];
-  zz = fma(zn, zn, zz);
-  zr = fma(zn, r[n], zr);
-  FG_POINT_LOOP_END
-  double v2[2] = {(double)zz, (double)zr};
-  reduce_and_finalize<2>(v2, red, slot, st, fin, out);
-}
-
-// ------------------------------------------------------------------ smoothers
-// One Chebyshev (or Richardson) step preconditioned by Jacobi:
-//   out = ckm1*xkm1 + ck*xk + crd*(b - A xk),   crd = c_r / scdiag.
-// HAS_XK=false means xk = 0 (first step from a zero iterate);
-// HAS_KM1=false drops the xkm1 term.  out may alias xkm1 (read at n only).
-template <int DIM, typename T, bool HAS_XK, bool HAS_KM1>
-__global__ void __launch_bounds__(256) k_cheb(Geom g, Tiles tm, KspState *st, const T *__restrict__ b,
-                                              const T *xkm1, const T *__restrict__ xk, T *out,
-                                              T ckm1, T ck, T crd) {
-  if (ksp_done(st)) return;
-  const Wt<T> w(g);
-  const Range R = full_range(g);
-  FG_POINT_LOOP_BEGIN(R)
-  T v;
-  if (HAS_XK) {
-    T t = resid_at<DIM, T>(b, xk, n, i, j, k, g, w);
-    T base = ck * xk[n];
-    if (HAS_KM1) base = fma(ckm1, xkm1[n], base);
-    v = fma(crd, t, base);
-  } else {
-    v = crd * b[n];
-    if (HAS_KM1) v = fma(ckm1, xkm1[n], v);
-  }
-  out[n] = v;
-  FG_POINT_LOOP_END
-}
-
-// r = b - A x
-template <int DIM, typename T>
-__global__ void __launch_bounds__(256) k_resid(Geom g, Tiles tm, KspState *st, const T *__restrict__ b,
-                                               const T *__restrict__ x, T *__restrict__ r) {
-  if (ksp_done(st)) return;
-  const Wt<T> w(g);
-  const Range R = full_range(g);
-  FG_POINT_LOOP_BEGIN(R)
-  r[n] = resid_at<DIM, T>(b, x, n, i, j, k, g, w);
-  FG_POINT_LOOP_END
-}
-
-// ------------------------------------------------------------------ grid transfers
-// b_c = P^T r_f : full weighting with weights prod_d (1 - |delta_d|/2), the
-// transpose of DMDA's Q1 interpolation, over every coarse node.
-template <int DIM, typename T>
-__global__ void __launch_bounds__(256) k_restrict(Geom gf, Geom g, Tiles tm, KspState *st,
-                                                  const T *__restrict__ rf, T *__restrict__ bc) {
-  if (ksp_done(st)) return;
-  const Range R = full_range(g);
-  FG_POINT_LOOP_BEGIN(R)
-  const int fi = 2 * i;
-  const bool hw = fi - 1 >= 0, he = fi + 1 < gf.mx;
-  T acc = T(0);
-  const int dk = DIM >= 3 ? 1 : 0, dj = DIM >= 2 ? 1 : 0;
-  for (int a = -dk; a <= dk; a++) {
-    const int fk = 2 * k + a;
-    if (fk < 0 || fk >= gf.mz) continue;
-    T accy = T(0);
-    for (int bb = -dj; bb <= dj; bb++) {
-      const int fj = 2 * j + bb;
-      if (fj < 0 || fj >= gf.my) continue;
-      const long long m = gidx(gf, fi, fj, fk);
-      T side = (hw ? rf[m - 1] : T(0)) + (he ? rf[m + 1] : T(0));
-      T row = fma(T(0.5), side, rf[m]);
-      accy = bb ? fma(T(0.5), row, accy) : accy + row;
-    }
-    acc = a ? fma(T(0.5), accy, acc) : acc + accy;
-  }
-  bc[n] = acc;
-  FG_POINT_LOOP_END
-}
-
-// x_f += P x_c : DMDA Q1 interpolation, vertex-centred, ratio 2
-template <int DIM, typename T>
-__global__ void __launch_bounds__(256) k_prolong(Geom g, Geom gc, Tiles tm, KspState *st,
-                                                 const T *__restrict__ xc, T *__restrict__ xf) {
-  if (ksp_done(st)) return;
-  const Range R = full_range(g);
-  FG_POINT_LOOP_BEGIN(R)
-  const int I = i >> 1, J = j >> 1, K = k >> 1;
-  const bool oi = i & 1, oj = DIM >= 2 && (j & 1), ok = DIM >= 3 && (k & 1);
-  const long long m = gidx(gc, I, J, K);
-  T s = xc[m];
-  if (oi) s += xc[m + 1];
-  if (oj) {
-    T t = xc[m + gc.pitch];
-    if (oi) t += xc[m + gc.pitch + 1];
-    s += t;
-  }
-  if (ok) {
-    const long long m2 = m + gc.plane;
-    T t = xc[m2];
-    if (oi) t += xc[m2 + 1];
-    if (oj) {
-      T u = xc[m2 + gc.pitch];
-      if (oi) u += xc[m2 + gc.pitch + 1];
-      t += u;
-    }
-    s += t;
-  }
-  const int nodd = (int)oi + (int)oj + (int)ok;
-  const T wgt = nodd == 0 ? T(1) : nodd == 1 ? T(0.5) : nodd == 2 ? T(0.25) : T(0.125);
-  xf[n] = fma(wgt, s, xf[n]);
-  FG_POINT_LOOP_END
-}
-
 // ------------------------------------------------------------------ coarse solve
 // Exact solve on the coarsest level in ONE block: boundary rows x = b/scdiag;
 // interior by sine-transform diagonalisation x = S (Lambda^{-1} (S b)) with
@@ -333,25 +178,6 @@ __global__ void __launch_bounds__(1024) k_coarse(Geom g, KspState *st, int batch
     int i = q % n0, j = (q / n0) % n1, k = q / (n0 * n1);
     x[gidx(g, i + 1, j + oj, k + ok)] = A[q];
   }
-}
-
-// ------------------------------------------------------------------ misc
-template <int DIM, typename T>
-__global__ void __launch_bounds__(256) k_zero(Geom g, Tiles tm, T *__restrict__ a) {
-  const Range R = full_range(g);
-  FG_POINT_LOOP_BEGIN(R)
-  a[n] = T(0);
-  FG_POINT_LOOP_END
-}
-
-template <int DIM, typename T>
-__global__ void __launch_bounds__(256) k_copy(Geom g, Tiles tm, KspState *st, const T *__restrict__ a,
-                                              T *__restrict__ b) {
-  if (ksp_done(st)) return;
-  const Range R = full_range(g);
-  FG_POINT_LOOP_BEGIN(R)
-  b[n] = a[n];
-  FG_POINT_LOOP_END
 }
 
 }  // namespace fg

@@ -234,6 +234,23 @@ static inline int third(int a, int b) { return 3 - a - b; }
 // (the arithmetic is identical).  Rotates the level's three buffers.
 // dots: when >= 0, the last step also reduces z.z and z.b and runs Fin(dots)
 // (the CG scalar update), so the separate dot kernel is not needed.
+// Smoothing step that also reduces z.z and z.b: per-plane reductions for a
+// batch (2D only), one reduction over the grid otherwise.
+template <int DIM, typename T, bool HAS_KM1>
+static void launch_cheb_dots(fishgpu_solver *S, Level<T> &lv, const T *xkm1, const T *xk, T *out, T ckm1, T ck,
+                             T crd, Fin fin) {
+  const unsigned gb = slot_blocks(lv.sl);
+  if constexpr (DIM == 2) {
+    if (S->batch) {
+      v_cheb<DIM, T, HAS_KM1, true, true><<<gb, lv.sl.chunk, 0, S->stream>>>(lv.g, lv.sl, S->st, lv.b, xkm1, xk, out,
+                                                                         ckm1, ck, crd, S->red, 0, fin);
+      return;
+    }
+  }
+  v_cheb<DIM, T, HAS_KM1, true, false><<<gb, lv.sl.chunk, 0, S->stream>>>(lv.g, lv.sl, S->st, lv.b, xkm1, xk, out, ckm1,
+                                                                       ck, crd, S->red, 0, fin);
+}
+
 template <int DIM, typename T>
 static void enq_smooth(fishgpu_solver *S, Level<T> &lv, bool from_zero, int dots = -1) {
   const fishgpu_opts &o = S->o;
@@ -252,8 +269,7 @@ static void enq_smooth(fishgpu_solver *S, Level<T> &lv, bool from_zero, int dots
       if (from_zero && it == 0)
         v_scale<T><<<gb, lv.sl.chunk, 0, s>>>(lv.g, lv.sl, st, lv.b, crd, lv.X[nxt]);
       else if (last)
-        v_cheb<DIM, T, false, true><<<gb, lv.sl.chunk, 0, s>>>(lv.g, lv.sl, st, lv.b, nullptr, lv.X[cur], lv.X[nxt], T(0), T(1),
-                                                       crd, S->red, 0, fin);
+        launch_cheb_dots<DIM, T, false>(S, lv, nullptr, lv.X[cur], lv.X[nxt], T(0), T(1), crd, fin);
       else
         v_cheb<DIM, T, false><<<gb, lv.sl.chunk, 0, s>>>(lv.g, lv.sl, st, lv.b, nullptr, lv.X[cur], lv.X[nxt], T(0), T(1), crd);
       cur = nxt;
@@ -283,8 +299,7 @@ static void enq_smooth(fishgpu_solver *S, Level<T> &lv, bool from_zero, int dots
     km1 = lv.cur;
     kk = (lv.cur + 1) % 3;
     if (o.smooth_its == 1 && dots >= 0)
-      v_cheb<DIM, T, false, true><<<gb, lv.sl.chunk, 0, s>>>(lv.g, lv.sl, st, lv.b, nullptr, lv.X[km1], lv.X[kk], T(0), T(1),
-                                                     (T)c1, S->red, 0, fin);
+      launch_cheb_dots<DIM, T, false>(S, lv, nullptr, lv.X[km1], lv.X[kk], T(0), T(1), (T)c1, fin);
     else
       v_cheb<DIM, T, false><<<gb, lv.sl.chunk, 0, s>>>(lv.g, lv.sl, st, lv.b, nullptr, lv.X[km1], lv.X[kk], T(0), T(1), (T)c1);
   }
@@ -299,8 +314,8 @@ static void enq_smooth(fishgpu_solver *S, Level<T> &lv, bool from_zero, int dots
       v_cheb<DIM, T, false><<<gb, lv.sl.chunk, 0, s>>>(lv.g, lv.sl, st, lv.b, nullptr, lv.X[kk], lv.X[out], T(0), (T)omega,
                                                (T)(omega * c1));
     else if (last)
-      v_cheb<DIM, T, true, true><<<gb, lv.sl.chunk, 0, s>>>(lv.g, lv.sl, st, lv.b, lv.X[km1], lv.X[kk], lv.X[out],
-                                                    (T)(1.0 - omega), (T)omega, (T)(omega * c1), S->red, 0, fin);
+      launch_cheb_dots<DIM, T, true>(S, lv, lv.X[km1], lv.X[kk], lv.X[out], (T)(1.0 - omega), (T)omega,
+                                     (T)(omega * c1), fin);
     else
       v_cheb<DIM, T, true><<<gb, lv.sl.chunk, 0, s>>>(lv.g, lv.sl, st, lv.b, lv.X[km1], lv.X[kk], lv.X[out],
                                               (T)(1.0 - omega), (T)omega, (T)(omega * c1));
@@ -383,7 +398,17 @@ static void enq_cg_iter(fishgpu_solver *S, Hier<T> &H, KspVecs<T> v, int par) {
   const unsigned gf = S->gfl;
   T *pold = v.p[par], *pnew = v.p[1 - par];
   // p = z + beta/betaold p (z of the previous application), w = A p, p.w
-  v_cgp_apply<DIM, T><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(S->fine, S->sf, st, H.z, pold, pnew, v.w, S->red, 0);
+  bool planes = false;
+  if constexpr (DIM == 2) {
+    if (S->batch) {
+      v_cgp_apply<DIM, T, true><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(S->fine, S->sf, st, H.z, pold, pnew, v.w,
+                                                                       S->red, 0);
+      planes = true;
+    }
+  }
+  if (!planes)
+    v_cgp_apply<DIM, T, false><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(S->fine, S->sf, st, H.z, pold, pnew, v.w,
+                                                                      S->red, 0);
   if (S->ksp_norm == FISHGPU_NORM_UNPRECONDITIONED)
     v_cg_xr<T, true><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(S->fine, S->sf, st, pnew, v.w, v.y, v.r, S->red, 0);
   else
@@ -676,6 +701,27 @@ static int time_kernel_dim(fishgpu_solver *S, const char *name, int reps, double
   Level<double> &cd = S->h64.lev[S->h64.nlev > 1 ? S->h64.nlev - 2 : 0];
   const double sz = mixed ? 4.0 : 8.0;
   float t = 0.f;
+  // cgp_apply and cg_update read a CG state: one past its first iteration
+  // (beta/betaold = 1, a small alpha); p.w > 0 keeps it running, and a stop
+  // (non-finite data) is reported
+  KspState *tst = nullptr;
+  if (!strcmp(name, "cgp_apply") || !strcmp(name, "cg_update")) {
+    KspState h;
+    memset(&h, 0, sizeof(h));
+    h.i = 1;
+    h.beta = h.betaold = h.dpi = 1.0;
+    h.alpha = 1e-3;
+    h.norm_type = FISHGPU_NORM_UNPRECONDITIONED;
+    if (cudaMalloc((void **)&tst, sizeof(KspState)) != cudaSuccess) return FISHGPU_ERR_NOMEM;
+    if (cudaMemcpy(tst, &h, sizeof(h), cudaMemcpyHostToDevice) != cudaSuccess) {
+      cudaFree(tst);
+      return FISHGPU_ERR_CUDA;
+    }
+  }
+  struct Free {
+    KspState *p;
+    ~Free() { if (p) cudaFree(p); }
+  } free_tst{tst};
   FG_CUDA(cudaEventRecord(S->ev0, s));
   for (int q = 0; q < reps; q++) {
     if (!strcmp(name, "smooth")) {  // one Chebyshev step with x_{k-1}: reads b, x_{k-1}, x_k, writes x_{k+1}
@@ -683,6 +729,20 @@ static int time_kernel_dim(fishgpu_solver *S, const char *name, int reps, double
         v_cheb<DIM, float, true><<<gb, sl.chunk, 0, s>>>(g, sl, nullptr, S->r32, lf.X[0], lf.X[1], lf.X[2], 0.5f, 0.5f, 0.1f);
       else
         v_cheb<DIM, double, true><<<gb, sl.chunk, 0, s>>>(g, sl, nullptr, S->r64, ld.X[0], ld.X[1], ld.X[2], 0.5, 0.5, 0.1);
+      *bytes = 4.0 * sz * N;
+    } else if (!strcmp(name, "smooth_dots")) {  // the same step with z.z and z.b reduced (last post-smoothing step)
+      if (mixed)
+        v_cheb<DIM, float, true, true><<<gb, sl.chunk, 0, s>>>(g, sl, nullptr, S->r32, lf.X[0], lf.X[1], lf.X[2], 0.5f,
+                                                               0.5f, 0.1f, S->red, 1, FIN_STORE);
+      else
+        v_cheb<DIM, double, true, true><<<gb, sl.chunk, 0, s>>>(g, sl, nullptr, S->r64, ld.X[0], ld.X[1], ld.X[2], 0.5,
+                                                                0.5, 0.1, S->red, 1, FIN_STORE);
+      *bytes = 4.0 * sz * N;
+    } else if (!strcmp(name, "cgp_apply")) {  // p = z + beta p_old, w = A p, p.w: reads z, p_old, writes p, w
+      if (mixed)
+        v_cgp_apply<DIM, float><<<gb, sl.chunk, 0, s>>>(g, sl, tst, lf.X[0], S->p32, S->q32, S->w32, S->red, 1);
+      else
+        v_cgp_apply<DIM, double><<<gb, sl.chunk, 0, s>>>(g, sl, tst, ld.X[0], S->p64, S->q64, S->w64, S->red, 1);
       *bytes = 4.0 * sz * N;
     } else if (!strcmp(name, "smooth_zero")) {  // two steps from zero: reads b, writes x
       if (mixed)
@@ -704,9 +764,9 @@ static int time_kernel_dim(fishgpu_solver *S, const char *name, int reps, double
       *bytes = 2.0 * sz * N;
     } else if (!strcmp(name, "cg_update")) {
       if (mixed)
-        v_cg_xr<float, false><<<gb, sl.chunk, 0, s>>>(g, sl, nullptr, S->p32, S->w32, S->y32, S->r32, S->red, 1);
+        v_cg_xr<float, false><<<gb, sl.chunk, 0, s>>>(g, sl, tst, S->p32, S->w32, S->y32, S->r32, S->red, 1);
       else
-        v_cg_xr<double, false><<<gb, sl.chunk, 0, s>>>(g, sl, nullptr, S->p64, S->w64, S->y64, S->r64, S->red, 1);
+        v_cg_xr<double, false><<<gb, sl.chunk, 0, s>>>(g, sl, tst, S->p64, S->w64, S->y64, S->r64, S->red, 1);
       *bytes = 6.0 * sz * N;
     } else if (!strcmp(name, "restrict")) {
       if (mixed)
@@ -732,6 +792,11 @@ static int time_kernel_dim(fishgpu_solver *S, const char *name, int reps, double
   FG_CUDA(cudaGetLastError());
   FG_CUDA(cudaEventElapsedTime(&t, S->ev0, S->ev1));
   *ms = (double)t / reps;
+  if (tst) {
+    int done = 0;
+    FG_CUDA(cudaMemcpy(&done, &tst->done, sizeof(int), cudaMemcpyDeviceToHost));
+    if (done) return FISHGPU_ERR_NONFINITE;  // the state stopped: launches exited early
+  }
   return FISHGPU_OK;
 }
 
@@ -869,6 +934,45 @@ extern "C" int fishgpu_solver_create(const fishgpu_opts *o, void *stream, fishgp
 
 extern "C" long long fishgpu_solver_bytes(const fishgpu_solver *S) { return S ? S->bytes : 0; }
 
+// Device bytes fishgpu_solver_create would allocate for these options (plus
+// the host-array buffers of fishgpu_solver_solve_host), without allocating.
+extern "C" long long fishgpu_solver_estimate_bytes(const fishgpu_opts *o) {
+  if (validate_opts(o)) return -1;
+  const int dim = o->ctx.dim;
+  auto rnd = [](long long b) { return (b + 255) / 256 * 256; };
+  Geom d = make_geom(dim, o->mx, dim >= 2 ? o->my : 1, dim >= 3 ? o->mz : 1, 1, 1, 1, 1, 1, 1);
+  Geom g = padded(d);
+  const long long N = (long long)nelem(g), Nd = (long long)d.plane * d.mz;
+  long long b = rnd(sizeof(KspState)) + rnd(64);  // state, scalars
+  const long long cap = slot_blocks(make_slots(g, ZC));
+  b += rnd(8LL * 4 * cap) + rnd(16);
+  b += 4 * rnd(8LL * N);                                          // u, beff, y, r
+  if (o->ctx.problem == FISHGPU_USER && !o->ctx.f) b += 3 * rnd(8LL * Nd);  // f, g, u (host-array form)
+  const int es = o->precision == FISHGPU_MIXED ? 4 : 8;
+  if (o->precision == FISHGPU_MIXED) b += rnd(8LL * N) + 5 * rnd(4LL * N);  // b64; r p q w y (FP32)
+  else b += 3 * rnd(8LL * N);                                              // p q w
+  if (o->pc_type != FISHGPU_PC_MG) return b + rnd((long long)es * N);
+  Geom lv = g;
+  for (int l = o->mg_levels - 1; l >= 0; l--) {
+    const long long Nl = (long long)nelem(lv);
+    b += 3 * rnd((long long)es * Nl) + (l > 0 ? rnd((long long)es * Nl) : 0) + (l < o->mg_levels - 1 ? rnd((long long)es * Nl) : 0);
+    if (l > 0) {
+      const int m[3] = {lv.mx, lv.my, lv.mz};
+      for (int q = 0; q < dim; q++)
+        if (m[q] < 3 || (m[q] - 1) % 2) return -1;
+      lv = padded(make_geom(dim, (lv.mx - 1) / 2 + 1, dim >= 2 ? (lv.my - 1) / 2 + 1 : 1,
+                            dim >= 3 ? (lv.mz - 1) / 2 + 1 : 1, 1, 1, 1, 1, 1, 1));
+    } else {
+      const int m[3] = {lv.mx, lv.my, lv.mz};
+      long long ni = 1;
+      for (int q = 0; q < dim; q++) ni *= m[q] - 2;
+      for (int q = 0; q < dim && ni > 0; q++) b += rnd((long long)es * (m[q] - 2) * (m[q] - 2));
+      if (ni > 0) b += rnd((long long)es * ni) + rnd((long long)es * 2 * ni);  // 1/lambda, work area
+    }
+  }
+  return b;
+}
+
 extern "C" int fishgpu_solver_solve(fishgpu_solver *S, double *u_dev, fishgpu_report *rep) {
   if (!S || !u_dev || !rep) return FISHGPU_ERR_ARG;
   memset(rep, 0, sizeof(*rep));
@@ -912,7 +1016,7 @@ extern "C" int fishgpu_solver_solve_host(fishgpu_solver *S, const double *f_host
                                          double *u_host, fishgpu_report *rep) {
   if (!S || !u_host || !rep) return FISHGPU_ERR_ARG;
   const bool user = S->o.ctx.problem == FISHGPU_USER;
-  if (user && (!S->f_own || !f_host || !g_host)) return FISHGPU_ERR_ARG;
+  if (user && (!S->f_own || !f_host)) return FISHGPU_ERR_ARG;  // g_host NULL: zero boundary data
   const size_t N = (size_t)S->dense.plane * S->dense.mz;
   cudaStream_t s = S->stream;
   if (!S->u_own) {
@@ -924,7 +1028,8 @@ extern "C" int fishgpu_solver_solve_host(fishgpu_solver *S, const double *f_host
   int rc = FISHGPU_OK;
   cudaEventRecord(e0, s);
   if (user && (cudaMemcpyAsync(S->f_own, f_host, sizeof(double) * N, cudaMemcpyHostToDevice, s) != cudaSuccess ||
-               cudaMemcpyAsync(S->g_own, g_host, sizeof(double) * N, cudaMemcpyHostToDevice, s) != cudaSuccess))
+               (g_host ? cudaMemcpyAsync(S->g_own, g_host, sizeof(double) * N, cudaMemcpyHostToDevice, s)
+                       : cudaMemsetAsync(S->g_own, 0, sizeof(double) * N, s)) != cudaSuccess))
     rc = FISHGPU_ERR_CUDA;
   if (!rc && S->o.initial_type == FISHGPU_INITIAL_GIVEN &&
       cudaMemcpyAsync(S->u_own, u_host, sizeof(double) * N, cudaMemcpyHostToDevice, s) != cudaSuccess)

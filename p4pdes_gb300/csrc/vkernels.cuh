@@ -114,12 +114,14 @@ __device__ __forceinline__ SlotPos slot_pos(const Geom &g, const Slots &s) {
   return p;
 }
 
-// Resident blocks per SM the compiler is asked to fit: 5 x 256 threads for
-// FP32 stencils (48 registers, no spills) to cover HBM latency; FP64 stencils
+// Resident blocks per SM the compiler is asked to fit: 4 x 256 threads for
+// FP32 stencils (up to 64 registers).  Measured on the 513^3 Chebyshev step:
+// a cap of 48 registers (5 blocks) made the z-march 14% slower without a
+// reduction and 2.1x slower with the fused z.z/z.b reduction; FP64 stencils
 // are FP64-pipe-bound and keep their registers.
 template <typename T>
 struct MinBlocks {
-  static constexpr int value = sizeof(T) == 4 ? 5 : 1;
+  static constexpr int value = sizeof(T) == 4 ? 4 : 1;
 };
 
 template <typename T>
@@ -209,19 +211,16 @@ __device__ __forceinline__ KspState *block_state(KspState *st, const Slots &s) {
   return st + blockIdx.x / s.nchunk;
 }
 
-// Sum over the blocks of a launch (or, for a batch, over the blocks of one
-// plane: tickets and the finaliser are per plane) and run `fin`.
+// Batched form of reduce_and_finalize: sum over the blocks of one plane
+// (tickets and the finaliser are per plane).  Not inlined, so that the
+// register allocation of the single-grid stencils does not carry it.
 template <int NV>
-__device__ __forceinline__ void reduce_slots(double (&v)[NV], Reducer red, int slot, KspState *st, Fin fin,
-                                             double *out, const Slots &s) {
-  if (!s.batch) {
-    reduce_and_finalize<NV>(v, red, slot, st, fin, out);
-    return;
-  }
+__device__ __noinline__ void reduce_planes(double (&v)[NV], Reducer red, int slot, KspState *st, Fin fin,
+                                           double *out, int nchunk) {
   __shared__ bool am_last;
   const int tid = threadIdx.x;
   const int nt = blockDim.x;
-  const int plane = blockIdx.x / s.nchunk, first = plane * s.nchunk, nb = s.nchunk;
+  const int plane = blockIdx.x / nchunk, first = plane * nchunk, nb = nchunk;
   block_sum<NV>(v);
   unsigned int *ticket = red.tickets + (size_t)slot * red.tcap + plane;
   if (tid == 0) {
@@ -245,6 +244,32 @@ __device__ __forceinline__ void reduce_slots(double (&v)[NV], Reducer red, int s
     *ticket = 0u;
     if (st || fin == FIN_STORE) ksp_finalize(st, fin, sum, NV, out ? out + plane * NV : nullptr);
   }
+}
+
+// Sum over the blocks of a launch (or, for a batch, over the blocks of one
+// plane) and run `fin`.
+template <int NV>
+__device__ __forceinline__ void reduce_slots(double (&v)[NV], Reducer red, int slot, KspState *st, Fin fin,
+                                             double *out, const Slots &s) {
+  if (!s.batch) reduce_and_finalize<NV>(v, red, slot, st, fin, out);
+  else reduce_planes<NV>(v, red, slot, st, fin, out, s.nchunk);
+}
+
+// The same with the batch flag fixed at compile time: the stencil kernels
+// that reduce are instantiated twice, so the single-grid form carries no
+// per-plane code (a runtime branch there cost registers and spills in the
+// z-march).
+template <int NV, bool PL>
+__device__ __forceinline__ void reduce_sel(double (&v)[NV], Reducer red, int slot, KspState *st, Fin fin,
+                                           double *out, const Slots &s) {
+  if constexpr (PL) reduce_planes<NV>(v, red, slot, st, fin, out, s.nchunk);
+  else reduce_and_finalize<NV>(v, red, slot, st, fin, out);
+}
+
+template <bool PL>
+__device__ __forceinline__ KspState *block_state_sel(KspState *st, const Slots &s) {
+  if constexpr (PL) return st ? st + blockIdx.x / s.nchunk : st;
+  else return st;
 }
 
 // Generic z-march over the slot's planes.  `Op` is called once per plane
@@ -291,12 +316,12 @@ __device__ __forceinline__ bool jk_bdry(const Geom &g, int dim, int j, int k) {
 // smoother rotates three buffers per level).
 // DOTS: also reduces out.out and out.b (the preconditioned residual's z.z and
 // z.r when this is the last smoothing step on the finest level) and runs `fin`.
-template <int DIM, typename T, bool HAS_KM1, bool DOTS = false>
+template <int DIM, typename T, bool HAS_KM1, bool DOTS = false, bool PL = false>
 __global__ void __launch_bounds__(256, MinBlocks<T>::value) v_cheb(Geom g, Slots s, KspState *st, const T *__restrict__ b,
                                               const T *__restrict__ xkm1, const T *__restrict__ xk,
                                               T *__restrict__ out, T ckm1, T ck, T crd, Reducer red = Reducer{},
                                               int slot = 0, Fin fin = FIN_STORE) {
-  st = block_state(st, s);
+  st = DOTS ? block_state_sel<PL>(st, s) : block_state(st, s);
   if (ksp_done_v(st)) return;
   const SlotPos p = slot_pos(g, s);
   const Wv<T> w(g);
@@ -327,7 +352,7 @@ __global__ void __launch_bounds__(256, MinBlocks<T>::value) v_cheb(Geom g, Slots
   march<DIM, T>(g, s, p, xk, op);
   if (DOTS) {
     double v2[2] = {(double)zz, (double)zr};
-    reduce_slots<2>(v2, red, slot, st, fin, nullptr, s);
+    reduce_sel<2, PL>(v2, red, slot, st, fin, nullptr, s);
   }
 }
 
@@ -387,7 +412,7 @@ template <int DIM, typename T>
 __global__ void __launch_bounds__(256, MinBlocks<T>::value) v_apply_dot(Geom g, Slots s, KspState *st, const T *__restrict__ pv,
                                                    T *__restrict__ wv, Reducer red, int slot, Fin fin,
                                                    double *out) {
-  st = block_state(st, s);
+  st = block_state_sel<false>(st, s);
   if (ksp_done_v(st)) return;
   const SlotPos p = slot_pos(g, s);
   const Wv<T> w(g);
@@ -409,21 +434,21 @@ __global__ void __launch_bounds__(256, MinBlocks<T>::value) v_apply_dot(Geom g, 
   };
   march<DIM, T>(g, s, p, pv, op);
   double v1[1] = {(double)acc};
-  reduce_slots<1>(v1, red, slot, st, fin, out, s);
+  reduce_sel<1, false>(v1, red, slot, st, fin, out, s);
 }
 
 // p_new = z + (beta/betaold) p_old (p_new = z on the first CG iteration),
 // w = A p_new, p_new.w reduced: the CG direction update fused into the apply.
 // p_old and p_new are different buffers (neighbours read p_old).
-template <int DIM, typename T>
+template <int DIM, typename T, bool PL = false>
 __global__ void __launch_bounds__(256, MinBlocks<T>::value) v_cgp_apply(Geom g, Slots s, KspState *st, const T *__restrict__ z,
                                                    const T *__restrict__ pold, T *__restrict__ pnew,
                                                    T *__restrict__ wv, Reducer red, int slot) {
-  st = block_state(st, s);
+  st = block_state_sel<PL>(st, s);
   if (ksp_done_v(st)) return;
   const SlotPos p = slot_pos(g, s);
   const Wv<T> w(g);
-  const bool first = st->i == 0;
+  const bool first = !st || st->i == 0;  // no state: p = z
   const AxpySrc<T> src{z, pold, first ? T(0) : (T)(st->beta / st->betaold), first};
   T acc = T(0);
   auto op = [&](int k, long long n, const Nb<T> &nb) {
@@ -444,7 +469,7 @@ __global__ void __launch_bounds__(256, MinBlocks<T>::value) v_cgp_apply(Geom g, 
   };
   march_src<DIM, T>(g, s, p, src, op);
   double v1[1] = {(double)acc};
-  reduce_slots<1>(v1, red, slot, st, FIN_PW, nullptr, s);
+  reduce_sel<1, PL>(v1, red, slot, st, FIN_PW, nullptr, s);
 }
 
 // ------------------------------------------------------------------ grid transfers
@@ -511,8 +536,13 @@ __global__ void __launch_bounds__(256) v_restrict(Geom gf, Geom g, Slots s, KspS
 // writes the 8 fine x-points 2I4 .. 2I4+7 of fine rows 2J, 2J+1 and planes
 // 2K, 2K+1 (those inside the fine grid).  The x-interpolated coarse rows J and
 // J+1 of plane K+1 are kept for the next plane (one plane window).
-template <int DIM, typename T>
-__global__ void __launch_bounds__(256, 4) v_prolong(Geom gf, Geom g, Slots s, KspState *st, const T *__restrict__ xc,
+template <typename T>
+struct ProlongBlocks {  // FP32: 4 x 256 threads per SM; FP64: no cap (a cap of 64 spilled)
+  static constexpr int value = sizeof(T) == 4 ? 4 : 1;
+};
+
+template <int DIM, typename T, int MB = ProlongBlocks<T>::value>
+__global__ void __launch_bounds__(256, MB) v_prolong(Geom gf, Geom g, Slots s, KspState *st, const T *__restrict__ xc,
                                                  T *__restrict__ xf) {
   st = block_state(st, s);
   if (ksp_done_v(st)) return;
@@ -588,7 +618,7 @@ __global__ void __launch_bounds__(256) v_cg_xr(Geom g, Slots s, KspState *st, co
                                                Reducer red, int slot) {
   st = block_state(st, s);
   if (ksp_done_v(st)) return;
-  const T a = (T)st->alpha;
+  const T a = st ? (T)st->alpha : T(0);  // no state: alpha = 0
   T acc = T(0);
   FG_PW_BEGIN
   const V4<T> pp = ld4(pv + n), ww = ld4(wv + n), yy = ld4(y + n), rr = ld4(r + n);

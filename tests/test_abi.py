@@ -46,6 +46,35 @@ def test_struct_sizes_match_the_header(built, tmp_path):
     assert got == want
 
 
+def test_batch_and_server_structs_match_the_header(built, tmp_path):
+    import subprocess
+    import p4pdes_gb300 as fg
+    src = tmp_path / "sz2.c"
+    src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "fishgpu.h"\n'
+                   'int main(void){printf("%zu %zu %zu %zu %zu %zu\\n", sizeof(fishgpu_batch_opts),'
+                   ' sizeof(fishgpu_batch_report), sizeof(fishgpu_server_opts), sizeof(fishgpu_server_result),'
+                   ' offsetof(fishgpu_server_opts, rtol), offsetof(fishgpu_server_result, latency_ms));return 0;}\n')
+    exe = tmp_path / "sz2"
+    subprocess.run(["gcc", "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)],
+                   check=True)
+    got = [int(v) for v in subprocess.run([str(exe)], stdout=subprocess.PIPE, text=True).stdout.split()]
+    want = [ctypes.sizeof(fg.BatchOpts), ctypes.sizeof(fg.BatchReport), ctypes.sizeof(fg.ServerOpts),
+            ctypes.sizeof(fg.ServerResult), fg.ServerOpts.rtol.offset, fg.ServerResult.latency_ms.offset]
+    assert got == want
+
+
+def test_server_options_for_a_request(built):
+    import p4pdes_gb300 as fg
+    o = fg.server_request_opts(3, 257)
+    assert (o.mx, o.my, o.mz, o.mg_levels, o.ctx.problem) == (257, 257, 257, 8, fg.USER)
+    est = fg.estimate_bytes(o)
+    # mixed form: 6 FP64 + 9 FP32 fine-grid arrays, f, g, u on the host side, coarser levels
+    assert 20 * 4 * 257 ** 3 < est < 40 * 4 * 257 ** 3
+    bad = fg.server_request_opts(3, 257)
+    bad.mx = 2
+    assert fg.estimate_bytes(bad) == -1
+
+
 def test_default_options_are_fish_defaults(built):
     import p4pdes_gb300 as fg
     o = fg.options([])
