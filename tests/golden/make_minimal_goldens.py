@@ -1,0 +1,41 @@
+"""Regenerate tests/golden/minimal_goldens.json from the reference's regression
+files: the run lines of c/ch7/makefile (options, MPI process count) and the
+expected stdout in c/ch7/output/minimal.test{1..4}.  Run where the reference
+tree is mounted:
+
+    python tests/golden/make_minimal_goldens.py /path/to/p4pdes
+"""
+import json
+import os
+import re
+import sys
+
+
+def main(ref):
+    mk = open(os.path.join(ref, "c", "ch7", "makefile")).read()
+    runs = re.findall(r'runminimal_(\d+):\s*\n\s*-@\.\./testit\.sh minimal "([^"]*)" (\d+) (\d+)', mk)
+    out = []
+    for num, opts, nproc, testn in runs:
+        text = open(os.path.join(ref, "c", "ch7", "output", "minimal.test%s" % testn)).read()
+        rec = {"test": int(testn), "args": opts.split(), "nproc": int(nproc), "stdout": text}
+        rec["snes_norms"] = re.findall(r"\d+ SNES Function norm (\S+)", text)
+        rec["snes_its"] = [int(v) for v in re.findall(r"Nonlinear solve converged due to \S+ iterations (\d+)", text)]
+        rec["snes_reasons"] = re.findall(r"Nonlinear solve converged due to (\S+)", text)
+        rec["ksp_its"] = [int(v) for v in re.findall(r"Linear solve converged due to \S+ iterations (\d+)", text)]
+        rec["areas"] = [[float(a), float(b), float(c)] for a, b, c in
+                        re.findall(r"area = (\S+); (\S+) <= D <= (\S+)", text)]
+        m = re.search(r"done on (\d+) x (\d+) grid and problem (\w+)", text)
+        rec["grid"], rec["problem"] = [int(m.group(1)), int(m.group(2))], m.group(3)
+        m = re.search(r"error \|u-uexact\|_inf = (\S+)", text)
+        rec["errinf"] = m.group(1) if m else None
+        out.append(rec)
+    out.sort(key=lambda r: r["test"])
+    here = os.path.dirname(os.path.abspath(__file__))
+    with open(os.path.join(here, "minimal_goldens.json"), "w") as f:
+        json.dump(out, f, indent=1)
+        f.write("\n")
+    print("wrote %d records" % len(out))
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

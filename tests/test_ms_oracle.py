@@ -1,0 +1,108 @@
+"""The minimal-surface oracle (oracle/minimal_oracle.c + tests/_ms_oracle.py)
+pinned against the reference's regression outputs c/ch7/output/minimal.test*
+(tests/golden/minimal_goldens.json), and its Jacobian against differences of
+the residual."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import _ms_oracle as ms
+
+GOLD = {r["test"]: r for r in json.load(open(os.path.join(os.path.dirname(__file__), "golden",
+                                                          "minimal_goldens.json")))}
+
+
+def test_golden_1_catenoid_newton_history_and_error():
+    """-snes_fd_color -ms_catenoid_c 2.0 -da_refine 1 (5 x 5): the reference
+    solves each Newton step to KSP rtol 1e-5; the oracle solves exactly, so the
+    first norm agrees to the printed digits, the following ones to the size of
+    the reference's linear-solve error, and the converged error exactly."""
+    gold = GOLD[1]
+    levels, g, u, err = ms.solve(refine=1, c=2.0)
+    r = levels[0]
+    assert (g.mx, g.my) == tuple(gold["grid"])
+    assert r["its"] == gold["snes_its"][0] and ms.REASONS[r["reason"]] == gold["snes_reasons"][0]
+    norms = [float(v) for v in gold["snes_norms"]]
+    assert "%g" % r["fnorms"][0] == gold["snes_norms"][0]
+    for k in (1, 2, 3, 4):
+        assert abs(r["fnorms"][k] - norms[k]) <= 3e-3 * norms[k], k
+    assert r["fnorms"][5] < 1e-8 * r["fnorms"][0] and norms[5] < 1e-8 * norms[0]
+    assert "%.5e" % err == gold["errinf"]
+
+
+def test_golden_3_grid_sequence_areas_and_error():
+    """-snes_grid_sequence 2 -ms_monitor -ms_quaddegree 2 (3x3 -> 5x5 -> 9x9):
+    Newton iterations per grid, every monitored area / diffusivity bound, and
+    the final error."""
+    gold = GOLD[3]
+    levels, g, u, err = ms.solve(grid_sequence=2, monitor_degree=2)
+    assert [r["its"] for r in levels] == gold["snes_its"]
+    got = [a for r in levels for a in r["areas"]]
+    assert len(got) == len(gold["areas"])
+    for (a, lo, hi), (ga, glo, ghi) in zip(got, gold["areas"]):
+        assert abs(a - ga) <= 1e-7                       # intermediate iterates: reference's inexact steps
+        assert "%.4f" % lo == "%.4f" % glo and "%.4f" % hi == "%.4f" % ghi
+    # converged iterates agree to every printed digit
+    for r, k in zip(levels, (5, 9, 13)):
+        assert "%.8f" % r["areas"][-1][0] == "%.8f" % gold["areas"][k][0]
+    assert "%.5e" % err == gold["errinf"]
+
+
+def test_golden_4_tent_grid_sequence_iterations():
+    gold = GOLD[4]
+    levels, g, u, err = ms.solve(grid_sequence=2, problem=ms.TENT)
+    assert [r["its"] for r in levels] == gold["snes_its"]
+    assert [ms.REASONS[r["reason"]] for r in levels] == gold["snes_reasons"]
+    assert err is None and (g.mx, g.my) == tuple(gold["grid"])
+
+
+def test_golden_2_q0_is_the_five_point_laplacian():
+    """-ms_q 0 (test 2) turns the equation into Laplace's: the Jacobian is the
+    5-point stencil with fish's 2D scaling and identity boundary rows (the
+    reference's CG iteration counts there depend on PETSc's ILU and are not
+    restated)."""
+    g = ms.grid(9, ms.TENT, q=0.0)
+    J = ms.jacobian(g, ms.initial(g)).toarray()
+    n = 4 * 9 + 4
+    row = J[n].reshape(9, 9)
+    assert row[4, 4] == pytest.approx(4.0)
+    assert row[4, 3] == row[4, 5] == row[3, 4] == row[5, 4] == pytest.approx(-1.0)
+    assert row[3, 3] == row[5, 5] == row[3, 5] == row[5, 3] == 0.0
+    assert J[0, 0] == 1.0 and np.count_nonzero(J[0]) == 1
+    assert GOLD[2]["grid"] == [9, 9] and GOLD[2]["problem"] == "tent"
+
+
+@pytest.mark.parametrize("problem,q,c", [(ms.CATENOID, -0.5, 1.1), (ms.CATENOID, -0.5, 2.0), (ms.TENT, -0.5, 1.0),
+                                         (ms.TENT, 0.3, 1.0), (ms.CATENOID, 0.0, 1.5)])
+def test_jacobian_is_the_derivative_of_the_residual(problem, q, c):
+    rng = np.random.default_rng(7)
+    g = ms.grid(17, problem, q=q, c=c)
+    u = ms.initial(g) + 0.2 * rng.standard_normal(17 * 17)
+    v = rng.standard_normal(17 * 17)
+    h = 1e-6
+    fd = (ms.residual(g, u + h * v) - ms.residual(g, u - h * v)) / (2 * h)
+    jv = ms.jv(g, u, v)
+    assert np.max(np.abs(jv - fd)) <= 1e-7 * np.max(np.abs(fd))
+    assert np.allclose(ms.jacobian(g, u) @ v, jv, rtol=0, atol=1e-13 * np.max(np.abs(jv)))
+
+
+def test_interpolation_is_exact_for_bilinear_functions():
+    gc, gf = ms.grid(5), ms.grid(9)
+    xc = np.linspace(0, 1, 5)
+    xf = np.linspace(0, 1, 9)
+    f = lambda x, y: 1.0 + 2.0 * x - 3.0 * y + 0.5 * x * y
+    uc = f(xc[None, :], xc[:, None]).ravel()
+    uf = ms.interpolate(gc, uc, gf)
+    assert np.allclose(uf, f(xf[None, :], xf[:, None]).ravel(), atol=1e-14)
+
+
+def test_exact_catenoid_has_small_residual_and_converges_with_h():
+    """FormExactFromG: the continuum catenoid is not the discrete solution;
+    the discrete error shrinks like h^2."""
+    errs = []
+    for m in (9, 17, 33):
+        levels, g, u, err = ms.solve(base=m)
+        errs.append(err)
+    assert errs[0] / errs[1] > 3.0 and errs[1] / errs[2] > 3.0
