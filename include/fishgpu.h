@@ -289,6 +289,81 @@ int fishgpu_server_stats(fishgpu_server *s, long long *pooled_bytes, int *pooled
                          long long *evicted);
 int fishgpu_server_destroy(fishgpu_server *s);
 
+/* ---- minimal-surface equation (c/ch7/minimal.c) -------------------------
+   -div( (1 + |grad u|^2)^q grad u ) = 0 on the unit square, u = g on the
+   boundary (catenoid or tent data, minimal.c:27-42), 9-point finite
+   differences (FormFunctionLocal, minimal.c:210-282).  Newton (PETSc
+   SNESNEWTONLS with the cubic backtracking line search, SNESConvergedDefault)
+   with the exact Jacobian applied matrix-free; each Newton step J Y = F is
+   solved by FP32 BiCGStab right-preconditioned with the FP32 Poisson
+   multigrid V-cycle (the preconditioning matrix of minimal.c:142-145), while
+   F(u), the norms, the line search and the update stay FP64. */
+#define FISHGPU_MS_TENT     0
+#define FISHGPU_MS_CATENOID 1
+
+typedef struct {          /* MinimalCtx + the boundary function of PoissonCtx */
+  int problem;            /* FISHGPU_MS_TENT / FISHGPU_MS_CATENOID          */
+  double q;               /* exponent (default -1/2)                        */
+  double catenoid_c;      /* catenoid parameter, >= 1 (default 1.1)         */
+  double tent_H;          /* tent door height (default 1)                   */
+} fishgpu_ms_ctx;
+
+typedef struct {
+  fishgpu_ms_ctx ctx;
+  int mx, my;             /* first grid: 3x3 refined -da_refine times        */
+  int grid_sequence;      /* -snes_grid_sequence: further refinements        */
+  int exact_init;         /* -ms_exact_init (catenoid, q = -1/2)             */
+  double rtol, atol, stol;/* -snes_rtol/atol/stol: 1e-8, 1e-50, 1e-8         */
+  int max_it;             /* -snes_max_it: 50                                */
+  int line_search;        /* 1: bt (default), 0: basic (full Newton steps)  */
+  double ksp_rtol;        /* -ksp_rtol: 1e-5                                 */
+  int ksp_max_it;         /* -ksp_max_it: 10000                              */
+  int pc_type;            /* FISHGPU_PC_MG (default) or FISHGPU_PC_NONE      */
+  int mg_levels;          /* 0: down to 3x3                                  */
+  int monitor_degree;     /* -ms_monitor: quadrature degree 1..3, 0 = off    */
+  int snes_monitor, converged_reason, ksp_converged_reason; /* driver flags  */
+} fishgpu_ms_opts;
+
+#define FISHGPU_MS_MAX_GRIDS 12
+#define FISHGPU_MS_MAX_ITS   64
+
+typedef struct {
+  int ngrids;                                  /* grids solved (1 + grid_sequence) */
+  int m[FISHGPU_MS_MAX_GRIDS];                 /* nodes per side of each grid      */
+  int its[FISHGPU_MS_MAX_GRIDS];               /* Newton iterations                */
+  int reason[FISHGPU_MS_MAX_GRIDS];            /* SNES converged reason            */
+  int ksp_its[FISHGPU_MS_MAX_GRIDS][FISHGPU_MS_MAX_ITS]; /* inner iterations per step */
+  int ksp_reason[FISHGPU_MS_MAX_GRIDS][FISHGPU_MS_MAX_ITS];
+  double fnorm[FISHGPU_MS_MAX_GRIDS][FISHGPU_MS_MAX_ITS + 1];
+  double area[FISHGPU_MS_MAX_GRIDS][FISHGPU_MS_MAX_ITS + 1][3]; /* area, Dmin, Dmax */
+  double errinf;                               /* catenoid, q = -1/2; else -1      */
+  double solve_ms;                             /* all grids, device time           */
+  long long dofs;                              /* nodes of the last grid           */
+  long long total_ksp_its;
+} fishgpu_ms_report;
+
+int fishgpu_ms_opts_default(fishgpu_ms_opts *o);
+/* minimal.c's options (-ms_*, -da_refine, -da_grid_x/y, -snes_*, -ksp_rtol,
+   -ksp_max_it, -pc_type mg|none, -snes_linesearch_type bt|basic); options of
+   PETSc's Jacobian handling (-snes_fd_color, -snes_mf_operator,
+   -mat_is_symmetric) are accepted: the Jacobian is always the exact one */
+int fishgpu_ms_opts_parse(fishgpu_ms_opts *o, int argc, const char *const *argv);
+const char *fishgpu_snes_reason_name(int reason);
+
+typedef struct fishgpu_ms_solver_s fishgpu_ms_solver;
+/* set-up of every grid (hierarchies, buffers, graphs); stream NULL: own */
+int fishgpu_ms_solver_create(const fishgpu_ms_opts *o, void *stream, fishgpu_ms_solver **out);
+/* one solve from the initial iterate; u_host (last grid, mx*my doubles, x
+   fastest) may be NULL */
+int fishgpu_ms_solver_solve(fishgpu_ms_solver *s, double *u_host, fishgpu_ms_report *rep);
+int fishgpu_ms_solver_destroy(fishgpu_ms_solver *s);
+int fishgpu_ms_solve(const fishgpu_ms_opts *o, double *u_host, fishgpu_ms_report *rep);
+
+/* Drop-in residual call-back: FormFunctionLocal, c/ch7/minimal.c:210-282;
+   info->dim must be 2, whole-grid device arrays, global (i,j) indexing */
+int MinimalFunctionLocal_gpu(const fishgpu_info *info, const double *au, double *aF, const fishgpu_ms_ctx *ctx,
+                             void *stream);
+
 #ifdef __cplusplus
 }
 #endif

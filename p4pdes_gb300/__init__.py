@@ -28,6 +28,7 @@ __all__ = [
     "Poisson1DOperatorApply", "Poisson2DOperatorApply", "Poisson3DOperatorApply",
     "FormUExact", "InitialState", "error_norms", "reason_name",
     "Solver", "Batch", "Server", "estimate_bytes", "server_request_opts",
+    "MsSolver", "ms_options", "ms_solve", "MinimalFunctionLocal", "snes_reason_name",
 ]
 
 LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "lib", "libfishgpu.so")
@@ -117,6 +118,37 @@ class ServerResult(ctypes.Structure):
                 ("queue_ms", c_double), ("service_ms", c_double), ("latency_ms", c_double)]
 
 
+MS_TENT, MS_CATENOID = 0, 1
+MS_MAX_GRIDS, MS_MAX_ITS = 12, 64
+
+
+class MsCtx(ctypes.Structure):
+    _fields_ = [("problem", c_int), ("q", c_double), ("catenoid_c", c_double), ("tent_H", c_double)]
+
+
+class MsOpts(ctypes.Structure):
+    _fields_ = [("ctx", MsCtx), ("mx", c_int), ("my", c_int), ("grid_sequence", c_int), ("exact_init", c_int),
+                ("rtol", c_double), ("atol", c_double), ("stol", c_double), ("max_it", c_int),
+                ("line_search", c_int), ("ksp_rtol", c_double), ("ksp_max_it", c_int), ("pc_type", c_int),
+                ("mg_levels", c_int), ("monitor_degree", c_int), ("snes_monitor", c_int),
+                ("converged_reason", c_int), ("ksp_converged_reason", c_int)]
+
+
+class MsReport(ctypes.Structure):
+    _fields_ = [("ngrids", c_int), ("m", c_int * MS_MAX_GRIDS), ("its", c_int * MS_MAX_GRIDS),
+                ("reason", c_int * MS_MAX_GRIDS), ("ksp_its", (c_int * MS_MAX_ITS) * MS_MAX_GRIDS),
+                ("ksp_reason", (c_int * MS_MAX_ITS) * MS_MAX_GRIDS),
+                ("fnorm", (c_double * (MS_MAX_ITS + 1)) * MS_MAX_GRIDS),
+                ("area", ((c_double * 3) * (MS_MAX_ITS + 1)) * MS_MAX_GRIDS),
+                ("errinf", c_double), ("solve_ms", c_double), ("dofs", c_ll), ("total_ksp_its", c_ll)]
+
+    def fnorms(self, k):
+        return [self.fnorm[k][i] for i in range(self.its[k] + 1)]
+
+    def areas(self, k):
+        return [tuple(self.area[k][i]) for i in range(self.its[k] + 1)]
+
+
 class FishError(RuntimeError):
     def __init__(self, code, what=""):
         self.code = code
@@ -172,6 +204,19 @@ def load():
                  "fishgpu_batch_results", "fishgpu_batch_destroy"):
         getattr(lib, name).restype = c_int
     lib.fishgpu_solver_time_kernel.argtypes = [c_void_p, ctypes.c_char_p, c_int, _P(c_double), _P(c_double)]
+    lib.fishgpu_ms_opts_default.argtypes = [_P(MsOpts)]
+    lib.fishgpu_ms_opts_parse.argtypes = [_P(MsOpts), c_int, _P(ctypes.c_char_p)]
+    lib.fishgpu_ms_solver_create.argtypes = [_P(MsOpts), c_void_p, _P(c_void_p)]
+    lib.fishgpu_ms_solver_solve.argtypes = [c_void_p, c_void_p, _P(MsReport)]
+    lib.fishgpu_ms_solver_destroy.argtypes = [c_void_p]
+    lib.fishgpu_ms_solve.argtypes = [_P(MsOpts), c_void_p, _P(MsReport)]
+    lib.MinimalFunctionLocal_gpu.argtypes = [_P(Info), c_void_p, c_void_p, _P(MsCtx), c_void_p]
+    lib.fishgpu_snes_reason_name.argtypes = [c_int]
+    lib.fishgpu_snes_reason_name.restype = ctypes.c_char_p
+    for name in ("fishgpu_ms_opts_default", "fishgpu_ms_opts_parse", "fishgpu_ms_solver_create",
+                 "fishgpu_ms_solver_solve", "fishgpu_ms_solver_destroy", "fishgpu_ms_solve",
+                 "MinimalFunctionLocal_gpu"):
+        getattr(lib, name).restype = c_int
     lib.fishgpu_solver_estimate_bytes.argtypes = [_P(Opts)]
     lib.fishgpu_solver_estimate_bytes.restype = c_ll
     lib.fishgpu_server_opts_default.argtypes = [_P(ServerOpts)]
@@ -490,6 +535,75 @@ def server_request_opts(dim, n, rtol=1e-8, precision=MIXED):
     o.rtol = rtol
     o.norm_type = NORM_UNPRECONDITIONED
     return o
+
+
+def ms_options(argv=()):
+    """Parse minimal.c's flags into an MsOpts."""
+    if isinstance(argv, str):
+        argv = argv.split()
+    o = MsOpts()
+    _check(load().fishgpu_ms_opts_default(ctypes.byref(o)), "fishgpu_ms_opts_default")
+    arr = (ctypes.c_char_p * max(1, len(argv)))(*[a.encode() for a in argv])
+    _check(load().fishgpu_ms_opts_parse(ctypes.byref(o), len(argv), arr), "fishgpu_ms_opts_parse")
+    return o
+
+
+def snes_reason_name(reason):
+    return load().fishgpu_snes_reason_name(reason).decode()
+
+
+class MsSolver:
+    """Minimal-surface Newton solver (every grid of the sequence set up once)."""
+
+    def __init__(self, opts, stream=None):
+        self.opts = opts
+        self._h = c_void_p()
+        _check(load().fishgpu_ms_solver_create(ctypes.byref(opts), None if stream is None else int(stream),
+                                               ctypes.byref(self._h)), "fishgpu_ms_solver_create")
+
+    def solve(self, u=None):
+        """Returns the report; u: optional host float64 array (my, mx) of the last grid."""
+        rep = MsReport()
+        rc = load().fishgpu_ms_solver_solve(self._h, None if u is None else _host_addr(u), ctypes.byref(rep))
+        if rc not in (0, 4):
+            raise FishError(rc, "fishgpu_ms_solver_solve")
+        return rep
+
+    def close(self):
+        if self._h:
+            load().fishgpu_ms_solver_destroy(self._h)
+            self._h = c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def ms_solve(opts):
+    """minimal.c's flow; returns (u (numpy, last grid), report)."""
+    import numpy as np
+    with MsSolver(opts) as s:
+        m = opts.mx
+        my = opts.my
+        for _ in range(opts.grid_sequence):
+            m, my = 2 * m - 1, 2 * my - 1
+        u = np.empty((my, m))
+        rep = s.solve(u)
+    return u, rep
+
+
+def MinimalFunctionLocal(info, au, aF, ctx, stream=None):
+    """FormFunctionLocal of c/ch7/minimal.c:210-282 on the device."""
+    _check(load().MinimalFunctionLocal_gpu(ctypes.byref(info), _ptr(au), _ptr(aF), ctypes.byref(ctx),
+                                           _stream(stream)), "MinimalFunctionLocal_gpu")
 
 
 def solve(opts, u=None):

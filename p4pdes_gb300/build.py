@@ -20,8 +20,8 @@ LIBDIR = os.path.join(PKG, "lib")
 BINDIR = os.path.join(PKG, "bin")
 LIB = os.path.join(LIBDIR, "libfishgpu.so")
 
-SOURCES = ["common.cu", "callbacks.cu", "solver.cu", "noalloc.cu", "server.cu"]
-HEADERS = ["fishgpu_internal.cuh", "kernels.cuh", "common.cuh", "vkernels.cuh"]
+SOURCES = ["common.cu", "callbacks.cu", "solver.cu", "noalloc.cu", "server.cu", "msurf.cu"]
+HEADERS = ["fishgpu_internal.cuh", "kernels.cuh", "common.cuh", "vkernels.cuh", "mg_hooks.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -81,14 +81,18 @@ def build_library(verbose=False, extra_flags=()):
 
 
 def build_driver(verbose=False):
+    """The C drivers: fish (c/ch6/fish.c's flags) and minimal (c/ch7/minimal.c's)."""
     os.makedirs(BINDIR, exist_ok=True)
-    src = os.path.join(PKG, "host", "fish.c")
-    exe = os.path.join(BINDIR, "fish")
-    if _stale(exe, [src, LIB, os.path.join(INCLUDE, "fishgpu.h")]):
-        cc = os.environ.get("CC", "gcc")
-        _run([cc, "-O2", "-std=c99", "-Wall", "-I", INCLUDE, src, "-o", exe, "-L", LIBDIR,
-              "-lfishgpu", "-Wl,-rpath," + LIBDIR, "-lm"], verbose)
-    return exe
+    exes = []
+    for name in ("fish", "minimal"):
+        src = os.path.join(PKG, "host", name + ".c")
+        exe = os.path.join(BINDIR, name)
+        if _stale(exe, [src, LIB, os.path.join(INCLUDE, "fishgpu.h")]):
+            cc = os.environ.get("CC", "gcc")
+            _run([cc, "-O2", "-std=c99", "-Wall", "-I", INCLUDE, src, "-o", exe, "-L", LIBDIR,
+                  "-lfishgpu", "-Wl,-rpath," + LIBDIR, "-lm"], verbose)
+        exes.append(exe)
+    return exes[0]
 
 
 def build_oracle(verbose=False):

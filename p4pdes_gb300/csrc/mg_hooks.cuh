@@ -1,0 +1,23 @@
+// mg_hooks.cuh -- internal interface of solver.cu for other solvers of the
+// library that reuse a 2D mixed-form fish solver's geometry, stream and FP32
+// Poisson multigrid hierarchy (the minimal-surface Newton solver
+// preconditions its inner Krylov solves with that V-cycle).
+#pragma once
+
+#include "common.cuh"
+#include "vkernels.cuh"
+
+struct fishgpu_solver_s;
+
+namespace fg {
+
+const Geom &solver_fine(const fishgpu_solver_s *S);
+const Slots &solver_slots(const fishgpu_solver_s *S);
+cudaStream_t solver_stream(const fishgpu_solver_s *S);
+// Enqueues z = V-cycle(r) (Poisson operator, FP32, zero initial iterate) on
+// the solver's stream; kernels return at once while st->done is set.  Returns
+// the hierarchy buffer that holds z (valid until the next V-cycle), or null
+// when the solver is not a 2D mixed-form multigrid solver.
+const float *solver_vcycle32(fishgpu_solver_s *S, const float *r, KspState *st);
+
+}  // namespace fg

@@ -800,6 +800,22 @@ static int time_kernel_dim(fishgpu_solver *S, const char *name, int reps, double
   return FISHGPU_OK;
 }
 
+// ------------------------------------------------------------------ hooks
+// For other solvers of this library that precondition with the Poisson
+// multigrid hierarchy of a 2D mixed-form solver (mg_hooks.cuh).
+const Geom &solver_fine(const fishgpu_solver *S) { return S->fine; }
+const Slots &solver_slots(const fishgpu_solver *S) { return S->sf; }
+cudaStream_t solver_stream(const fishgpu_solver *S) { return S->stream; }
+
+const float *solver_vcycle32(fishgpu_solver *S, const float *r, KspState *st) {
+  if (S->o.ctx.dim != 2 || S->o.precision != FISHGPU_MIXED || S->o.pc_type != FISHGPU_PC_MG) return nullptr;
+  KspState *saved = S->st;
+  S->st = st;  // the V-cycle's kernels return at once when st->done is set
+  enq_pc<2, float>(S, S->h32, r, -1);
+  S->st = saved;
+  return S->h32.z;
+}
+
 }  // namespace fg
 
 // ------------------------------------------------------------------ C ABI

@@ -669,7 +669,7 @@ __global__ void __launch_bounds__(256) v_zero(Geom g, Slots s, T *__restrict__ a
 }
 
 // r32 = (float)(r64 * inv_s); inv_s per plane for a batch (scale[plane])
-__global__ void __launch_bounds__(256) v_demote(Geom g, Slots s, const double *__restrict__ r, const double *scale,
+static __global__ void __launch_bounds__(256) v_demote(Geom g, Slots s, const double *__restrict__ r, const double *scale,
                                                 double inv_s, float *__restrict__ r32) {
   FG_PW_BEGIN
   const double is = scale ? scale[k] : inv_s;
@@ -679,7 +679,7 @@ __global__ void __launch_bounds__(256) v_demote(Geom g, Slots s, const double *_
 }
 
 // y64 += s * (double)e32; s per plane for a batch (scale[plane])
-__global__ void __launch_bounds__(256) v_promote_add(Geom g, Slots s, const float *__restrict__ e, const double *scale,
+static __global__ void __launch_bounds__(256) v_promote_add(Geom g, Slots s, const float *__restrict__ e, const double *scale,
                                                      double sc, double *__restrict__ y) {
   FG_PW_BEGIN
   const double f = scale ? scale[k] : sc;
@@ -691,7 +691,7 @@ __global__ void __launch_bounds__(256) v_promote_add(Geom g, Slots s, const floa
 }
 
 // a += b
-__global__ void __launch_bounds__(256) v_add(Geom g, Slots s, const double *__restrict__ b, double *__restrict__ a) {
+static __global__ void __launch_bounds__(256) v_add(Geom g, Slots s, const double *__restrict__ b, double *__restrict__ a) {
   FG_PW_BEGIN
   const V4<double> x = ld4(a + n), y = ld4(b + n);
   st4(a + n, V4<double>{x.x + y.x, x.y + y.y, x.z + y.z, x.w + y.w});

@@ -63,6 +63,46 @@ def test_batch_and_server_structs_match_the_header(built, tmp_path):
     assert got == want
 
 
+def test_minimal_structs_match_the_header(built, tmp_path):
+    import subprocess
+    import p4pdes_gb300 as fg
+    src = tmp_path / "sz3.c"
+    src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "fishgpu.h"\n'
+                   'int main(void){printf("%zu %zu %zu %zu %zu %zu\\n", sizeof(fishgpu_ms_ctx),'
+                   ' sizeof(fishgpu_ms_opts), sizeof(fishgpu_ms_report), offsetof(fishgpu_ms_opts, ksp_rtol),'
+                   ' offsetof(fishgpu_ms_report, area), offsetof(fishgpu_ms_report, total_ksp_its));return 0;}\n')
+    exe = tmp_path / "sz3"
+    subprocess.run(["gcc", "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)],
+                   check=True)
+    got = [int(v) for v in subprocess.run([str(exe)], stdout=subprocess.PIPE, text=True).stdout.split()]
+    want = [ctypes.sizeof(fg.MsCtx), ctypes.sizeof(fg.MsOpts), ctypes.sizeof(fg.MsReport),
+            fg.MsOpts.ksp_rtol.offset, fg.MsReport.area.offset, fg.MsReport.total_ksp_its.offset]
+    assert got == want
+
+
+@pytest.mark.parametrize("args,grid,gs,deg", [
+    ("", (3, 3), 0, 0),
+    ("-da_refine 1 -ms_catenoid_c 2.0", (5, 5), 0, 0),
+    ("-snes_grid_sequence 2 -ms_monitor -ms_quaddegree 2", (3, 3), 2, 2),
+    ("-ms_quaddegree 2 -ms_monitor -da_refine 9", (1025, 1025), 0, 2),
+    ("-ms_monitor", (3, 3), 0, 3),
+    ("-ms_quaddegree 1", (3, 3), 0, 0),
+])
+def test_minimal_options(built, args, grid, gs, deg):
+    import p4pdes_gb300 as fg
+    o = fg.ms_options(args)
+    assert (o.mx, o.my) == grid and o.grid_sequence == gs and o.monitor_degree == deg
+    assert o.ctx.q == -0.5 and o.rtol == 1e-8 and o.ksp_rtol == 1e-5 and o.max_it == 50
+
+
+@pytest.mark.parametrize("args", ["-ms_catenoid_c 0.5", "-ms_problem nosuch", "-ms_quaddegree 4",
+                                  "-ms_exact_init -ms_problem tent", "-ms_exact_init -ms_q 0"])
+def test_minimal_bad_options(built, args):
+    import p4pdes_gb300 as fg
+    with pytest.raises(fg.FishError):
+        fg.ms_options(args)
+
+
 def test_server_options_for_a_request(built):
     import p4pdes_gb300 as fg
     o = fg.server_request_opts(3, 257)
