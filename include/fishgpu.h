@@ -364,6 +364,18 @@ int fishgpu_ms_solve(const fishgpu_ms_opts *o, double *u_host, fishgpu_ms_report
 int MinimalFunctionLocal_gpu(const fishgpu_info *info, const double *au, double *aF, const fishgpu_ms_ctx *ctx,
                              void *stream);
 
+/* ---- PETSc binary files (host arrays) ----------------------------------
+   The format of PETSc's binary viewer (VecView/MatView, VecLoad/MatLoad;
+   c/ch12/obstacle.c:138-144, c/ch2/loadsolve.c): big-endian; a Vec is
+   classid 1211214, n, n doubles; an AIJ Mat is classid 1211216, M, N, nz,
+   row lengths, column indices, values.  `index` counts objects in the file. */
+int fishgpu_petsc_vec_write(const char *path, int append, const double *x, long long n);
+int fishgpu_petsc_vec_read(const char *path, int index, double *x, long long cap, long long *n);
+int fishgpu_petsc_mat_write_aij(const char *path, int append, int M, int N, const long long *rowptr,
+                                const int *col, const double *val);
+int fishgpu_petsc_mat_read_aij(const char *path, int index, int *M, int *N, long long *nz, long long *rowptr,
+                               int *col, double *val);
+
 #ifdef __cplusplus
 }
 #endif

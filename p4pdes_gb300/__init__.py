@@ -217,6 +217,14 @@ def load():
                  "fishgpu_ms_solver_solve", "fishgpu_ms_solver_destroy", "fishgpu_ms_solve",
                  "MinimalFunctionLocal_gpu"):
         getattr(lib, name).restype = c_int
+    lib.fishgpu_petsc_vec_write.argtypes = [ctypes.c_char_p, c_int, c_void_p, c_ll]
+    lib.fishgpu_petsc_vec_read.argtypes = [ctypes.c_char_p, c_int, c_void_p, c_ll, _P(c_ll)]
+    lib.fishgpu_petsc_mat_write_aij.argtypes = [ctypes.c_char_p, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p]
+    lib.fishgpu_petsc_mat_read_aij.argtypes = [ctypes.c_char_p, c_int, _P(c_int), _P(c_int), _P(c_ll), c_void_p,
+                                               c_void_p, c_void_p]
+    for name in ("fishgpu_petsc_vec_write", "fishgpu_petsc_vec_read", "fishgpu_petsc_mat_write_aij",
+                 "fishgpu_petsc_mat_read_aij"):
+        getattr(lib, name).restype = c_int
     lib.fishgpu_solver_estimate_bytes.argtypes = [_P(Opts)]
     lib.fishgpu_solver_estimate_bytes.restype = c_ll
     lib.fishgpu_server_opts_default.argtypes = [_P(ServerOpts)]
@@ -604,6 +612,54 @@ def MinimalFunctionLocal(info, au, aF, ctx, stream=None):
     """FormFunctionLocal of c/ch7/minimal.c:210-282 on the device."""
     _check(load().MinimalFunctionLocal_gpu(ctypes.byref(info), _ptr(au), _ptr(aF), ctypes.byref(ctx),
                                            _stream(stream)), "MinimalFunctionLocal_gpu")
+
+
+def petsc_vec_write(path, x, append=False):
+    """Write a float64 host array as a PETSc binary Vec (natural ordering)."""
+    import numpy as np
+    a = np.ascontiguousarray(x, dtype=np.float64).ravel()
+    _check(load().fishgpu_petsc_vec_write(str(path).encode(), int(append), a.ctypes.data, a.size),
+           "fishgpu_petsc_vec_write")
+
+
+def petsc_vec_read(path, index=0):
+    """The index-th object of a PETSc binary file, which must be a Vec."""
+    import numpy as np
+    n = c_ll()
+    _check(load().fishgpu_petsc_vec_read(str(path).encode(), index, None, 0, ctypes.byref(n)),
+           "fishgpu_petsc_vec_read")
+    a = np.empty(n.value)
+    _check(load().fishgpu_petsc_vec_read(str(path).encode(), index, a.ctypes.data, a.size, ctypes.byref(n)),
+           "fishgpu_petsc_vec_read")
+    return a
+
+
+def petsc_mat_write(path, csr, append=False):
+    """Write a scipy CSR matrix as a PETSc binary AIJ Mat."""
+    import numpy as np
+    rp = np.ascontiguousarray(csr.indptr, dtype=np.int64)
+    col = np.ascontiguousarray(csr.indices, dtype=np.int32)
+    val = np.ascontiguousarray(csr.data, dtype=np.float64)
+    M, N = csr.shape
+    _check(load().fishgpu_petsc_mat_write_aij(str(path).encode(), int(append), M, N, rp.ctypes.data,
+                                              col.ctypes.data, val.ctypes.data), "fishgpu_petsc_mat_write_aij")
+
+
+def petsc_mat_read(path, index=0):
+    """The index-th object of a PETSc binary file, which must be an AIJ Mat:
+    returns (M, N, rowptr, col, val)."""
+    import numpy as np
+    M, N, nz = c_int(), c_int(), c_ll()
+    p = str(path).encode()
+    _check(load().fishgpu_petsc_mat_read_aij(p, index, ctypes.byref(M), ctypes.byref(N), ctypes.byref(nz), None,
+                                             None, None), "fishgpu_petsc_mat_read_aij")
+    rp = np.empty(M.value + 1, np.int64)
+    col = np.empty(nz.value, np.int32)
+    val = np.empty(nz.value)
+    _check(load().fishgpu_petsc_mat_read_aij(p, index, ctypes.byref(M), ctypes.byref(N), ctypes.byref(nz),
+                                             rp.ctypes.data, col.ctypes.data, val.ctypes.data),
+           "fishgpu_petsc_mat_read_aij")
+    return M.value, N.value, rp, col, val
 
 
 def solve(opts, u=None):

@@ -880,6 +880,8 @@ extern "C" int fishgpu_ms_opts_parse(fishgpu_ms_opts *o, int argc, const char *c
       if (a + 1 < argc && argv[a + 1][0] != '-') a++;
     } else if (!strcmp(k, "-snes_fd_color") || !strcmp(k, "-snes_mf_operator") || !strcmp(k, "-snes_mf")) {
       // Jacobian handling of PETSc: the exact Jacobian is always used
+    } else if (!strcmp(k, "-snes_view_solution")) {
+      if (a + 1 < argc && argv[a + 1][0] != '-') a++;  // written by the driver
     } else if (!strcmp(k, "-log_view")) {
     } else {
       return FISHGPU_ERR_ARG;

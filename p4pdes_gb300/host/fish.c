@@ -74,6 +74,11 @@ int main(int argc, char **argv) {
   if (log_view)
     printf("solve time (incl. host copies) %.6f s, %.4e DOF/s, iterations %d, outer %d\n",
            rep.solve_ms * 1e-3, (double)rep.dofs / (rep.solve_ms * 1e-3), rep.its, rep.outer_its);
+  for (int a = 1; a + 1 < argc; a++)  /* -snes_view_solution binary:FILE (PETSc binary Vec, natural order) */
+    if (!strcmp(argv[a], "-snes_view_solution") && !strncmp(argv[a + 1], "binary:", 7)) {
+      const int wrc = fishgpu_petsc_vec_write(argv[a + 1] + 7, 0, u, (long long)N);
+      if (wrc) fprintf(stderr, "fish: cannot write %s\n", argv[a + 1] + 7);
+    }
   free(u);
   return rc;
 }

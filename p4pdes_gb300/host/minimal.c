@@ -39,10 +39,18 @@ int main(int argc, char **argv) {
   }
   for (int a = 1; a < argc; a++)
     if (!strcmp(argv[a], "-log_view")) log_view = 1;
-  rc = fishgpu_ms_solve(&o, NULL, rep);
+  int mx = o.mx, my = o.my;
+  for (int k = 0; k < o.grid_sequence; k++) {
+    mx = 2 * mx - 1;
+    my = 2 * my - 1;
+  }
+  double *u = (double *)malloc(sizeof(double) * (size_t)mx * my);
+  if (!u) return FISHGPU_ERR_NOMEM;
+  rc = fishgpu_ms_solve(&o, u, rep);
   if (rc && rc != FISHGPU_ERR_NOT_CONVERGED) {
     fprintf(stderr, "minimal: %s\n", fishgpu_strerror(rc));
     free(rep);
+    free(u);
     return rc;
   }
   for (int k = 0; k < rep->ngrids; k++) {
@@ -81,6 +89,12 @@ int main(int argc, char **argv) {
   if (log_view)
     printf("solve time %.6f s, %.4e DOF/s, Newton iterations %d, inner iterations %lld\n", rep->solve_ms * 1e-3,
            (double)rep->dofs / (rep->solve_ms * 1e-3), rep->its[last], rep->total_ksp_its);
+  for (int a = 1; a + 1 < argc; a++)  /* -snes_view_solution binary:FILE (PETSc binary Vec, natural order) */
+    if (!strcmp(argv[a], "-snes_view_solution") && !strncmp(argv[a + 1], "binary:", 7)) {
+      const int wrc = fishgpu_petsc_vec_write(argv[a + 1] + 7, 0, u, (long long)mx * my);
+      if (wrc) fprintf(stderr, "minimal: cannot write %s\n", argv[a + 1] + 7);
+    }
   free(rep);
+  free(u);
   return rc;
 }

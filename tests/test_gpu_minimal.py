@@ -171,3 +171,24 @@ def test_driver_prints_the_reference_lines(cuda, test):
             assert a == b
         else:
             assert num.sub("#", a) == num.sub("#", b)  # same line and indentation, numbers aside
+
+
+def test_drivers_write_the_solution_as_petsc_binary(cuda, tmp_path):
+    """-snes_view_solution binary:FILE writes the final iterate as a PETSc
+    binary Vec in natural ordering."""
+    import p4pdes_gb300 as fg
+    f = tmp_path / "u.dat"
+    p = driver(["-da_refine", "3", "-snes_view_solution", "binary:%s" % f])
+    assert p.returncode == 0, p.stderr
+    u = fg.petsc_vec_read(f)
+    lv, g, uo, err = ms.solve(refine=3)
+    assert u.size == g.mx * g.my and np.max(np.abs(u - uo)) <= 1e-7
+    exe = os.path.join(ROOT, "p4pdes_gb300", "bin", "fish")
+    f2 = tmp_path / "fish.dat"
+    args = "-fsh_dim 2 -da_refine 4 -pc_type mg -ksp_rtol 1e-12".split()
+    p = subprocess.run([exe] + args + ["-snes_view_solution", "binary:%s" % f2], stdout=subprocess.PIPE,
+                       stderr=subprocess.PIPE, text=True)
+    assert p.returncode == 0, p.stderr
+    import _oracle as orc
+    uref, ref = orc.fish_solve(orc.options(args))
+    assert np.max(np.abs(fg.petsc_vec_read(f2) - uref.ravel())) <= 1e-9 * np.max(np.abs(uref))
