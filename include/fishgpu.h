@@ -300,12 +300,22 @@ int fishgpu_server_destroy(fishgpu_server *s);
    F(u), the norms, the line search and the update stay FP64. */
 #define FISHGPU_MS_TENT     0
 #define FISHGPU_MS_CATENOID 1
+/* The same Newton solver serves the Liouville-Bratu equation of
+   c/ch7/solns/bratu2D.c, -Laplace(u) - lambda e^u = 0 (model FISHGPU_NL_BRATU,
+   5-point residual bratu2D.c:188-217, u = 0 or Liouville's exact solution on
+   the boundary, initial iterate 0). */
+#define FISHGPU_NL_MINIMAL       0
+#define FISHGPU_NL_BRATU         1
+#define FISHGPU_BRATU_ZERO       0
+#define FISHGPU_BRATU_LIOUVILLE  1
 
-typedef struct {          /* MinimalCtx + the boundary function of PoissonCtx */
-  int problem;            /* FISHGPU_MS_TENT / FISHGPU_MS_CATENOID          */
+typedef struct {          /* MinimalCtx / BratuCtx + the boundary function   */
+  int problem;            /* minimal: TENT / CATENOID; Bratu: ZERO / LIOUVILLE */
   double q;               /* exponent (default -1/2)                        */
   double catenoid_c;      /* catenoid parameter, >= 1 (default 1.1)         */
   double tent_H;          /* tent door height (default 1)                   */
+  int model;              /* FISHGPU_NL_MINIMAL (default) / FISHGPU_NL_BRATU */
+  double lambda;          /* Bratu: coefficient of e^u (default 1)          */
 } fishgpu_ms_ctx;
 
 typedef struct {
@@ -340,11 +350,14 @@ typedef struct {
   double solve_ms;                             /* all grids, device time           */
   long long dofs;                              /* nodes of the last grid           */
   long long total_ksp_its;
+  long long nfuncs;                            /* residual evaluations            */
 } fishgpu_ms_report;
 
 int fishgpu_ms_opts_default(fishgpu_ms_opts *o);
+int fishgpu_bratu_opts_default(fishgpu_ms_opts *o);  /* model Bratu, lambda 1, u = 0 on the boundary */
 /* minimal.c's options (-ms_*, -da_refine, -da_grid_x/y, -snes_*, -ksp_rtol,
-   -ksp_max_it, -pc_type mg|none, -snes_linesearch_type bt|basic); options of
+   -ksp_max_it, -pc_type mg|none, -snes_linesearch_type bt|basic, and bratu2D.c's
+   -lb_lambda, -lb_exact, -lb_showcounts); options of
    PETSc's Jacobian handling (-snes_fd_color, -snes_mf_operator,
    -mat_is_symmetric) are accepted: the Jacobian is always the exact one */
 int fishgpu_ms_opts_parse(fishgpu_ms_opts *o, int argc, const char *const *argv);
@@ -363,6 +376,9 @@ int fishgpu_ms_solve(const fishgpu_ms_opts *o, double *u_host, fishgpu_ms_report
    info->dim must be 2, whole-grid device arrays, global (i,j) indexing */
 int MinimalFunctionLocal_gpu(const fishgpu_info *info, const double *au, double *aF, const fishgpu_ms_ctx *ctx,
                              void *stream);
+/* FormFunctionLocal of c/ch7/solns/bratu2D.c:188-217 (liouville: g of :62-68) */
+int BratuFunctionLocal_gpu(const fishgpu_info *info, const double *au, double *aF, double lambda, int liouville,
+                           void *stream);
 
 /* ---- PETSc binary files (host arrays) ----------------------------------
    The format of PETSc's binary viewer (VecView/MatView, VecLoad/MatLoad;

@@ -29,6 +29,7 @@ __all__ = [
     "FormUExact", "InitialState", "error_norms", "reason_name",
     "Solver", "Batch", "Server", "estimate_bytes", "server_request_opts",
     "MsSolver", "ms_options", "ms_solve", "MinimalFunctionLocal", "snes_reason_name",
+    "bratu_options", "BratuFunctionLocal",
 ]
 
 LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "lib", "libfishgpu.so")
@@ -122,8 +123,13 @@ MS_TENT, MS_CATENOID = 0, 1
 MS_MAX_GRIDS, MS_MAX_ITS = 12, 64
 
 
+NL_MINIMAL, NL_BRATU = 0, 1
+BRATU_ZERO, BRATU_LIOUVILLE = 0, 1
+
+
 class MsCtx(ctypes.Structure):
-    _fields_ = [("problem", c_int), ("q", c_double), ("catenoid_c", c_double), ("tent_H", c_double)]
+    _fields_ = [("problem", c_int), ("q", c_double), ("catenoid_c", c_double), ("tent_H", c_double),
+                ("model", c_int), ("lam", c_double)]
 
 
 class MsOpts(ctypes.Structure):
@@ -140,7 +146,8 @@ class MsReport(ctypes.Structure):
                 ("ksp_reason", (c_int * MS_MAX_ITS) * MS_MAX_GRIDS),
                 ("fnorm", (c_double * (MS_MAX_ITS + 1)) * MS_MAX_GRIDS),
                 ("area", ((c_double * 3) * (MS_MAX_ITS + 1)) * MS_MAX_GRIDS),
-                ("errinf", c_double), ("solve_ms", c_double), ("dofs", c_ll), ("total_ksp_its", c_ll)]
+                ("errinf", c_double), ("solve_ms", c_double), ("dofs", c_ll), ("total_ksp_its", c_ll),
+                ("nfuncs", c_ll)]
 
     def fnorms(self, k):
         return [self.fnorm[k][i] for i in range(self.its[k] + 1)]
@@ -205,6 +212,10 @@ def load():
         getattr(lib, name).restype = c_int
     lib.fishgpu_solver_time_kernel.argtypes = [c_void_p, ctypes.c_char_p, c_int, _P(c_double), _P(c_double)]
     lib.fishgpu_ms_opts_default.argtypes = [_P(MsOpts)]
+    lib.fishgpu_bratu_opts_default.argtypes = [_P(MsOpts)]
+    lib.fishgpu_bratu_opts_default.restype = c_int
+    lib.BratuFunctionLocal_gpu.argtypes = [_P(Info), c_void_p, c_void_p, c_double, c_int, c_void_p]
+    lib.BratuFunctionLocal_gpu.restype = c_int
     lib.fishgpu_ms_opts_parse.argtypes = [_P(MsOpts), c_int, _P(ctypes.c_char_p)]
     lib.fishgpu_ms_solver_create.argtypes = [_P(MsOpts), c_void_p, _P(c_void_p)]
     lib.fishgpu_ms_solver_solve.argtypes = [c_void_p, c_void_p, _P(MsReport)]
@@ -554,6 +565,23 @@ def ms_options(argv=()):
     arr = (ctypes.c_char_p * max(1, len(argv)))(*[a.encode() for a in argv])
     _check(load().fishgpu_ms_opts_parse(ctypes.byref(o), len(argv), arr), "fishgpu_ms_opts_parse")
     return o
+
+
+def bratu_options(argv=()):
+    """Parse bratu2D.c's flags (-lb_lambda, -lb_exact, -da_refine, -snes_*) into an MsOpts."""
+    if isinstance(argv, str):
+        argv = argv.split()
+    o = MsOpts()
+    _check(load().fishgpu_bratu_opts_default(ctypes.byref(o)), "fishgpu_bratu_opts_default")
+    arr = (ctypes.c_char_p * max(1, len(argv)))(*[a.encode() for a in argv])
+    _check(load().fishgpu_ms_opts_parse(ctypes.byref(o), len(argv), arr), "fishgpu_ms_opts_parse")
+    return o
+
+
+def BratuFunctionLocal(info, au, aF, lam=1.0, liouville=False, stream=None):
+    """FormFunctionLocal of c/ch7/solns/bratu2D.c:188-217 on the device."""
+    _check(load().BratuFunctionLocal_gpu(ctypes.byref(info), _ptr(au), _ptr(aF), lam, int(liouville),
+                                         _stream(stream)), "BratuFunctionLocal_gpu")
 
 
 def snes_reason_name(reason):

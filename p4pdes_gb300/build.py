@@ -81,10 +81,10 @@ def build_library(verbose=False, extra_flags=()):
 
 
 def build_driver(verbose=False):
-    """The C drivers: fish (c/ch6/fish.c's flags) and minimal (c/ch7/minimal.c's)."""
+    """The C drivers: fish, minimal and bratu2D, with the reference programs' flags."""
     os.makedirs(BINDIR, exist_ok=True)
     exes = []
-    for name in ("fish", "minimal"):
+    for name in ("fish", "minimal", "bratu2D"):
         src = os.path.join(PKG, "host", name + ".c")
         exe = os.path.join(BINDIR, name)
         if _stale(exe, [src, LIB, os.path.join(INCLUDE, "fishgpu.h")]):

@@ -35,12 +35,28 @@ namespace fg {
 struct MsP {
   int problem;
   double q, c, H;
+  int model;      // FISHGPU_NL_MINIMAL / FISHGPU_NL_BRATU
+  double lambda;  // Bratu's coefficient of e^u
 };
 
-// boundary data, minimal.c:27-42
+// boundary data: minimal.c:27-42 (tent, catenoid); bratu2D.c:58-68 (zero, Liouville)
 __host__ __device__ inline double ms_gd(const MsP &P, double x, double y) {
+  if (P.model == FISHGPU_NL_BRATU) {
+    if (P.problem != FISHGPU_BRATU_LIOUVILLE) return 0.0;
+    const double r2 = (x + 1.0) * (x + 1.0) + (y + 1.0) * (y + 1.0), qq = r2 * r2 + 1.0, omega = r2 / (qq * qq);
+    return log(32.0 * omega);
+  }
   if (P.problem == FISHGPU_MS_TENT) return x < 1.0e-8 ? 2.0 * P.H * (y < 0.5 ? y : 1.0 - y) : 0.0;
   return P.c * cosh(x / P.c) * sin(acos((y / P.c) / cosh(x / P.c)));
+}
+
+// Bratu at interior node (i,j), bratu2D.c:205-211: the neighbours are the array's values
+__device__ __forceinline__ double lb_f_interior(const Geom &g, const MsP &P, const double *__restrict__ u,
+                                                long long pitch, int i, int j) {
+  const double hx = g.h[0], hy = g.h[1], darea = hx * hy, hxhy = hx / hy, hyhx = hy / hx;
+  const long long n = (long long)j * pitch + i;
+  return hyhx * (2.0 * u[n] - u[n - 1] - u[n + 1]) + hxhy * (2.0 * u[n] - u[n - pitch] - u[n + pitch]) -
+         darea * P.lambda * exp(u[n]);
 }
 
 __device__ __forceinline__ bool ms_bdry(const Geom &g, int i, int j) {
@@ -140,7 +156,9 @@ __global__ void __launch_bounds__(256) k_ms_resid(Geom g, MsP P, const double *_
   double acc = 0.0;
   if (in_) {
     double f = 0.0;
-    if (node) f = ms_bdry(g, i, j) ? u[n] - ms_gd(P, i * g.h[0], j * g.h[1]) : ms_f_interior(g, P, u, g.pitch, i, j);
+    if (node)
+      f = ms_bdry(g, i, j) ? u[n] - ms_gd(P, i * g.h[0], j * g.h[1])
+          : P.model == FISHGPU_NL_BRATU ? lb_f_interior(g, P, u, g.pitch, i, j) : ms_f_interior(g, P, u, g.pitch, i, j);
     F[n] = f;
     acc = f * f;
   }
@@ -163,7 +181,9 @@ __global__ void __launch_bounds__(256) k_ms_coef(Geom g, MsP P, const double *__
   MS_NODE_BEGIN
   if (!in_) return;
   float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
-  if (node && !ms_bdry(g, i, j)) {
+  if (node && !ms_bdry(g, i, j) && P.model == FISHGPU_NL_BRATU) {
+    a.x = (float)(g.h[0] * g.h[1] * P.lambda * exp(u[n]));  // the diagonal shift darea lambda e^u
+  } else if (node && !ms_bdry(g, i, j)) {
     const double hx = g.h[0], hy = g.h[1];
     double v[8];
     ms_nb(g, P, u, g.pitch, i, j, v);
@@ -178,13 +198,17 @@ __global__ void __launch_bounds__(256) k_ms_coef(Geom g, MsP P, const double *__
   C2[n] = b;
 }
 
-// (J v) at node n in FP32: identity on boundary rows, boundary neighbours
-// do not enter interior rows.
-__device__ __forceinline__ float ms_jv_node(const Geom &g, int i, int j, long long n, float a, float b,
+// (J v) at node n in FP32: identity on boundary rows.  Minimal surface:
+// boundary neighbours do not enter interior rows (their values are g).
+// Bratu: the 5-point rows couple to every neighbour, diagonal shifted by
+// -darea lambda e^u (C1.x).
+__device__ __forceinline__ float ms_jv_node(const Geom &g, int model, int i, int j, long long n, float a, float b,
                                             const float4 *__restrict__ C1, const float4 *__restrict__ C2,
                                             const float *__restrict__ v) {
   if (ms_bdry(g, i, j)) return v[n];
   const long long P = g.pitch;
+  if (model == FISHGPU_NL_BRATU)
+    return (2.f * (a + b) - C1[n].x) * v[n] - a * (v[n - 1] + v[n + 1]) - b * (v[n - P] + v[n + P]);
   const bool E = i + 1 < g.mx - 1, Wb = i - 1 > 0, N = j + 1 < g.my - 1, S = j - 1 > 0;
   const float vc = v[n];
   const float ve = E ? v[n + 1] : 0.f, vw = Wb ? v[n - 1] : 0.f;
@@ -291,14 +315,14 @@ struct OmegaFin {
 };
 
 // v = J ph; rhat.v -> alpha
-__global__ void __launch_bounds__(256) k_bi_jv1(Geom g, MsKsp *st, float a, float b, const float4 *__restrict__ C1,
+__global__ void __launch_bounds__(256) k_bi_jv1(Geom g, int model, MsKsp *st, float a, float b, const float4 *__restrict__ C1,
                                                 const float4 *__restrict__ C2, const float *__restrict__ ph,
                                                 float *__restrict__ v, const float *__restrict__ rh, Reducer red) {
   if (msk_done(st)) return;
   MS_NODE_BEGIN
   double acc = 0.0;
   if (in_) {
-    const float o = node ? ms_jv_node(g, i, j, n, a, b, C1, C2, ph) : 0.f;
+    const float o = node ? ms_jv_node(g, model, i, j, n, a, b, C1, C2, ph) : 0.f;
     v[n] = o;
     acc = (double)rh[n] * o;
   }
@@ -316,14 +340,14 @@ __global__ void __launch_bounds__(256) k_bi_s(Geom g, MsKsp *st, const float *__
 }
 
 // t = J sh; t.s, t.t -> omega
-__global__ void __launch_bounds__(256) k_bi_jv2(Geom g, MsKsp *st, float a, float b, const float4 *__restrict__ C1,
+__global__ void __launch_bounds__(256) k_bi_jv2(Geom g, int model, MsKsp *st, float a, float b, const float4 *__restrict__ C1,
                                                 const float4 *__restrict__ C2, const float *__restrict__ sh,
                                                 float *__restrict__ t, const float *__restrict__ s, Reducer red) {
   if (msk_done(st)) return;
   MS_NODE_BEGIN
   double ts = 0.0, tt = 0.0;
   if (in_) {
-    const float o = node ? ms_jv_node(g, i, j, n, a, b, C1, C2, sh) : 0.f;
+    const float o = node ? ms_jv_node(g, model, i, j, n, a, b, C1, C2, sh) : 0.f;
     t[n] = o;
     ts = (double)o * s[n];
     tt = (double)o * o;
@@ -377,13 +401,13 @@ __global__ void __launch_bounds__(256) k_ms_demote(Geom g, const double *__restr
 }
 
 // t = J x (FP32); out = {F.t, x.x}
-__global__ void __launch_bounds__(256) k_ms_slope(Geom g, float a, float b, const float4 *__restrict__ C1,
+__global__ void __launch_bounds__(256) k_ms_slope(Geom g, int model, float a, float b, const float4 *__restrict__ C1,
                                                   const float4 *__restrict__ C2, const float *__restrict__ x,
                                                   const double *__restrict__ F, Reducer red, double *out) {
   MS_NODE_BEGIN
   double ft = 0.0, xx = 0.0;
   if (node) {
-    const float o = ms_jv_node(g, i, j, n, a, b, C1, C2, x);
+    const float o = ms_jv_node(g, model, i, j, n, a, b, C1, C2, x);
     ft = F[n] * (double)o;
     xx = (double)x[n] * x[n];
   }
@@ -406,12 +430,13 @@ __global__ void __launch_bounds__(256) k_ms_norm2(Geom g, const double *__restri
   ms_reduce<1>(v1, red, StoreFin{out});
 }
 
-// u = g on the boundary and 0 inside (InitialState ZEROS with g), or g
-// everywhere (FormExactFromG, minimal.c:193-208); padding 0
-__global__ void __launch_bounds__(256) k_ms_init(Geom g, MsP P, int exact, double *__restrict__ u) {
+// mode 0: u = g on the boundary and 0 inside (InitialState ZEROS with g,
+// minimal.c:155-157); 1: g everywhere (FormExactFromG, minimal.c:193-208);
+// 2: 0 everywhere (VecSet(u,0), bratu2D.c:133); padding 0
+__global__ void __launch_bounds__(256) k_ms_init(Geom g, MsP P, int mode, double *__restrict__ u) {
   MS_NODE_BEGIN
   if (!in_) return;
-  u[n] = (node && (exact || ms_bdry(g, i, j))) ? ms_gd(P, i * g.h[0], j * g.h[1]) : 0.0;
+  u[n] = (node && mode != 2 && (mode == 1 || ms_bdry(g, i, j))) ? ms_gd(P, i * g.h[0], j * g.h[1]) : 0.0;
 }
 
 // DMDA Q1 interpolation coarse -> fine, ratio 2
@@ -533,7 +558,8 @@ __global__ void __launch_bounds__(256) k_ms_funclocal(Geom g, MsP P, int xs, int
   const int i = xs + blockIdx.x * blockDim.x + threadIdx.x, j = ys + blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= xs + xm || j >= ys + ym) return;
   const long long n = (long long)j * g.mx + i;
-  F[n] = ms_bdry(g, i, j) ? u[n] - ms_gd(P, i * g.h[0], j * g.h[1]) : ms_f_interior(g, P, u, g.mx, i, j);
+  F[n] = ms_bdry(g, i, j) ? u[n] - ms_gd(P, i * g.h[0], j * g.h[1])
+         : P.model == FISHGPU_NL_BRATU ? lb_f_interior(g, P, u, g.mx, i, j) : ms_f_interior(g, P, u, g.mx, i, j);
 }
 
 }  // namespace fg
@@ -571,6 +597,7 @@ struct fishgpu_ms_solver_s {
   double *dval = nullptr, *hval = nullptr;
   std::vector<void *> allocs;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  long long nfuncs = 0;  // residual evaluations of the current solve
 };
 
 #define MS_CK(x)                                   \
@@ -612,11 +639,11 @@ static void enq_bicg_iter(fishgpu_ms_solver *S, MsLevel &L) {
   k_bi_p<<<L.grid, L.block, 0, s>>>(g, S->st, L.r, L.p, L.v);
   const float *z = mg ? solver_vcycle32(L.P, L.p, &S->st->k) : nullptr;
   k_bi_pcout<<<L.grid, L.block, 0, s>>>(g, S->st, z, L.p, L.ph);
-  k_bi_jv1<<<L.grid, L.block, 0, s>>>(g, S->st, a, b, L.C1, L.C2, L.ph, L.v, L.rh, S->red);
+  k_bi_jv1<<<L.grid, L.block, 0, s>>>(g, S->P.model, S->st, a, b, L.C1, L.C2, L.ph, L.v, L.rh, S->red);
   k_bi_s<<<L.grid, L.block, 0, s>>>(g, S->st, L.r, L.v, L.s);
   z = mg ? solver_vcycle32(L.P, L.s, &S->st->k) : nullptr;
   k_bi_pcout<<<L.grid, L.block, 0, s>>>(g, S->st, z, L.s, L.sh);
-  k_bi_jv2<<<L.grid, L.block, 0, s>>>(g, S->st, a, b, L.C1, L.C2, L.sh, L.t, L.s, S->red);
+  k_bi_jv2<<<L.grid, L.block, 0, s>>>(g, S->P.model, S->st, a, b, L.C1, L.C2, L.sh, L.t, L.s, S->red);
   k_bi_xr<<<L.grid, L.block, 0, s>>>(g, S->st, L.ph, L.sh, L.s, L.t, L.rh, L.x, L.r, S->red);
 }
 
@@ -649,6 +676,7 @@ static int read_vals(fishgpu_ms_solver *S, int n) {
 }
 
 static int residual(fishgpu_ms_solver *S, MsLevel &L, const double *u, double *F, double *fnorm) {
+  S->nfuncs++;
   k_ms_resid<<<L.grid, L.block, 0, S->stream>>>(L.g, S->P, u, F, S->red, S->dval);
   MS_CK(cudaGetLastError());
   int rc = read_vals(S, 1);
@@ -721,7 +749,7 @@ static int newton(fishgpu_ms_solver *S, MsLevel &L, int k, fishgpu_ms_report *re
     rep->ksp_reason[k][its] = kreason;
     rep->total_ksp_its += kits;
     // slope of ||F||^2/2 along -Y: -(F, J Y) = -||F|| (F, J x); ||Y|| = ||F|| ||x||
-    k_ms_slope<<<L.grid, L.block, 0, s>>>(g, a, b, L.C1, L.C2, L.x, L.F, S->red, S->dval);
+    k_ms_slope<<<L.grid, L.block, 0, s>>>(g, S->P.model, a, b, L.C1, L.C2, L.x, L.F, S->red, S->dval);
     MS_CK(cudaGetLastError());
     if ((rc = read_vals(S, 2))) return rc;
     double initslope = -fnorm * S->hval[0];
@@ -795,6 +823,8 @@ extern "C" int fishgpu_ms_opts_default(fishgpu_ms_opts *o) {
   o->ctx.q = -0.5;
   o->ctx.catenoid_c = 1.1;
   o->ctx.tent_H = 1.0;
+  o->ctx.model = FISHGPU_NL_MINIMAL;
+  o->ctx.lambda = 1.0;
   o->mx = o->my = 3;
   o->rtol = 1e-8;
   o->atol = 1e-50;
@@ -804,6 +834,15 @@ extern "C" int fishgpu_ms_opts_default(fishgpu_ms_opts *o) {
   o->ksp_rtol = 1e-5;
   o->ksp_max_it = 10000;
   o->pc_type = FISHGPU_PC_MG;
+  return FISHGPU_OK;
+}
+
+extern "C" int fishgpu_bratu_opts_default(fishgpu_ms_opts *o) {
+  const int rc = fishgpu_ms_opts_default(o);
+  if (rc) return rc;
+  o->ctx.model = FISHGPU_NL_BRATU;  // bratu2D.c:87-98: lambda 1, u = 0 on the boundary
+  o->ctx.problem = FISHGPU_BRATU_ZERO;
+  o->ctx.lambda = 1.0;
   return FISHGPU_OK;
 }
 
@@ -839,6 +878,9 @@ extern "C" int fishgpu_ms_opts_parse(fishgpu_ms_opts *o, int argc, const char *c
       if (!strcmp(v, "catenoid")) o->ctx.problem = FISHGPU_MS_CATENOID;
       else if (!strcmp(v, "tent")) o->ctx.problem = FISHGPU_MS_TENT;
       else return FISHGPU_ERR_ARG;
+    } else if (!strcmp(k, "-lb_lambda")) rc = num(a, &o->ctx.lambda, nullptr);
+    else if (!strcmp(k, "-lb_exact")) o->ctx.problem = FISHGPU_BRATU_LIOUVILLE;
+    else if (!strcmp(k, "-lb_showcounts")) {  // the driver prints the counts
     } else if (!strcmp(k, "-ms_q")) rc = num(a, &o->ctx.q, nullptr);
     else if (!strcmp(k, "-ms_catenoid_c")) rc = num(a, &o->ctx.catenoid_c, nullptr);
     else if (!strcmp(k, "-ms_tent_H")) rc = num(a, &o->ctx.tent_H, nullptr);
@@ -880,6 +922,9 @@ extern "C" int fishgpu_ms_opts_parse(fishgpu_ms_opts *o, int argc, const char *c
       if (a + 1 < argc && argv[a + 1][0] != '-') a++;
     } else if (!strcmp(k, "-snes_fd_color") || !strcmp(k, "-snes_mf_operator") || !strcmp(k, "-snes_mf")) {
       // Jacobian handling of PETSc: the exact Jacobian is always used
+    } else if (!strcmp(k, "-snes_type")) {
+      if (a + 1 >= argc) return FISHGPU_ERR_ARG;
+      if (strcmp(argv[++a], "newtonls")) return FISHGPU_ERR_UNSUPPORTED;  // FAS, NGS, ... are not offered
     } else if (!strcmp(k, "-snes_view_solution")) {
       if (a + 1 < argc && argv[a + 1][0] != '-') a++;  // written by the driver
     } else if (!strcmp(k, "-log_view")) {
@@ -899,6 +944,11 @@ extern "C" int fishgpu_ms_opts_parse(fishgpu_ms_opts *o, int argc, const char *c
   }
   o->mx = mx;
   o->my = my;
+  if (o->ctx.model == FISHGPU_NL_BRATU) {
+    if (o->ctx.problem == FISHGPU_BRATU_LIOUVILLE && o->ctx.lambda != 1.0) return FISHGPU_ERR_ARG;  // bratu2D.c:109-113
+    if (o->exact_init || o->monitor_degree) return FISHGPU_ERR_ARG;
+    return FISHGPU_OK;
+  }
   if (o->ctx.problem == FISHGPU_MS_CATENOID && o->ctx.catenoid_c < 1.0) return FISHGPU_ERR_ARG;  // minimal.c:121-124
   if (o->exact_init && (o->ctx.problem != FISHGPU_MS_CATENOID || o->ctx.q != -0.5)) return FISHGPU_ERR_ARG;
   return FISHGPU_OK;
@@ -926,8 +976,13 @@ extern "C" int fishgpu_ms_solver_create(const fishgpu_ms_opts *o, void *stream, 
   if (!o || !out) return FISHGPU_ERR_ARG;
   *out = nullptr;
   if (o->mx < 3 || o->my < 3 || o->grid_sequence < 0 || o->grid_sequence >= FISHGPU_MS_MAX_GRIDS) return FISHGPU_ERR_ARG;
-  if (o->ctx.problem != FISHGPU_MS_TENT && o->ctx.problem != FISHGPU_MS_CATENOID) return FISHGPU_ERR_ARG;
-  if (o->ctx.problem == FISHGPU_MS_CATENOID && !(o->ctx.catenoid_c >= 1.0)) return FISHGPU_ERR_ARG;
+  if (o->ctx.model != FISHGPU_NL_MINIMAL && o->ctx.model != FISHGPU_NL_BRATU) return FISHGPU_ERR_ARG;
+  if (o->ctx.problem != 0 && o->ctx.problem != 1) return FISHGPU_ERR_ARG;
+  if (o->ctx.model == FISHGPU_NL_MINIMAL && o->ctx.problem == FISHGPU_MS_CATENOID && !(o->ctx.catenoid_c >= 1.0))
+    return FISHGPU_ERR_ARG;
+  if (o->ctx.model == FISHGPU_NL_BRATU && o->ctx.problem == FISHGPU_BRATU_LIOUVILLE && o->ctx.lambda != 1.0)
+    return FISHGPU_ERR_ARG;  // bratu2D.c:109-113
+  if (o->ctx.model == FISHGPU_NL_BRATU && o->monitor_degree) return FISHGPU_ERR_ARG;
   if (!(o->rtol >= 0) || !(o->atol >= 0) || !(o->stol >= 0) || o->max_it < 0 || !(o->ksp_rtol > 0) ||
       o->ksp_max_it < 1 || o->monitor_degree < 0 || o->monitor_degree > 3)
     return FISHGPU_ERR_ARG;
@@ -939,7 +994,7 @@ extern "C" int fishgpu_ms_solver_create(const fishgpu_ms_opts *o, void *stream, 
   }
   fishgpu_ms_solver *S = new fishgpu_ms_solver();
   S->o = *o;
-  S->P = MsP{o->ctx.problem, o->ctx.q, o->ctx.catenoid_c, o->ctx.tent_H};
+  S->P = MsP{o->ctx.problem, o->ctx.q, o->ctx.catenoid_c, o->ctx.tent_H, o->ctx.model, o->ctx.lambda};
   int rc = FISHGPU_OK;
 #define MS_FAIL(x)                 \
   do {                             \
@@ -1019,11 +1074,13 @@ extern "C" int fishgpu_ms_solver_solve(fishgpu_ms_solver *S, double *u_host, fis
   memset(rep, 0, sizeof(*rep));
   cudaStream_t s = S->stream;
   int rc;
+  S->nfuncs = 0;
   MS_CK(cudaEventRecord(S->ev0, s));
   for (size_t k = 0; k < S->lev.size(); k++) {
     MsLevel &L = S->lev[k];
     if (k == 0) {
-      k_ms_init<<<L.grid, L.block, 0, s>>>(L.g, S->P, S->o.exact_init, L.u);
+      const int mode = S->P.model == FISHGPU_NL_BRATU ? 2 : S->o.exact_init ? 1 : 0;
+      k_ms_init<<<L.grid, L.block, 0, s>>>(L.g, S->P, mode, L.u);
     } else {
       MsLevel &C = S->lev[k - 1];
       k_ms_interp<<<L.grid, L.block, 0, s>>>(C.g, C.u, L.g, L.u);
@@ -1036,7 +1093,10 @@ extern "C" int fishgpu_ms_solver_solve(fishgpu_ms_solver *S, double *u_host, fis
   MsLevel &L = S->lev.back();
   rep->dofs = (long long)L.g.mx * L.g.my;
   rep->errinf = -1.0;
-  if (S->o.ctx.problem == FISHGPU_MS_CATENOID && S->o.ctx.q == -0.5) {
+  const bool has_exact = S->P.model == FISHGPU_NL_BRATU
+                             ? S->o.ctx.problem == FISHGPU_BRATU_LIOUVILLE
+                             : (S->o.ctx.problem == FISHGPU_MS_CATENOID && S->o.ctx.q == -0.5);
+  if (has_exact) {
     k_ms_err<<<L.grid, L.block, 0, s>>>(L.g, S->P, L.u, S->part3, S->cap);
     k_ms_fin3<<<1, 256, 0, s>>>(S->part3, S->cap, (int)(L.grid.x * L.grid.y), S->dval);
     MS_CK(cudaGetLastError());
@@ -1050,6 +1110,7 @@ extern "C" int fishgpu_ms_solver_solve(fishgpu_ms_solver *S, double *u_host, fis
   float ms = 0.f;
   MS_CK(cudaEventElapsedTime(&ms, S->ev0, S->ev1));
   rep->solve_ms = ms;
+  rep->nfuncs = S->nfuncs;
   for (int k = 0; k < rep->ngrids; k++)
     if (rep->reason[k] <= 0) return FISHGPU_ERR_NOT_CONVERGED;
   return FISHGPU_OK;
@@ -1070,7 +1131,8 @@ extern "C" int MinimalFunctionLocal_gpu(const fishgpu_info *info, const double *
   if (info->mx < 2 || info->my < 2 || info->xs < 0 || info->ys < 0 || info->xm < 0 || info->ym < 0 ||
       info->xs + info->xm > info->mx || info->ys + info->ym > info->my)
     return FISHGPU_ERR_ARG;
-  if (ctx->problem != FISHGPU_MS_TENT && ctx->problem != FISHGPU_MS_CATENOID) return FISHGPU_ERR_ARG;
+  if ((ctx->problem != 0 && ctx->problem != 1) || (ctx->model != FISHGPU_NL_MINIMAL && ctx->model != FISHGPU_NL_BRATU))
+    return FISHGPU_ERR_ARG;
   if (info->xm == 0 || info->ym == 0) return FISHGPU_OK;
   Geom g;
   memset(&g, 0, sizeof(g));
@@ -1082,8 +1144,19 @@ extern "C" int MinimalFunctionLocal_gpu(const fishgpu_info *info, const double *
   g.plane = (long long)info->mx * info->my;
   g.h[0] = (info->xmax[0] - info->xmin[0]) / (info->mx - 1);  // minimal.c:221-222
   g.h[1] = (info->xmax[1] - info->xmin[1]) / (info->my - 1);
-  const MsP P{ctx->problem, ctx->q, ctx->catenoid_c, ctx->tent_H};
+  const MsP P{ctx->problem, ctx->q, ctx->catenoid_c, ctx->tent_H, ctx->model, ctx->lambda};
   const dim3 block(32, 8), grid((info->xm + 31) / 32, (info->ym + 7) / 8);
   k_ms_funclocal<<<grid, block, 0, (cudaStream_t)stream>>>(g, P, info->xs, info->ys, info->xm, info->ym, au, aF);
   return cudaGetLastError() == cudaSuccess ? FISHGPU_OK : FISHGPU_ERR_CUDA;
+}
+
+extern "C" int BratuFunctionLocal_gpu(const fishgpu_info *info, const double *au, double *aF, double lambda,
+                                      int liouville, void *stream) {
+  fishgpu_ms_ctx c;
+  memset(&c, 0, sizeof(c));
+  c.model = FISHGPU_NL_BRATU;
+  c.problem = liouville ? FISHGPU_BRATU_LIOUVILLE : FISHGPU_BRATU_ZERO;
+  c.lambda = lambda;
+  if (liouville && lambda != 1.0) return FISHGPU_ERR_ARG;
+  return MinimalFunctionLocal_gpu(info, au, aF, &c, stream);
 }

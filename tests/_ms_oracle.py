@@ -1,7 +1,9 @@
-"""CPU oracle of the minimal-surface solve of c/ch7/minimal.c (test
-infrastructure only): ctypes bindings of oracle/minimal_oracle.c plus a
-restatement of PETSc's SNESNEWTONLS with the cubic backtracking line search
-and SNESConvergedDefault, using exact sparse linear solves (scipy).
+"""CPU oracle of the nonlinear clients of the Poisson call-backs (test
+infrastructure only): the minimal-surface equation of c/ch7/minimal.c and the
+Liouville-Bratu equation of c/ch7/solns/bratu2D.c (ctypes bindings of
+oracle/minimal_oracle.c and oracle/bratu_oracle.c), plus a restatement of
+PETSc's SNESNEWTONLS with the cubic backtracking line search and
+SNESConvergedDefault, using exact sparse linear solves (scipy).
 
 Newton steps here solve J Y = F exactly; the reference's runs solve them to
 KSP rtol 1e-5, so intermediate residual norms agree to about that relative
@@ -101,6 +103,66 @@ def interpolate(gc, uc, gf):
     return uf
 
 
+class LbGrid(ctypes.Structure):
+    _fields_ = [("mx", ctypes.c_int), ("my", ctypes.c_int), ("lam", ctypes.c_double), ("exact", ctypes.c_int)]
+
+
+_lb_bound = False
+
+
+def _lb():
+    global _lb_bound
+    L = lib()
+    if not _lb_bound:
+        P = ctypes.POINTER
+        dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+        ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+        L.lb_exact.argtypes = [P(LbGrid), dp]
+        L.lb_residual.argtypes = [P(LbGrid), dp, dp]
+        L.lb_jacobian_csr.argtypes = [P(LbGrid), dp, ip, ip, dp]
+        L.lb_jacobian_csr.restype = ctypes.c_int
+        _lb_bound = True
+    return L
+
+
+class Bratu:
+    """The Bratu residual/Jacobian on an mx x my grid (bratu2D.c)."""
+
+    def __init__(self, m, lam=1.0, exact=False):
+        self.g = LbGrid(m, m, lam, int(exact))
+        self.mx = self.my = m
+
+    def residual(self, u):
+        F = np.empty_like(u)
+        _lb().lb_residual(ctypes.byref(self.g), np.ascontiguousarray(u), F)
+        return F
+
+    def jacobian(self, u):
+        import scipy.sparse as sp
+        n = self.mx * self.my
+        rp = np.empty(n + 1, np.int32)
+        col = np.empty(5 * n, np.int32)
+        val = np.empty(5 * n)
+        nz = _lb().lb_jacobian_csr(ctypes.byref(self.g), np.ascontiguousarray(u), rp, col, val)
+        return sp.csr_matrix((val[:nz], col[:nz], rp), shape=(n, n))
+
+    def exact(self):
+        u = np.empty(self.mx * self.my)
+        _lb().lb_exact(ctypes.byref(self.g), u)
+        return u
+
+
+class Minimal:
+    def __init__(self, g):
+        self.g = g
+
+    def residual(self, u):
+        return residual(self.g, u)
+
+    def jacobian(self, u):
+        return jacobian(self.g, u)
+
+
 def line_search_bt(g, X, F, fnorm, Y, J, alpha=1e-4, maxstep=1e8, minlambda=1e-12, max_it=40):
     """Cubic backtracking (Dennis & Schnabel A6.3.1) on f = ||F||^2 / 2 along
     X - lambda Y, PETSc's SNESLINESEARCHBT defaults.  Returns
@@ -114,9 +176,10 @@ def line_search_bt(g, X, F, fnorm, Y, J, alpha=1e-4, maxstep=1e8, minlambda=1e-1
         initslope = -initslope
     if initslope == 0.0:
         initslope = -1.0
+    res = g.residual if hasattr(g, "residual") else (lambda w: residual(g, w))
     lam = 1.0
     W = X - lam * Y
-    G = residual(g, W)
+    G = res(W)
     gnorm = np.linalg.norm(G)
     nf = 1
     if 0.5 * gnorm * gnorm <= 0.5 * fnorm * fnorm + lam * alpha * initslope:
@@ -129,7 +192,7 @@ def line_search_bt(g, X, F, fnorm, Y, J, alpha=1e-4, maxstep=1e8, minlambda=1e-1
         if lam < minlambda:
             return False, X, F, fnorm, 0.0, 0.0, nf
         W = X - lam * Y
-        G = residual(g, W)
+        G = res(W)
         gnorm = np.linalg.norm(G)
         nf += 1
         if 0.5 * gnorm * gnorm <= 0.5 * fnorm * fnorm + lam * alpha * initslope:
@@ -150,11 +213,12 @@ def newton(g, u0, rtol=1e-8, atol=1e-50, stol=1e-8, max_it=50, monitor_degree=0)
     Returns a dict: u, its, reason, fnorms, areas (per iterate when
     monitor_degree > 0: (area, Dmin, Dmax))."""
     from scipy.sparse.linalg import spsolve
+    model = g if hasattr(g, "residual") else Minimal(g)
     X = np.array(u0, dtype=np.float64)
-    F = residual(g, X)
+    F = model.residual(X)
     fnorm = np.linalg.norm(F)
     fnorms = [fnorm]
-    areas = [area(g, X, monitor_degree)] if monitor_degree else []
+    areas = [area(g, X, monitor_degree)] if monitor_degree else []  # minimal surface only
     ttol = rtol * fnorm
     reason = 0
     if math.isnan(fnorm):
@@ -163,9 +227,9 @@ def newton(g, u0, rtol=1e-8, atol=1e-50, stol=1e-8, max_it=50, monitor_degree=0)
         reason = 2
     its = 0
     while reason == 0:
-        J = jacobian(g, X)
+        J = model.jacobian(X)
         Y = spsolve(J.tocsc(), F)
-        ok, X, F, fnorm, lam, ynorm, _ = line_search_bt(g, X, F, fnorm, Y, J)
+        ok, X, F, fnorm, lam, ynorm, _ = line_search_bt(model, X, F, fnorm, Y, J)
         its += 1
         fnorms.append(fnorm)
         if monitor_degree:
@@ -211,3 +275,25 @@ def solve(base=3, refine=0, grid_sequence=0, problem=CATENOID, q=-0.5, c=1.1, H=
     if problem == CATENOID and q == -0.5:
         err = float(np.max(np.abs(u - exact(g))))
     return levels, g, u, err
+
+
+def bratu_solve(base=3, refine=0, grid_sequence=0, lam=1.0, exact=False, rtol=1e-8):
+    """bratu2D.c's Newton flow from u = 0 (bratu2D.c:133-135) with optional
+    grid sequencing; returns (levels, model, u, errinf or None)."""
+    m = base
+    for _ in range(refine):
+        m = 2 * m - 1
+    levels = []
+    model = Bratu(m, lam, exact)
+    u0 = np.zeros(m * m)
+    for lev in range(grid_sequence + 1):
+        r = newton(model, u0, rtol=rtol)
+        r["m"] = model.mx
+        levels.append(r)
+        if lev < grid_sequence:
+            fine = Bratu(2 * model.mx - 1, lam, exact)
+            u0 = interpolate(grid(model.mx), r["u"], grid(fine.mx))
+            model = fine
+    u = levels[-1]["u"]
+    err = float(np.max(np.abs(u - model.exact()))) if exact else None
+    return levels, model, u, err

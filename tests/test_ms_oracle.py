@@ -106,3 +106,34 @@ def test_exact_catenoid_has_small_residual_and_converges_with_h():
         levels, g, u, err = ms.solve(base=m)
         errs.append(err)
     assert errs[0] / errs[1] > 3.0 and errs[1] / errs[2] > 3.0
+
+
+BRATU = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "bratu_goldens.json")))[0]
+
+
+def test_bratu_golden_first_norm_and_error():
+    """c/ch7/solns/output/bratu2D.test1 (9 x 9, Liouville data): the first
+    residual norm to every printed digit; the reference's final iterate (FAS +
+    nonlinear Gauss-Seidel, stopped at ||F|| = 8.9e-9) has an error within
+    1e-7 of the discrete solution's, which the oracle's Newton reaches."""
+    levels, model, u, err = ms.bratu_solve(refine=2, exact=True)
+    assert "%g" % levels[0]["fnorms"][0] == BRATU["snes_norms"][0]
+    assert (model.mx, model.my) == tuple(BRATU["grid"])
+    assert abs(err - float(BRATU["errinf"])) <= 1e-7
+    assert levels[0]["reason"] == 3 and levels[0]["its"] == 3
+
+
+def test_bratu_jacobian_is_the_derivative():
+    rng = np.random.default_rng(5)
+    for lam, exact in ((1.0, True), (5.0, False)):
+        b = ms.Bratu(17, lam, exact)
+        u = 0.3 * rng.standard_normal(17 * 17)
+        v = rng.standard_normal(17 * 17)
+        h = 1e-6
+        fd = (b.residual(u + h * v) - b.residual(u - h * v)) / (2 * h)
+        assert np.max(np.abs(b.jacobian(u) @ v - fd)) <= 1e-7 * np.max(np.abs(fd))
+
+
+def test_bratu_error_is_second_order():
+    errs = [ms.bratu_solve(refine=r, exact=True, rtol=1e-12)[3] for r in (3, 4, 5)]
+    assert errs[0] / errs[1] > 3.5 and errs[1] / errs[2] > 3.5
