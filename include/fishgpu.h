@@ -351,6 +351,7 @@ typedef struct {
   long long dofs;                              /* nodes of the last grid           */
   long long total_ksp_its;
   long long nfuncs;                            /* residual evaluations            */
+  double grid_ms[FISHGPU_MS_MAX_GRIDS];        /* device time per grid            */
 } fishgpu_ms_report;
 
 int fishgpu_ms_opts_default(fishgpu_ms_opts *o);

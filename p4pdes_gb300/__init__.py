@@ -147,7 +147,7 @@ class MsReport(ctypes.Structure):
                 ("fnorm", (c_double * (MS_MAX_ITS + 1)) * MS_MAX_GRIDS),
                 ("area", ((c_double * 3) * (MS_MAX_ITS + 1)) * MS_MAX_GRIDS),
                 ("errinf", c_double), ("solve_ms", c_double), ("dofs", c_ll), ("total_ksp_its", c_ll),
-                ("nfuncs", c_ll)]
+                ("nfuncs", c_ll), ("grid_ms", c_double * MS_MAX_GRIDS)]
 
     def fnorms(self, k):
         return [self.fnorm[k][i] for i in range(self.its[k] + 1)]

@@ -596,7 +596,7 @@ struct fishgpu_ms_solver_s {
   MsKsp *st = nullptr, *st_h = nullptr;
   double *dval = nullptr, *hval = nullptr;
   std::vector<void *> allocs;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, evg = nullptr, evg2 = nullptr;
   long long nfuncs = 0;  // residual evaluations of the current solve
 };
 
@@ -967,6 +967,8 @@ extern "C" int fishgpu_ms_solver_destroy(fishgpu_ms_solver *S) {
   if (S->hval) cudaFreeHost(S->hval);
   if (S->ev0) cudaEventDestroy(S->ev0);
   if (S->ev1) cudaEventDestroy(S->ev1);
+  if (S->evg) cudaEventDestroy(S->evg);
+  if (S->evg2) cudaEventDestroy(S->evg2);
   if (S->own_stream && S->stream) cudaStreamDestroy(S->stream);
   delete S;
   return FISHGPU_OK;
@@ -1014,7 +1016,8 @@ extern "C" int fishgpu_ms_solver_create(const fishgpu_ms_opts *o, void *stream, 
   }
   if (cudaMallocHost((void **)&S->st_h, sizeof(MsKsp)) != cudaSuccess ||
       cudaMallocHost((void **)&S->hval, sizeof(double) * 8) != cudaSuccess ||
-      cudaEventCreate(&S->ev0) != cudaSuccess || cudaEventCreate(&S->ev1) != cudaSuccess)
+      cudaEventCreate(&S->ev0) != cudaSuccess || cudaEventCreate(&S->ev1) != cudaSuccess ||
+      cudaEventCreate(&S->evg) != cudaSuccess || cudaEventCreate(&S->evg2) != cudaSuccess)
     MS_FAIL(FISHGPU_ERR_CUDA);
   int mx = o->mx, my = o->my;
   S->lev.resize(o->grid_sequence + 1);
@@ -1086,7 +1089,13 @@ extern "C" int fishgpu_ms_solver_solve(fishgpu_ms_solver *S, double *u_host, fis
       k_ms_interp<<<L.grid, L.block, 0, s>>>(C.g, C.u, L.g, L.u);
     }
     MS_CK(cudaGetLastError());
+    MS_CK(cudaEventRecord(S->evg, s));
     if ((rc = newton(S, L, (int)k, rep))) return rc;
+    MS_CK(cudaEventRecord(S->evg2, s));
+    MS_CK(cudaEventSynchronize(S->evg2));
+    float gms = 0.f;
+    MS_CK(cudaEventElapsedTime(&gms, S->evg, S->evg2));
+    rep->grid_ms[k] = gms;
     rep->ngrids = (int)k + 1;
   }
   MS_CK(cudaEventRecord(S->ev1, s));
