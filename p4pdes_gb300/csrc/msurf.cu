@@ -1032,8 +1032,16 @@ extern "C" int fishgpu_ms_solver_create(const fishgpu_ms_opts *o, void *stream, 
     po.mz = 1;
     po.pc_type = FISHGPU_PC_MG;
     po.precision = FISHGPU_MIXED;
+    // default hierarchy: coarsen only down to about 33 x 33 and solve that
+    // grid exactly (one block, sine transform): the V-cycle of these 2D grids
+    // is launch-bound, and the deepest levels cost launches, not work
     const int lmax = ms_levels_for(mx, my);
-    po.mg_levels = o->mg_levels > 0 && o->mg_levels < lmax ? o->mg_levels : lmax;
+    int ldef = 1, cm = std::min(mx, my);
+    while (ldef < lmax && cm > 33) {
+      cm = (cm - 1) / 2 + 1;
+      ldef++;
+    }
+    po.mg_levels = o->mg_levels > 0 && o->mg_levels < lmax ? o->mg_levels : ldef;
     MS_FAIL(fishgpu_solver_create(&po, (void *)S->stream, &L.P));
     L.g = solver_fine(L.P);
     L.N = (long long)L.g.plane;
