@@ -306,6 +306,14 @@ int fishgpu_server_destroy(fishgpu_server *s);
    the boundary, initial iterate 0). */
 #define FISHGPU_NL_MINIMAL       0
 #define FISHGPU_NL_BRATU         1
+/* ... and the obstacle problem of c/ch12/obstacle.c (model FISHGPU_NL_OBSTACLE):
+   -Laplace(u) = 0 on (-2,2)^2, u >= psi (hemisphere with a skirt), g = the
+   exact solution, Poisson2DFunctionLocal as residual; the variational
+   inequality is solved by the reduced-space active-set Newton method (PETSc
+   SNESVINEWTONRSLS semantics: projection onto the bounds, active set
+   u <= psi + 1e-8 with F > 0, Newton on the inactive set, residual norm over
+   the inactive set). */
+#define FISHGPU_NL_OBSTACLE      2
 #define FISHGPU_BRATU_ZERO       0
 #define FISHGPU_BRATU_LIOUVILLE  1
 
@@ -352,10 +360,14 @@ typedef struct {
   long long total_ksp_its;
   long long nfuncs;                            /* residual evaluations            */
   double grid_ms[FISHGPU_MS_MAX_GRIDS];        /* device time per grid            */
+  double err1;                                 /* obstacle: mean |u - u_exact|    */
+  double active_area_err;                      /* obstacle: |area(A) - pi a^2| / pi a^2 */
+  long long n_active;                          /* obstacle: nodes of the active set */
 } fishgpu_ms_report;
 
 int fishgpu_ms_opts_default(fishgpu_ms_opts *o);
 int fishgpu_bratu_opts_default(fishgpu_ms_opts *o);  /* model Bratu, lambda 1, u = 0 on the boundary */
+int fishgpu_obstacle_opts_default(fishgpu_ms_opts *o); /* model obstacle (c/ch12/obstacle.c defaults) */
 /* minimal.c's options (-ms_*, -da_refine, -da_grid_x/y, -snes_*, -ksp_rtol,
    -ksp_max_it, -pc_type mg|none, -snes_linesearch_type bt|basic, and bratu2D.c's
    -lb_lambda, -lb_exact, -lb_showcounts); options of

@@ -29,7 +29,7 @@ __all__ = [
     "FormUExact", "InitialState", "error_norms", "reason_name",
     "Solver", "Batch", "Server", "estimate_bytes", "server_request_opts",
     "MsSolver", "ms_options", "ms_solve", "MinimalFunctionLocal", "snes_reason_name",
-    "bratu_options", "BratuFunctionLocal",
+    "bratu_options", "BratuFunctionLocal", "obstacle_options",
 ]
 
 LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "lib", "libfishgpu.so")
@@ -123,7 +123,7 @@ MS_TENT, MS_CATENOID = 0, 1
 MS_MAX_GRIDS, MS_MAX_ITS = 12, 64
 
 
-NL_MINIMAL, NL_BRATU = 0, 1
+NL_MINIMAL, NL_BRATU, NL_OBSTACLE = 0, 1, 2
 BRATU_ZERO, BRATU_LIOUVILLE = 0, 1
 
 
@@ -147,7 +147,8 @@ class MsReport(ctypes.Structure):
                 ("fnorm", (c_double * (MS_MAX_ITS + 1)) * MS_MAX_GRIDS),
                 ("area", ((c_double * 3) * (MS_MAX_ITS + 1)) * MS_MAX_GRIDS),
                 ("errinf", c_double), ("solve_ms", c_double), ("dofs", c_ll), ("total_ksp_its", c_ll),
-                ("nfuncs", c_ll), ("grid_ms", c_double * MS_MAX_GRIDS)]
+                ("nfuncs", c_ll), ("grid_ms", c_double * MS_MAX_GRIDS), ("err1", c_double),
+                ("active_area_err", c_double), ("n_active", c_ll)]
 
     def fnorms(self, k):
         return [self.fnorm[k][i] for i in range(self.its[k] + 1)]
@@ -214,6 +215,8 @@ def load():
     lib.fishgpu_ms_opts_default.argtypes = [_P(MsOpts)]
     lib.fishgpu_bratu_opts_default.argtypes = [_P(MsOpts)]
     lib.fishgpu_bratu_opts_default.restype = c_int
+    lib.fishgpu_obstacle_opts_default.argtypes = [_P(MsOpts)]
+    lib.fishgpu_obstacle_opts_default.restype = c_int
     lib.BratuFunctionLocal_gpu.argtypes = [_P(Info), c_void_p, c_void_p, c_double, c_int, c_void_p]
     lib.BratuFunctionLocal_gpu.restype = c_int
     lib.fishgpu_ms_opts_parse.argtypes = [_P(MsOpts), c_int, _P(ctypes.c_char_p)]
@@ -573,6 +576,17 @@ def bratu_options(argv=()):
         argv = argv.split()
     o = MsOpts()
     _check(load().fishgpu_bratu_opts_default(ctypes.byref(o)), "fishgpu_bratu_opts_default")
+    arr = (ctypes.c_char_p * max(1, len(argv)))(*[a.encode() for a in argv])
+    _check(load().fishgpu_ms_opts_parse(ctypes.byref(o), len(argv), arr), "fishgpu_ms_opts_parse")
+    return o
+
+
+def obstacle_options(argv=()):
+    """Parse obstacle.c's flags (-da_refine, -snes_grid_sequence, -snes_*, -ksp_rtol) into an MsOpts."""
+    if isinstance(argv, str):
+        argv = argv.split()
+    o = MsOpts()
+    _check(load().fishgpu_obstacle_opts_default(ctypes.byref(o)), "fishgpu_obstacle_opts_default")
     arr = (ctypes.c_char_p * max(1, len(argv)))(*[a.encode() for a in argv])
     _check(load().fishgpu_ms_opts_parse(ctypes.byref(o), len(argv), arr), "fishgpu_ms_opts_parse")
     return o

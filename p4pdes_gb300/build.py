@@ -84,7 +84,7 @@ def build_driver(verbose=False):
     """The C drivers: fish, minimal and bratu2D, with the reference programs' flags."""
     os.makedirs(BINDIR, exist_ok=True)
     exes = []
-    for name in ("fish", "minimal", "bratu2D"):
+    for name in ("fish", "minimal", "bratu2D", "obstacle"):
         src = os.path.join(PKG, "host", name + ".c")
         exe = os.path.join(BINDIR, name)
         if _stale(exe, [src, LIB, os.path.join(INCLUDE, "fishgpu.h")]):

@@ -50,6 +50,36 @@ __host__ __device__ inline double ms_gd(const MsP &P, double x, double y) {
   return P.c * cosh(x / P.c) * sin(acos((y / P.c) / cosh(x / P.c)));
 }
 
+// Obstacle problem (c/ch12/obstacle.c:15-49) on (-2,2)^2: the hemispherical
+// obstacle with a C^1 skirt at r0 = 0.9, and the exact solution of the
+// radial free-boundary problem (free boundary at r = a).
+__host__ __device__ inline double obs_psi(double x, double y) {
+  const double r = sqrt(x * x + y * y), r0 = 0.9, psi0 = sqrt(1.0 - r0 * r0), dpsi0 = -r0 / psi0;
+  return r <= r0 ? sqrt(1.0 - r * r) : psi0 + dpsi0 * (r - r0);
+}
+
+__host__ __device__ inline double obs_uexact(double x, double y) {
+  const double afree = 0.697965148223374, A = 0.680259411891719, B = 0.471519893402112;
+  const double r = sqrt(x * x + y * y);
+  return r <= afree ? obs_psi(x, y) : -A * log(r) + B;
+}
+
+constexpr double OBS_ZEROTOL = 1.0e-8;  // PETSc's active-set tolerance (obstacle.c:191)
+
+// Poisson2DFunctionLocal (c/ch6/poissonfunctions.c:27-64) with f = 0 and
+// g = the exact solution, on (-2,2)^2: interior rows; boundary neighbours are g
+__device__ __forceinline__ double obs_f_interior(const Geom &g, const double *__restrict__ u, long long pitch, int i,
+                                                 int j) {
+  const double hx = g.h[0], hy = g.h[1], x = -2.0 + i * hx, y = -2.0 + j * hy;
+  const double scx = hy / hx, scy = hx / hy, scdiag = 2.0 * (scx + scy);
+  const long long n = (long long)j * pitch + i;
+  const double ue = (i + 1 == g.mx - 1) ? obs_uexact(x + hx, y) : u[n + 1];
+  const double uw = (i - 1 == 0) ? obs_uexact(x - hx, y) : u[n - 1];
+  const double un = (j + 1 == g.my - 1) ? obs_uexact(x, y + hy) : u[n + pitch];
+  const double us = (j - 1 == 0) ? obs_uexact(x, y - hy) : u[n - pitch];
+  return scdiag * u[n] - scx * (uw + ue) - scy * (us + un);
+}
+
 // Bratu at interior node (i,j), bratu2D.c:205-211: the neighbours are the array's values
 __device__ __forceinline__ double lb_f_interior(const Geom &g, const MsP &P, const double *__restrict__ u,
                                                 long long pitch, int i, int j) {
@@ -156,11 +186,18 @@ __global__ void __launch_bounds__(256) k_ms_resid(Geom g, MsP P, const double *_
   double acc = 0.0;
   if (in_) {
     double f = 0.0;
-    if (node)
+    if (node && P.model == FISHGPU_NL_OBSTACLE) {
+      const double x = -2.0 + i * g.h[0], y = -2.0 + j * g.h[1];
+      f = ms_bdry(g, i, j) ? 2.0 * (g.h[1] / g.h[0] + g.h[0] / g.h[1]) * (u[n] - obs_uexact(x, y))
+                           : obs_f_interior(g, u, g.pitch, i, j);
+      // the VI residual norm is taken over the inactive set (u > psi or F <= 0)
+      acc = (u[n] <= obs_psi(x, y) + OBS_ZEROTOL && f > 0.0) ? 0.0 : f * f;
+    } else if (node) {
       f = ms_bdry(g, i, j) ? u[n] - ms_gd(P, i * g.h[0], j * g.h[1])
           : P.model == FISHGPU_NL_BRATU ? lb_f_interior(g, P, u, g.pitch, i, j) : ms_f_interior(g, P, u, g.pitch, i, j);
+      acc = f * f;
+    }
     F[n] = f;
-    acc = f * f;
   }
   double v1[1] = {acc};
   ms_reduce<1>(v1, red, StoreFin{out});
@@ -177,11 +214,14 @@ __device__ __forceinline__ void ms_half(double q, double d, double hn, double dt
 
 // Jacobian coefficients at u: C1 = (Ae, Qe, Aw, Qw), C2 = (An, Qn, As, Qs)
 __global__ void __launch_bounds__(256) k_ms_coef(Geom g, MsP P, const double *__restrict__ u,
-                                                 float4 *__restrict__ C1, float4 *__restrict__ C2) {
+                                                 const double *__restrict__ F, float4 *__restrict__ C1,
+                                                 float4 *__restrict__ C2) {
   MS_NODE_BEGIN
   if (!in_) return;
   float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
-  if (node && !ms_bdry(g, i, j) && P.model == FISHGPU_NL_BRATU) {
+  if (node && P.model == FISHGPU_NL_OBSTACLE) {  // C1.x = 1 on the active set
+    a.x = (u[n] <= obs_psi(-2.0 + i * g.h[0], -2.0 + j * g.h[1]) + OBS_ZEROTOL && F[n] > 0.0) ? 1.f : 0.f;
+  } else if (node && !ms_bdry(g, i, j) && P.model == FISHGPU_NL_BRATU) {
     a.x = (float)(g.h[0] * g.h[1] * P.lambda * exp(u[n]));  // the diagonal shift darea lambda e^u
   } else if (node && !ms_bdry(g, i, j)) {
     const double hx = g.h[0], hy = g.h[1];
@@ -205,8 +245,15 @@ __global__ void __launch_bounds__(256) k_ms_coef(Geom g, MsP P, const double *__
 __device__ __forceinline__ float ms_jv_node(const Geom &g, int model, int i, int j, long long n, float a, float b,
                                             const float4 *__restrict__ C1, const float4 *__restrict__ C2,
                                             const float *__restrict__ v) {
-  if (ms_bdry(g, i, j)) return v[n];
   const long long P = g.pitch;
+  if (model == FISHGPU_NL_OBSTACLE) {  // Poisson2DJacobianLocal on the inactive set, identity on the active set
+    if (C1[n].x != 0.f) return v[n];
+    if (ms_bdry(g, i, j)) return 2.f * (a + b) * v[n];
+    const bool E = i + 1 < g.mx - 1, Wb = i - 1 > 0, N = j + 1 < g.my - 1, S = j - 1 > 0;
+    return 2.f * (a + b) * v[n] - a * ((E ? v[n + 1] : 0.f) + (Wb ? v[n - 1] : 0.f)) -
+           b * ((N ? v[n + P] : 0.f) + (S ? v[n - P] : 0.f));
+  }
+  if (ms_bdry(g, i, j)) return v[n];
   if (model == FISHGPU_NL_BRATU)
     return (2.f * (a + b) - C1[n].x) * v[n] - a * (v[n - 1] + v[n + 1]) - b * (v[n - P] + v[n + P]);
   const bool E = i + 1 < g.mx - 1, Wb = i - 1 > 0, N = j + 1 < g.my - 1, S = j - 1 > 0;
@@ -290,12 +337,18 @@ __global__ void __launch_bounds__(256) k_bi_p(Geom g, MsKsp *st, const float *__
 }
 
 // out = M in: the V-cycle's result inside, in itself on boundary rows (z null: no preconditioner)
-__global__ void __launch_bounds__(256) k_bi_pcout(Geom g, MsKsp *st, const float *__restrict__ z,
-                                                  const float *__restrict__ in, float *__restrict__ out) {
+// Obstacle: the Poisson V-cycle's result everywhere but on the active set
+// (boundary rows of its Jacobian are Poisson's too).
+__global__ void __launch_bounds__(256) k_bi_pcout(Geom g, int model, const float4 *__restrict__ C1, MsKsp *st,
+                                                  const float *__restrict__ z, const float *__restrict__ in,
+                                                  float *__restrict__ out) {
   if (msk_done(st)) return;
   MS_NODE_BEGIN
   if (!in_) return;
-  out[n] = (node && z && !ms_bdry(g, i, j)) ? z[n] : in[n];
+  bool use_z;
+  if (model == FISHGPU_NL_OBSTACLE) use_z = node && z && C1[n].x == 0.f;
+  else use_z = node && z && !ms_bdry(g, i, j);
+  out[n] = use_z ? z[n] : in[n];
 }
 
 struct AlphaFin {
@@ -394,10 +447,11 @@ __global__ void __launch_bounds__(256) k_bi_xr(Geom g, MsKsp *st, const float *_
 }
 
 // ------------------------------------------------------------------ Newton helpers
-// b = F / fnorm (FP32)
-__global__ void __launch_bounds__(256) k_ms_demote(Geom g, const double *__restrict__ F, double inv, float *__restrict__ b) {
+// b = F / fnorm (FP32); 0 on the active set of the obstacle problem (C1.x)
+__global__ void __launch_bounds__(256) k_ms_demote(Geom g, int model, const float4 *__restrict__ C1,
+                                                   const double *__restrict__ F, double inv, float *__restrict__ b) {
   MS_NODE_BEGIN
-  if (in_) b[n] = (float)(F[n] * inv);
+  if (in_) b[n] = (model == FISHGPU_NL_OBSTACLE && node && C1[n].x != 0.f) ? 0.f : (float)(F[n] * inv);
 }
 
 // t = J x (FP32); out = {F.t, x.x}
@@ -408,19 +462,33 @@ __global__ void __launch_bounds__(256) k_ms_slope(Geom g, int model, float a, fl
   double ft = 0.0, xx = 0.0;
   if (node) {
     const float o = ms_jv_node(g, model, i, j, n, a, b, C1, C2, x);
-    ft = F[n] * (double)o;
+    ft = (model == FISHGPU_NL_OBSTACLE && C1[n].x != 0.f) ? 0.0 : F[n] * (double)o;
     xx = (double)x[n] * x[n];
   }
   double v2[2] = {ft, xx};
   ms_reduce<2>(v2, red, Store2Fin{out});
 }
 
-// W = u - c x
-__global__ void __launch_bounds__(256) k_ms_trial(Geom g, const double *__restrict__ u, double c,
+// W = u - c x, projected onto u >= psi for the obstacle problem
+__global__ void __launch_bounds__(256) k_ms_trial(Geom g, int model, const double *__restrict__ u, double c,
                                                   const float *__restrict__ x, double *__restrict__ W) {
   MS_NODE_BEGIN
-  if (in_) W[n] = node ? u[n] - c * (double)x[n] : 0.0;
+  if (!in_) return;
+  double w = node ? u[n] - c * (double)x[n] : 0.0;
+  if (node && model == FISHGPU_NL_OBSTACLE) w = fmax(w, obs_psi(-2.0 + i * g.h[0], -2.0 + j * g.h[1]));
+  W[n] = w;
 }
+
+// u = max(u, psi) (SNESVIProjectOntoBounds at the start of a VI solve)
+__global__ void __launch_bounds__(256) k_obs_project(Geom g, double *__restrict__ u) {
+  MS_NODE_BEGIN
+  if (node) u[n] = fmax(u[n], obs_psi(-2.0 + i * g.h[0], -2.0 + j * g.h[1]));
+}
+
+// the obstacle report: sum and max of |u - u_exact| (sel 0), or the number of
+// active nodes (sel 1: u <= psi + zerotol and F > 0, obstacle.c:184-213)
+__global__ void __launch_bounds__(256) k_obs_report(Geom g, int sel, const double *__restrict__ u,
+                                                    const double *__restrict__ F, double *part, int cap);
 
 // u.u -> out[0]
 __global__ void __launch_bounds__(256) k_ms_norm2(Geom g, const double *__restrict__ u, Reducer red, double *out) {
@@ -552,6 +620,22 @@ __global__ void __launch_bounds__(256) k_ms_err(Geom g, MsP P, const double *__r
   block_3(s, lo, hi, part, cap);
 }
 
+__global__ void __launch_bounds__(256) k_obs_report(Geom g, int sel, const double *__restrict__ u,
+                                                    const double *__restrict__ F, double *part, int cap) {
+  MS_NODE_BEGIN
+  double s = 0.0, lo = INFINITY, hi = 0.0;
+  if (node) {
+    const double x = -2.0 + i * g.h[0], y = -2.0 + j * g.h[1];
+    if (sel == 0) {
+      s = fabs(u[n] - obs_uexact(x, y));
+      hi = s;
+    } else {
+      s = (u[n] <= obs_psi(x, y) + OBS_ZEROTOL && F[n] > 0.0) ? 1.0 : 0.0;
+    }
+  }
+  block_3(s, lo, hi, part, cap);
+}
+
 // The call-back: dense whole-grid arrays, owned box
 __global__ void __launch_bounds__(256) k_ms_funclocal(Geom g, MsP P, int xs, int ys, int xm, int ym,
                                                       const double *__restrict__ u, double *__restrict__ F) {
@@ -638,11 +722,11 @@ static void enq_bicg_iter(fishgpu_ms_solver *S, MsLevel &L) {
   const bool mg = S->o.pc_type == FISHGPU_PC_MG;
   k_bi_p<<<L.grid, L.block, 0, s>>>(g, S->st, L.r, L.p, L.v);
   const float *z = mg ? solver_vcycle32(L.P, L.p, &S->st->k) : nullptr;
-  k_bi_pcout<<<L.grid, L.block, 0, s>>>(g, S->st, z, L.p, L.ph);
+  k_bi_pcout<<<L.grid, L.block, 0, s>>>(g, S->P.model, L.C1, S->st, z, L.p, L.ph);
   k_bi_jv1<<<L.grid, L.block, 0, s>>>(g, S->P.model, S->st, a, b, L.C1, L.C2, L.ph, L.v, L.rh, S->red);
   k_bi_s<<<L.grid, L.block, 0, s>>>(g, S->st, L.r, L.v, L.s);
   z = mg ? solver_vcycle32(L.P, L.s, &S->st->k) : nullptr;
-  k_bi_pcout<<<L.grid, L.block, 0, s>>>(g, S->st, z, L.s, L.sh);
+  k_bi_pcout<<<L.grid, L.block, 0, s>>>(g, S->P.model, L.C1, S->st, z, L.s, L.sh);
   k_bi_jv2<<<L.grid, L.block, 0, s>>>(g, S->P.model, S->st, a, b, L.C1, L.C2, L.sh, L.t, L.s, S->red);
   k_bi_xr<<<L.grid, L.block, 0, s>>>(g, S->st, L.ph, L.sh, L.s, L.t, L.rh, L.x, L.r, S->red);
 }
@@ -710,6 +794,7 @@ static int newton(fishgpu_ms_solver *S, MsLevel &L, int k, fishgpu_ms_report *re
   const float a = (float)(g.h[1] / g.h[0]), b = (float)(g.h[0] / g.h[1]);
   int rc;
   double fnorm = 0.0;
+  if (S->P.model == FISHGPU_NL_OBSTACLE) k_obs_project<<<L.grid, L.block, 0, s>>>(g, L.u);
   if ((rc = residual(S, L, L.u, L.F, &fnorm))) return rc;
   rep->fnorm[k][0] = fnorm;
   if (o.monitor_degree > 0 && (rc = area(S, L, L.u, rep->area[k][0]))) return rc;
@@ -730,8 +815,8 @@ static int newton(fishgpu_ms_solver *S, MsLevel &L, int k, fishgpu_ms_report *re
       break;
     }
     // J Y = F: coefficients at u, b = F/||F||, BiCGStab for x = J^-1 b, Y = ||F|| x
-    k_ms_coef<<<L.grid, L.block, 0, s>>>(g, S->P, L.u, L.C1, L.C2);
-    k_ms_demote<<<L.grid, L.block, 0, s>>>(g, L.F, 1.0 / fnorm, L.b);
+    k_ms_coef<<<L.grid, L.block, 0, s>>>(g, S->P, L.u, L.F, L.C1, L.C2);
+    k_ms_demote<<<L.grid, L.block, 0, s>>>(g, S->P.model, L.C1, L.F, 1.0 / fnorm, L.b);
     MS_CK(cudaGetLastError());
     MS_CK(cudaGraphLaunch(L.g_init, s));
     int kits = 0, kreason = 0;
@@ -766,7 +851,7 @@ static int newton(fishgpu_ms_solver *S, MsLevel &L, int k, fishgpu_ms_report *re
     bool ok = false;
     const double alpha = 1e-4;
     for (int ls = 0; ls < 41; ls++) {
-      k_ms_trial<<<L.grid, L.block, 0, s>>>(g, L.u, lam * scale, L.x, L.W);
+      k_ms_trial<<<L.grid, L.block, 0, s>>>(g, S->P.model, L.u, lam * scale, L.x, L.W);
       if ((rc = residual(S, L, L.W, L.G, &gnorm))) return rc;
       if (!o.line_search || 0.5 * gnorm * gnorm <= 0.5 * fnorm * fnorm + lam * alpha * initslope) {
         ok = true;
@@ -843,6 +928,14 @@ extern "C" int fishgpu_bratu_opts_default(fishgpu_ms_opts *o) {
   o->ctx.model = FISHGPU_NL_BRATU;  // bratu2D.c:87-98: lambda 1, u = 0 on the boundary
   o->ctx.problem = FISHGPU_BRATU_ZERO;
   o->ctx.lambda = 1.0;
+  return FISHGPU_OK;
+}
+
+extern "C" int fishgpu_obstacle_opts_default(fishgpu_ms_opts *o) {
+  const int rc = fishgpu_ms_opts_default(o);
+  if (rc) return rc;
+  o->ctx.model = FISHGPU_NL_OBSTACLE;  // obstacle.c:89-107: 3x3 grid on (-2,2)^2, u0 = 0
+  o->ctx.problem = 0;
   return FISHGPU_OK;
 }
 
@@ -924,7 +1017,13 @@ extern "C" int fishgpu_ms_opts_parse(fishgpu_ms_opts *o, int argc, const char *c
       // Jacobian handling of PETSc: the exact Jacobian is always used
     } else if (!strcmp(k, "-snes_type")) {
       if (a + 1 >= argc) return FISHGPU_ERR_ARG;
-      if (strcmp(argv[++a], "newtonls")) return FISHGPU_ERR_UNSUPPORTED;  // FAS, NGS, ... are not offered
+      const char *v = argv[++a];
+      const bool vi = !strcmp(v, "vinewtonrsls") || !strcmp(v, "vinewtonssls");
+      // the obstacle problem is solved by the reduced-space method for either VI type
+      if (o->ctx.model == FISHGPU_NL_OBSTACLE ? !vi : strcmp(v, "newtonls")) return FISHGPU_ERR_UNSUPPORTED;
+    } else if (!strcmp(k, "-obs_dump_binary")) {
+      if (a + 1 >= argc) return FISHGPU_ERR_ARG;
+      a++;  // written by the driver
     } else if (!strcmp(k, "-snes_view_solution")) {
       if (a + 1 < argc && argv[a + 1][0] != '-') a++;  // written by the driver
     } else if (!strcmp(k, "-log_view")) {
@@ -944,6 +1043,7 @@ extern "C" int fishgpu_ms_opts_parse(fishgpu_ms_opts *o, int argc, const char *c
   }
   o->mx = mx;
   o->my = my;
+  if (o->ctx.model == FISHGPU_NL_OBSTACLE) return (o->exact_init || o->monitor_degree) ? FISHGPU_ERR_ARG : FISHGPU_OK;
   if (o->ctx.model == FISHGPU_NL_BRATU) {
     if (o->ctx.problem == FISHGPU_BRATU_LIOUVILLE && o->ctx.lambda != 1.0) return FISHGPU_ERR_ARG;  // bratu2D.c:109-113
     if (o->exact_init || o->monitor_degree) return FISHGPU_ERR_ARG;
@@ -978,7 +1078,9 @@ extern "C" int fishgpu_ms_solver_create(const fishgpu_ms_opts *o, void *stream, 
   if (!o || !out) return FISHGPU_ERR_ARG;
   *out = nullptr;
   if (o->mx < 3 || o->my < 3 || o->grid_sequence < 0 || o->grid_sequence >= FISHGPU_MS_MAX_GRIDS) return FISHGPU_ERR_ARG;
-  if (o->ctx.model != FISHGPU_NL_MINIMAL && o->ctx.model != FISHGPU_NL_BRATU) return FISHGPU_ERR_ARG;
+  if (o->ctx.model != FISHGPU_NL_MINIMAL && o->ctx.model != FISHGPU_NL_BRATU && o->ctx.model != FISHGPU_NL_OBSTACLE)
+    return FISHGPU_ERR_ARG;
+  if (o->ctx.model == FISHGPU_NL_OBSTACLE && (o->monitor_degree || o->exact_init)) return FISHGPU_ERR_ARG;
   if (o->ctx.problem != 0 && o->ctx.problem != 1) return FISHGPU_ERR_ARG;
   if (o->ctx.model == FISHGPU_NL_MINIMAL && o->ctx.problem == FISHGPU_MS_CATENOID && !(o->ctx.catenoid_c >= 1.0))
     return FISHGPU_ERR_ARG;
@@ -1027,6 +1129,7 @@ extern "C" int fishgpu_ms_solver_create(const fishgpu_ms_opts *o, void *stream, 
     fishgpu_opts_default(&po);
     po.ctx.dim = 2;
     po.ctx.problem = FISHGPU_ZERO;
+    if (o->ctx.model == FISHGPU_NL_OBSTACLE) po.ctx.Lx = po.ctx.Ly = 4.0;  // (-2,2)^2, obstacle.c:97
     po.mx = mx;
     po.my = my;
     po.mz = 1;
@@ -1090,7 +1193,7 @@ extern "C" int fishgpu_ms_solver_solve(fishgpu_ms_solver *S, double *u_host, fis
   for (size_t k = 0; k < S->lev.size(); k++) {
     MsLevel &L = S->lev[k];
     if (k == 0) {
-      const int mode = S->P.model == FISHGPU_NL_BRATU ? 2 : S->o.exact_init ? 1 : 0;
+      const int mode = S->P.model != FISHGPU_NL_MINIMAL ? 2 : S->o.exact_init ? 1 : 0;
       k_ms_init<<<L.grid, L.block, 0, s>>>(L.g, S->P, mode, L.u);
     } else {
       MsLevel &C = S->lev[k - 1];
@@ -1110,10 +1213,24 @@ extern "C" int fishgpu_ms_solver_solve(fishgpu_ms_solver *S, double *u_host, fis
   MsLevel &L = S->lev.back();
   rep->dofs = (long long)L.g.mx * L.g.my;
   rep->errinf = -1.0;
+  if (S->P.model == FISHGPU_NL_OBSTACLE) {
+    const int nb = (int)(L.grid.x * L.grid.y);
+    k_obs_report<<<L.grid, L.block, 0, s>>>(L.g, 0, L.u, L.F, S->part3, S->cap);
+    k_ms_fin3<<<1, 256, 0, s>>>(S->part3, S->cap, nb, S->dval);
+    k_obs_report<<<L.grid, L.block, 0, s>>>(L.g, 1, L.u, L.F, S->part3, S->cap);
+    k_ms_fin3<<<1, 256, 0, s>>>(S->part3, S->cap, nb, S->dval + 3);
+    MS_CK(cudaGetLastError());
+    if ((rc = read_vals(S, 6))) return rc;
+    const double afree = 0.697965148223374, exactarea = M_PI * afree * afree;
+    rep->err1 = S->hval[0] / ((double)L.g.mx * L.g.my);
+    rep->errinf = S->hval[2];
+    rep->n_active = (long long)S->hval[3];
+    rep->active_area_err = fabs(L.g.h[0] * L.g.h[1] * S->hval[3] - exactarea) / exactarea;
+  }
   const bool has_exact = S->P.model == FISHGPU_NL_BRATU
                              ? S->o.ctx.problem == FISHGPU_BRATU_LIOUVILLE
                              : (S->o.ctx.problem == FISHGPU_MS_CATENOID && S->o.ctx.q == -0.5);
-  if (has_exact) {
+  if (has_exact && S->P.model != FISHGPU_NL_OBSTACLE) {
     k_ms_err<<<L.grid, L.block, 0, s>>>(L.g, S->P, L.u, S->part3, S->cap);
     k_ms_fin3<<<1, 256, 0, s>>>(S->part3, S->cap, (int)(L.grid.x * L.grid.y), S->dval);
     MS_CK(cudaGetLastError());
