@@ -221,6 +221,26 @@ def minimal_leg(fg, reps=3):
     return out
 
 
+def clients_leg(fg):
+    """The other clients of the Poisson call-backs at 1025^2 (best of 3 solves)."""
+    out = {}
+    for name, opts, args in (
+            ("bratu", fg.bratu_options, "-lb_exact -da_refine 9 -snes_rtol 1e-10"),
+            ("obstacle", fg.obstacle_options, "-snes_grid_sequence 9")):
+        o = opts(args)
+        with fg.MsSolver(o) as s:
+            s.solve()
+            best = min((s.solve() for _ in range(3)), key=lambda r: r.solve_ms)
+        last = best.ngrids - 1
+        out[name] = {"options": args, "dofs": best.dofs, "solve_ms": best.solve_ms,
+                     "dof_per_s": best.dofs / (best.solve_ms * 1e-3), "newton_its": best.its[last],
+                     "inner_its_total": best.total_ksp_its, "errinf": best.errinf,
+                     "reason": fg.snes_reason_name(best.reason[last])}
+        if name == "obstacle":
+            out[name]["active_area_err"] = best.active_area_err
+    return out
+
+
 def serve_leg(fg, n_req, rate=2000.0, workers=16):
     """Mixed 2D/3D serving stream through the continuous-batching server."""
     from p4pdes_gb300 import serve
@@ -361,6 +381,8 @@ def run_ours(args):
     batch = batch_leg(torch, fg, args.batch_instances) if args.batch_instances > 0 else None
     serving = serve_leg(fg, args.serve_requests) if args.serve_requests > 0 else None
     minimal = minimal_leg(fg) if args.minimal else None
+    if minimal is not None:
+        minimal["other_clients"] = clients_leg(fg)
     line = {
         "metric": METRIC, "value": value, "unit": "DOF/s", "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,

@@ -206,7 +206,10 @@ static int build_hier(fishgpu_solver *S, Hier<T> &H) {
       for (int i = 1; i <= n; i++)
         for (int k = 1; k <= n; k++) hS[(size_t)(i - 1) * n + (k - 1)] = (T)(a * sin(M_PI * (double)i * k / (n + 1)));
       if ((rc = dalloc(S, &c.S[d], (size_t)n * n))) return rc;
-      if (cudaMemcpy(c.S[d], hS.data(), sizeof(T) * n * n, cudaMemcpyHostToDevice) != cudaSuccess)
+      // on the solver's stream: ordered after dalloc's memset of the same buffer
+      // (a legacy-stream copy is not ordered with a non-blocking stream); the
+      // pageable source is staged before the call returns
+      if (cudaMemcpyAsync(c.S[d], hS.data(), sizeof(T) * n * n, cudaMemcpyHostToDevice, S->stream) != cudaSuccess)
         return FISHGPU_ERR_CUDA;
     }
     for (int k = 0; k < c.n[2]; k++)
@@ -219,7 +222,7 @@ static int build_hier(fishgpu_solver *S, Hier<T> &H) {
         }
     const size_t nwork = 2 * (size_t)ni * (c.g.dim < 3 ? (size_t)c.g.mz : 1);  // one work area per block
     if ((rc = dalloc(S, &c.ilam, (size_t)ni)) || (rc = dalloc(S, &c.work, nwork))) return rc;
-    if (cudaMemcpy(c.ilam, hl.data(), sizeof(T) * ni, cudaMemcpyHostToDevice) != cudaSuccess)
+    if (cudaMemcpyAsync(c.ilam, hl.data(), sizeof(T) * ni, cudaMemcpyHostToDevice, S->stream) != cudaSuccess)
       return FISHGPU_ERR_CUDA;
     for (int d = c.g.dim; d < 3; d++) c.S[d] = c.S[0];  // unused
   }
@@ -713,7 +716,7 @@ static int time_kernel_dim(fishgpu_solver *S, const char *name, int reps, double
     h.alpha = 1e-3;
     h.norm_type = FISHGPU_NORM_UNPRECONDITIONED;
     if (cudaMalloc((void **)&tst, sizeof(KspState)) != cudaSuccess) return FISHGPU_ERR_NOMEM;
-    if (cudaMemcpy(tst, &h, sizeof(h), cudaMemcpyHostToDevice) != cudaSuccess) {
+    if (cudaMemcpyAsync(tst, &h, sizeof(h), cudaMemcpyHostToDevice, s) != cudaSuccess) {
       cudaFree(tst);
       return FISHGPU_ERR_CUDA;
     }
