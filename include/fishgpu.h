@@ -197,6 +197,11 @@ long long fishgpu_solver_bytes(const fishgpu_solver *s);
 int fishgpu_solver_solve_host(fishgpu_solver *s, const double *f_host, const double *g_host,
                               double *u_host, fishgpu_report *rep);
 
+/* host -> device bytes fishgpu_solver_solve_host moves for f and g (FISHGPU_USER):
+   all of f; all of g, or only its boundary nodes when g_host is pinned memory
+   (the solver reads g nowhere else) */
+long long fishgpu_solver_host_bytes_in(const fishgpu_solver *s, const double *g_host);
+
 /* device bytes fishgpu_solver_create would allocate (plus the host-array
    buffers of fishgpu_solver_solve_host for FISHGPU_USER); -1 if invalid */
 long long fishgpu_solver_estimate_bytes(const fishgpu_opts *o);

@@ -239,6 +239,8 @@ def load():
     for name in ("fishgpu_petsc_vec_write", "fishgpu_petsc_vec_read", "fishgpu_petsc_mat_write_aij",
                  "fishgpu_petsc_mat_read_aij"):
         getattr(lib, name).restype = c_int
+    lib.fishgpu_solver_host_bytes_in.argtypes = [c_void_p, c_void_p]
+    lib.fishgpu_solver_host_bytes_in.restype = c_ll
     lib.fishgpu_solver_estimate_bytes.argtypes = [_P(Opts)]
     lib.fishgpu_solver_estimate_bytes.restype = c_ll
     lib.fishgpu_server_opts_default.argtypes = [_P(ServerOpts)]
@@ -392,6 +394,11 @@ class Solver:
         if rc not in (0, 4):
             raise FishError(rc, "fishgpu_solver_solve_host")
         return rep
+
+    def host_bytes_in(self, g=None):
+        """Bytes solve_host moves to the device for f and g."""
+        ga = None if g is None else (g.data_ptr() if hasattr(g, "data_ptr") else g.ctypes.data)
+        return load().fishgpu_solver_host_bytes_in(self._h, ga)
 
     def time_kernel(self, name, reps):
         ms, by = c_double(), c_double()

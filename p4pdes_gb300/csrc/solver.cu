@@ -1031,6 +1031,85 @@ extern "C" int fishgpu_solve(const fishgpu_opts *o, double *u_dev, fishgpu_repor
   return rc;
 }
 
+namespace fg {
+// Boundary nodes of a dense mx x my x mz array, enumerated face by face
+// (3D: k faces, then j faces of the inner planes, then i faces of the inner
+// rows; 2D: j rows, then i ends of the inner rows; 1D: both ends).
+__host__ __device__ inline long long bdry_count(int dim, int mx, int my, int mz) {
+  if (dim == 1) return mx > 1 ? 2 : 1;
+  if (dim == 2) return 2LL * mx + 2LL * (my - 2);
+  return 2LL * mx * my + 2LL * mx * (mz - 2) + 2LL * (my - 2) * (mz - 2);
+}
+
+// dst[n] = src[n] on the boundary nodes only: the solver reads the boundary
+// data g nowhere else, so a host g in pinned memory is gathered through the
+// device's mapping of it instead of being copied whole (6 faces instead of
+// the volume in 3D).
+template <int DIM>
+__global__ void __launch_bounds__(256) k_gather_bdry(int mx, int my, int mz, const double *__restrict__ src,
+                                                     double *__restrict__ dst) {
+  const long long tot = bdry_count(DIM, mx, my, mz);
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot; t += (long long)gridDim.x * blockDim.x) {
+    int i, j = 0, k = 0;
+    if (DIM == 1) {
+      i = t == 0 ? 0 : mx - 1;
+    } else if (DIM == 2) {
+      if (t < 2LL * mx) {
+        i = (int)(t % mx);
+        j = t < mx ? 0 : my - 1;
+      } else {
+        const long long r = t - 2LL * mx;
+        j = 1 + (int)(r / 2);
+        i = (r & 1) ? mx - 1 : 0;
+      }
+    } else {
+      const long long fz = 2LL * mx * my, fy = 2LL * mx * (mz - 2);
+      if (t < fz) {
+        k = t < (long long)mx * my ? 0 : mz - 1;
+        const long long r = t % ((long long)mx * my);
+        j = (int)(r / mx);
+        i = (int)(r % mx);
+      } else if (t < fz + fy) {
+        const long long r = t - fz;
+        k = 1 + (int)(r / (2LL * mx));
+        const long long q = r % (2LL * mx);
+        j = q < mx ? 0 : my - 1;
+        i = (int)(q % mx);
+      } else {
+        const long long r = t - fz - fy;
+        k = 1 + (int)(r / (2LL * (my - 2)));
+        const long long q = r % (2LL * (my - 2));
+        j = 1 + (int)(q / 2);
+        i = (q & 1) ? mx - 1 : 0;
+      }
+    }
+    const long long n = ((long long)k * my + j) * mx + i;
+    dst[n] = src[n];
+  }
+}
+}  // namespace fg
+
+// A device-usable address of pinned (page-locked, mapped) host memory, or
+// null for any other pointer.
+static const double *pinned_device_view(const double *p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return (a.type == cudaMemoryTypeHost && a.devicePointer) ? (const double *)a.devicePointer : nullptr;
+}
+
+extern "C" long long fishgpu_solver_host_bytes_in(const fishgpu_solver *S, const double *g_host) {
+  // bytes fishgpu_solver_solve_host moves to the device for f and g (FISHGPU_USER)
+  if (!S || S->o.ctx.problem != FISHGPU_USER) return 0;
+  const long long N = (long long)S->dense.plane * S->dense.mz;
+  long long b = 8LL * N;  // f
+  if (g_host) b += pinned_device_view(g_host) ? 8LL * fg::bdry_count(S->dense.dim, S->dense.mx, S->dense.my, S->dense.mz)
+                                              : 8LL * N;
+  return b;
+}
+
 extern "C" int fishgpu_solver_solve_host(fishgpu_solver *S, const double *f_host, const double *g_host,
                                          double *u_host, fishgpu_report *rep) {
   if (!S || !u_host || !rep) return FISHGPU_ERR_ARG;
@@ -1046,10 +1125,23 @@ extern "C" int fishgpu_solver_solve_host(fishgpu_solver *S, const double *f_host
   if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return FISHGPU_ERR_CUDA;
   int rc = FISHGPU_OK;
   cudaEventRecord(e0, s);
-  if (user && (cudaMemcpyAsync(S->f_own, f_host, sizeof(double) * N, cudaMemcpyHostToDevice, s) != cudaSuccess ||
-               (g_host ? cudaMemcpyAsync(S->g_own, g_host, sizeof(double) * N, cudaMemcpyHostToDevice, s)
-                       : cudaMemsetAsync(S->g_own, 0, sizeof(double) * N, s)) != cudaSuccess))
+  if (user && cudaMemcpyAsync(S->f_own, f_host, sizeof(double) * N, cudaMemcpyHostToDevice, s) != cudaSuccess)
     rc = FISHGPU_ERR_CUDA;
+  if (user && !rc) {
+    const double *gdev = g_host ? pinned_device_view(g_host) : nullptr;
+    if (gdev) {  // boundary values only, read in place from pinned host memory
+      const Geom &d = S->dense;
+      const long long nb = fg::bdry_count(d.dim, d.mx, d.my, d.mz);
+      const unsigned blocks = (unsigned)std::min<long long>((nb + 255) / 256, 4LL * sm_count());
+      if (d.dim == 1) fg::k_gather_bdry<1><<<blocks, 256, 0, s>>>(d.mx, d.my, d.mz, gdev, S->g_own);
+      else if (d.dim == 2) fg::k_gather_bdry<2><<<blocks, 256, 0, s>>>(d.mx, d.my, d.mz, gdev, S->g_own);
+      else fg::k_gather_bdry<3><<<blocks, 256, 0, s>>>(d.mx, d.my, d.mz, gdev, S->g_own);
+      if (cudaGetLastError() != cudaSuccess) rc = FISHGPU_ERR_CUDA;
+    } else if ((g_host ? cudaMemcpyAsync(S->g_own, g_host, sizeof(double) * N, cudaMemcpyHostToDevice, s)
+                       : cudaMemsetAsync(S->g_own, 0, sizeof(double) * N, s)) != cudaSuccess) {
+      rc = FISHGPU_ERR_CUDA;
+    }
+  }
   if (!rc && S->o.initial_type == FISHGPU_INITIAL_GIVEN &&
       cudaMemcpyAsync(S->u_own, u_host, sizeof(double) * N, cudaMemcpyHostToDevice, s) != cudaSuccess)
     rc = FISHGPU_ERR_CUDA;
