@@ -113,6 +113,10 @@ def dist_setup():
     return world, rank, local
 
 
+WORKLOAD = "3D Poisson 513^3 7-point (-da_refine 8), CG+MG V(2,2) Chebyshev/Jacobi, 9 levels, " \
+           "rtol 1e-10 true residual"
+
+
 def run_reference(args):
     world, rank, _ = dist_setup()
     if rank != 0:
@@ -126,8 +130,13 @@ def run_reference(args):
             "steps": K, "warmup": W, "ms_per_step": 1e3 * info["dofs"] / v,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (manufactured manupoly problem)",
-            "config": {"workload": "3D Poisson 257^3 sample of the 513^3 solve, CPU restatement "
-                                   "(oracle) of CG+MG V(2,2) Chebyshev/Jacobi, rtol 1e-10"},
+            "config": {"workload": WORKLOAD, "dofs": 513 ** 3, "levels": 9,
+                       "parallelism": "host cores (OpenMP)",
+                       "measured_on": "a 257^3 sample of this workload per step (the whole 513^3 solve takes "
+                                      "minutes on the host); DOF/s of the sample",
+                       "implementation": "CPU restatement (oracle) of the reference's CG + MG V(2,2) "
+                                         "Chebyshev/Jacobi path, FP64; PETSc is not available to build "
+                                         "the reference's own fish"},
             "cpu_baseline": {"value": v, "unit": "DOF/s", "cores": info["cores"], "kind": "port",
                              "sample": info["sample"]},
             "e2e": {"value": v, "unit": "DOF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -389,9 +398,8 @@ def run_ours(args):
         "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32+f64", "data": "synthetic (manufactured manupoly problem; f and g sampled at the nodes)",
         "config": {
-            "workload": "3D Poisson 513^3 7-point (-da_refine 8), CG+MG V(2,2) Chebyshev/Jacobi, 9 levels, "
-                        "rtol 1e-10 true residual; mixed = FP32 V-cycle + FP32 inner CG inside FP64 "
-                        "iterative refinement",
+            "workload": WORKLOAD,
+            "form": "mixed = FP32 V-cycle + FP32 inner CG inside FP64 iterative refinement",
             "dofs": N, "levels": o_mx.mg_levels, "parallelism": "replicas" if world > 1 else "1 GPU",
             "l2": "no flush: every vector (1.08 GB FP64) exceeds L2",
             "mixed": {"ms": ms / K, "inner_its": rep_mx.its, "outer_its": rep_mx.outer_its,
