@@ -146,6 +146,11 @@ typedef struct {
   int monitor;              /* -ksp_monitor                                 */
   int converged_reason;     /* -ksp_converged_reason                        */
   int snes_monitor;         /* -snes_monitor[_short]                        */
+  int fuse_smooth;          /* -fsh_fuse_smooth 0|1: the two post-smoothing
+                               Chebyshev steps of a 3D FP32 level in one
+                               temporally blocked kernel (default 0: slower
+                               than two launches on GB300; the smoothed
+                               iterate is bit-identical either way)        */
 } fishgpu_opts;
 
 #define FISHGPU_MAX_HIST 512

@@ -150,6 +150,7 @@ extern "C" int fishgpu_opts_default(fishgpu_opts *o) {
   o->inner_max_it = 100;
   o->outer_max_it = 30;
   o->graph_iters = 0;
+  o->fuse_smooth = 0;
   return FISHGPU_OK;
 }
 
@@ -210,6 +211,7 @@ extern "C" int fishgpu_opts_parse(fishgpu_opts *o, int argc, const char *const *
     else if (!strcmp(k, "-fsh_inner_max_it")) { NEEDV(); o->inner_max_it = atoi(v); }
     else if (!strcmp(k, "-fsh_outer_max_it")) { NEEDV(); o->outer_max_it = atoi(v); }
     else if (!strcmp(k, "-fsh_graph_iters")) { NEEDV(); o->graph_iters = atoi(v); }
+    else if (!strcmp(k, "-fsh_fuse_smooth")) { NEEDV(); o->fuse_smooth = atoi(v) != 0; }
     else if (!strcmp(k, "-da_refine")) { NEEDV(); refine = atoi(v); }
     else if (!strcmp(k, "-da_grid_x")) { NEEDV(); base[0] = atoi(v); }
     else if (!strcmp(k, "-da_grid_y")) { NEEDV(); base[1] = atoi(v); }

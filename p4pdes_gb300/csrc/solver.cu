@@ -39,6 +39,7 @@ constexpr int FLAT_BLOCKS = 4096; // grid cap of the pointwise kernels
 
 template <typename T>
 struct Level {
+  Post2Z pz{};     // launch shape of the fused two-step post-smoother (3D FP32)
   Geom g;      // padded pitch
   Slots sl;
   T *b = nullptr, *r = nullptr;
@@ -172,6 +173,7 @@ static int build_hier(fishgpu_solver *S, Hier<T> &H) {
     if (S->batch) g.mz = S->nplanes;  // a batch keeps its instances as planes on every level
     lv.g = g;
     lv.sl = make_slots(g, ZC, 2432, 256, S->batch);
+    if (g.dim == 3) lv.pz = post2z_shape(g);
     double lmin, lmax;
     spectrum(g, &lmin, &lmax);
     lv.emin = o.esteig[0] * lmin + o.esteig[1] * lmax;
@@ -293,6 +295,23 @@ static void enq_smooth(fishgpu_solver *S, Level<T> &lv, bool from_zero, int dots
                                             (T)(omega * c1 * c1));
     lv.cur = nxt;
     return;
+  }
+  if constexpr (DIM == 3 && sizeof(T) == 4) {
+    if (!from_zero && o.smooth_its == 2 && o.fuse_smooth && !S->batch && lv.pz.ok()) {
+      // both steps in one temporally blocked kernel (bit-identical to the two below)
+      const double ckp1 = 2.0 * mu * mu - 1.0, omega = omegaprod * mu / ckp1;
+      const int km = lv.cur, out = third(km, (km + 1) % 3);
+      if (dots >= 0)
+        v_cheb_post2z<true><<<lv.pz.blocks(), lv.pz.threads, lv.pz.smem, s>>>(
+            lv.g, lv.pz, st, (const float *)lv.b, (const float *)lv.X[km], (float *)lv.X[out], (float)c1,
+            (float)(1.0 - omega), (float)omega, (float)(omega * c1), S->red, 0, fin);
+      else
+        v_cheb_post2z<false><<<lv.pz.blocks(), lv.pz.threads, lv.pz.smem, s>>>(
+            lv.g, lv.pz, st, (const float *)lv.b, (const float *)lv.X[km], (float *)lv.X[out], (float)c1,
+            (float)(1.0 - omega), (float)omega, (float)(omega * c1));
+      lv.cur = out;
+      return;
+    }
   }
   int km1 = -1, kk;  // -1: the zero iterate
   if (from_zero) {
@@ -747,6 +766,16 @@ static int time_kernel_dim(fishgpu_solver *S, const char *name, int reps, double
       else
         v_cgp_apply<DIM, double><<<gb, sl.chunk, 0, s>>>(g, sl, tst, ld.X[0], S->p64, S->q64, S->w64, S->red, 1);
       *bytes = 4.0 * sz * N;
+    } else if (!strcmp(name, "post2")) {  // both post-smoothing steps fused: reads b, x0, writes x2
+      if constexpr (DIM == 3) {
+        if (!mixed) return FISHGPU_ERR_UNSUPPORTED;
+        if (!lf.pz.ok()) return FISHGPU_ERR_UNSUPPORTED;
+        v_cheb_post2z<false><<<lf.pz.blocks(), lf.pz.threads, lf.pz.smem, s>>>(g, lf.pz, nullptr, S->r32, lf.X[0],
+                                                                               lf.X[2], 0.5f, 0.5f, 0.5f, 0.1f);
+        *bytes = 3.0 * sz * N;
+      } else {
+        return FISHGPU_ERR_UNSUPPORTED;
+      }
     } else if (!strcmp(name, "smooth_zero")) {  // two steps from zero: reads b, writes x
       if (mixed)
         v_cheb2_zero<DIM, float><<<gb, sl.chunk, 0, s>>>(g, sl, nullptr, S->r32, lf.X[0], 0.5f, 0.1f);
@@ -908,7 +937,18 @@ extern "C" int fishgpu_solver_create(const fishgpu_opts *o, void *stream, fishgp
     fishgpu_solver_destroy(S);
     return FISHGPU_ERR_CUDA;
   }
-  const int cap = reduction_blocks(S);
+  int cap = reduction_blocks(S);
+  if (dim == 3 && o->precision == FISHGPU_MIXED) {
+    const Post2Z pz = post2z_shape(S->fine);
+    if (pz.ok()) cap = std::max(cap, (int)pz.blocks());  // the fused post-smoother reduces too
+    const int smax = 96 * 1024;  // the largest ring of any level (3 x (R+2) x P4 float4 <= 3 x 1056 x 16 B)
+    if (cudaFuncSetAttribute(v_cheb_post2z<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax) != cudaSuccess ||
+        cudaFuncSetAttribute(v_cheb_post2z<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax) !=
+            cudaSuccess) {
+      fishgpu_solver_destroy(S);
+      return FISHGPU_ERR_CUDA;
+    }
+  }
   CK(dalloc(S, &S->st, 1));
   CK(dalloc(S, &S->dval, 8));
   CK(dalloc(S, &S->red.partials, (size_t)2 * 2 * cap));  // two slots of up to two values

@@ -472,6 +472,197 @@ __global__ void __launch_bounds__(256, MinBlocks<T>::value) v_cgp_apply(Geom g, 
   reduce_sel<1, PL>(v1, red, slot, st, FIN_PW, nullptr, s);
 }
 
+// ------------------------------------------------------------------ temporally blocked smoothing
+// Two Chebyshev steps from a nonzero iterate in one pass (3D, FP32):
+//   x1 = x0 + c1 (b - A x0)
+//   x2 = ckm1 x0 + ck x1 + crd (b - A x1)
+// (the post-smoothing of a V-cycle level), reading x0 and b once and writing
+// x2 only: 3 arrays instead of the 7 of two separate steps.  The arithmetic
+// of every point is that of v_cheb (same operations in the same order), so
+// x2 is bit-identical to the two-kernel form; DOTS reduces x2.x2 and x2.b as
+// the last v_cheb step of the finest level does.  Measured at 513^3 it is
+// slower than the two v_cheb launches (0.92 ms against 0.34 + 0.36 ms: one
+// block of ~900 threads per SM, a barrier per plane and 64 registers leave
+// the loads' latency exposed), so the solver uses it only on request
+// (-fsh_fuse_smooth 1).
+__device__ __forceinline__ float f4e(const float4 &v, int e) {
+  return e == 0 ? v.x : e == 1 ? v.y : e == 2 ? v.z : v.w;
+}
+__device__ __forceinline__ void f4set(float4 &v, int e, float a) {
+  if (e == 0) v.x = a; else if (e == 1) v.y = a; else if (e == 2) v.z = a; else v.w = a;
+}
+
+// b - A x for the 4 points of one slot from preloaded neighbours: c (the
+// slot), xl / xr (the points left of element 0 and right of element 3), ys / zs
+// (y and z neighbour slots, already masked to interior neighbours and summed in
+// the order of load_xy / march_src).  The operations of resid_el, in order.
+__device__ __forceinline__ float4 resid4(const Wv<float> &w, const Geom &g, int i4, bool jkb, const float4 &c,
+                                         float xl, float xr, const float4 &ys, const float4 &zs, const float4 &bv) {
+  float4 o;
+#pragma unroll
+  for (int e = 0; e < 4; e++) {
+    const int i = i4 + e;
+    const float xc = f4e(c, e);
+    float v;
+    if (jkb || i == 0 || i == g.mx - 1) {
+      v = fmaf(-w.sd, xc, f4e(bv, e));
+    } else {
+      const float l = e == 0 ? xl : f4e(c, e - 1);
+      const float r = e == 3 ? xr : f4e(c, e + 1);
+      const float a = (i - 1 > 0 ? l : 0.f) + (i + 1 < g.mx - 1 ? r : 0.f);
+      float sm = fmaf(w.sx, a, f4e(bv, e));
+      sm = fmaf(w.sy, f4e(ys, e), sm);
+      sm = fmaf(w.sz, f4e(zs, e), sm);
+      v = fmaf(-w.sd, xc, sm);
+    }
+    f4set(o, e, v);
+  }
+  return o;
+}
+
+// A block owns R full rows (all P4 slots of each) of a z-chunk plus one halo
+// row above and below; a thread owns one slot of one of those R+2 rows and
+// marches k keeping x0 (planes k..k+2), x1 (planes k-1..k+1) and b in
+// registers.  Per plane it computes x1 at plane k+1 for its slot (x0's
+// y-neighbours come from L1/L2 like v_cheb's), publishes it in a 3-plane
+// shared ring, and after one barrier computes x2 at plane k for the R inner
+// rows, taking x1's y-neighbours from the ring.  Threads of the halo rows
+// compute x1 only.  Per point: x0 and b read, x2 written (3 arrays).
+struct Post2Z {
+  int R, P4, threads, nyb, zc, nz;
+  size_t smem;
+  bool ok() const { return R > 0; }
+  unsigned blocks() const { return (unsigned)nyb * (unsigned)nz; }
+};
+
+inline Post2Z post2z_shape(const Geom &g, int min_blocks = 456) {
+  Post2Z q{};
+  q.P4 = g.pitch / 4;
+  if (g.dim != 3 || q.P4 < 33 || g.my < 3 || g.mz < 3) return q;  // small levels: the two-step form
+  int R = 1024 / q.P4 - 2;
+  if (R > g.my) R = g.my;
+  if (R < 2) return q;
+  q.R = R;
+  q.threads = ((R + 2) * q.P4 + 31) / 32 * 32;
+  q.nyb = (g.my + R - 1) / R;
+  int zc = (int)(((long long)q.nyb * g.mz) / (min_blocks > 0 ? min_blocks : 1));
+  zc = zc < 4 ? 4 : zc > 64 ? 64 : zc;
+  if (zc > g.mz) zc = g.mz;
+  q.zc = zc;
+  q.nz = (g.mz + zc - 1) / zc;
+  q.smem = sizeof(float4) * 3 * (size_t)(R + 2) * q.P4;
+  return q;
+}
+
+template <bool DOTS>
+__global__ void __launch_bounds__(1024, 1) v_cheb_post2z(Geom g, Post2Z q, KspState *st, const float *__restrict__ b,
+                                                       const float *__restrict__ x0, float *__restrict__ out,
+                                                       float c1, float ckm1, float ck, float crd,
+                                                       Reducer red = Reducer{}, int slot = 0, Fin fin = FIN_STORE) {
+  if (ksp_done_v(st)) return;
+  extern __shared__ float4 pz_smem[];  // [3][R+2][P4]: x1 of the block's rows, planes k-1..k+1
+  const int t = threadIdx.x, lane = t & 31;
+  const int rows = q.R + 2, plane_slots = rows * q.P4;
+  const bool act = t < plane_slots;
+  const int rho = act ? t / q.P4 : 0, sl = act ? t - rho * q.P4 : 0;  // row in the block (0 = halo), slot
+  const int yb = blockIdx.x % q.nyb, zt = blockIdx.x / q.nyb;
+  const int j = yb * q.R + rho - 1, i4 = 4 * sl;
+  const int k0 = zt * q.zc, k1 = k0 + q.zc < g.mz ? k0 + q.zc : g.mz;
+  const bool jin = act && j >= 0 && j < g.my;
+  const bool inner = jin && rho >= 1 && rho <= q.R;                     // writes x2
+  const bool hs = j - 1 > 0, hn = j + 1 < g.my - 1, jb = j == 0 || j == g.my - 1;
+  const long long col = (long long)j * g.pitch + i4;
+  const Wv<float> w(g);
+  const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+  auto ld = [&](const float *a, int kk) -> float4 {  // own slot of plane kk (0 outside the grid)
+    if (!jin || kk < 0 || kk >= g.mz) return zero;
+    return *reinterpret_cast<const float4 *>(a + (long long)kk * g.plane + col);
+  };
+  auto ldy = [&](int kk, int dj) -> float4 {  // x0 at row j+dj of plane kk, an interior neighbour
+    return *reinterpret_cast<const float4 *>(x0 + (long long)kk * g.plane + col + (long long)dj * g.pitch);
+  };
+  auto add = [](const float4 &a, const float4 &c) { return make_float4(a.x + c.x, a.y + c.y, a.z + c.z, a.w + c.w); };
+  // x-neighbours by shuffles (warp edges: the scalar beyond; row starts and ends
+  // are boundary or padding points, whose neighbours are never used)
+  auto xnb = [&](const float4 &c, const float *arr_plane, float &l, float &r) {
+    l = __shfl_up_sync(0xffffffffu, c.w, 1);
+    r = __shfl_down_sync(0xffffffffu, c.x, 1);
+    if (lane == 0) l = (jin && i4 > 0 && arr_plane) ? arr_plane[col - 1] : 0.f;
+    if (lane == 31) r = (jin && i4 + 4 < g.mx && arr_plane) ? arr_plane[col + 4] : 0.f;
+  };
+  auto ring = [&](int kk, int r) -> float4 & { return pz_smem[(((kk % 3) + 3) % 3 * rows + r) * q.P4 + sl]; };
+  // x1 at plane kk for this slot from x0 planes kk-1, kk, kk+1 (xd, xc, xu)
+  auto step1 = [&](int kk, const float4 &xd, const float4 &xc, const float4 &xu, const float4 &bv) -> float4 {
+    float l, r;
+    xnb(xc, (kk >= 0 && kk < g.mz) ? x0 + (long long)kk * g.plane : nullptr, l, r);
+    float4 o = zero;
+    if (jin && kk >= 0 && kk < g.mz && i4 < g.mx) {
+      const float4 ys = add((hs ? ldy(kk, -1) : zero), (hn ? ldy(kk, 1) : zero));
+      const float4 zs = add((kk - 1 > 0 ? xd : zero), (kk + 1 < g.mz - 1 ? xu : zero));
+      const float4 rr = resid4(w, g, i4, jb || kk == 0 || kk == g.mz - 1, xc, l, r, ys, zs, bv);
+#pragma unroll
+      for (int e = 0; e < 4; e++) f4set(o, e, i4 + e < g.mx ? fmaf(c1, f4e(rr, e), 1.f * f4e(xc, e)) : 0.f);
+    }
+    return o;
+  };
+  // prologue: x1 at planes k0-1 (registers) and k0 (registers and ring)
+  float4 xa = ld(x0, k0 - 2), xb = ld(x0, k0 - 1), xcur = ld(x0, k0), xn = ld(x0, k0 + 1);
+  float4 x1d = step1(k0 - 1, xa, xb, xcur, ld(b, k0 - 1));
+  float4 bk = ld(b, k0);
+  float4 x1c = step1(k0, xb, xcur, xn, bk);
+  if (act) ring(k0, rho) = x1c;
+  // window: xcur = x0(k), xn = x0(k+1)
+  float zz = 0.f, zr = 0.f;
+  for (int k = k0; k < k1; k++) {
+    const float4 xnn = ld(x0, k + 2);
+    const float4 bn = ld(b, k + 1);
+    const float4 x1n = step1(k + 1, xcur, xn, xnn, bn);
+    if (act) ring(k + 1, rho) = x1n;
+    __syncthreads();  // x1 planes k and k+1 of every row are in the ring
+    // x2 = ckm1 x0 + ck x1 + crd (b - A x1) at plane k
+    float l, r;
+    {
+      l = __shfl_up_sync(0xffffffffu, x1c.w, 1);
+      r = __shfl_down_sync(0xffffffffu, x1c.x, 1);
+      const float4 *rowp = pz_smem + ((((k % 3) + 3) % 3) * rows + rho) * q.P4;  // x1 plane k, this row
+      if (lane == 0) l = (act && sl > 0) ? rowp[sl - 1].w : 0.f;
+      if (lane == 31) r = (act && sl + 1 < q.P4) ? rowp[sl + 1].x : 0.f;
+    }
+    if (inner && i4 < g.pitch) {
+      float4 o = zero;
+      if (i4 < g.mx) {
+        const float4 ys = add((hs ? ring(k, rho - 1) : zero), (hn ? ring(k, rho + 1) : zero));
+        const float4 zs = add((k - 1 > 0 ? x1d : zero), (k + 1 < g.mz - 1 ? x1n : zero));
+        const float4 rr = resid4(w, g, i4, jb || k == 0 || k == g.mz - 1, x1c, l, r, ys, zs, bk);
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+          float v = 0.f;
+          if (i4 + e < g.mx) {
+            float base = ck * f4e(x1c, e);
+            base = fmaf(ckm1, f4e(xcur, e), base);
+            v = fmaf(crd, f4e(rr, e), base);
+            if (DOTS) {
+              zz = fmaf(v, v, zz);
+              zr = fmaf(v, f4e(bk, e), zr);
+            }
+          }
+          f4set(o, e, v);
+        }
+      }
+      *reinterpret_cast<float4 *>(out + (long long)k * g.plane + col) = o;
+    }
+    x1d = x1c;
+    x1c = x1n;
+    xcur = xn;
+    xn = xnn;
+    bk = bn;
+  }
+  if (DOTS) {
+    double v2[2] = {(double)zz, (double)zr};
+    reduce_and_finalize<2>(v2, red, slot, st, fin, nullptr);
+  }
+}
+
 // ------------------------------------------------------------------ grid transfers
 // b_c = P^T r_f (full weighting; weights 1, 1/2 per offset and dimension).
 // A thread owns a coarse slot (I4..I4+3) and marches coarse planes; the fine

@@ -241,6 +241,28 @@ def test_mixed_form_inner_iterations_do_not_depend_on_the_outer_norm_option(cuda
     assert a.history() == b.history()
 
 
+@pytest.mark.parametrize("args", [
+    "-fsh_dim 3 -fsh_problem manupoly -da_refine 5 -pc_type mg -ksp_rtol 1e-10",
+    "-fsh_dim 3 -fsh_problem manuexp -da_grid_x 5 -da_grid_y 3 -da_grid_z 9 -da_refine 5 -pc_type mg -ksp_rtol 1e-10",
+    "-fsh_dim 3 -fsh_problem manupoly -da_refine 6 -pc_mg_levels 4 -fsh_cx 0.5 -fsh_cz 2 -ksp_rtol 1e-10",
+])
+def test_fused_post_smoother_matches_two_steps(cuda, args):
+    """The temporally blocked post-smoother computes every point with the
+    operations of the two separate Chebyshev steps: same iteration counts,
+    the same solution to FP32 rounding of the fused dot products."""
+    fg = fgmod()
+    u1, a = fg.solve(fg.options(args + " -fsh_precision mixed -fsh_fuse_smooth 1"))
+    u0, b = fg.solve(fg.options(args + " -fsh_precision mixed -fsh_fuse_smooth 0"))
+    assert a.reason == b.reason == 2 and a.its == b.its and a.outer_its == b.outer_its
+    h0 = b.history()[0]
+    assert a.history()[0] == h0  # the FP64 residual before any V-cycle
+    for x, y in zip(a.history(), b.history()):  # later steps carry FP32 rounding of the inner solves
+        assert abs(x - y) <= 1e-2 * abs(y) + 1e-13 * h0
+    d = (u1 - u0).abs().max().item() / u0.abs().max().item()
+    assert d <= 1e-9, d
+    assert abs(a.errinf - b.errinf) <= 1e-6 * b.errinf
+
+
 def test_zero_problem_converges_at_iteration_zero(cuda):
     fg = fgmod()
     u, rep = fg.solve(fg.options("-fsh_dim 2 -fsh_problem zero -da_refine 3 -pc_type mg"))
