@@ -106,6 +106,19 @@ def cpu_baseline(steps=None, budget_s=12.0):
                                       "%d solve(s), %.2f s" % (o.grid.mx, n, tot)}
 
 
+def job_rate(units_per_rank, ms_local, world, device):
+    """Whole-job throughput of N replicas: every rank processed
+    `units_per_rank`; the job took the slowest rank's time (max over ranks).
+    Returns (units per second, max ms)."""
+    import torch
+    t = torch.tensor([float(ms_local)], dtype=torch.float64, device=device)
+    if world > 1:
+        import torch.distributed as dist
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms = t.item()
+    return world * units_per_rank / (ms * 1e-3), ms
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -317,12 +330,7 @@ def run_ours(args):
     launches = sum(r.launches for r in reps)
     rep_mx = reps[-1]
     err_mx = fg.error_norms(info, u, ctx_exact)
-    ms_t = torch.tensor([ms], device=dev)
-    if world > 1:
-        import torch.distributed as dist
-        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
-    ms = ms_t.item()
-    value = world * N * K / (ms * 1e-3)
+    value, ms = job_rate(N * K, ms, world, dev)
 
     # roofline of the dominant kernel (FP32 Chebyshev step on the 513^3 level)
     rk = args.roofline_kernel
@@ -370,11 +378,7 @@ def run_ours(args):
     barrier()
     ms_e = h0.elapsed_time(h1)
     s_e.close()
-    ms_e_t = torch.tensor([ms_e], device=dev)
-    if world > 1:
-        import torch.distributed as dist
-        dist.all_reduce(ms_e_t, op=dist.ReduceOp.MAX)
-    e2e = world * N * K / (ms_e_t.item() * 1e-3)
+    e2e, _ = job_rate(N * K, ms_e, world, dev)
 
     if rank != 0:
         return
