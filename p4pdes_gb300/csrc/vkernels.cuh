@@ -752,41 +752,48 @@ __global__ void __launch_bounds__(256, MB) v_prolong(Geom gf, Geom g, Slots s, K
     lo = V4<T>{C.x, h * (C.x + C.y), C.y, h * (C.y + C.z)};
     hi = V4<T>{C.z, h * (C.z + C.w), C.w, h * (C.w + nx)};
   };
-  // x_f[fk][fj][fi..fi+7] += wgt * (lo, hi); points past mx_f are padding
-  auto addrow = [&](int fk, int fj, const V4<T> &lo, const V4<T> &hi, T wgt) {
-    const long long fm = (long long)fk * gf.plane + (long long)fj * gf.pitch + fi;
-    if (fi < gf.mx) {
-      V4<T> a = ld4(xf + fm);
+  // x_f[fk][fj][fi..fi+7] += wgt * (lo, hi): the current values of a batch of
+  // fine rows are loaded together (no load waits behind another row's store),
+  // then updated and stored; points past mx_f are padding
+  const bool lo_ok = fi < gf.mx, hi_ok = fi + 4 < gf.mx;
+  auto fload = [&](long long fm, bool ok, V4<T> &l, V4<T> &h2) {
+    l = (ok && lo_ok) ? ld4(xf + fm) : zero4<T>();
+    h2 = (ok && hi_ok) ? ld4(xf + fm + 4) : zero4<T>();
+  };
+  auto fstore = [&](long long fm, bool ok, V4<T> l, V4<T> h2, const V4<T> &lo, const V4<T> &hi, T wgt) {
+    if (!ok) return;
 #pragma unroll
-      for (int e = 0; e < 4; e++)
-        if (fi + e < gf.mx) set_el(a, e, fma(wgt, el(lo, e), el(a, e)));
-      st4(xf + fm, a);
+    for (int e = 0; e < 4; e++) {
+      if (fi + e < gf.mx) set_el(l, e, fma(wgt, el(lo, e), el(l, e)));
+      if (fi + 4 + e < gf.mx) set_el(h2, e, fma(wgt, el(hi, e), el(h2, e)));
     }
-    if (fi + 4 < gf.mx) {
-      V4<T> a = ld4(xf + fm + 4);
-#pragma unroll
-      for (int e = 0; e < 4; e++)
-        if (fi + 4 + e < gf.mx) set_el(a, e, fma(wgt, el(hi, e), el(a, e)));
-      st4(xf + fm + 4, a);
-    }
+    if (lo_ok) st4(xf + fm, l);
+    if (hi_ok) st4(xf + fm + 4, h2);
   };
   V4<T> a0l, a0h, a1l, a1h;  // plane k: rows J, J+1
   xrow(p.k0, p.j, ok0, a0l, a0h);
   xrow(p.k0, p.j + (ok1 ? 1 : 0), ok1, a1l, a1h);
   for (int k = p.k0; k < p.k1; k++) {
     const bool up = DIM >= 3 && k + 1 < g.mz;  // fine plane 2k+1 exists (uniform in the block)
+    const int fk = DIM >= 3 ? 2 * k : k, fj = DIM >= 2 ? 2 * p.j : 0;
+    const long long fa = (long long)fk * gf.plane + (long long)fj * gf.pitch + fi;
+    // fine plane fk: rows fj, fj+1
+    V4<T> r0l, r0h, r1l, r1h;
+    fload(fa, ok0, r0l, r0h);
+    fload(fa + gf.pitch, ok1, r1l, r1h);
     V4<T> b0l = zero4<T>(), b0h = zero4<T>(), b1l = zero4<T>(), b1h = zero4<T>();
     if (up) {
       xrow(k + 1, p.j, ok0, b0l, b0h);
       xrow(k + 1, p.j + (ok1 ? 1 : 0), ok1, b1l, b1h);
     }
-    const int fk = DIM >= 3 ? 2 * k : k, fj = DIM >= 2 ? 2 * p.j : 0;
-    if (ok0) addrow(fk, fj, a0l, a0h, T(1));
-    if (ok1) addrow(fk, fj + 1, add4(a0l, a1l), add4(a0h, a1h), h);
-    if (up) {
-      if (ok0) addrow(fk + 1, fj, add4(a0l, b0l), add4(a0h, b0h), h);
-      if (ok1) addrow(fk + 1, fj + 1, add4(add4(a0l, a1l), add4(b0l, b1l)), add4(add4(a0h, a1h), add4(b0h, b1h)),
-                      T(0.25));
+    fstore(fa, ok0, r0l, r0h, a0l, a0h, T(1));
+    fstore(fa + gf.pitch, ok1, r1l, r1h, add4(a0l, a1l), add4(a0h, a1h), h);
+    if (up) {  // fine plane fk+1: rows fj, fj+1
+      fload(fa + gf.plane, ok0, r0l, r0h);
+      fload(fa + gf.plane + gf.pitch, ok1, r1l, r1h);
+      fstore(fa + gf.plane, ok0, r0l, r0h, add4(a0l, b0l), add4(a0h, b0h), h);
+      fstore(fa + gf.plane + gf.pitch, ok1, r1l, r1h, add4(add4(a0l, a1l), add4(b0l, b1l)),
+             add4(add4(a0h, a1h), add4(b0h, b1h)), T(0.25));
     }
     a0l = b0l; a0h = b0h; a1l = b1l; a1h = b1h;
   }
