@@ -64,7 +64,7 @@ struct KspState {
   int reason;
   int done;    // nonzero: every kernel of the iteration returns at once
   int nhist;
-  int pad_;
+  int pend;    // y += alpha p deferred: 0 none, 1 in p buffer 0, 2 in p buffer 1
   double dp, rnorm0, ttol, beta, betaold, dpi, dpiold, alpha;
   double acc[4];
   unsigned int *ndone;  // batches: incremented once when this instance stops
@@ -231,10 +231,11 @@ static __device__ __noinline__ void ksp_finalize(KspState *st, Fin fin, const do
     if (st->beta == 0.0) { st->its = 1; ksp_stop(st, R_CONVERGED_ATOL); }
     break;
   }
-  case FIN_PW: {  // w = A p done: tot = {p.w}
+  case FIN_PW: {  // w = A p done: tot = {p.w}; the previous y update was applied
     double dpi = tot[0];
     st->its = st->i + 1;
     st->betaold = st->beta;
+    st->pend = 0;
     if (isnan(dpi) || isinf(dpi)) { ksp_stop(st, R_DIVERGED_NANORINF); break; }
     if (dpi == 0.0 || (st->i > 0 && ((dpi > 0.0) != (st->dpi > 0.0)))) {
       ksp_stop(st, R_DIVERGED_INDEFINITE_MAT);
@@ -242,6 +243,8 @@ static __device__ __noinline__ void ksp_finalize(KspState *st, Fin fin, const do
     }
     st->dpi = dpi;
     st->alpha = st->beta / dpi;
+    // iteration i wrote its direction to p buffer 1 - (i & 1); y += alpha p is now owed
+    st->pend = 2 - (st->i & 1);
     break;
   }
   case FIN_RR: {  // unpreconditioned norm after x += a p, r -= a w

@@ -424,17 +424,17 @@ static void enq_cg_iter(fishgpu_solver *S, Hier<T> &H, KspVecs<T> v, int par) {
   if constexpr (DIM == 2) {
     if (S->batch) {
       v_cgp_apply<DIM, T, true><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(S->fine, S->sf, st, H.z, pold, pnew, v.w,
-                                                                       S->red, 0);
+                                                                       v.y, S->red, 0);
       planes = true;
     }
   }
   if (!planes)
     v_cgp_apply<DIM, T, false><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(S->fine, S->sf, st, H.z, pold, pnew, v.w,
-                                                                      S->red, 0);
+                                                                      v.y, S->red, 0);
   if (S->ksp_norm == FISHGPU_NORM_UNPRECONDITIONED)
-    v_cg_xr<T, true><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(S->fine, S->sf, st, pnew, v.w, v.y, v.r, S->red, 0);
+    v_cg_r<T, true><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(S->fine, S->sf, st, v.w, v.r, S->red, 0);
   else
-    v_cg_xr<T, false><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(S->fine, S->sf, st, pnew, v.w, v.y, v.r, S->red, 0);
+    v_cg_r<T, false><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(S->fine, S->sf, st, v.w, v.r, S->red, 0);
   if (!enq_pc<DIM, T>(S, H, v.r, FIN_ZZZR))
     v_dots<T><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(S->fine, S->sf, st, H.z, v.r, S->red, 0, FIN_ZZZR, nullptr);
 }
@@ -508,6 +508,9 @@ static int run_ksp(fishgpu_solver *S, Hier<T> &H, KspVecs<T> v, double rtol, int
     FG_CUDA(cudaGraphLaunch(S->gexec, s));
     S->launches += S->n_iter;
   }
+  // the last iteration's deferred y += alpha p
+  v_cg_pend<T><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(S->fine, S->sf, S->st, v.p[0], v.p[1], v.y);
+  S->launches += 1;
   FG_CUDA(cudaMemcpyAsync(S->st_h, S->st, sizeof(KspState), cudaMemcpyDeviceToHost, s));
   FG_CUDA(cudaStreamSynchronize(s));
   return FISHGPU_OK;
@@ -733,6 +736,7 @@ static int time_kernel_dim(fishgpu_solver *S, const char *name, int reps, double
     h.i = 1;
     h.beta = h.betaold = h.dpi = 1.0;
     h.alpha = 1e-3;
+    h.pend = 1;  // cgp_apply also applies a deferred y update
     h.norm_type = FISHGPU_NORM_UNPRECONDITIONED;
     if (cudaMalloc((void **)&tst, sizeof(KspState)) != cudaSuccess) return FISHGPU_ERR_NOMEM;
     if (cudaMemcpyAsync(tst, &h, sizeof(h), cudaMemcpyHostToDevice, s) != cudaSuccess) {
@@ -760,12 +764,12 @@ static int time_kernel_dim(fishgpu_solver *S, const char *name, int reps, double
         v_cheb<DIM, double, true, true><<<gb, sl.chunk, 0, s>>>(g, sl, nullptr, S->r64, ld.X[0], ld.X[1], ld.X[2], 0.5,
                                                                 0.5, 0.1, S->red, 1, FIN_STORE);
       *bytes = 4.0 * sz * N;
-    } else if (!strcmp(name, "cgp_apply")) {  // p = z + beta p_old, w = A p, p.w: reads z, p_old, writes p, w
+    } else if (!strcmp(name, "cgp_apply")) {  // p = z + beta p_old, w = A p, p.w, y += alpha p_old: reads z, p_old, y, writes p, w, y
       if (mixed)
-        v_cgp_apply<DIM, float><<<gb, sl.chunk, 0, s>>>(g, sl, tst, lf.X[0], S->p32, S->q32, S->w32, S->red, 1);
+        v_cgp_apply<DIM, float><<<gb, sl.chunk, 0, s>>>(g, sl, tst, lf.X[0], S->p32, S->q32, S->w32, S->y32, S->red, 1);
       else
-        v_cgp_apply<DIM, double><<<gb, sl.chunk, 0, s>>>(g, sl, tst, ld.X[0], S->p64, S->q64, S->w64, S->red, 1);
-      *bytes = 4.0 * sz * N;
+        v_cgp_apply<DIM, double><<<gb, sl.chunk, 0, s>>>(g, sl, tst, ld.X[0], S->p64, S->q64, S->w64, S->y64, S->red, 1);
+      *bytes = 6.0 * sz * N;
     } else if (!strcmp(name, "post2")) {  // both post-smoothing steps fused: reads b, x0, writes x2
       if constexpr (DIM == 3) {
         if (!mixed) return FISHGPU_ERR_UNSUPPORTED;
@@ -796,10 +800,10 @@ static int time_kernel_dim(fishgpu_solver *S, const char *name, int reps, double
       *bytes = 2.0 * sz * N;
     } else if (!strcmp(name, "cg_update")) {
       if (mixed)
-        v_cg_xr<float, false><<<gb, sl.chunk, 0, s>>>(g, sl, tst, S->p32, S->w32, S->y32, S->r32, S->red, 1);
+        v_cg_r<float, false><<<gb, sl.chunk, 0, s>>>(g, sl, tst, S->w32, S->r32, S->red, 1);
       else
-        v_cg_xr<double, false><<<gb, sl.chunk, 0, s>>>(g, sl, tst, S->p64, S->w64, S->y64, S->r64, S->red, 1);
-      *bytes = 6.0 * sz * N;
+        v_cg_r<double, false><<<gb, sl.chunk, 0, s>>>(g, sl, tst, S->w64, S->r64, S->red, 1);
+      *bytes = 3.0 * sz * N;
     } else if (!strcmp(name, "restrict")) {
       if (mixed)
         v_restrict<DIM, float><<<slot_blocks(cf.sl), cf.sl.chunk, 0, s>>>(g, cf.g, cf.sl, nullptr, lf.X[0], cf.b);
@@ -1502,6 +1506,8 @@ static int group_solve(fishgpu_solver *S, const double *const *f, double *const 
       FG_CUDA(cudaGraphLaunch(S->gexec, s));
       S->launches += S->n_iter;
     }
+    v_cg_pend<float><<<gb, S->sf.chunk, 0, s>>>(g, S->sf, S->st, v.p[0], v.p[1], v.y);
+    S->launches += 1;
     FG_CUDA(cudaMemcpyAsync(S->st_h, S->st, sizeof(KspState) * count, cudaMemcpyDeviceToHost, s));
     v_promote_add<<<gb, S->sf.chunk, 0, s>>>(g, S->sf, S->y32, S->scl, 0.0, S->y64);
     v_resid<2, double><<<gb, S->sf.chunk, 0, s>>>(g, S->sf, nullptr, S->b64, S->y64, S->r64);

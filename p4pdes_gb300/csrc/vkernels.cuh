@@ -439,16 +439,23 @@ __global__ void __launch_bounds__(256, MinBlocks<T>::value) v_apply_dot(Geom g, 
 
 // p_new = z + (beta/betaold) p_old (p_new = z on the first CG iteration),
 // w = A p_new, p_new.w reduced: the CG direction update fused into the apply.
-// p_old and p_new are different buffers (neighbours read p_old).
+// p_old and p_new are different buffers (neighbours read p_old).  The
+// solution update of the previous iteration, y += alpha p_old, is deferred
+// to here (the state's `pend`): this kernel reads p_old anyway, so the
+// update costs y's read and write only, and v_cg_r no longer reads p and y.
+// alpha is still the previous iteration's: FIN_PW replaces it only after
+// every block has finished.
 template <int DIM, typename T, bool PL = false>
 __global__ void __launch_bounds__(256, MinBlocks<T>::value) v_cgp_apply(Geom g, Slots s, KspState *st, const T *__restrict__ z,
                                                    const T *__restrict__ pold, T *__restrict__ pnew,
-                                                   T *__restrict__ wv, Reducer red, int slot) {
+                                                   T *__restrict__ wv, T *__restrict__ y, Reducer red, int slot) {
   st = block_state_sel<PL>(st, s);
   if (ksp_done_v(st)) return;
   const SlotPos p = slot_pos(g, s);
   const Wv<T> w(g);
   const bool first = !st || st->i == 0;  // no state: p = z
+  const bool pend = st && st->pend && y;
+  const T a = pend ? (T)st->alpha : T(0);
   const AxpySrc<T> src{z, pold, first ? T(0) : (T)(st->beta / st->betaold), first};
   T acc = T(0);
   auto op = [&](int k, long long n, const Nb<T> &nb) {
@@ -466,6 +473,10 @@ __global__ void __launch_bounds__(256, MinBlocks<T>::value) v_cgp_apply(Geom g, 
     }
     st4(pnew + n, nb.c);
     st4(wv + n, o);
+    if (pend) {
+      const V4<T> pp = ld4(pold + n), yy = ld4(y + n);
+      st4(y + n, V4<T>{fma(a, pp.x, yy.x), fma(a, pp.y, yy.y), fma(a, pp.z, yy.z), fma(a, pp.w, yy.w)});
+    }
   };
   march_src<DIM, T>(g, s, p, src, op);
   double v1[1] = {(double)acc};
@@ -809,18 +820,18 @@ __global__ void __launch_bounds__(256, MB) v_prolong(Geom gf, Geom g, Slots s, K
       const long long n = (long long)k * g.plane + p.col;
 #define FG_PW_END }
 
-// y += alpha p; r -= alpha w; RR: r.r reduced (unpreconditioned norm test)
+// r -= alpha w; RR: r.r reduced (unpreconditioned norm test).  The matching
+// y += alpha p is deferred to the next v_cgp_apply, or to v_cg_pend when the
+// solve stops.
 template <typename T, bool RR>
-__global__ void __launch_bounds__(256) v_cg_xr(Geom g, Slots s, KspState *st, const T *__restrict__ pv,
-                                               const T *__restrict__ wv, T *__restrict__ y, T *__restrict__ r,
-                                               Reducer red, int slot) {
+__global__ void __launch_bounds__(256) v_cg_r(Geom g, Slots s, KspState *st, const T *__restrict__ wv,
+                                              T *__restrict__ r, Reducer red, int slot) {
   st = block_state(st, s);
   if (ksp_done_v(st)) return;
   const T a = st ? (T)st->alpha : T(0);  // no state: alpha = 0
   T acc = T(0);
   FG_PW_BEGIN
-  const V4<T> pp = ld4(pv + n), ww = ld4(wv + n), yy = ld4(y + n), rr = ld4(r + n);
-  st4(y + n, V4<T>{fma(a, pp.x, yy.x), fma(a, pp.y, yy.y), fma(a, pp.z, yy.z), fma(a, pp.w, yy.w)});
+  const V4<T> ww = ld4(wv + n), rr = ld4(r + n);
   const V4<T> rn{fma(-a, ww.x, rr.x), fma(-a, ww.y, rr.y), fma(-a, ww.z, rr.z), fma(-a, ww.w, rr.w)};
   st4(r + n, rn);
   if (RR) acc = fma(rn.x, rn.x, fma(rn.y, rn.y, fma(rn.z, rn.z, fma(rn.w, rn.w, acc))));
@@ -829,6 +840,21 @@ __global__ void __launch_bounds__(256) v_cg_xr(Geom g, Slots s, KspState *st, co
     double v1[1] = {(double)acc};
     reduce_slots<1>(v1, red, slot, st, FIN_RR, nullptr, s);
   }
+}
+
+// The deferred y += alpha p of the last CG iteration, after the loop has
+// stopped (the state is done): `pend` names the buffer, 1 for p0, 2 for p1.
+template <typename T>
+__global__ void __launch_bounds__(256) v_cg_pend(Geom g, Slots s, const KspState *st, const T *__restrict__ p0,
+                                                 const T *__restrict__ p1, T *__restrict__ y) {
+  st = block_state(const_cast<KspState *>(st), s);
+  if (!st || !st->pend) return;
+  const T a = (T)st->alpha;
+  const T *__restrict__ pv = st->pend == 1 ? p0 : p1;
+  FG_PW_BEGIN
+  const V4<T> pp = ld4(pv + n), yy = ld4(y + n);
+  st4(y + n, V4<T>{fma(a, pp.x, yy.x), fma(a, pp.y, yy.y), fma(a, pp.z, yy.z), fma(a, pp.w, yy.w)});
+  FG_PW_END
 }
 
 // z.z and z.r reduced together (out: per plane for a batch)
