@@ -569,13 +569,17 @@ __global__ void __launch_bounds__(256) k_initial64(Geom g, Geom gd, Tiles tm, Pr
   FG_POINT_LOOP_END
 }
 
-// the caller's dense u from the padded one
+// u = u0 + y into the caller's dense u (y NULL: y = +0, an update never made);
+// keep: u0 is overwritten with u as well
 template <int DIM>
-__global__ void __launch_bounds__(256) k_unpack64(Geom g, Geom gd, Tiles tm, const double *__restrict__ up,
-                                                  double *__restrict__ ud) {
+__global__ void __launch_bounds__(256) k_unpack_add64(Geom g, Geom gd, Tiles tm, double *__restrict__ up,
+                                                      const double *__restrict__ y, double *__restrict__ ud,
+                                                      bool keep) {
   const Range R = full_range(g);
   FG_POINT_LOOP_BEGIN(R)
-  ud[gidx(gd, i, j, k)] = up[n];
+  const double v = up[n] + (y ? y[n] : 0.0);
+  ud[gidx(gd, i, j, k)] = v;
+  if (keep) up[n] = v;
   FG_POINT_LOOP_END
 }
 
@@ -593,11 +597,6 @@ static void fill_from_state(const KspState *h, fishgpu_report *rep) {
   for (int q = 0; q < n; q++) rep->hist[q] = h->hist[q];
 }
 
-// sum of squares of the padded FP64 vector a into dval[slot]
-static void enq_norm2(fishgpu_solver *S, const double *a, int slot) {
-  v_dots<double><<<slot_blocks(S->sf), S->sf.chunk, 0, S->stream>>>(S->fine, S->sf, nullptr, a, a, S->red, 1, FIN_STORE, S->dval + slot);
-}
-
 template <int DIM>
 static int solve_dim(fishgpu_solver *S, double *u, fishgpu_report *rep) {
   const fishgpu_opts &o = S->o;
@@ -607,7 +606,7 @@ static int solve_dim(fishgpu_solver *S, double *u, fishgpu_report *rep) {
   const long long tot4 = S->sf.tot4;
   const unsigned gfl = S->gfl;
   FG_CUDA(cudaEventRecord(S->ev0, s));
-  S->launches = 3;  // initial state, -F(u0), ||F(u0)||
+  S->launches = 2;  // initial state, -F(u0) with its norm
   k_initial64<DIM><<<L.grid, L.block, 0, s>>>(g, S->dense, L.tm, S->prob, o.initial_type, o.initial_gonboundary,
                                                o.seed, u, S->u64);
   if (!S->beff_ready) {
@@ -615,10 +614,14 @@ static int solve_dim(fishgpu_solver *S, double *u, fishgpu_report *rep) {
     S->launches += 1;
     S->beff_ready = S->o.ctx.problem != FISHGPU_USER;  // user data may change between solves
   }
-  // the KSP right-hand side is -F(u0) = beff - A u0; it solves for -y and u = u0 + (-y)
+  // the KSP right-hand side is -F(u0) = beff - A u0 and its norm; it solves
+  // for -y and u = u0 + (-y)
   double *F = o.precision == FISHGPU_MIXED ? S->b64 : S->r64;
-  v_resid<DIM, double><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(g, S->sf, nullptr, S->beff, S->u64, F);
-  enq_norm2(S, F, 0);
+  if (o.initial_type == FISHGPU_INITIAL_ZEROS)
+    v_resid_zero0<DIM><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(g, S->sf, S->beff, S->u64, F, S->red, 1, S->dval);
+  else
+    v_resid<DIM, double, true><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(g, S->sf, nullptr, S->beff, S->u64, F,
+                                                                         S->red, 1, S->dval);
   FG_CUDA(cudaGetLastError());
   int rc = read_vals(S, 1);
   if (rc) return rc;
@@ -634,8 +637,6 @@ static int solve_dim(fishgpu_solver *S, double *u, fishgpu_report *rep) {
     const double ttol = fmax(o.rtol * bn, o.atol);
     double rn = bn;
     int reason = 0, its = 0, outer = 0, nh = 0;
-    v_zero<double><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(g, S->sf, S->y64);
-    S->launches += 1;
     rep->hist[nh++] = rn;
     KspVecs<float> v{S->r32, {S->p32, S->q32}, S->w32, S->y32};
     // The first correction is smooth and carries the FP32 rounding of its
@@ -652,7 +653,7 @@ static int solve_dim(fishgpu_solver *S, double *u, fishgpu_report *rep) {
       if (outer >= o.outer_max_it || its >= o.max_it) { reason = R_DIVERGED_ITS; break; }
       const double *rsrc = outer == 0 ? S->b64 : S->r64;
       v_demote<<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(g, S->sf, rsrc, nullptr, 1.0 / rn, S->r32);
-      S->launches += 4;  // demote, promote-add, FP64 residual, its norm
+      S->launches += 3;  // demote, promote-add, FP64 residual with its norm
       // inner tolerance: what is still needed, never below the FP32 floor
       double irtol = fmax(o.inner_rtol, 0.5 * ttol / rn);
       if (outer == 0) irtol = fmax(irtol, first_floor);
@@ -666,10 +667,11 @@ static int solve_dim(fishgpu_solver *S, double *u, fishgpu_report *rep) {
         reason = h->reason;
         break;
       }
-      v_promote_add<<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(g, S->sf, S->y32, nullptr, rn, S->y64);
+      // y64 = 0 before the first step: that step writes it without reading
+      v_promote_add<<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(g, S->sf, S->y32, nullptr, rn, S->y64, outer == 0);
       // FP64 true residual r = b - J y and its norm
-      v_resid<DIM, double><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(g, S->sf, nullptr, S->b64, S->y64, S->r64);
-      enq_norm2(S, S->r64, 0);
+      v_resid<DIM, double, true><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(g, S->sf, nullptr, S->b64, S->y64,
+                                                                           S->r64, S->red, 1, S->dval);
       FG_CUDA(cudaGetLastError());
       if ((rc = read_vals(S, 1))) return rc;
       rn = sqrt(S->hval[0]);
@@ -682,19 +684,21 @@ static int solve_dim(fishgpu_solver *S, double *u, fishgpu_report *rep) {
     rep->outer_its = outer;
     rep->nhist = nh;
   }
-  // u = u0 + (-y), then the caller's dense copy
-  v_add<<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(g, S->sf, S->y64, S->u64);
-  k_unpack64<DIM><<<L.grid, L.block, 0, s>>>(g, S->dense, L.tm, S->u64, u);
-  S->launches += 2;  // update, unpack
+  // u = u0 + (-y) into the caller's dense u (the FP64 form keeps it for F(u);
+  // a mixed solve that stopped before its first step has y = 0)
+  const bool fp64 = o.precision != FISHGPU_MIXED;
+  const double *yv = fp64 || rep->outer_its > 0 ? S->y64 : nullptr;
+  k_unpack_add64<DIM><<<L.grid, L.block, 0, s>>>(g, S->dense, L.tm, S->u64, yv, u, fp64);
+  S->launches += 1;
   if (o.precision == FISHGPU_MIXED) {
     // the last refinement step computed the FP64 residual beff - A(u0 + y) = -F(u)
     FG_CUDA(cudaEventRecord(S->ev1, s));
     rep->fnorm1 = rep->nhist > 0 ? rep->hist[(rep->nhist < FISHGPU_MAX_HIST ? rep->nhist : FISHGPU_MAX_HIST) - 1] : bn;
   } else {
     // F(u) for the final SNES norm (r64 is free now)
-    v_resid<DIM, double><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(g, S->sf, nullptr, S->beff, S->u64, S->r64);
-    enq_norm2(S, S->r64, 1);
-    S->launches += 2;
+    v_resid<DIM, double, true><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(g, S->sf, nullptr, S->beff, S->u64,
+                                                                         S->r64, S->red, 1, S->dval + 1);
+    S->launches += 1;
     FG_CUDA(cudaEventRecord(S->ev1, s));
     FG_CUDA(cudaGetLastError());
     if ((rc = read_vals(S, 2))) return rc;

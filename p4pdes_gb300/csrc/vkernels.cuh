@@ -385,14 +385,17 @@ __global__ void __launch_bounds__(256, MinBlocks<T>::value) v_cheb2_zero(Geom g,
   march<DIM, T>(g, s, p, b, op);
 }
 
-// r = b - A x
-template <int DIM, typename T>
+// r = b - A x; NORM: r.r reduced into *out as v_dots(r, r) reduces it (same
+// per-thread order over the slot's planes, same block order)
+template <int DIM, typename T, bool NORM = false>
 __global__ void __launch_bounds__(256, MinBlocks<T>::value) v_resid(Geom g, Slots s, KspState *st, const T *__restrict__ b,
-                                               const T *__restrict__ x, T *__restrict__ r) {
+                                               const T *__restrict__ x, T *__restrict__ r, Reducer red = Reducer{},
+                                               int slot = 0, double *out = nullptr) {
   st = block_state(st, s);
   if (ksp_done_v(st)) return;
   const SlotPos p = slot_pos(g, s);
   const Wv<T> w(g);
+  T rr = T(0);
   auto op = [&](int k, long long n, const Nb<T> &nb) {
     const V4<T> bv = ld4(b + n);
     const bool jkb = jk_bdry(g, DIM, p.j, k);
@@ -403,9 +406,15 @@ __global__ void __launch_bounds__(256, MinBlocks<T>::value) v_resid(Geom g, Slot
       set_el(o, e, i < g.mx ? resid_el<DIM, T>(g, w, nb, e, i, jkb, el(bv, e)) : T(0));
     }
     st4(r + n, o);
+    if (NORM) rr = fma(o.x, o.x, fma(o.y, o.y, fma(o.z, o.z, fma(o.w, o.w, rr))));
   };
   march<DIM, T>(g, s, p, x, op);
+  if (NORM) {
+    double v1[1] = {(double)rr};
+    reduce_sel<1, false>(v1, red, slot, nullptr, FIN_STORE, out, s);
+  }
 }
+
 
 // w = A p; p.w reduced (per-thread partials in T, blocks in FP64)
 template <int DIM, typename T>
@@ -892,6 +901,36 @@ __global__ void __launch_bounds__(256) v_zero(Geom g, Slots s, T *__restrict__ a
   FG_PW_END
 }
 
+// The FP64 residual b - A u0 of an initial iterate that is zero on every
+// interior node (the zero initial state, with or without g on the boundary),
+// and its r.r as v_dots reduces it.  The Jacobian's interior rows do not see
+// boundary columns, so there r = b - A 0 = b + 0 (the value resid_el returns:
+// its fused terms all add +0); boundary rows keep fma(-scdiag, u0, b).  A
+// pointwise pass instead of the FP64 stencil, with identical results.
+template <int DIM>
+__global__ void __launch_bounds__(256) v_resid_zero0(Geom g, Slots s, const double *__restrict__ b,
+                                                     const double *__restrict__ u0, double *__restrict__ r,
+                                                     Reducer red, int slot, double *out) {
+  const double sd = g.scdiag;
+  double rr = 0.0;
+  FG_PW_BEGIN
+  const bool jkb = jk_bdry(g, DIM, p.j, k);
+  const V4<double> bv = ld4(b + n), uv = ld4(u0 + n);
+  V4<double> o;
+#pragma unroll
+  for (int e = 0; e < 4; e++) {
+    const int i = p.i4 + e;
+    double v = 0.0;
+    if (i < g.mx) v = (jkb || i == 0 || i == g.mx - 1) ? fma(-sd, el(uv, e), el(bv, e)) : el(bv, e) + 0.0;
+    set_el(o, e, v);
+  }
+  st4(r + n, o);
+  rr = fma(o.x, o.x, fma(o.y, o.y, fma(o.z, o.z, fma(o.w, o.w, rr))));
+  FG_PW_END
+  double v1[1] = {rr};
+  reduce_slots<1>(v1, red, slot, nullptr, FIN_STORE, out, s);
+}
+
 // r32 = (float)(r64 * inv_s); inv_s per plane for a batch (scale[plane])
 static __global__ void __launch_bounds__(256) v_demote(Geom g, Slots s, const double *__restrict__ r, const double *scale,
                                                 double inv_s, float *__restrict__ r32) {
@@ -902,13 +941,14 @@ static __global__ void __launch_bounds__(256) v_demote(Geom g, Slots s, const do
   FG_PW_END
 }
 
-// y64 += s * (double)e32; s per plane for a batch (scale[plane])
+// y64 += s * (double)e32; s per plane for a batch (scale[plane]); fresh: y64
+// is taken as +0 (not read), as after v_zero
 static __global__ void __launch_bounds__(256) v_promote_add(Geom g, Slots s, const float *__restrict__ e, const double *scale,
-                                                     double sc, double *__restrict__ y) {
+                                                     double sc, double *__restrict__ y, bool fresh = false) {
   FG_PW_BEGIN
   const double f = scale ? scale[k] : sc;
   const V4<float> a = ld4(e + n);
-  const V4<double> b = ld4(y + n);
+  const V4<double> b = fresh ? zero4<double>() : ld4(y + n);
   st4(y + n, V4<double>{fma(f, (double)a.x, b.x), fma(f, (double)a.y, b.y), fma(f, (double)a.z, b.z),
                         fma(f, (double)a.w, b.w)});
   FG_PW_END
