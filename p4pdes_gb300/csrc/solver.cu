@@ -123,6 +123,7 @@ struct fishgpu_solver_s {
   float *r32 = nullptr, *p32 = nullptr, *q32 = nullptr, *w32 = nullptr, *y32 = nullptr;
   cudaGraphExec_t gexec = nullptr;       // giters CG iterations
   cudaGraphExec_t gexec_init = nullptr;  // the KSP set-up sequence
+  cudaGraphExec_t gexec_init64[2] = {nullptr, nullptr};  // the same from b64 / r64 (mixed form)
   long long n_init = 0, n_iter = 0;      // kernel nodes of the two graphs
   long long launches = 0;                // kernels launched by the current solve
   int giters = 1;
@@ -400,10 +401,22 @@ struct KspVecs {
   T *r, *p[2], *w, *y;  // p: two buffers, the direction update reads one and writes the other
 };
 
+// src64 (FP32 solves of the mixed form, unpreconditioned norm): the FP64
+// residual the right-hand side is demoted from, its r.r in dval[0]
 template <int DIM, typename T>
-static void enq_cg_init(fishgpu_solver *S, Hier<T> &H, KspVecs<T> v) {
+static void enq_cg_init(fishgpu_solver *S, Hier<T> &H, KspVecs<T> v, const double *src64 = nullptr) {
   cudaStream_t s = S->stream;
   const long long tot4 = S->sf.tot4;
+  if constexpr (sizeof(T) == 4) {
+    if (src64) {
+      v_demote_init<<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(S->fine, S->sf, S->st, src64, S->dval, v.r, v.y,
+                                                               S->red, 0);
+      if (!enq_pc<DIM, T>(S, H, v.r, FIN_INIT_ZZZR))
+        v_dots<T><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(S->fine, S->sf, S->st, H.z, v.r, S->red, 0, FIN_INIT_ZZZR,
+                                                             nullptr);
+      return;
+    }
+  }
   v_zero<T><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(S->fine, S->sf, v.y);
   if (S->ksp_norm == FISHGPU_NORM_UNPRECONDITIONED)
     v_dots<T><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(S->fine, S->sf, S->st, v.r, v.r, S->red, 0, FIN_INIT_RR, nullptr);
@@ -482,22 +495,24 @@ static void reset_state(fishgpu_solver *S, double rtol, double atol, double dtol
 }
 
 // CG solve of J y = r from y = 0 (r is overwritten), on the solver's stream.
+// from64 >= 0 (FP32 solves of the mixed form): r is set up from the FP64
+// residual in b64 (0) or r64 (1), scaled by 1/||.|| from dval[0].
 // The caller reads S->st_h for its, reason and the history.
 template <int DIM, typename T>
-static int run_ksp(fishgpu_solver *S, Hier<T> &H, KspVecs<T> v, double rtol, int max_it) {
+static int run_ksp(fishgpu_solver *S, Hier<T> &H, KspVecs<T> v, double rtol, int max_it, int from64 = -1) {
   cudaStream_t s = S->stream;
   const int norm = S->ksp_norm;  // the captured graphs compute this norm
   int rc;
-  if (!S->gexec_init &&
-      (rc = capture(S, [&] { enq_cg_init<DIM, T>(S, H, v); }, &S->gexec_init, &S->n_init)))
-    return rc;
+  cudaGraphExec_t *gi = from64 < 0 ? &S->gexec_init : &S->gexec_init64[from64 & 1];
+  const double *src64 = from64 < 0 ? nullptr : from64 ? S->r64 : S->b64;
+  if (!*gi && (rc = capture(S, [&] { enq_cg_init<DIM, T>(S, H, v, src64); }, gi, &S->n_init))) return rc;
   if (!S->gexec &&
       (rc = capture(S, [&] { for (int g = 0; g < S->giters; g++) enq_cg_iter<DIM, T>(S, H, v, g & 1); },
                     &S->gexec, &S->n_iter)))
     return rc;
   reset_state(S, rtol, S->o.atol, S->o.dtol, max_it, norm);
   FG_CUDA(cudaMemcpyAsync(S->st, S->st_h, sizeof(KspState), cudaMemcpyHostToDevice, s));
-  FG_CUDA(cudaGraphLaunch(S->gexec_init, s));
+  FG_CUDA(cudaGraphLaunch(*gi, s));
   S->launches += S->n_init;
   const long long guard = (long long)max_it / S->giters + 4;
   for (long long launch = 0;; launch++) {
@@ -651,14 +666,13 @@ static int solve_dim(fishgpu_solver *S, double *u, fishgpu_report *rep) {
       if (isnan(rn) || isinf(rn)) { reason = R_DIVERGED_NANORINF; break; }
       if (rn <= ttol) { reason = rn < o.atol ? R_CONVERGED_ATOL : R_CONVERGED_RTOL; break; }
       if (outer >= o.outer_max_it || its >= o.max_it) { reason = R_DIVERGED_ITS; break; }
-      const double *rsrc = outer == 0 ? S->b64 : S->r64;
-      v_demote<<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(g, S->sf, rsrc, nullptr, 1.0 / rn, S->r32);
-      S->launches += 3;  // demote, promote-add, FP64 residual with its norm
+      S->launches += 2;  // promote-add, FP64 residual with its norm
       // inner tolerance: what is still needed, never below the FP32 floor
       double irtol = fmax(o.inner_rtol, 0.5 * ttol / rn);
       if (outer == 0) irtol = fmax(irtol, first_floor);
       if (irtol > 0.5) irtol = 0.5;
-      if ((rc = run_ksp<DIM, float>(S, S->h32, v, irtol, o.inner_max_it))) return rc;
+      // r32 = r / ||r|| (r: b64 in the first step, r64 after) inside the KSP set-up
+      if ((rc = run_ksp<DIM, float>(S, S->h32, v, irtol, o.inner_max_it, outer == 0 ? 0 : 1))) return rc;
       const KspState *h = S->st_h;
       its += h->its;
       if (outer < FISHGPU_MAX_OUTER) rep->inner_its[outer] = h->its;
@@ -864,6 +878,8 @@ extern "C" int fishgpu_solver_destroy(fishgpu_solver *S) {
   if (S->stream) cudaStreamSynchronize(S->stream);
   if (S->gexec) cudaGraphExecDestroy(S->gexec);
   if (S->gexec_init) cudaGraphExecDestroy(S->gexec_init);
+  for (cudaGraphExec_t &e : S->gexec_init64)
+    if (e) cudaGraphExecDestroy(e);
   for (void *p : S->allocs) cudaFree(p);
   if (S->st_h) cudaFreeHost(S->st_h);
   if (S->hval) cudaFreeHost(S->hval);

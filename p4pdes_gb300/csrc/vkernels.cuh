@@ -931,6 +931,28 @@ __global__ void __launch_bounds__(256) v_resid_zero0(Geom g, Slots s, const doub
   reduce_slots<1>(v1, red, slot, nullptr, FIN_STORE, out, s);
 }
 
+// The set-up of an inner FP32 solve from an FP64 residual in one pass:
+// r32 = (float)(r64 * (1 / sqrt(rr))) with rr = r64.r64 as stored by the
+// residual kernel (the host's 1.0 / ||r|| to the bit: sqrt and the division
+// are correctly rounded), y32 = 0, and r32.r32 reduced as v_dots<float>
+// reduces it, finalised as FIN_INIT_RR.  Replaces v_demote, v_zero and v_dots.
+static __global__ void __launch_bounds__(256) v_demote_init(Geom g, Slots s, KspState *st, const double *__restrict__ r,
+                                                     const double *__restrict__ rr, float *__restrict__ r32,
+                                                     float *__restrict__ y32, Reducer red, int slot) {
+  if (ksp_done_v(st)) return;
+  const double is = 1.0 / sqrt(*rr);
+  float zz = 0.f;
+  FG_PW_BEGIN
+  const V4<double> a = ld4(r + n);
+  const V4<float> o{(float)(a.x * is), (float)(a.y * is), (float)(a.z * is), (float)(a.w * is)};
+  st4(r32 + n, o);
+  st4(y32 + n, zero4<float>());
+  zz = fmaf(o.x, o.x, fmaf(o.y, o.y, fmaf(o.z, o.z, fmaf(o.w, o.w, zz))));
+  FG_PW_END
+  double v1[1] = {(double)zz};
+  reduce_slots<1>(v1, red, slot, st, FIN_INIT_RR, nullptr, s);
+}
+
 // r32 = (float)(r64 * inv_s); inv_s per plane for a batch (scale[plane])
 static __global__ void __launch_bounds__(256) v_demote(Geom g, Slots s, const double *__restrict__ r, const double *scale,
                                                 double inv_s, float *__restrict__ r32) {
