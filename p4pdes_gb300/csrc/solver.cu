@@ -496,7 +496,8 @@ static void reset_state(fishgpu_solver *S, double rtol, double atol, double dtol
 
 // CG solve of J y = r from y = 0 (r is overwritten), on the solver's stream.
 // from64 >= 0 (FP32 solves of the mixed form): r is set up from the FP64
-// residual in b64 (0) or r64 (1), scaled by 1/||.|| from dval[0].
+// residual in b64 (0) or r64 (1), scaled by 1/||.|| from dval[0], and the
+// last deferred y += alpha p is left to the caller (v_pend_promote).
 // The caller reads S->st_h for its, reason and the history.
 template <int DIM, typename T>
 static int run_ksp(fishgpu_solver *S, Hier<T> &H, KspVecs<T> v, double rtol, int max_it, int from64 = -1) {
@@ -523,9 +524,10 @@ static int run_ksp(fishgpu_solver *S, Hier<T> &H, KspVecs<T> v, double rtol, int
     FG_CUDA(cudaGraphLaunch(S->gexec, s));
     S->launches += S->n_iter;
   }
-  // the last iteration's deferred y += alpha p
-  v_cg_pend<T><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(S->fine, S->sf, S->st, v.p[0], v.p[1], v.y);
-  S->launches += 1;
+  if (from64 < 0) {  // the last iteration's deferred y += alpha p
+    v_cg_pend<T><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(S->fine, S->sf, S->st, v.p[0], v.p[1], v.y);
+    S->launches += 1;
+  }
   FG_CUDA(cudaMemcpyAsync(S->st_h, S->st, sizeof(KspState), cudaMemcpyDeviceToHost, s));
   FG_CUDA(cudaStreamSynchronize(s));
   return FISHGPU_OK;
@@ -681,8 +683,10 @@ static int solve_dim(fishgpu_solver *S, double *u, fishgpu_report *rep) {
         reason = h->reason;
         break;
       }
-      // y64 = 0 before the first step: that step writes it without reading
-      v_promote_add<<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(g, S->sf, S->y32, nullptr, rn, S->y64, outer == 0);
+      // y32 += alpha p (deferred), y64 += rn y32; y64 = 0 before the first
+      // step: that step writes it without reading
+      v_pend_promote<<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(g, S->sf, S->st, S->p32, S->q32, S->y32, rn, S->y64,
+                                                                outer == 0);
       // FP64 true residual r = b - J y and its norm
       v_resid<DIM, double, true><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(g, S->sf, nullptr, S->b64, S->y64,
                                                                            S->r64, S->red, 1, S->dval);

@@ -976,6 +976,28 @@ static __global__ void __launch_bounds__(256) v_promote_add(Geom g, Slots s, con
   FG_PW_END
 }
 
+// The end of an inner FP32 solve and the FP64 update in one pass: the last
+// CG iteration's deferred y32 += alpha p (v_cg_pend), then y64 += sc *
+// (double)y32 (v_promote_add, fresh as there); y32 itself is not written back.
+static __global__ void __launch_bounds__(256) v_pend_promote(Geom g, Slots s, const KspState *st,
+                                                      const float *__restrict__ p0, const float *__restrict__ p1,
+                                                      const float *__restrict__ e, double sc, double *__restrict__ y,
+                                                      bool fresh) {
+  const int pend = st ? st->pend : 0;
+  const float a = pend ? (float)st->alpha : 0.f;
+  const float *__restrict__ pv = pend == 1 ? p0 : p1;
+  FG_PW_BEGIN
+  V4<float> ev = ld4(e + n);
+  if (pend) {
+    const V4<float> pp = ld4(pv + n);
+    ev = V4<float>{fmaf(a, pp.x, ev.x), fmaf(a, pp.y, ev.y), fmaf(a, pp.z, ev.z), fmaf(a, pp.w, ev.w)};
+  }
+  const V4<double> b = fresh ? zero4<double>() : ld4(y + n);
+  st4(y + n, V4<double>{fma(sc, (double)ev.x, b.x), fma(sc, (double)ev.y, b.y), fma(sc, (double)ev.z, b.z),
+                        fma(sc, (double)ev.w, b.w)});
+  FG_PW_END
+}
+
 // a += b
 static __global__ void __launch_bounds__(256) v_add(Geom g, Slots s, const double *__restrict__ b, double *__restrict__ a) {
   FG_PW_BEGIN
