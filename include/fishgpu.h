@@ -223,11 +223,17 @@ int fishgpu_solve_host(const fishgpu_opts *o, const double *f_host, const double
 
 /* Times `reps` launches of one solver kernel on the finest level with the
    solver's resident data (CUDA events on the solver's stream).  Names:
-   "apply", "cg_update", "smooth", "resid_restrict", "prolong_smooth",
-   "residual64".  Reports the mean ms per launch and the algorithmic bytes
-   one launch moves. */
+   "smooth", "smooth_dots", "smooth_zero", "post2", "cgp_apply", "cg_update",
+   "resid", "apply", "restrict", "prolong", "residual64".  Reports the mean ms
+   per launch and the algorithmic bytes one launch moves. */
 int fishgpu_solver_time_kernel(fishgpu_solver *s, const char *name, int reps,
                                double *ms_per_launch, double *bytes_per_launch);
+
+/* Measures the current device's FP64 FMA throughput in TFLOP/s (an FMA is 2
+   flops): `reps` timed launches of a kernel of independent FMA chains on
+   every SM, after one warm-up launch; the best launch counts.  The
+   denominator for the FP64-bound kernels (the FP64 residual). */
+int fishgpu_fp64_fma_rate(int reps, double *tflops);
 
 /* ---- batches: many independent 2D problems of uneven sizes -------------
    -Laplace(u) = f on the unit square, u = 0 on the boundary, fish's 5-point

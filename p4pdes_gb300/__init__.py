@@ -212,6 +212,8 @@ def load():
                  "fishgpu_batch_results", "fishgpu_batch_destroy"):
         getattr(lib, name).restype = c_int
     lib.fishgpu_solver_time_kernel.argtypes = [c_void_p, ctypes.c_char_p, c_int, _P(c_double), _P(c_double)]
+    lib.fishgpu_fp64_fma_rate.argtypes = [c_int, _P(c_double)]
+    lib.fishgpu_fp64_fma_rate.restype = c_int
     lib.fishgpu_ms_opts_default.argtypes = [_P(MsOpts)]
     lib.fishgpu_bratu_opts_default.argtypes = [_P(MsOpts)]
     lib.fishgpu_bratu_opts_default.restype = c_int
@@ -478,6 +480,13 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+def fp64_fma_rate(reps=5):
+    """FP64 FMA throughput of the current device in TFLOP/s (FMA = 2 flops)."""
+    t = c_double()
+    _check(load().fishgpu_fp64_fma_rate(reps, ctypes.byref(t)), "fp64_fma_rate")
+    return t.value
 
 
 def estimate_bytes(opts):

@@ -1250,6 +1250,57 @@ extern "C" int fishgpu_solver_time_kernel(fishgpu_solver *S, const char *name, i
   }
 }
 
+// Eight independent FMA chains per thread; the multiplier and addend are
+// kernel arguments, so nothing folds, and one store per thread keeps the work.
+static __global__ void __launch_bounds__(256) k_dfma_rate(double *__restrict__ out, double m, double c, int iters) {
+  double a[8];
+#pragma unroll
+  for (int q = 0; q < 8; q++) a[q] = threadIdx.x * 1e-3 + q;
+  for (int t = 0; t < iters; t++) {
+#pragma unroll
+    for (int q = 0; q < 8; q++) a[q] = fma(a[q], m, c);
+  }
+  double sum = 0.0;
+#pragma unroll
+  for (int q = 0; q < 8; q++) sum += a[q];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = sum;
+}
+
+extern "C" int fishgpu_fp64_fma_rate(int reps, double *tflops) {
+  if (reps < 1 || !tflops) return FISHGPU_ERR_ARG;
+  int dev = 0, sms = 0;
+  FG_CUDA(cudaGetDevice(&dev));
+  FG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int blocks = sms * 8, threads = 256, iters = 4096;
+  double *out = nullptr;
+  if (cudaMalloc((void **)&out, sizeof(double) * blocks * threads) != cudaSuccess) return FISHGPU_ERR_NOMEM;
+  cudaStream_t s = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int rc = FISHGPU_OK;
+  if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess || cudaEventCreate(&e0) != cudaSuccess ||
+      cudaEventCreate(&e1) != cudaSuccess)
+    rc = FISHGPU_ERR_CUDA;
+  float best = 0.f;
+  for (int q = 0; q <= reps && rc == FISHGPU_OK; q++) {
+    float ms = 0.f;
+    k_dfma_rate<<<blocks, threads, 0, s>>>(out, 0.999999, 1e-6, iters);  // launch 0 warms up
+    if (q == 0) continue;
+    if (cudaEventRecord(e0, s) != cudaSuccess) rc = FISHGPU_ERR_CUDA;
+    k_dfma_rate<<<blocks, threads, 0, s>>>(out, 0.999999, 1e-6, iters);
+    if (rc == FISHGPU_OK && (cudaEventRecord(e1, s) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+                             cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess))
+      rc = FISHGPU_ERR_CUDA;
+    if (rc == FISHGPU_OK && (best == 0.f || ms < best)) best = ms;
+  }
+  if (rc == FISHGPU_OK && cudaGetLastError() != cudaSuccess) rc = FISHGPU_ERR_CUDA;
+  if (rc == FISHGPU_OK) *tflops = 2.0 * 8.0 * iters * (double)blocks * threads / (best * 1e-3) / 1e12;
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (s) cudaStreamDestroy(s);
+  cudaFree(out);
+  return rc;
+}
+
 // ====================================================================== batches
 // Thousands of independent 2D problems -Laplace(u) = f on the unit square with
 // u = 0 on the boundary (fish's operator with cx = cy = 1), of uneven sizes
