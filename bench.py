@@ -228,6 +228,8 @@ def minimal_leg(fg, reps=3):
         "newton_its": [rep.its[k] for k in range(rep.ngrids)],
         "reasons": [fg.snes_reason_name(rep.reason[k]) for k in range(rep.ngrids)],
         "inner_its_total": rep.total_ksp_its, "errinf": rep.errinf,
+        "grid_ms": [rep.grid_ms[k] for k in range(rep.ngrids)],
+        "inner_its_per_grid": [sum(rep.ksp_its[k][i] for i in range(rep.its[k])) for k in range(rep.ngrids)],
     }
     # the oracle's Newton (exact sparse solves, one host core) on a bounded sample of the same flow
     try:

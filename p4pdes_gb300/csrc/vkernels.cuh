@@ -998,12 +998,4 @@ static __global__ void __launch_bounds__(256) v_pend_promote(Geom g, Slots s, co
   FG_PW_END
 }
 
-// a += b
-static __global__ void __launch_bounds__(256) v_add(Geom g, Slots s, const double *__restrict__ b, double *__restrict__ a) {
-  FG_PW_BEGIN
-  const V4<double> x = ld4(a + n), y = ld4(b + n);
-  st4(a + n, V4<double>{x.x + y.x, x.y + y.y, x.z + y.z, x.w + y.w});
-  FG_PW_END
-}
-
 }  // namespace fg

@@ -296,6 +296,43 @@ def test_nonfinite_user_data_is_reported(cuda):
     assert e.value.code == 5
 
 
+@pytest.mark.parametrize("prec", ["mixed", "fp64"])
+@pytest.mark.parametrize("args", [
+    "-fsh_dim 3 -fsh_problem manupoly -da_refine 4 -pc_type mg -ksp_rtol 1e-10",
+    "-fsh_dim 3 -fsh_problem manuexp -da_grid_x 5 -da_grid_y 3 -da_grid_z 9 -da_refine 3 -pc_type mg -ksp_rtol 1e-10",
+    "-fsh_dim 2 -fsh_problem manupoly -da_refine 6 -pc_type mg -fsh_cx 0.5 -ksp_rtol 1e-10",
+    "-fsh_dim 1 -fsh_problem manupoly -da_refine 6 -pc_type mg -ksp_rtol 1e-10",
+])
+def test_zero_initial_residual_matches_the_stencil(cuda, args, prec):
+    """The initial residual from the zero initial state is a pointwise pass
+    (interior rows of the Jacobian do not see boundary columns); the same u0
+    given explicitly takes the FP64 stencil.  Histories and solutions agree to
+    the bit."""
+    import torch
+    fg = fgmod()
+    oa = fg.options(args + " -fsh_precision " + prec)
+    ob = fg.options(args + " -fsh_precision " + prec)
+    ob.initial_type = fg.INITIAL_GIVEN
+    u0 = torch.empty(oa.shape, dtype=torch.float64, device=cuda)
+    fg.InitialState(fg.info_for(oa), fg.INITIAL_ZEROS, 1, u0, oa.ctx)
+    ua, ub = torch.empty_like(u0), u0.clone()
+    with fg.Solver(oa) as s:
+        ra = s.solve(ua)
+    with fg.Solver(ob) as s:
+        rb = s.solve(ub)
+    assert ra.reason == rb.reason == 2 and ra.its == rb.its
+    assert ra.history() == rb.history() and ra.fnorm0 == rb.fnorm0
+    assert torch.equal(ua, ub)
+
+
+def test_fp64_fma_rate_is_plausible(cuda):
+    """The FP64 FMA probe used as the FP64 residual's roofline denominator:
+    GB300's FP64 rate is ~1.2 TFLOP/s nominal, far below its FP32 rate."""
+    fg = fgmod()
+    t = fg.fp64_fma_rate(3)
+    assert 0.3 < t < 5.0, t
+
+
 def test_solver_is_reusable_and_deterministic(cuda):
     import torch
     fg = fgmod()
