@@ -339,8 +339,8 @@ def run_ours(args):
     rk = args.roofline_kernel
     kms, kbytes = s_mx.time_kernel(rk, 20)
     kernel_table = {}
-    for name in ("smooth", "smooth_dots", "smooth_zero", "cgp_apply", "cg_update", "resid", "restrict", "prolong",
-                 "residual64"):
+    for name in ("smooth", "smooth_first", "smooth_dots", "smooth_zero", "cgp_apply", "cg_update", "resid", "restrict",
+                 "prolong", "residual64"):
         try:
             t, b = s_mx.time_kernel(name, 10)
         except fg.FishError:

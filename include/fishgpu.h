@@ -223,7 +223,7 @@ int fishgpu_solve_host(const fishgpu_opts *o, const double *f_host, const double
 
 /* Times `reps` launches of one solver kernel on the finest level with the
    solver's resident data (CUDA events on the solver's stream).  Names:
-   "smooth", "smooth_dots", "smooth_zero", "post2", "cgp_apply", "cg_update",
+   "smooth", "smooth_first", "smooth_dots", "smooth_zero", "post2", "cgp_apply", "cg_update",
    "resid", "apply", "restrict", "prolong", "residual64".  Reports the mean ms
    per launch and the algorithmic bytes one launch moves. */
 int fishgpu_solver_time_kernel(fishgpu_solver *s, const char *name, int reps,

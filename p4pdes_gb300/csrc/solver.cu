@@ -778,6 +778,12 @@ static int time_kernel_dim(fishgpu_solver *S, const char *name, int reps, double
       else
         v_cheb<DIM, double, true><<<gb, sl.chunk, 0, s>>>(g, sl, nullptr, S->r64, ld.X[0], ld.X[1], ld.X[2], 0.5, 0.5, 0.1);
       *bytes = 4.0 * sz * N;
+    } else if (!strcmp(name, "smooth_first")) {  // a Chebyshev step without x_{k-1}: reads b, x_k, writes x_{k+1}
+      if (mixed)
+        v_cheb<DIM, float, false><<<gb, sl.chunk, 0, s>>>(g, sl, nullptr, S->r32, nullptr, lf.X[1], lf.X[2], 0.f, 0.5f, 0.1f);
+      else
+        v_cheb<DIM, double, false><<<gb, sl.chunk, 0, s>>>(g, sl, nullptr, S->r64, nullptr, ld.X[1], ld.X[2], 0.0, 0.5, 0.1);
+      *bytes = 3.0 * sz * N;
     } else if (!strcmp(name, "smooth_dots")) {  // the same step with z.z and z.b reduced (last post-smoothing step)
       if (mixed)
         v_cheb<DIM, float, true, true><<<gb, sl.chunk, 0, s>>>(g, sl, nullptr, S->r32, lf.X[0], lf.X[1], lf.X[2], 0.5f,

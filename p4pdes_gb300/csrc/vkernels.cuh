@@ -124,6 +124,16 @@ struct MinBlocks {
   static constexpr int value = sizeof(T) == 4 ? 4 : 1;
 };
 
+// Stencils with at most two input streams and no reduction fit 48 registers
+// without spills: 5 blocks per SM.  Measured at 513^3: the two-step smoother
+// from zero 0.248 -> 0.228 ms (6 blocks: no further gain), the residual
+// 0.288 -> 0.267 ms; the Chebyshev step with x_{k-1} (three streams) is
+// slower at 5 blocks (0.339 -> 0.377 ms) and keeps 4.
+template <typename T>
+struct MinBlocksLean {
+  static constexpr int value = sizeof(T) == 4 ? 5 : 1;
+};
+
 template <typename T>
 struct Wv {
   T sx, sy, sz, sd;
@@ -317,7 +327,7 @@ __device__ __forceinline__ bool jk_bdry(const Geom &g, int dim, int j, int k) {
 // DOTS: also reduces out.out and out.b (the preconditioned residual's z.z and
 // z.r when this is the last smoothing step on the finest level) and runs `fin`.
 template <int DIM, typename T, bool HAS_KM1, bool DOTS = false, bool PL = false>
-__global__ void __launch_bounds__(256, MinBlocks<T>::value) v_cheb(Geom g, Slots s, KspState *st, const T *__restrict__ b,
+__global__ void __launch_bounds__(256, ((DOTS || HAS_KM1) ? MinBlocks<T>::value : MinBlocksLean<T>::value)) v_cheb(Geom g, Slots s, KspState *st, const T *__restrict__ b,
                                               const T *__restrict__ xkm1, const T *__restrict__ xk,
                                               T *__restrict__ out, T ckm1, T ck, T crd, Reducer red = Reducer{},
                                               int slot = 0, Fin fin = FIN_STORE) {
@@ -360,7 +370,7 @@ __global__ void __launch_bounds__(256, MinBlocks<T>::value) v_cheb(Geom g, Slots
 //   x1 = c1 b,  x2 = omega x1 + omega c1 (b - A x1) = a0 b - a1 (A b)
 // with a0 = 2 omega c1, a1 = omega c1^2 (c1 = scale/scdiag).
 template <int DIM, typename T>
-__global__ void __launch_bounds__(256, MinBlocks<T>::value) v_cheb2_zero(Geom g, Slots s, KspState *st, const T *__restrict__ b,
+__global__ void __launch_bounds__(256, MinBlocksLean<T>::value) v_cheb2_zero(Geom g, Slots s, KspState *st, const T *__restrict__ b,
                                                     T *__restrict__ out, T a0, T a1) {
   st = block_state(st, s);
   if (ksp_done_v(st)) return;
@@ -388,7 +398,7 @@ __global__ void __launch_bounds__(256, MinBlocks<T>::value) v_cheb2_zero(Geom g,
 // r = b - A x; NORM: r.r reduced into *out as v_dots(r, r) reduces it (same
 // per-thread order over the slot's planes, same block order)
 template <int DIM, typename T, bool NORM = false>
-__global__ void __launch_bounds__(256, MinBlocks<T>::value) v_resid(Geom g, Slots s, KspState *st, const T *__restrict__ b,
+__global__ void __launch_bounds__(256, (NORM ? MinBlocks<T>::value : MinBlocksLean<T>::value)) v_resid(Geom g, Slots s, KspState *st, const T *__restrict__ b,
                                                const T *__restrict__ x, T *__restrict__ r, Reducer red = Reducer{},
                                                int slot = 0, double *out = nullptr) {
   st = block_state(st, s);
