@@ -128,7 +128,10 @@ struct MinBlocks {
 // without spills: 5 blocks per SM.  Measured at 513^3: the two-step smoother
 // from zero 0.248 -> 0.228 ms (6 blocks: no further gain), the residual
 // 0.288 -> 0.267 ms; the Chebyshev step with x_{k-1} (three streams) is
-// slower at 5 blocks (0.339 -> 0.377 ms) and keeps 4.
+// slower at 5 blocks (0.339 -> 0.377 ms) and keeps 4.  Of the kernels that
+// reduce, the fused CG direction update + apply gains a little at 5 blocks
+// (0.670 -> 0.657 ms) while the Chebyshev step with fused dots is 2.2x slower
+// there (0.361 -> 0.803 ms) and keeps 4.
 template <typename T>
 struct MinBlocksLean {
   static constexpr int value = sizeof(T) == 4 ? 5 : 1;
@@ -465,7 +468,7 @@ __global__ void __launch_bounds__(256, MinBlocks<T>::value) v_apply_dot(Geom g, 
 // alpha is still the previous iteration's: FIN_PW replaces it only after
 // every block has finished.
 template <int DIM, typename T, bool PL = false>
-__global__ void __launch_bounds__(256, MinBlocks<T>::value) v_cgp_apply(Geom g, Slots s, KspState *st, const T *__restrict__ z,
+__global__ void __launch_bounds__(256, MinBlocksLean<T>::value) v_cgp_apply(Geom g, Slots s, KspState *st, const T *__restrict__ z,
                                                    const T *__restrict__ pold, T *__restrict__ pnew,
                                                    T *__restrict__ wv, T *__restrict__ y, Reducer red, int slot) {
   st = block_state_sel<PL>(st, s);
