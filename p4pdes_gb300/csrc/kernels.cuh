@@ -120,12 +120,26 @@ __global__ void __launch_bounds__(256) k_apply(Geom g, Range R, Tiles tm, KspSta
 // interior by sine-transform diagonalisation x = S (Lambda^{-1} (S b)) with
 // S_d[i][k] = sqrt(2/(n+1)) sin(ik pi/(n+1)) (symmetric, orthogonal) and
 // Lambda = sum_d sc_d (2 - 2cos(k_d pi/(n_d+1))).  S and 1/Lambda come from
-// the host (setup); work holds 2 * prod(n_d) entries.
+// the host (setup).  With `smem` the transform matrices, 1/Lambda and the two
+// work arrays are staged in dynamic shared memory (coarse_smem_bytes); else
+// `work` (global, 2 * prod(n_d) entries per block) holds the work arrays.
+// Every output is the same FMA chain in either form.
+template <typename T>
+inline size_t coarse_smem_bytes(int dim, int n0, int n1, int n2) {
+  const size_t ni = (size_t)n0 * n1 * n2;
+  size_t e = 3 * ni + (size_t)n0 * n0;
+  if (dim >= 2) e += (size_t)n1 * n1;
+  if (dim >= 3) e += (size_t)n2 * n2;
+  return e * sizeof(T);
+}
+
 template <int DIM, typename T>
 __global__ void __launch_bounds__(1024) k_coarse(Geom g, KspState *st, int batch, const T *__restrict__ b,
                                                  T *__restrict__ x, const T *__restrict__ S0,
                                                  const T *__restrict__ S1, const T *__restrict__ S2,
-                                                 const T *__restrict__ ilam, T *work, int n0, int n1, int n2) {
+                                                 const T *__restrict__ ilam, T *work, int n0, int n1, int n2,
+                                                 int smem) {
+  extern __shared__ __align__(16) unsigned char fg_coarse_sm[];
   // 3D: one block for the grid; 1D/2D: block q solves k-plane q (a batch of
   // independent instances when batch != 0, else the single plane)
   const int plane = DIM < 3 ? (int)blockIdx.x : 0;
@@ -137,45 +151,68 @@ __global__ void __launch_bounds__(1024) k_coarse(Geom g, KspState *st, int batch
   }
   const int tid = threadIdx.x, nt = blockDim.x;
   const int mzl = DIM < 3 ? 1 : g.mz;
-  const long long N = (long long)g.mx * g.my * mzl;
+  const int N = g.mx * g.my * mzl;
   const T dinv = (T)(1.0 / g.scdiag);
-  for (long long q = tid; q < N; q += nt) {
-    int i = (int)(q % g.mx), j = (int)((q / g.mx) % g.my), k = (int)(q / ((long long)g.mx * g.my));
-    long long n = gidx(g, i, j, k);
+  for (int q = tid; q < N; q += nt) {
+    const int i = q % g.mx, r = q / g.mx, j = r % g.my, k = r / g.my;
+    const long long n = gidx(g, i, j, k);
     x[n] = b[n] * dinv;
   }
   const int ni = n0 * n1 * n2;
   if (ni <= 0) return;
-  T *A = work + (size_t)blockIdx.x * 2 * ni, *B = A + ni;
+  T *A, *B;
+  const T *Sd[3] = {S0, S1, S2};
+  const T *il = ilam;
+  if (smem) {
+    T *sm = reinterpret_cast<T *>(fg_coarse_sm);
+    A = sm;
+    B = A + ni;
+    T *sl = B + ni, *s0 = sl + ni, *s1 = s0 + n0 * n0, *s2 = s1 + (DIM >= 2 ? n1 * n1 : 0);
+    for (int q = tid; q < ni; q += nt) sl[q] = ilam[q];
+    for (int q = tid; q < n0 * n0; q += nt) s0[q] = S0[q];
+    if (DIM >= 2)
+      for (int q = tid; q < n1 * n1; q += nt) s1[q] = S1[q];
+    if (DIM >= 3)
+      for (int q = tid; q < n2 * n2; q += nt) s2[q] = S2[q];
+    Sd[0] = s0;
+    Sd[1] = s1;
+    Sd[2] = s2;
+    il = sl;
+  } else {
+    A = work + (size_t)blockIdx.x * 2 * ni;
+    B = A + ni;
+  }
   const int oj = DIM >= 2 ? 1 : 0, ok = DIM >= 3 ? 1 : 0;
   __syncthreads();
   for (int q = tid; q < ni; q += nt) {
-    int i = q % n0, j = (q / n0) % n1, k = q / (n0 * n1);
+    const int i = q % n0, j = (q / n0) % n1, k = q / (n0 * n1);
     A[q] = b[gidx(g, i + 1, j + oj, k + ok)];
   }
   __syncthreads();
   for (int pass = 0; pass < 2; pass++) {
     for (int d = 0; d < DIM; d++) {
-      const T *S = d == 0 ? S0 : d == 1 ? S1 : S2;
+      const T *S = Sd[d];
       const int nd = d == 0 ? n0 : d == 1 ? n1 : n2;
       const int st_d = d == 0 ? 1 : d == 1 ? n0 : n0 * n1;
       for (int q = tid; q < ni; q += nt) {
-        int c = d == 0 ? q % n0 : d == 1 ? (q / n0) % n1 : q / (n0 * n1);
-        int base = q - c * st_d;
+        const int c = d == 0 ? q % n0 : d == 1 ? (q / n0) % n1 : q / (n0 * n1);
+        const int base = q - c * st_d;
         T s = T(0);
         for (int kk = 0; kk < nd; kk++) s = fma(S[c * nd + kk], A[base + kk * st_d], s);
         B[q] = s;
       }
       __syncthreads();
-      T *t = A; A = B; B = t;
+      T *t = A;
+      A = B;
+      B = t;
     }
     if (pass == 0) {
-      for (int q = tid; q < ni; q += nt) A[q] *= ilam[q];
+      for (int q = tid; q < ni; q += nt) A[q] *= il[q];
       __syncthreads();
     }
   }
   for (int q = tid; q < ni; q += nt) {
-    int i = q % n0, j = (q / n0) % n1, k = q / (n0 * n1);
+    const int i = q % n0, j = (q / n0) % n1, k = q / (n0 * n1);
     x[gidx(g, i + 1, j + oj, k + ok)] = A[q];
   }
 }

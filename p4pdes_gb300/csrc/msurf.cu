@@ -107,6 +107,14 @@ __device__ __forceinline__ void ms_nb(const Geom &g, const MsP &P, const double 
   }
 }
 
+// The diffusivity (1 + W)^q (minimal.c:46-48).  For the minimal surface
+// equation q = -1/2 and it is the reciprocal square root: CUDA's rsqrt (1 ulp)
+// instead of pow (2 ulp), which costs many times the FP64 instructions on a
+// part whose FP64 rate is low.
+__device__ __forceinline__ double ms_diffusivity(double onepw, double q) {
+  return q == -0.5 ? rsqrt(onepw) : pow(onepw, q);
+}
+
 // F at interior node (i,j), minimal.c:257-280
 __device__ __forceinline__ double ms_f_interior(const Geom &g, const MsP &P, const double *__restrict__ u,
                                                 long long pitch, int i, int j) {
@@ -118,16 +126,16 @@ __device__ __forceinline__ double ms_f_interior(const Geom &g, const MsP &P, con
   double dx, dy;
   dx = (ue - uc) / hx;
   dy = (un + une - us - use) / (4.0 * hy);
-  const double De = pow(1.0 + dx * dx + dy * dy, P.q);
+  const double De = ms_diffusivity(1.0 + dx * dx + dy * dy, P.q);
   dx = (uc - uw) / hx;
   dy = (unw + un - usw - us) / (4.0 * hy);
-  const double Dw = pow(1.0 + dx * dx + dy * dy, P.q);
+  const double Dw = ms_diffusivity(1.0 + dx * dx + dy * dy, P.q);
   dx = (ue + une - uw - unw) / (4.0 * hx);
   dy = (un - uc) / hy;
-  const double Dn = pow(1.0 + dx * dx + dy * dy, P.q);
+  const double Dn = ms_diffusivity(1.0 + dx * dx + dy * dy, P.q);
   dx = (ue + use - uw - usw) / (4.0 * hx);
   dy = (uc - us) / hy;
-  const double Ds = pow(1.0 + dx * dx + dy * dy, P.q);
+  const double Ds = ms_diffusivity(1.0 + dx * dx + dy * dy, P.q);
   return -hyhx * (De * (ue - uc) - Dw * (uc - uw)) - hxhy * (Dn * (un - uc) - Ds * (uc - us));
 }
 
@@ -206,7 +214,7 @@ __global__ void __launch_bounds__(256) k_ms_resid(Geom g, MsP P, const double *_
 // Linearisation of one half-point flux D(W) d (d the normal difference):
 //   A = D + K dn/hn,  Q = K dt/(4 ht),  K = 2 q D/(1+W) d
 __device__ __forceinline__ void ms_half(double q, double d, double hn, double dt, double ht, float &A, float &Q) {
-  const double dn = d / hn, W = dn * dn + dt * dt, D = pow(1.0 + W, q);
+  const double dn = d / hn, W = dn * dn + dt * dt, D = ms_diffusivity(1.0 + W, q);
   const double K = 2.0 * q * D / (1.0 + W) * d;
   A = (float)(D + K * dn / hn);
   Q = (float)(K * dt / (4.0 * ht));
@@ -602,7 +610,7 @@ __global__ void __launch_bounds__(256) k_ms_area(Geom g, double q, int degree, c
         const double y = yj - hy + hy * 0.5 * (pt + 1.0);
         const double ux = ((u11 - u01) * (y - (yj - hy)) + (u10 - u00) * (yj - y)) / (hx * hy);
         const double uy = ((u11 - u10) * (x - (xi_ - hx)) + (u01 - u00) * (xi_ - x)) / (hx * hy);
-        const double W = ux * ux + uy * uy, D = pow(1.0 + W, q);
+        const double W = ux * ux + uy * uy, D = ms_diffusivity(1.0 + W, q);
         lo = fmin(lo, D);
         hi = fmax(hi, D);
         s += wr * wt * sqrt(1.0 + W);

@@ -357,8 +357,15 @@ static void enq_vcycle(fishgpu_solver *S, Hier<T> &H, int l, bool from_zero, int
   KspState *st = S->st;
   if (l == 0) {
     lv.cur = 0;
-    k_coarse<DIM, T><<<DIM < 3 ? lv.g.mz : 1, 1024, 0, s>>>(lv.g, st, lv.sl.batch, lv.b, lv.X[0], lv.S[0], lv.S[1], lv.S[2], lv.ilam, lv.work,
-                                        lv.n[0], lv.n[1], lv.n[2]);
+    // a block of just enough threads (tiny coarsest grids start and synchronise
+    // faster), the transforms staged in shared memory when they fit 48 KB
+    const int per = lv.g.mx * lv.g.my * (DIM < 3 ? 1 : lv.g.mz), ni = lv.n[0] * lv.n[1] * lv.n[2];
+    const int nt = std::min(1024, std::max(32, (std::max(per, ni) + 31) / 32 * 32));
+    const size_t smb = coarse_smem_bytes<T>(DIM, lv.n[0], lv.n[1], lv.n[2]);
+    const bool sm = ni > 0 && smb <= 48 * 1024;
+    k_coarse<DIM, T><<<DIM < 3 ? lv.g.mz : 1, nt, sm ? smb : 0, s>>>(lv.g, st, lv.sl.batch, lv.b, lv.X[0], lv.S[0],
+                                                                    lv.S[1], lv.S[2], lv.ilam, lv.work, lv.n[0],
+                                                                    lv.n[1], lv.n[2], sm ? 1 : 0);
     return;
   }
   Level<T> &lc = H.lev[l - 1];
