@@ -66,6 +66,7 @@ struct KspState {
   int nhist;
   int pend;    // y += alpha p deferred: 0 none, 1 in p buffer 0, 2 in p buffer 1
   double dp, rnorm0, ttol, beta, betaold, dpi, dpiold, alpha;
+  double bratio;  // beta / betaold for the next direction update (one division, in the finaliser)
   double acc[4];
   unsigned int *ndone;  // batches: incremented once when this instance stops
   double hist[FISHGPU_MAX_HIST];
@@ -262,6 +263,7 @@ static __device__ __noinline__ void ksp_finalize(KspState *st, Fin fin, const do
       if (r) { ksp_stop(st, r); break; }
     }
     st->beta = tot[1];
+    st->bratio = st->beta / st->betaold;
     st->i += 1;
     if (st->i >= st->max_it) { ksp_stop(st, R_DIVERGED_ITS); break; }
     if (isnan(st->beta) || isinf(st->beta)) { st->its = st->i + 1; ksp_stop(st, R_DIVERGED_NANORINF); break; }

@@ -138,7 +138,7 @@ __global__ void __launch_bounds__(1024) k_coarse(Geom g, KspState *st, int batch
                                                  T *__restrict__ x, const T *__restrict__ S0,
                                                  const T *__restrict__ S1, const T *__restrict__ S2,
                                                  const T *__restrict__ ilam, T *work, int n0, int n1, int n2,
-                                                 int smem) {
+                                                 int smem, T dinv) {
   extern __shared__ __align__(16) unsigned char fg_coarse_sm[];
   // 3D: one block for the grid; 1D/2D: block q solves k-plane q (a batch of
   // independent instances when batch != 0, else the single plane)
@@ -152,8 +152,7 @@ __global__ void __launch_bounds__(1024) k_coarse(Geom g, KspState *st, int batch
   const int tid = threadIdx.x, nt = blockDim.x;
   const int mzl = DIM < 3 ? 1 : g.mz;
   const int N = g.mx * g.my * mzl;
-  const T dinv = (T)(1.0 / g.scdiag);
-  for (int q = tid; q < N; q += nt) {
+  for (int q = tid; q < N; q += nt) {  // dinv = (T)(1 / scdiag), from the host
     const int i = q % g.mx, r = q / g.mx, j = r % g.my, k = r / g.my;
     const long long n = gidx(g, i, j, k);
     x[n] = b[n] * dinv;

@@ -37,6 +37,10 @@ struct MsP {
   double q, c, H;
   int model;      // FISHGPU_NL_MINIMAL / FISHGPU_NL_BRATU
   double lambda;  // Bratu's coefficient of e^u
+  // boundary data of one grid, precomputed (k_ms_gtab): nullptr = evaluate g
+  // where it is needed
+  const double *gt = nullptr;
+  int gtm = 0;  // max(mx, my): the length of each of its 16 rows
 };
 
 // boundary data: minimal.c:27-42 (tent, catenoid); bratu2D.c:58-68 (zero, Liouville)
@@ -93,6 +97,53 @@ __device__ __forceinline__ bool ms_bdry(const Geom &g, int i, int j) {
   return i == 0 || j == 0 || i == g.mx - 1 || j == g.my - 1;
 }
 
+// Boundary-data table of one grid (P.gt, rows of length M = P.gtm).  The
+// values g(x +- hx, y +- hy) that interior nodes next to the boundary ask for
+// are stored by asker: rows 0-2 for the askers of row j = 1 (neighbour row
+// j - 1 = 0, x-offsets -1, 0, +1), rows 3-5 for row j = my-2 (neighbour row
+// my-1), rows 6-8 for column i = 1 (neighbour column 0, y-offsets -1, 0, +1),
+// rows 9-11 for column i = mx-2; rows 12-15 hold g at the boundary nodes
+// themselves (bottom, top by i; left, right by j).  Every entry is ms_gd at the
+// argument expression of the direct evaluation, so the table changes no bit;
+// it keeps FP64 transcendentals out of the residual, whose boundary blocks
+// otherwise wait on them.
+__device__ __forceinline__ int ms_gt_row(int e, int d) { return e * 3 + d; }
+
+__global__ void __launch_bounds__(128) k_ms_gtab(Geom g, MsP P, double *__restrict__ gt, int M) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= M) return;
+  const double hx = g.h[0], hy = g.h[1];
+  if (t >= 1 && t <= g.mx - 2) {
+    const double x = t * hx, ys = 1 * hy, yn = (g.my - 2) * hy;
+    for (int d = 0; d < 3; d++) {
+      gt[(size_t)ms_gt_row(0, d) * M + t] = ms_gd(P, x + (d - 1) * hx, ys + (-1) * hy);
+      gt[(size_t)ms_gt_row(1, d) * M + t] = ms_gd(P, x + (d - 1) * hx, yn + 1 * hy);
+    }
+  }
+  if (t >= 1 && t <= g.my - 2) {
+    const double y = t * hy, xw = 1 * hx, xe = (g.mx - 2) * hx;
+    for (int d = 0; d < 3; d++) {
+      gt[(size_t)ms_gt_row(2, d) * M + t] = ms_gd(P, xw + (-1) * hx, y + (d - 1) * hy);
+      gt[(size_t)ms_gt_row(3, d) * M + t] = ms_gd(P, xe + 1 * hx, y + (d - 1) * hy);
+    }
+  }
+  if (t < g.mx) {
+    gt[(size_t)12 * M + t] = ms_gd(P, t * hx, 0 * hy);
+    gt[(size_t)13 * M + t] = ms_gd(P, t * hx, (g.my - 1) * hy);
+  }
+  if (t < g.my) {
+    gt[(size_t)14 * M + t] = ms_gd(P, 0 * hx, t * hy);
+    gt[(size_t)15 * M + t] = ms_gd(P, (g.mx - 1) * hx, t * hy);
+  }
+}
+
+// g at boundary node (i,j)
+__device__ __forceinline__ double ms_gown(const Geom &g, const MsP &P, int i, int j) {
+  if (!P.gt) return ms_gd(P, i * g.h[0], j * g.h[1]);
+  const size_t M = (size_t)P.gtm;
+  return j == 0 ? P.gt[12 * M + i] : j == g.my - 1 ? P.gt[13 * M + i] : i == 0 ? P.gt[14 * M + j] : P.gt[15 * M + j];
+}
+
 // The eight neighbours of interior node (i,j) (order e w n s ne nw se sw):
 // the array value, or g at x +- hx, y +- hy when the neighbour is a boundary
 // node (minimal.c:227-255).
@@ -100,10 +151,19 @@ __device__ __forceinline__ void ms_nb(const Geom &g, const MsP &P, const double 
                                       int i, int j, double v[8]) {
   const double hx = g.h[0], hy = g.h[1], x = i * hx, y = j * hy;
   const int di[8] = {1, -1, 0, 0, 1, -1, 1, -1}, dj[8] = {0, 0, 1, -1, 1, 1, -1, -1};
+  const size_t M = (size_t)P.gtm;
 #pragma unroll
   for (int q = 0; q < 8; q++) {
     const int a = i + di[q], b = j + dj[q];
-    v[q] = ms_bdry(g, a, b) ? ms_gd(P, x + di[q] * hx, y + dj[q] * hy) : u[(long long)b * pitch + a];
+    if (!ms_bdry(g, a, b)) {
+      v[q] = u[(long long)b * pitch + a];
+    } else if (!P.gt) {
+      v[q] = ms_gd(P, x + di[q] * hx, y + dj[q] * hy);
+    } else {
+      const int e = (dj[q] == -1 && b == 0) ? 0 : (dj[q] == 1 && b == g.my - 1) ? 1 : (di[q] == -1 && a == 0) ? 2 : 3;
+      const int d = e < 2 ? di[q] + 1 : dj[q] + 1, t = e < 2 ? i : j;
+      v[q] = P.gt[(size_t)ms_gt_row(e, d) * M + t];
+    }
   }
 }
 
@@ -201,7 +261,7 @@ __global__ void __launch_bounds__(256) k_ms_resid(Geom g, MsP P, const double *_
       // the VI residual norm is taken over the inactive set (u > psi or F <= 0)
       acc = (u[n] <= obs_psi(x, y) + OBS_ZEROTOL && f > 0.0) ? 0.0 : f * f;
     } else if (node) {
-      f = ms_bdry(g, i, j) ? u[n] - ms_gd(P, i * g.h[0], j * g.h[1])
+      f = ms_bdry(g, i, j) ? u[n] - ms_gown(g, P, i, j)
           : P.model == FISHGPU_NL_BRATU ? lb_f_interior(g, P, u, g.pitch, i, j) : ms_f_interior(g, P, u, g.pitch, i, j);
       acc = f * f;
     }
@@ -664,6 +724,8 @@ namespace {
 struct MsLevel {
   fishgpu_solver *P = nullptr;  // Poisson multigrid of this grid (geometry, V-cycle)
   Geom g;
+  double *gt = nullptr;  // boundary-data table (k_ms_gtab), minimal surface and Bratu
+  int gtm = 0;
   long long N = 0;
   dim3 grid, block;
   double *u = nullptr, *F = nullptr, *W = nullptr, *G = nullptr;
@@ -710,6 +772,14 @@ static int ms_alloc(fishgpu_ms_solver *S, T **p, long long n) {
   S->allocs.push_back(q);
   *p = (T *)q;
   return FISHGPU_OK;
+}
+
+// The problem parameters with the boundary-data table of grid L
+static MsP level_params(const fishgpu_ms_solver *S, const MsLevel &L) {
+  MsP P = S->P;
+  P.gt = L.gt;
+  P.gtm = L.gtm;
+  return P;
 }
 
 static int ms_levels_for(int mx, int my) {
@@ -769,7 +839,7 @@ static int read_vals(fishgpu_ms_solver *S, int n) {
 
 static int residual(fishgpu_ms_solver *S, MsLevel &L, const double *u, double *F, double *fnorm) {
   S->nfuncs++;
-  k_ms_resid<<<L.grid, L.block, 0, S->stream>>>(L.g, S->P, u, F, S->red, S->dval);
+  k_ms_resid<<<L.grid, L.block, 0, S->stream>>>(L.g, level_params(S, L), u, F, S->red, S->dval);
   MS_CK(cudaGetLastError());
   int rc = read_vals(S, 1);
   if (rc) return rc;
@@ -823,7 +893,7 @@ static int newton(fishgpu_ms_solver *S, MsLevel &L, int k, fishgpu_ms_report *re
       break;
     }
     // J Y = F: coefficients at u, b = F/||F||, BiCGStab for x = J^-1 b, Y = ||F|| x
-    k_ms_coef<<<L.grid, L.block, 0, s>>>(g, S->P, L.u, L.F, L.C1, L.C2);
+    k_ms_coef<<<L.grid, L.block, 0, s>>>(g, level_params(S, L), L.u, L.F, L.C1, L.C2);
     k_ms_demote<<<L.grid, L.block, 0, s>>>(g, S->P.model, L.C1, L.F, 1.0 / fnorm, L.b);
     MS_CK(cudaGetLastError());
     MS_CK(cudaGraphLaunch(L.g_init, s));
@@ -1168,6 +1238,12 @@ extern "C" int fishgpu_ms_solver_create(const fishgpu_ms_opts *o, void *stream, 
     float **vs[10] = {&L.b, &L.r, &L.rh, &L.p, &L.v, &L.s, &L.t, &L.x, &L.ph, &L.sh};
     for (float **q : vs) MS_FAIL(ms_alloc(S, q, L.N));
     L.giters = L.N >= (1LL << 20) ? 1 : 2;
+    if (S->P.model != FISHGPU_NL_OBSTACLE) {
+      L.gtm = std::max(L.g.mx, L.g.my);
+      MS_FAIL(ms_alloc(S, &L.gt, 16LL * L.gtm));
+      k_ms_gtab<<<(L.gtm + 127) / 128, 128, 0, S->stream>>>(L.g, S->P, L.gt, L.gtm);
+      if (cudaGetLastError() != cudaSuccess) MS_FAIL(FISHGPU_ERR_CUDA);
+    }
     mx = 2 * mx - 1;
     my = 2 * my - 1;
   }

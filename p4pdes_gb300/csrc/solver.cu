@@ -365,7 +365,8 @@ static void enq_vcycle(fishgpu_solver *S, Hier<T> &H, int l, bool from_zero, int
     const bool sm = ni > 0 && smb <= 48 * 1024;
     k_coarse<DIM, T><<<DIM < 3 ? lv.g.mz : 1, nt, sm ? smb : 0, s>>>(lv.g, st, lv.sl.batch, lv.b, lv.X[0], lv.S[0],
                                                                     lv.S[1], lv.S[2], lv.ilam, lv.work, lv.n[0],
-                                                                    lv.n[1], lv.n[2], sm ? 1 : 0);
+                                                                    lv.n[1], lv.n[2], sm ? 1 : 0,
+                                                                    (T)(1.0 / lv.g.scdiag));
     return;
   }
   Level<T> &lc = H.lev[l - 1];
@@ -763,7 +764,7 @@ static int time_kernel_dim(fishgpu_solver *S, const char *name, int reps, double
     KspState h;
     memset(&h, 0, sizeof(h));
     h.i = 1;
-    h.beta = h.betaold = h.dpi = 1.0;
+    h.beta = h.betaold = h.dpi = h.bratio = 1.0;
     h.alpha = 1e-3;
     h.pend = 1;  // cgp_apply also applies a deferred y update
     h.norm_type = FISHGPU_NORM_UNPRECONDITIONED;

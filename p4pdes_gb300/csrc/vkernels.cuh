@@ -478,7 +478,7 @@ __global__ void __launch_bounds__(256, MinBlocksLean<T>::value) v_cgp_apply(Geom
   const bool first = !st || st->i == 0;  // no state: p = z
   const bool pend = st && st->pend && y;
   const T a = pend ? (T)st->alpha : T(0);
-  const AxpySrc<T> src{z, pold, first ? T(0) : (T)(st->beta / st->betaold), first};
+  const AxpySrc<T> src{z, pold, first ? T(0) : (T)st->bratio, first};
   T acc = T(0);
   auto op = [&](int k, long long n, const Nb<T> &nb) {
     const bool jkb = jk_bdry(g, DIM, p.j, k);
@@ -953,7 +953,11 @@ static __global__ void __launch_bounds__(256) v_demote_init(Geom g, Slots s, Ksp
                                                      const double *__restrict__ rr, float *__restrict__ r32,
                                                      float *__restrict__ y32, Reducer red, int slot) {
   if (ksp_done_v(st)) return;
-  const double is = 1.0 / sqrt(*rr);
+  // one sqrt and division per block (FP64 is slow on this part), shared
+  __shared__ double s_is;
+  if (threadIdx.x == 0) s_is = 1.0 / sqrt(*rr);
+  __syncthreads();
+  const double is = s_is;
   float zz = 0.f;
   FG_PW_BEGIN
   const V4<double> a = ld4(r + n);
