@@ -384,7 +384,6 @@ static void enq_vcycle(fishgpu_solver *S, Hier<T> &H, int l, bool from_zero, int
 template <int DIM, typename T>
 static bool enq_pc(fishgpu_solver *S, Hier<T> &H, const T *r, int dots) {
   const fishgpu_opts &o = S->o;
-  const long long tot4 = S->sf.tot4;
   if (o.pc_type == FISHGPU_PC_NONE) {
     v_scale<T><<<slot_blocks(S->sf), S->sf.chunk, 0, S->stream>>>(S->fine, S->sf, S->st, r, T(1), H.zbuf);
     H.z = H.zbuf;
@@ -414,7 +413,6 @@ struct KspVecs {
 template <int DIM, typename T>
 static void enq_cg_init(fishgpu_solver *S, Hier<T> &H, KspVecs<T> v, const double *src64 = nullptr) {
   cudaStream_t s = S->stream;
-  const long long tot4 = S->sf.tot4;
   if constexpr (sizeof(T) == 4) {
     if (src64) {
       v_demote_init<<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(S->fine, S->sf, S->st, src64, S->dval, v.r, v.y,
@@ -437,8 +435,6 @@ template <int DIM, typename T>
 static void enq_cg_iter(fishgpu_solver *S, Hier<T> &H, KspVecs<T> v, int par) {
   cudaStream_t s = S->stream;
   KspState *st = S->st;
-  const long long tot4 = S->sf.tot4;
-  const unsigned gf = S->gfl;
   T *pold = v.p[par], *pnew = v.p[1 - par];
   // p = z + beta/betaold p (z of the previous application), w = A p, p.w
   bool planes = false;
@@ -628,8 +624,6 @@ static int solve_dim(fishgpu_solver *S, double *u, fishgpu_report *rep) {
   cudaStream_t s = S->stream;
   const Launch &L = S->Lf;
   const Geom &g = S->fine;
-  const long long tot4 = S->sf.tot4;
-  const unsigned gfl = S->gfl;
   FG_CUDA(cudaEventRecord(S->ev0, s));
   S->launches = 2;  // initial state, -F(u0) with its norm
   k_initial64<DIM><<<L.grid, L.block, 0, s>>>(g, S->dense, L.tm, S->prob, o.initial_type, o.initial_gonboundary,
