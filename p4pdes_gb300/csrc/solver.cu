@@ -41,7 +41,8 @@ template <typename T>
 struct Level {
   Post2Z pz{};     // launch shape of the fused two-step post-smoother (3D FP32)
   Geom g;      // padded pitch
-  Slots sl;
+  Slots sl;    // pointwise kernels and grid transfers
+  Slots st;    // stencils: sl, or the 2D row march for batches
   T *b = nullptr, *r = nullptr;
   T *X[3] = {nullptr, nullptr, nullptr};  // rotating iterate buffers
   int cur = 0;                            // buffer holding the iterate (enqueue time)
@@ -104,6 +105,7 @@ struct fishgpu_solver_s {
   Geom fine;       // padded
   Geom dense;      // the caller's layout (pitch = mx)
   Slots sf;        // slots of the fine level
+  Slots sfst;      // stencil slots of the fine level (sf, or the fine level's row march)
   Launch Lf;       // scalar launch over the fine grid
   unsigned gfl = 1;  // grid of the pointwise kernels on the fine level
   Prob prob;
@@ -155,6 +157,12 @@ static int dalloc(fishgpu_solver *S, T **p, size_t n) {
   return FISHGPU_OK;
 }
 
+// Rows per thread of the batch stencils (2D instances stacked as planes): the
+// planes give the parallelism, so a thread can march a strip of rows with the
+// y-neighbours in registers.  A function of the instance size only, so an
+// instance is decomposed alike alone and in any batch.
+static int batch_rows(const Geom &g) { return g.dim == 2 && g.mx >= 129 ? 16 : 0; }
+
 template <typename T>
 static int build_hier(fishgpu_solver *S, Hier<T> &H) {
   const fishgpu_opts &o = S->o;
@@ -174,6 +182,7 @@ static int build_hier(fishgpu_solver *S, Hier<T> &H) {
     if (S->batch) g.mz = S->nplanes;  // a batch keeps its instances as planes on every level
     lv.g = g;
     lv.sl = make_slots(g, ZC, 2432, 256, S->batch);
+    lv.st = S->batch ? make_slots(g, ZC, 2432, 256, 1, batch_rows(g)) : lv.sl;
     if (g.dim == 3) lv.pz = post2z_shape(g);
     double lmin, lmax;
     spectrum(g, &lmin, &lmax);
@@ -245,15 +254,15 @@ static inline int third(int a, int b) { return 3 - a - b; }
 template <int DIM, typename T, bool HAS_KM1>
 static void launch_cheb_dots(fishgpu_solver *S, Level<T> &lv, const T *xkm1, const T *xk, T *out, T ckm1, T ck,
                              T crd, Fin fin) {
-  const unsigned gb = slot_blocks(lv.sl);
+  const unsigned gb = slot_blocks(lv.st);
   if constexpr (DIM == 2) {
     if (S->batch) {
-      v_cheb<DIM, T, HAS_KM1, true, true><<<gb, lv.sl.chunk, 0, S->stream>>>(lv.g, lv.sl, S->st, lv.b, xkm1, xk, out,
+      v_cheb<DIM, T, HAS_KM1, true, true><<<gb, lv.st.chunk, 0, S->stream>>>(lv.g, lv.st, S->st, lv.b, xkm1, xk, out,
                                                                          ckm1, ck, crd, S->red, 0, fin);
       return;
     }
   }
-  v_cheb<DIM, T, HAS_KM1, true, false><<<gb, lv.sl.chunk, 0, S->stream>>>(lv.g, lv.sl, S->st, lv.b, xkm1, xk, out, ckm1,
+  v_cheb<DIM, T, HAS_KM1, true, false><<<gb, lv.st.chunk, 0, S->stream>>>(lv.g, lv.st, S->st, lv.b, xkm1, xk, out, ckm1,
                                                                        ck, crd, S->red, 0, fin);
 }
 
@@ -264,7 +273,7 @@ static void enq_smooth(fishgpu_solver *S, Level<T> &lv, bool from_zero, int dots
   const double dinv = 1.0 / lv.g.scdiag;
   cudaStream_t s = S->stream;
   KspState *st = S->st;
-  const unsigned gb = slot_blocks(lv.sl);
+  const unsigned gb = slot_blocks(lv.sl), gbs = slot_blocks(lv.st);
   const unsigned gf = flat_grid(lv.sl.tot4);
   if (o.smooth_type == FISHGPU_SMOOTH_RICHARDSON) {
     const T crd = (T)(o.richardson_scale * dinv);
@@ -277,7 +286,7 @@ static void enq_smooth(fishgpu_solver *S, Level<T> &lv, bool from_zero, int dots
       else if (last)
         launch_cheb_dots<DIM, T, false>(S, lv, nullptr, lv.X[cur], lv.X[nxt], T(0), T(1), crd, fin);
       else
-        v_cheb<DIM, T, false><<<gb, lv.sl.chunk, 0, s>>>(lv.g, lv.sl, st, lv.b, nullptr, lv.X[cur], lv.X[nxt], T(0), T(1), crd);
+        v_cheb<DIM, T, false><<<gbs, lv.st.chunk, 0, s>>>(lv.g, lv.st, st, lv.b, nullptr, lv.X[cur], lv.X[nxt], T(0), T(1), crd);
       cur = nxt;
     }
     lv.cur = cur;
@@ -292,7 +301,7 @@ static void enq_smooth(fishgpu_solver *S, Level<T> &lv, bool from_zero, int dots
     // x1 = c1 b; x2 = omega x1 + omega c1 (b - A x1) = 2 omega c1 b - omega c1^2 (A b)
     const double ckp1 = 2.0 * mu * mu - 1.0, omega = omegaprod * mu / ckp1;
     const int nxt = (lv.cur + 1) % 3;
-    v_cheb2_zero<DIM, T><<<gb, lv.sl.chunk, 0, s>>>(lv.g, lv.sl, st, lv.b, lv.X[nxt], (T)(2.0 * omega * c1),
+    v_cheb2_zero<DIM, T><<<gbs, lv.st.chunk, 0, s>>>(lv.g, lv.st, st, lv.b, lv.X[nxt], (T)(2.0 * omega * c1),
                                             (T)(omega * c1 * c1));
     lv.cur = nxt;
     return;
@@ -324,7 +333,7 @@ static void enq_smooth(fishgpu_solver *S, Level<T> &lv, bool from_zero, int dots
     if (o.smooth_its == 1 && dots >= 0)
       launch_cheb_dots<DIM, T, false>(S, lv, nullptr, lv.X[km1], lv.X[kk], T(0), T(1), (T)c1, fin);
     else
-      v_cheb<DIM, T, false><<<gb, lv.sl.chunk, 0, s>>>(lv.g, lv.sl, st, lv.b, nullptr, lv.X[km1], lv.X[kk], T(0), T(1), (T)c1);
+      v_cheb<DIM, T, false><<<gbs, lv.st.chunk, 0, s>>>(lv.g, lv.st, st, lv.b, nullptr, lv.X[km1], lv.X[kk], T(0), T(1), (T)c1);
   }
   double ckm1 = 1.0, ck = mu;
   for (int it = 1; it < o.smooth_its; it++) {
@@ -334,13 +343,13 @@ static void enq_smooth(fishgpu_solver *S, Level<T> &lv, bool from_zero, int dots
     const int out = km1 < 0 ? (kk + 1) % 3 : third(km1, kk);
     const bool last = it == o.smooth_its - 1 && dots >= 0;
     if (km1 < 0)
-      v_cheb<DIM, T, false><<<gb, lv.sl.chunk, 0, s>>>(lv.g, lv.sl, st, lv.b, nullptr, lv.X[kk], lv.X[out], T(0), (T)omega,
+      v_cheb<DIM, T, false><<<gbs, lv.st.chunk, 0, s>>>(lv.g, lv.st, st, lv.b, nullptr, lv.X[kk], lv.X[out], T(0), (T)omega,
                                                (T)(omega * c1));
     else if (last)
       launch_cheb_dots<DIM, T, true>(S, lv, lv.X[km1], lv.X[kk], lv.X[out], (T)(1.0 - omega), (T)omega,
                                      (T)(omega * c1), fin);
     else
-      v_cheb<DIM, T, true><<<gb, lv.sl.chunk, 0, s>>>(lv.g, lv.sl, st, lv.b, lv.X[km1], lv.X[kk], lv.X[out],
+      v_cheb<DIM, T, true><<<gbs, lv.st.chunk, 0, s>>>(lv.g, lv.st, st, lv.b, lv.X[km1], lv.X[kk], lv.X[out],
                                               (T)(1.0 - omega), (T)omega, (T)(omega * c1));
     km1 = kk;
     kk = out;
@@ -371,7 +380,7 @@ static void enq_vcycle(fishgpu_solver *S, Hier<T> &H, int l, bool from_zero, int
   }
   Level<T> &lc = H.lev[l - 1];
   enq_smooth<DIM, T>(S, lv, from_zero);
-  v_resid<DIM, T><<<slot_blocks(lv.sl), lv.sl.chunk, 0, s>>>(lv.g, lv.sl, st, lv.b, lv.X[lv.cur], lv.r);
+  v_resid<DIM, T><<<slot_blocks(lv.st), lv.st.chunk, 0, s>>>(lv.g, lv.st, st, lv.b, lv.X[lv.cur], lv.r);
   v_restrict<DIM, T><<<slot_blocks(lc.sl), lc.sl.chunk, 0, s>>>(lv.g, lc.g, lc.sl, st, lv.r, lc.b);
   for (int c = 0; c < S->o.mg_cycles; c++) enq_vcycle<DIM, T>(S, H, l - 1, c == 0);
   v_prolong<DIM, T><<<slot_blocks(lc.sl), lc.sl.chunk, 0, s>>>(lv.g, lc.g, lc.sl, st, lc.X[lc.cur], lv.X[lv.cur]);
@@ -440,13 +449,13 @@ static void enq_cg_iter(fishgpu_solver *S, Hier<T> &H, KspVecs<T> v, int par) {
   bool planes = false;
   if constexpr (DIM == 2) {
     if (S->batch) {
-      v_cgp_apply<DIM, T, true><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(S->fine, S->sf, st, H.z, pold, pnew, v.w,
+      v_cgp_apply<DIM, T, true><<<slot_blocks(S->sfst), S->sfst.chunk, 0, s>>>(S->fine, S->sfst, st, H.z, pold, pnew, v.w,
                                                                        v.y, S->red, 0);
       planes = true;
     }
   }
   if (!planes)
-    v_cgp_apply<DIM, T, false><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(S->fine, S->sf, st, H.z, pold, pnew, v.w,
+    v_cgp_apply<DIM, T, false><<<slot_blocks(S->sfst), S->sfst.chunk, 0, s>>>(S->fine, S->sfst, st, H.z, pold, pnew, v.w,
                                                                       v.y, S->red, 0);
   if (S->ksp_norm == FISHGPU_NORM_UNPRECONDITIONED)
     v_cg_r<T, true><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(S->fine, S->sf, st, v.w, v.r, S->red, 0);
@@ -948,6 +957,7 @@ extern "C" int fishgpu_solver_create(const fishgpu_opts *o, void *stream, fishgp
                        o->ctx.cx, o->ctx.cy, o->ctx.cz);
   S->fine = padded(S->dense);
   S->sf = make_slots(S->fine, ZC);
+  S->sfst = S->sf;
   S->Lf = launch_for(S->fine);
   S->gfl = flat_grid(S->sf.tot4);
   S->prob = Prob{o->ctx.problem, dim, o->ctx.cx, o->ctx.cy, o->ctx.cz, o->ctx.f, o->ctx.g, S->dense.pitch,
@@ -1358,7 +1368,7 @@ static int tune_chunk(fishgpu_solver *S, Level<float> &lv) {
   float best_ms = 1e30f;
   cudaStream_t s = S->stream;
   for (int c = 0; c < 3; c++) {
-    const Slots sl = make_slots(lv.g, ZC, 2432, cand[c], 1);
+    const Slots sl = make_slots(lv.g, ZC, 2432, cand[c], 1, batch_rows(lv.g));
     const unsigned gb = slot_blocks(sl);
     // b = the level's residual buffer, x_{k-1}, x_k, out: its three iterate buffers
     for (int w = 0; w < 2; w++)
@@ -1472,10 +1482,13 @@ static int group_create(const fishgpu_batch_opts &bo, int n, int count, fishgpu_
     }
     for (int l = S->h32.nlev - 1; l >= 1; l--) {
       Level<float> &lv = S->h32.lev[l];
-      lv.sl = make_slots(lv.g, ZC, 2432, tune_chunk(S, lv), 1);
+      const int c = tune_chunk(S, lv);
+      lv.sl = make_slots(lv.g, ZC, 2432, c, 1);
+      lv.st = make_slots(lv.g, ZC, 2432, c, 1, batch_rows(lv.g));
     }
     S->sf = S->h32.lev[S->h32.nlev - 1].sl;
   }
+  S->sfst = S->h32.lev[S->h32.nlev - 1].st;
   // reductions are over the fine level's blocks, tickets per plane
   const int cap = (int)slot_blocks(S->sf);
   CK(dalloc(S, &S->red.partials, (size_t)2 * 2 * cap));

@@ -69,15 +69,22 @@ struct Slots {
   int zc, nz;     // planes per block, z-chunks
   int batch;      // 1: planes are independent instances
   long long tot4; // slots in the whole array
+  int ry;         // 2D row march: a thread owns one x-slot of ry consecutive rows (0: one slot)
 };
 
 // zc_max planes per block at most, fewer when needed to keep at least
 // `min_blocks` blocks (small levels, and the coarse-grid launches of the
 // grid transfers, would otherwise leave SMs idle).
-inline Slots make_slots(const Geom &g, int zc_max, int min_blocks = 2432, int chunk = 256, int batch = 0) {
+// ry > 1 (2D stencils only): a thread marches ry rows of one x-slot, with
+// the rows j-1, j, j+1 in registers (the 2D counterpart of the z-march); a
+// plane then holds P4 * ceil(my / ry) thread slots.  Pointwise kernels keep
+// the plain form (ry = 0).
+inline Slots make_slots(const Geom &g, int zc_max, int min_blocks = 2432, int chunk = 256, int batch = 0,
+                        int ry = 0) {
   Slots s;
   s.P4 = g.pitch / 4;
-  s.per_plane = s.P4 * g.my;
+  s.ry = (g.dim == 2 && ry > 1) ? ry : 0;
+  s.per_plane = s.P4 * (s.ry ? (g.my + s.ry - 1) / s.ry : g.my);
   s.chunk = chunk;
   s.batch = batch;
   s.nchunk = (s.per_plane + chunk - 1) / chunk;
@@ -89,7 +96,7 @@ inline Slots make_slots(const Geom &g, int zc_max, int min_blocks = 2432, int ch
   }
   s.zc = zc;
   s.nz = (g.mz + s.zc - 1) / s.zc;
-  s.tot4 = (long long)s.per_plane * g.mz;
+  s.tot4 = (long long)s.P4 * g.my * g.mz;  // vector slots, whatever the thread decomposition
   return s;
 }
 inline unsigned slot_blocks(const Slots &s) { return (unsigned)s.nchunk * (unsigned)s.nz; }
@@ -106,8 +113,9 @@ __device__ __forceinline__ SlotPos slot_pos(const Geom &g, const Slots &s) {
   const int c = blockIdx.x % s.nchunk, kz = blockIdx.x / s.nchunk;
   const int f = c * s.chunk + threadIdx.x;
   p.in = f < s.per_plane;
-  p.j = p.in ? f / s.P4 : 0;
-  p.i4 = p.in ? (f - p.j * s.P4) * 4 : 0;
+  const int row = p.in ? f / s.P4 : 0;  // row, or strip of ry rows
+  p.i4 = p.in ? (f - row * s.P4) * 4 : 0;
+  p.j = s.ry ? row * s.ry : row;  // first row of a strip
   p.k0 = kz * s.zc;
   p.k1 = min(p.k0 + s.zc, g.mz);
   p.col = (long long)p.j * g.pitch + p.i4;
@@ -151,6 +159,7 @@ struct Nb {
   T l, r;    // x-neighbours of element 0 (i4-1) and element 3 (i4+4)
   V4<T> ys;  // sum of the y-neighbours that are interior nodes
   V4<T> zs;  // sum of the z-neighbours that are interior nodes
+  bool jkb;  // the slot's row or plane is on the boundary
 };
 
 // Stencil input read from one array.
@@ -288,8 +297,53 @@ __device__ __forceinline__ KspState *block_state_sel(KspState *st, const Slots &
 // Generic z-march over the slot's planes.  `Op` is called once per plane
 // with (k, n, nb) after the neighbour data is assembled; it performs its own
 // loads/stores of other arrays at n.  `x` is the stencil input.
+__device__ __forceinline__ bool jk_bdry(const Geom &g, int dim, int j, int k) {
+  return (dim >= 2 && (j == 0 || j == g.my - 1)) || (dim >= 3 && (k == 0 || k == g.mz - 1));
+}
+
+// 2D row march (s.ry rows of one x-slot): the same neighbour data as the
+// plain form, the y-neighbour rows from the register window instead of
+// loads, in the plain form's order (south + north).  Every thread runs ry
+// steps (the shuffles need all lanes); rows past the grid are skipped.
+template <typename T, class Op, class Src>
+__device__ __forceinline__ void march_rows(const Geom &g, const Slots &s, const SlotPos &p, const Src &x, Op &op) {
+  const int lane = threadIdx.x & 31;
+  const long long base = (long long)p.k0 * g.plane + p.i4;
+  V4<T> xs = zero4<T>(), xc = zero4<T>();
+  if (p.in && p.j - 1 >= 0) xs = x.v4(base + (long long)(p.j - 1) * g.pitch);
+  if (p.in && p.j < g.my) xc = x.v4(base + (long long)p.j * g.pitch);
+  for (int t = 0; t < s.ry; t++) {
+    const int j = p.j + t;
+    const bool valid = p.in && j < g.my;
+    const long long n = base + (long long)j * g.pitch;
+    V4<T> xn = zero4<T>();
+    if (valid && j + 1 < g.my) xn = x.v4(n + g.pitch);
+    Nb<T> nb;
+    T l = __shfl_up_sync(0xffffffffu, xc.w, 1);
+    T r = __shfl_down_sync(0xffffffffu, xc.x, 1);
+    if (lane == 0) l = (valid && p.i4 > 0) ? x.s(n - 1) : T(0);
+    if (lane == 31) r = (valid && p.i4 + 4 < g.mx) ? x.s(n + 4) : T(0);
+    nb.c = xc;
+    nb.l = l;
+    nb.r = r;
+    const bool hs = j - 1 > 0, hn = j + 1 < g.my - 1;
+    nb.ys = add4(hs ? xs : zero4<T>(), hn ? xn : zero4<T>());
+    nb.zs = zero4<T>();
+    nb.jkb = j == 0 || j == g.my - 1;
+    if (valid) op(p.k0, n, nb);
+    xs = xc;
+    xc = xn;
+  }
+}
+
 template <int DIM, typename T, class Op, class Src>
 __device__ __forceinline__ void march_src(const Geom &g, const Slots &s, const SlotPos &p, const Src &x, Op &op) {
+  if constexpr (DIM == 2) {
+    if (s.ry) {
+      march_rows<T>(g, s, p, x, op);
+      return;
+    }
+  }
   V4<T> zd = zero4<T>(), zc = zero4<T>();
   if (p.in) {
     if (DIM >= 3 && p.k0 > 0) zd = x.v4((long long)(p.k0 - 1) * g.plane + p.col);
@@ -307,6 +361,7 @@ __device__ __forceinline__ void march_src(const Geom &g, const Slots &s, const S
     } else {
       nb.zs = zero4<T>();
     }
+    nb.jkb = jk_bdry(g, DIM, p.j, k);
     if (p.in) op(k, n, nb);
     zd = zc;
     zc = zu;
@@ -319,9 +374,7 @@ __device__ __forceinline__ void march(const Geom &g, const Slots &s, const SlotP
   march_src<DIM, T>(g, s, p, ArraySrc<T>{x}, op);
 }
 
-__device__ __forceinline__ bool jk_bdry(const Geom &g, int dim, int j, int k) {
-  return (dim >= 2 && (j == 0 || j == g.my - 1)) || (dim >= 3 && (k == 0 || k == g.mz - 1));
-}
+
 
 // ------------------------------------------------------------------ stencil ops
 // out = ckm1*xkm1 + ck*xk + crd*(b - A xk)   (Chebyshev / Richardson step)
@@ -342,7 +395,7 @@ __global__ void __launch_bounds__(256, ((DOTS || HAS_KM1) ? MinBlocks<T>::value 
   auto op = [&](int k, long long n, const Nb<T> &nb) {
     const V4<T> bv = ld4(b + n);
     V4<T> km = HAS_KM1 ? ld4(xkm1 + n) : zero4<T>();
-    const bool jkb = jk_bdry(g, DIM, p.j, k);
+    const bool jkb = nb.jkb;
     V4<T> o;
 #pragma unroll
     for (int e = 0; e < 4; e++) {
@@ -380,7 +433,7 @@ __global__ void __launch_bounds__(256, MinBlocksLean<T>::value) v_cheb2_zero(Geo
   const SlotPos p = slot_pos(g, s);
   const Wv<T> w(g);
   auto op = [&](int k, long long n, const Nb<T> &nb) {
-    const bool jkb = jk_bdry(g, DIM, p.j, k);
+    const bool jkb = nb.jkb;
     V4<T> o;
 #pragma unroll
     for (int e = 0; e < 4; e++) {
@@ -411,7 +464,7 @@ __global__ void __launch_bounds__(256, (NORM ? MinBlocks<T>::value : MinBlocksLe
   T rr = T(0);
   auto op = [&](int k, long long n, const Nb<T> &nb) {
     const V4<T> bv = ld4(b + n);
-    const bool jkb = jk_bdry(g, DIM, p.j, k);
+    const bool jkb = nb.jkb;
     V4<T> o;
 #pragma unroll
     for (int e = 0; e < 4; e++) {
@@ -440,7 +493,7 @@ __global__ void __launch_bounds__(256, MinBlocks<T>::value) v_apply_dot(Geom g, 
   const Wv<T> w(g);
   T acc = T(0);
   auto op = [&](int k, long long n, const Nb<T> &nb) {
-    const bool jkb = jk_bdry(g, DIM, p.j, k);
+    const bool jkb = nb.jkb;
     V4<T> o;
 #pragma unroll
     for (int e = 0; e < 4; e++) {
@@ -481,7 +534,7 @@ __global__ void __launch_bounds__(256, MinBlocksLean<T>::value) v_cgp_apply(Geom
   const AxpySrc<T> src{z, pold, first ? T(0) : (T)st->bratio, first};
   T acc = T(0);
   auto op = [&](int k, long long n, const Nb<T> &nb) {
-    const bool jkb = jk_bdry(g, DIM, p.j, k);
+    const bool jkb = nb.jkb;
     V4<T> o;
 #pragma unroll
     for (int e = 0; e < 4; e++) {
