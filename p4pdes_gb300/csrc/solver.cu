@@ -160,8 +160,13 @@ static int dalloc(fishgpu_solver *S, T **p, size_t n) {
 // Rows per thread of the batch stencils (2D instances stacked as planes): the
 // planes give the parallelism, so a thread can march a strip of rows with the
 // y-neighbours in registers.  A function of the instance size only, so an
-// instance is decomposed alike alone and in any batch.
-static int batch_rows(const Geom &g) { return g.dim == 2 && g.mx >= 129 ? 16 : 0; }
+// instance is decomposed alike alone and in any batch.  Swept at 820
+// instances per size: 16 rows beat 8 and 32 at 257^2-513^2, 8 is best at
+// 65^2-129^2 and 4 at 33^2.
+static int batch_rows(const Geom &g) {
+  if (g.dim != 2) return 0;
+  return g.mx >= 257 ? 16 : g.mx >= 65 ? 8 : g.mx >= 33 ? 4 : 0;  // measured per size: 4096-instance batch
+}
 
 template <typename T>
 static int build_hier(fishgpu_solver *S, Hier<T> &H) {
