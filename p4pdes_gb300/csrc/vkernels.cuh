@@ -113,12 +113,27 @@ __device__ __forceinline__ SlotPos slot_pos(const Geom &g, const Slots &s) {
   const int c = blockIdx.x % s.nchunk, kz = blockIdx.x / s.nchunk;
   const int f = c * s.chunk + threadIdx.x;
   p.in = f < s.per_plane;
-  const int row = p.in ? f / s.P4 : 0;  // row, or strip of ry rows
-  p.i4 = p.in ? (f - row * s.P4) * 4 : 0;
-  p.j = s.ry ? row * s.ry : row;  // first row of a strip
+  p.j = p.in ? f / s.P4 : 0;  // row (the strip of a 2D row march: slot_pos_st)
+  p.i4 = p.in ? (f - p.j * s.P4) * 4 : 0;
   p.k0 = kz * s.zc;
   p.k1 = min(p.k0 + s.zc, g.mz);
   p.col = (long long)p.j * g.pitch + p.i4;
+  return p;
+}
+
+// Slot coordinates of a stencil thread: in a 2D row march p.j is the first
+// row of the thread's strip.  A compile-time split, so that the 3D stencils
+// carry no trace of it (a runtime test in slot_pos cost the 3D CG update
+// kernel 6%).
+template <int DIM>
+__device__ __forceinline__ SlotPos slot_pos_st(const Geom &g, const Slots &s) {
+  SlotPos p = slot_pos(g, s);
+  if constexpr (DIM == 2) {
+    if (s.ry) {
+      p.j *= s.ry;
+      p.col = (long long)p.j * g.pitch + p.i4;
+    }
+  }
   return p;
 }
 
@@ -389,7 +404,7 @@ __global__ void __launch_bounds__(256, ((DOTS || HAS_KM1) ? MinBlocks<T>::value 
                                               int slot = 0, Fin fin = FIN_STORE) {
   st = DOTS ? block_state_sel<PL>(st, s) : block_state(st, s);
   if (ksp_done_v(st)) return;
-  const SlotPos p = slot_pos(g, s);
+  const SlotPos p = slot_pos_st<DIM>(g, s);
   const Wv<T> w(g);
   T zz = T(0), zr = T(0);
   auto op = [&](int k, long long n, const Nb<T> &nb) {
@@ -430,7 +445,7 @@ __global__ void __launch_bounds__(256, MinBlocksLean<T>::value) v_cheb2_zero(Geo
                                                     T *__restrict__ out, T a0, T a1) {
   st = block_state(st, s);
   if (ksp_done_v(st)) return;
-  const SlotPos p = slot_pos(g, s);
+  const SlotPos p = slot_pos_st<DIM>(g, s);
   const Wv<T> w(g);
   auto op = [&](int k, long long n, const Nb<T> &nb) {
     const bool jkb = nb.jkb;
@@ -459,7 +474,7 @@ __global__ void __launch_bounds__(256, (NORM ? MinBlocks<T>::value : MinBlocksLe
                                                int slot = 0, double *out = nullptr) {
   st = block_state(st, s);
   if (ksp_done_v(st)) return;
-  const SlotPos p = slot_pos(g, s);
+  const SlotPos p = slot_pos_st<DIM>(g, s);
   const Wv<T> w(g);
   T rr = T(0);
   auto op = [&](int k, long long n, const Nb<T> &nb) {
@@ -489,7 +504,7 @@ __global__ void __launch_bounds__(256, MinBlocks<T>::value) v_apply_dot(Geom g, 
                                                    double *out) {
   st = block_state_sel<false>(st, s);
   if (ksp_done_v(st)) return;
-  const SlotPos p = slot_pos(g, s);
+  const SlotPos p = slot_pos_st<DIM>(g, s);
   const Wv<T> w(g);
   T acc = T(0);
   auto op = [&](int k, long long n, const Nb<T> &nb) {
@@ -526,7 +541,7 @@ __global__ void __launch_bounds__(256, MinBlocksLean<T>::value) v_cgp_apply(Geom
                                                    T *__restrict__ wv, T *__restrict__ y, Reducer red, int slot) {
   st = block_state_sel<PL>(st, s);
   if (ksp_done_v(st)) return;
-  const SlotPos p = slot_pos(g, s);
+  const SlotPos p = slot_pos_st<DIM>(g, s);
   const Wv<T> w(g);
   const bool first = !st || st->i == 0;  // no state: p = z
   const bool pend = st && st->pend && y;
