@@ -364,8 +364,8 @@ __device__ __forceinline__ void march_src(const Geom &g, const Slots &s, const S
     if (DIM >= 3 && p.k0 > 0) zd = x.v4((long long)(p.k0 - 1) * g.plane + p.col);
     zc = x.v4((long long)p.k0 * g.plane + p.col);
   }
-  for (int k = p.k0; k < p.k1; k++) {
-    const long long n = (long long)k * g.plane + p.col;
+  long long n = (long long)p.k0 * g.plane + p.col;  // advanced by a plane per step
+  for (int k = p.k0; k < p.k1; k++, n += g.plane) {
     V4<T> zu = zero4<T>();
     if (DIM >= 3 && p.in && k + 1 < g.mz) zu = x.v4(n + g.plane);
     Nb<T> nb;
