@@ -185,20 +185,18 @@ struct ArraySrc {
   __device__ __forceinline__ T s(long long n) const { return x[n]; }
 };
 
-// Stencil input p = z + bb * q formed on the fly (p = z when first).
+// Stencil input p = z + bb * q formed on the fly (the first CG iteration,
+// p = z, marches z itself through ArraySrc: no load here tests for it).
 template <typename T>
 struct AxpySrc {
   const T *__restrict__ z;
   const T *__restrict__ q;
   T bb;
-  bool first;
   __device__ __forceinline__ V4<T> v4(long long n) const {
-    const V4<T> a = ld4(z + n);
-    if (first) return a;
-    const V4<T> b = ld4(q + n);
+    const V4<T> a = ld4(z + n), b = ld4(q + n);
     return V4<T>{fma(bb, b.x, a.x), fma(bb, b.y, a.y), fma(bb, b.z, a.z), fma(bb, b.w, a.w)};
   }
-  __device__ __forceinline__ T s(long long n) const { return first ? z[n] : fma(bb, q[n], z[n]); }
+  __device__ __forceinline__ T s(long long n) const { return fma(bb, q[n], z[n]); }
 };
 
 // Loads everything but the z-window for plane k; shuffles need all lanes.
@@ -546,7 +544,6 @@ __global__ void __launch_bounds__(256, MinBlocksLean<T>::value) v_cgp_apply(Geom
   const bool first = !st || st->i == 0;  // no state: p = z
   const bool pend = st && st->pend && y;
   const T a = pend ? (T)st->alpha : T(0);
-  const AxpySrc<T> src{z, pold, first ? T(0) : (T)st->bratio, first};
   T acc = T(0);
   auto op = [&](int k, long long n, const Nb<T> &nb) {
     const bool jkb = nb.jkb;
@@ -568,7 +565,10 @@ __global__ void __launch_bounds__(256, MinBlocksLean<T>::value) v_cgp_apply(Geom
       st4(y + n, V4<T>{fma(a, pp.x, yy.x), fma(a, pp.y, yy.y), fma(a, pp.z, yy.z), fma(a, pp.w, yy.w)});
     }
   };
-  march_src<DIM, T>(g, s, p, src, op);
+  // the first iteration (p = z) and the others (p = z + beta/betaold p_old)
+  // march separately, so that no load of the common case tests `first`
+  if (first) march_src<DIM, T>(g, s, p, ArraySrc<T>{z}, op);
+  else march_src<DIM, T>(g, s, p, AxpySrc<T>{z, pold, (T)st->bratio}, op);
   double v1[1] = {(double)acc};
   reduce_sel<1, PL>(v1, red, slot, st, FIN_PW, nullptr, s);
 }
