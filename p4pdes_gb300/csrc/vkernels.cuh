@@ -13,7 +13,9 @@
 // registers.  x-neighbours across slots come from warp shuffles (the warp's
 // edge lanes load one scalar); y-neighbours are two vector loads (L1/L2
 // hits); z-neighbours are the register window.  Grid = chunks x z-chunks,
-// one block per (chunk, z-chunk): no grid-stride tail.
+// one block per (chunk, z-chunk): no grid-stride tail.  Batched 2D instances
+// (planes) march rows instead: a thread owns one x-slot of a strip of rows
+// with the rows j-1, j, j+1 in registers (march_rows).
 #pragma once
 
 #include "fishgpu_internal.cuh"
@@ -138,10 +140,9 @@ __device__ __forceinline__ SlotPos slot_pos_st(const Geom &g, const Slots &s) {
 }
 
 // Resident blocks per SM the compiler is asked to fit: 4 x 256 threads for
-// FP32 stencils (up to 64 registers).  Measured on the 513^3 Chebyshev step:
-// a cap of 48 registers (5 blocks) made the z-march 14% slower without a
-// reduction and 2.1x slower with the fused z.z/z.b reduction; FP64 stencils
-// are FP64-pipe-bound and keep their registers.
+// the FP32 stencils that keep more streams or a reduction in flight (up to 64
+// registers; see MinBlocksLean for the others).  FP64 stencils are
+// FP64-pipe-bound and keep their registers.
 template <typename T>
 struct MinBlocks {
   static constexpr int value = sizeof(T) == 4 ? 4 : 1;
