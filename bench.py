@@ -202,6 +202,41 @@ def batch_leg(torch, fg, n_inst, reps=3):
     }
 
 
+def c1_leg(torch, fg, reps=20):
+    """fish.c's own CPU-runnable case (2D manupoly 257^2, -da_refine 7, CG + 8-level MG V(2,2)
+    Chebyshev/Jacobi, rtol 1e-10): the FP64 form (the reference's arithmetic) and the mixed form,
+    iterations and discretisation error, beside the oracle's CPU time for the same FP64 solve."""
+    args = ("-fsh_dim 2 -fsh_problem manupoly -da_refine 7 -pc_type mg -mg_levels_ksp_type chebyshev "
+            "-mg_levels_pc_type jacobi -ksp_rtol 1e-10")
+    out = {"workload": "2D Poisson, manupoly, 257^2 nodes, 8 MG levels, rtol 1e-10", "options": args}
+    for prec in ("fp64", "mixed"):
+        o = fg.options(args + " -fsh_precision " + prec)
+        with fg.Solver(o) as s:
+            u = torch.empty(o.shape, dtype=torch.float64, device="cuda")
+            s.solve(u)
+            ms = min(s.solve(u).solve_ms for _ in range(reps))
+            rep = s.solve(u)
+        out[prec] = {"ms": ms, "dof_per_s": o.dofs / (ms * 1e-3), "its": rep.its, "outer_its": rep.outer_its,
+                     "errinf": rep.errinf, "err2h": rep.err2h}
+    try:
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        import _oracle as orc
+        oo = orc.options(args.split())
+        best = None
+        for _ in range(3):
+            t0 = time.perf_counter()
+            _, r = orc.fish_solve(oo)
+            dt = time.perf_counter() - t0
+            best = dt if best is None or dt < best else best
+        dofs = oo.grid.mx * oo.grid.my
+        out["cpu_baseline"] = {"value": dofs / best, "unit": "DOF/s", "cores": orc.lib().or_num_threads(),
+                               "kind": "port", "its": r["its"], "errinf": r["errinf"],
+                               "sample": "oracle FP64 CG+MG on the same 257^2 solve, best of 3 (%.1f ms)" % (best * 1e3)}
+    except Exception as e:  # oracle library missing: report why
+        out["cpu_baseline"] = {"unavailable": str(e)[:200]}
+    return out
+
+
 def minimal_leg(fg, reps=3):
     """Minimal-surface equation (c/ch7/minimal.c), catenoid c = 1.1 on the unit
     square, 1025 x 1025 reached by grid sequencing from 33 x 33 (5 refinements),
@@ -410,6 +445,7 @@ def run_ours(args):
         # the same stream at a rate one GB300 sustains (the 2000 req/s stream offers ~2.8x its
         # throughput, so its latencies are mostly queueing): latency without a growing queue
         serving["at_sustainable_rate"] = serve_leg(fg, max(200, args.serve_requests // 2), rate=500.0)
+    c1 = c1_leg(torch, fg)
     minimal = minimal_leg(fg) if args.minimal else None
     if minimal is not None:
         minimal["other_clients"] = clients_leg(fg)
@@ -433,6 +469,7 @@ def run_ours(args):
             "batch": batch,
             "serving": serving,
             "minimal": minimal,
+            "c1_2d_257": c1,
         },
         "e2e": {"value": e2e, "unit": "DOF/s", "h2d_bytes_per_step": h2d_bytes, "d2h_bytes_per_step": 8 * N,
                 "note": "f whole, g only on the boundary (read in place from pinned host memory), u back"},
