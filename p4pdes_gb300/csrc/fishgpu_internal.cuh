@@ -65,6 +65,7 @@ struct KspState {
   int done;    // nonzero: every kernel of the iteration returns at once
   int nhist;
   int pend;    // y += alpha p deferred: 0 none, 1 in p buffer 0, 2 in p buffer 1
+  unsigned int loops;  // bodies run by the device-side solve loop (graph_loop.cuh)
   double dp, rnorm0, ttol, beta, betaold, dpi, dpiold, alpha;
   double bratio;  // beta / betaold for the next direction update (one division, in the finaliser)
   double acc[4];

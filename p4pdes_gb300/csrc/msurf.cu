@@ -28,6 +28,7 @@
 
 #include <vector>
 
+#include "graph_loop.cuh"
 #include "mg_hooks.cuh"
 
 namespace fg {
@@ -367,6 +368,7 @@ struct InitFin {
     st->first = 1;
     st->reason = 0;
     st->k.done = 0;
+    st->k.loops = 0;  // bodies of the device loop, counted per inner solve
     if (!(st->rnorm0 > st->ttol)) msk_stop(st, isfinite(st->rnorm0) ? MSK_CONVERGED_ATOL : MSK_DIVERGED_NANORINF);
   }
 };
@@ -733,6 +735,8 @@ struct MsLevel {
   float *b = nullptr, *r = nullptr, *rh = nullptr, *p = nullptr, *v = nullptr, *s = nullptr, *t = nullptr,
         *x = nullptr, *ph = nullptr, *sh = nullptr;
   cudaGraphExec_t g_init = nullptr, g_iter = nullptr;
+  cudaGraphExec_t g_loop = nullptr;  // g_iter's body repeated on the device until the inner solve stops
+  long long n_loop = 0;
   int giters = 2;
 };
 
@@ -898,6 +902,7 @@ static int newton(fishgpu_ms_solver *S, MsLevel &L, int k, fishgpu_ms_report *re
     MS_CK(cudaGetLastError());
     MS_CK(cudaGraphLaunch(L.g_init, s));
     int kits = 0, kreason = 0;
+    if (L.g_loop) MS_CK(cudaGraphLaunch(L.g_loop, s));
     for (;;) {
       MS_CK(cudaMemcpyAsync(S->st_h, S->st, sizeof(MsKsp), cudaMemcpyDeviceToHost, s));
       MS_CK(cudaStreamSynchronize(s));
@@ -906,6 +911,7 @@ static int newton(fishgpu_ms_solver *S, MsLevel &L, int k, fishgpu_ms_report *re
         kreason = S->st_h->reason;
         break;
       }
+      if (L.g_loop) return FISHGPU_ERR_TIMEOUT;  // the capped device loop ended unfinished
       MS_CK(cudaGraphLaunch(L.g_iter, s));
     }
     rep->ksp_its[k][its] = kits;
@@ -1138,6 +1144,7 @@ extern "C" int fishgpu_ms_solver_destroy(fishgpu_ms_solver *S) {
   for (auto &L : S->lev) {
     if (L.g_init) cudaGraphExecDestroy(L.g_init);
     if (L.g_iter) cudaGraphExecDestroy(L.g_iter);
+    if (L.g_loop) cudaGraphExecDestroy(L.g_loop);
     if (L.P) fishgpu_solver_destroy(L.P);
   }
   for (void *p : S->allocs) cudaFree(p);
@@ -1259,7 +1266,12 @@ extern "C" int fishgpu_ms_solver_create(const fishgpu_ms_opts *o, void *stream, 
     MS_FAIL(FISHGPU_ERR_CUDA);
   for (auto &L : S->lev) {
     MS_FAIL(capture(S, L, true, &L.g_init));
-    MS_FAIL(capture(S, L, false, &L.g_iter));
+    // the BiCGStab loop on the device (bodies of giters iterations until the
+    // inner solve stops, capped); the host-polled graph if the driver refuses
+    const unsigned int cap = (unsigned int)(std::max(1, o->ksp_max_it) / L.giters + 5);
+    if (!build_loop_graph(S->stream, [&] { for (int k = 0; k < L.giters; k++) enq_bicg_iter(S, L); },
+                          &S->st->k.done, nullptr, 0u, &S->st->k.loops, cap, &L.g_loop, &L.n_loop))
+      MS_FAIL(capture(S, L, false, &L.g_iter));
   }
   if (cudaStreamSynchronize(S->stream) != cudaSuccess) MS_FAIL(FISHGPU_ERR_CUDA);
 #undef MS_FAIL

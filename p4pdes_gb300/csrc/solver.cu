@@ -29,6 +29,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "graph_loop.cuh"
 #include "vkernels.cuh"
 
 namespace fg {
@@ -124,6 +125,9 @@ struct fishgpu_solver_s {
   // FP32 inner KSP vectors (mixed form)
   float *r32 = nullptr, *p32 = nullptr, *q32 = nullptr, *w32 = nullptr, *y32 = nullptr;
   cudaGraphExec_t gexec = nullptr;       // giters CG iterations
+  cudaGraphExec_t gloop = nullptr;       // the same repeated on the device until the solve stops
+  bool loop_refused = false;             // the driver refused the device loop: poll from the host
+  long long n_loop = 0;                  // kernel nodes of one body of gloop
   cudaGraphExec_t gexec_init = nullptr;  // the KSP set-up sequence
   cudaGraphExec_t gexec_init64[2] = {nullptr, nullptr};  // the same from b64 / r64 (mixed form)
   long long n_init = 0, n_iter = 0;      // kernel nodes of the two graphs
@@ -525,7 +529,16 @@ static int run_ksp(fishgpu_solver *S, Hier<T> &H, KspVecs<T> v, double rtol, int
   cudaGraphExec_t *gi = from64 < 0 ? &S->gexec_init : &S->gexec_init64[from64 & 1];
   const double *src64 = from64 < 0 ? nullptr : from64 ? S->r64 : S->b64;
   if (!*gi && (rc = capture(S, [&] { enq_cg_init<DIM, T>(S, H, v, src64); }, gi, &S->n_init))) return rc;
-  if (!S->gexec &&
+  const long long guard = (long long)max_it / S->giters + 4;
+  // The loop on the device: one launch runs bodies of giters iterations until
+  // the state says stop (or guard bodies ran).  A driver that refuses the
+  // conditional node gets the host loop: a graph of giters iterations per
+  // launch and a read of the stop flag after each.
+  if (!S->gloop && !S->loop_refused)
+    S->loop_refused = !build_loop_graph(
+        s, [&] { for (int g = 0; g < S->giters; g++) enq_cg_iter<DIM, T>(S, H, v, g & 1); }, &S->st->done, nullptr,
+        0u, &S->st->loops, (unsigned int)(guard + 1), &S->gloop, &S->n_loop);
+  if (!S->gloop && !S->gexec &&
       (rc = capture(S, [&] { for (int g = 0; g < S->giters; g++) enq_cg_iter<DIM, T>(S, H, v, g & 1); },
                     &S->gexec, &S->n_iter)))
     return rc;
@@ -533,14 +546,17 @@ static int run_ksp(fishgpu_solver *S, Hier<T> &H, KspVecs<T> v, double rtol, int
   FG_CUDA(cudaMemcpyAsync(S->st, S->st_h, sizeof(KspState), cudaMemcpyHostToDevice, s));
   FG_CUDA(cudaGraphLaunch(*gi, s));
   S->launches += S->n_init;
-  const long long guard = (long long)max_it / S->giters + 4;
-  for (long long launch = 0;; launch++) {
-    FG_CUDA(cudaMemcpyAsync(&S->st_h->done, &S->st->done, sizeof(int), cudaMemcpyDeviceToHost, s));
-    FG_CUDA(cudaStreamSynchronize(s));
-    if (S->st_h->done) break;
-    if (launch > guard) return FISHGPU_ERR_TIMEOUT;
-    FG_CUDA(cudaGraphLaunch(S->gexec, s));
-    S->launches += S->n_iter;
+  if (S->gloop) {
+    FG_CUDA(cudaGraphLaunch(S->gloop, s));
+  } else {
+    for (long long launch = 0;; launch++) {
+      FG_CUDA(cudaMemcpyAsync(&S->st_h->done, &S->st->done, sizeof(int), cudaMemcpyDeviceToHost, s));
+      FG_CUDA(cudaStreamSynchronize(s));
+      if (S->st_h->done) break;
+      if (launch > guard) return FISHGPU_ERR_TIMEOUT;
+      FG_CUDA(cudaGraphLaunch(S->gexec, s));
+      S->launches += S->n_iter;
+    }
   }
   if (from64 < 0) {  // the last iteration's deferred y += alpha p
     v_cg_pend<T><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(S->fine, S->sf, S->st, v.p[0], v.p[1], v.y);
@@ -548,6 +564,10 @@ static int run_ksp(fishgpu_solver *S, Hier<T> &H, KspVecs<T> v, double rtol, int
   }
   FG_CUDA(cudaMemcpyAsync(S->st_h, S->st, sizeof(KspState), cudaMemcpyDeviceToHost, s));
   FG_CUDA(cudaStreamSynchronize(s));
+  if (S->gloop) {
+    S->launches += (long long)S->st_h->loops * S->n_loop;
+    if (!S->st_h->done) return FISHGPU_ERR_TIMEOUT;
+  }
   return FISHGPU_OK;
 }
 
@@ -903,6 +923,7 @@ extern "C" int fishgpu_solver_destroy(fishgpu_solver *S) {
   if (!S) return FISHGPU_OK;
   if (S->stream) cudaStreamSynchronize(S->stream);
   if (S->gexec) cudaGraphExecDestroy(S->gexec);
+  if (S->gloop) cudaGraphExecDestroy(S->gloop);
   if (S->gexec_init) cudaGraphExecDestroy(S->gexec_init);
   for (cudaGraphExec_t &e : S->gexec_init64)
     if (e) cudaGraphExecDestroy(e);
@@ -1591,21 +1612,31 @@ static int group_solve(fishgpu_solver *S, const double *const *f, double *const 
     if (!S->gexec_init &&
         (rc = capture(S, [&] { enq_cg_init<2, float>(S, S->h32, v); }, &S->gexec_init, &S->n_init)))
       return rc;
-    if (!S->gexec &&
+    const long long guard = (long long)o.inner_max_it / S->giters + 4;
+    // the CG loop on the device until every plane has stopped (plane 0's state
+    // counts the bodies); the host loop is kept for a driver that refuses it
+    if (!S->gloop && !S->loop_refused)
+      S->loop_refused = !build_loop_graph(
+          s, [&] { for (int q = 0; q < S->giters; q++) enq_cg_iter<2, float>(S, S->h32, v, q & 1); }, nullptr,
+          S->ndone, (unsigned int)count, &S->st[0].loops, (unsigned int)(guard + 1), &S->gloop, &S->n_loop);
+    if (!S->gloop && !S->gexec &&
         (rc = capture(S, [&] { for (int q = 0; q < S->giters; q++) enq_cg_iter<2, float>(S, S->h32, v, q & 1); },
                       &S->gexec, &S->n_iter)))
       return rc;
     FG_CUDA(cudaGraphLaunch(S->gexec_init, s));
     S->launches += S->n_init + 2;
-    unsigned int *hdone = (unsigned int *)S->hval;  // reuse pinned scratch for the counter
-    const long long guard = (long long)o.inner_max_it / S->giters + 4;
-    for (long long l = 0;; l++) {
-      FG_CUDA(cudaMemcpyAsync(hdone, S->ndone, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
-      FG_CUDA(cudaStreamSynchronize(s));
-      if (*hdone >= (unsigned)count) break;
-      if (l > guard) return FISHGPU_ERR_TIMEOUT;
-      FG_CUDA(cudaGraphLaunch(S->gexec, s));
-      S->launches += S->n_iter;
+    if (S->gloop) {
+      FG_CUDA(cudaGraphLaunch(S->gloop, s));
+    } else {
+      unsigned int *hdone = (unsigned int *)S->hval;  // reuse pinned scratch for the counter
+      for (long long l = 0;; l++) {
+        FG_CUDA(cudaMemcpyAsync(hdone, S->ndone, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
+        FG_CUDA(cudaStreamSynchronize(s));
+        if (*hdone >= (unsigned)count) break;
+        if (l > guard) return FISHGPU_ERR_TIMEOUT;
+        FG_CUDA(cudaGraphLaunch(S->gexec, s));
+        S->launches += S->n_iter;
+      }
     }
     v_cg_pend<float><<<gb, S->sf.chunk, 0, s>>>(g, S->sf, S->st, v.p[0], v.p[1], v.y);
     S->launches += 1;
@@ -1613,7 +1644,12 @@ static int group_solve(fishgpu_solver *S, const double *const *f, double *const 
     v_promote_add<<<gb, S->sf.chunk, 0, s>>>(g, S->sf, S->y32, S->scl, 0.0, S->y64);
     v_resid<2, double><<<gb, S->sf.chunk, 0, s>>>(g, S->sf, nullptr, S->b64, S->y64, S->r64);
     S->launches += 3;
-    if ((rc = plane_norms(S, S->r64))) return rc;
+    if ((rc = plane_norms(S, S->r64))) return rc;  // synchronises: st_h holds the planes' states
+    if (S->gloop) {
+      S->launches += (long long)S->st_h[0].loops * S->n_loop;
+      for (int q = 0; q < count; q++)
+        if (active[q] && !S->st_h[q].done) return FISHGPU_ERR_TIMEOUT;
+    }
     for (int q = 0; q < count; q++) {
       if (!active[q]) continue;
       const KspState *h = &S->st_h[q];
