@@ -151,6 +151,12 @@ typedef struct {
                                temporally blocked kernel (default 0: slower
                                than two launches on GB300; the smoothed
                                iterate is bit-identical either way)        */
+  int device_loop;          /* -fsh_device_loop 0|1: the CG loop as a
+                               conditional graph node, one launch per inner
+                               solve (default 1); 0 launches a graph of
+                               graph_iters iterations per host read of the
+                               stop flag (same kernels; profilers that skip
+                               conditional bodies list every launch)        */
 } fishgpu_opts;
 
 #define FISHGPU_MAX_HIST 512

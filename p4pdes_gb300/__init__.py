@@ -72,7 +72,7 @@ class Opts(ctypes.Structure):
                 ("esteig", c_double * 4), ("richardson_scale", c_double), ("precision", c_int),
                 ("inner_rtol", c_double), ("inner_max_it", c_int), ("outer_max_it", c_int),
                 ("graph_iters", c_int), ("monitor", c_int), ("converged_reason", c_int),
-                ("snes_monitor", c_int), ("fuse_smooth", c_int)]
+                ("snes_monitor", c_int), ("fuse_smooth", c_int), ("device_loop", c_int)]
 
     @property
     def dofs(self):

@@ -534,7 +534,7 @@ static int run_ksp(fishgpu_solver *S, Hier<T> &H, KspVecs<T> v, double rtol, int
   // the state says stop (or guard bodies ran).  A driver that refuses the
   // conditional node gets the host loop: a graph of giters iterations per
   // launch and a read of the stop flag after each.
-  if (!S->gloop && !S->loop_refused)
+  if (!S->gloop && !S->loop_refused && S->o.device_loop)
     S->loop_refused = !build_loop_graph(
         s, [&] { for (int g = 0; g < S->giters; g++) enq_cg_iter<DIM, T>(S, H, v, g & 1); }, &S->st->done, nullptr,
         0u, &S->st->loops, (unsigned int)(guard + 1), &S->gloop, &S->n_loop);
@@ -1615,7 +1615,7 @@ static int group_solve(fishgpu_solver *S, const double *const *f, double *const 
     const long long guard = (long long)o.inner_max_it / S->giters + 4;
     // the CG loop on the device until every plane has stopped (plane 0's state
     // counts the bodies); the host loop is kept for a driver that refuses it
-    if (!S->gloop && !S->loop_refused)
+    if (!S->gloop && !S->loop_refused && S->o.device_loop)
       S->loop_refused = !build_loop_graph(
           s, [&] { for (int q = 0; q < S->giters; q++) enq_cg_iter<2, float>(S, S->h32, v, q & 1); }, nullptr,
           S->ndone, (unsigned int)count, &S->st[0].loops, (unsigned int)(guard + 1), &S->gloop, &S->n_loop);

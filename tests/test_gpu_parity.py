@@ -325,6 +325,24 @@ def test_zero_initial_residual_matches_the_stencil(cuda, args, prec):
     assert torch.equal(ua, ub)
 
 
+@pytest.mark.parametrize("args", [
+    "-fsh_dim 3 -fsh_problem manupoly -da_refine 4 -pc_type mg -ksp_rtol 1e-10 -fsh_precision mixed",
+    "-fsh_dim 3 -fsh_problem manuexp -da_refine 4 -pc_type mg -ksp_rtol 1e-10",
+    "-fsh_dim 2 -fsh_problem manupoly -da_refine 5 -pc_type mg -ksp_rtol 1e-10 -fsh_graph_iters 6",
+])
+def test_device_loop_matches_host_loop(cuda, args):
+    """The CG loop as a conditional graph node (one launch per inner solve)
+    runs the same kernels as the host-polled graphs: identical histories and
+    solutions."""
+    fg = fgmod()
+    u1, a = fg.solve(fg.options(args + " -fsh_device_loop 1"))
+    u0, b = fg.solve(fg.options(args + " -fsh_device_loop 0"))
+    assert a.reason == b.reason == 2 and a.its == b.its and a.outer_its == b.outer_its
+    assert a.history() == b.history()
+    import torch
+    assert torch.equal(u1, u0)
+
+
 def test_fp64_fma_rate_is_plausible(cuda):
     """The FP64 FMA probe used as the FP64 residual's roofline denominator:
     GB300's FP64 rate is ~1.2 TFLOP/s nominal, far below its FP32 rate."""
