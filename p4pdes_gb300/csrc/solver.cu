@@ -433,15 +433,14 @@ static void enq_cg_init(fishgpu_solver *S, Hier<T> &H, KspVecs<T> v, const doubl
   cudaStream_t s = S->stream;
   if constexpr (sizeof(T) == 4) {
     if (src64) {
-      v_demote_init<<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(S->fine, S->sf, S->st, src64, S->dval, v.r, v.y,
-                                                               S->red, 0);
+      v_demote_init<<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(S->fine, S->sf, S->st, src64, S->dval, v.r, S->red,
+                                                               0);
       if (!enq_pc<DIM, T>(S, H, v.r, FIN_INIT_ZZZR))
         v_dots<T><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(S->fine, S->sf, S->st, H.z, v.r, S->red, 0, FIN_INIT_ZZZR,
                                                              nullptr);
       return;
     }
   }
-  v_zero<T><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(S->fine, S->sf, v.y);
   if (S->ksp_norm == FISHGPU_NORM_UNPRECONDITIONED)
     v_dots<T><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(S->fine, S->sf, S->st, v.r, v.r, S->red, 0, FIN_INIT_RR, nullptr);
   if (!enq_pc<DIM, T>(S, H, v.r, FIN_INIT_ZZZR))
@@ -791,7 +790,7 @@ static int time_kernel_dim(fishgpu_solver *S, const char *name, int reps, double
   if (!strcmp(name, "cgp_apply") || !strcmp(name, "cg_update")) {
     KspState h;
     memset(&h, 0, sizeof(h));
-    h.i = 1;
+    h.i = 2;  // a direction update that also reads y (the first one, i = 1, starts y from 0)
     h.beta = h.betaold = h.dpi = h.bratio = 1.0;
     h.alpha = 1e-3;
     h.pend = 1;  // cgp_apply also applies a deferred y update
@@ -991,7 +990,9 @@ extern "C" int fishgpu_solver_create(const fishgpu_opts *o, void *stream, fishgp
   const size_t N = nelem(S->fine);
   const long long dofs = (long long)S->dense.plane * S->dense.mz;
   // iterations per graph launch: even, since consecutive iterations alternate the two p buffers
-  S->giters = o->graph_iters > 0 ? o->graph_iters : (dofs >= (1LL << 20) ? 2 : 4);
+  // iterations per graph body: with the device-side loop a body costs no host
+  // round trip, so short bodies waste fewer early-exit launches after the stop
+  S->giters = o->graph_iters > 0 ? o->graph_iters : (o->device_loop || dofs >= (1LL << 20) ? 2 : 4);
   S->giters += S->giters & 1;
   // FP64 form: the user's norm; mixed form: the inner CG stops on its own
   // (unpreconditioned) residual, which the refinement loop relates to the true one

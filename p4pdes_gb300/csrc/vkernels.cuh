@@ -544,6 +544,7 @@ __global__ void __launch_bounds__(256, MinBlocksLean<T>::value) v_cgp_apply(Geom
   const Wv<T> w(g);
   const bool first = !st || st->i == 0;  // no state: p = z
   const bool pend = st && st->pend && y;
+  const bool yfresh = pend && st->i == 1;  // no update has reached y yet (it is not zero-filled)
   const T a = pend ? (T)st->alpha : T(0);
   T acc = T(0);
   auto op = [&](int k, long long n, const Nb<T> &nb) {
@@ -561,8 +562,8 @@ __global__ void __launch_bounds__(256, MinBlocksLean<T>::value) v_cgp_apply(Geom
     }
     st4(pnew + n, nb.c);
     st4(wv + n, o);
-    if (pend) {
-      const V4<T> pp = ld4(pold + n), yy = ld4(y + n);
+    if (pend) {  // the first update (iteration 1) starts y from 0 without reading it
+      const V4<T> pp = ld4(pold + n), yy = yfresh ? zero4<T>() : ld4(y + n);
       st4(y + n, V4<T>{fma(a, pp.x, yy.x), fma(a, pp.y, yy.y), fma(a, pp.z, yy.z), fma(a, pp.w, yy.w)});
     }
   };
@@ -935,16 +936,28 @@ __global__ void __launch_bounds__(256) v_cg_r(Geom g, Slots s, KspState *st, con
 
 // The deferred y += alpha p of the last CG iteration, after the loop has
 // stopped (the state is done): `pend` names the buffer, 1 for p0, 2 for p1.
+// y is not zero-filled when a solve starts: an update reached it only if a
+// direction update ran after a successful FIN_PW (its >= 2), otherwise y is
+// written here from 0 (alpha p, or zeros).
+__device__ __forceinline__ bool ksp_y_written(const KspState *st) { return st->its >= 2; }
+
 template <typename T>
 __global__ void __launch_bounds__(256) v_cg_pend(Geom g, Slots s, const KspState *st, const T *__restrict__ p0,
                                                  const T *__restrict__ p1, T *__restrict__ y) {
   st = block_state(const_cast<KspState *>(st), s);
-  if (!st || !st->pend) return;
-  const T a = (T)st->alpha;
-  const T *__restrict__ pv = st->pend == 1 ? p0 : p1;
+  if (!st) return;
+  const bool written = ksp_y_written(st);
+  const int pend = st->pend;
+  if (written && !pend) return;
+  const T a = pend ? (T)st->alpha : T(0);
+  const T *__restrict__ pv = pend == 1 ? p0 : p1;
   FG_PW_BEGIN
-  const V4<T> pp = ld4(pv + n), yy = ld4(y + n);
-  st4(y + n, V4<T>{fma(a, pp.x, yy.x), fma(a, pp.y, yy.y), fma(a, pp.z, yy.z), fma(a, pp.w, yy.w)});
+  V4<T> yy = written ? ld4(y + n) : zero4<T>();
+  if (pend) {
+    const V4<T> pp = ld4(pv + n);
+    yy = V4<T>{fma(a, pp.x, yy.x), fma(a, pp.y, yy.y), fma(a, pp.z, yy.z), fma(a, pp.w, yy.w)};
+  }
+  st4(y + n, yy);
   FG_PW_END
 }
 
@@ -1016,11 +1029,12 @@ __global__ void __launch_bounds__(256) v_resid_zero0(Geom g, Slots s, const doub
 // The set-up of an inner FP32 solve from an FP64 residual in one pass:
 // r32 = (float)(r64 * (1 / sqrt(rr))) with rr = r64.r64 as stored by the
 // residual kernel (the host's 1.0 / ||r|| to the bit: sqrt and the division
-// are correctly rounded), y32 = 0, and r32.r32 reduced as v_dots<float>
-// reduces it, finalised as FIN_INIT_RR.  Replaces v_demote, v_zero and v_dots.
+// are correctly rounded) and r32.r32 reduced as v_dots<float> reduces it,
+// finalised as FIN_INIT_RR.  Replaces v_demote and v_dots (y32 is not
+// zero-filled: see v_cg_pend).
 static __global__ void __launch_bounds__(256) v_demote_init(Geom g, Slots s, KspState *st, const double *__restrict__ r,
                                                      const double *__restrict__ rr, float *__restrict__ r32,
-                                                     float *__restrict__ y32, Reducer red, int slot) {
+                                                     Reducer red, int slot) {
   if (ksp_done_v(st)) return;
   // one sqrt and division per block (FP64 is slow on this part), shared
   __shared__ double s_is;
@@ -1032,7 +1046,6 @@ static __global__ void __launch_bounds__(256) v_demote_init(Geom g, Slots s, Ksp
   const V4<double> a = ld4(r + n);
   const V4<float> o{(float)(a.x * is), (float)(a.y * is), (float)(a.z * is), (float)(a.w * is)};
   st4(r32 + n, o);
-  st4(y32 + n, zero4<float>());
   zz = fmaf(o.x, o.x, fmaf(o.y, o.y, fmaf(o.z, o.z, fmaf(o.w, o.w, zz))));
   FG_PW_END
   double v1[1] = {(double)zz};
@@ -1070,10 +1083,11 @@ static __global__ void __launch_bounds__(256) v_pend_promote(Geom g, Slots s, co
                                                       const float *__restrict__ e, double sc, double *__restrict__ y,
                                                       bool fresh) {
   const int pend = st ? st->pend : 0;
+  const bool written = st && ksp_y_written(st);  // else the inner solution starts from 0 (not stored)
   const float a = pend ? (float)st->alpha : 0.f;
   const float *__restrict__ pv = pend == 1 ? p0 : p1;
   FG_PW_BEGIN
-  V4<float> ev = ld4(e + n);
+  V4<float> ev = written ? ld4(e + n) : zero4<float>();
   if (pend) {
     const V4<float> pp = ld4(pv + n);
     ev = V4<float>{fmaf(a, pp.x, ev.x), fmaf(a, pp.y, ev.y), fmaf(a, pp.z, ev.z), fmaf(a, pp.w, ev.w)};
