@@ -637,6 +637,59 @@ __global__ void __launch_bounds__(256) k_unpack_add64(Geom g, Geom gd, Tiles tm,
   FG_POINT_LOOP_END
 }
 
+// The start of a mixed solve of user data (FISHGPU_USER f, g) from the zero
+// initial state, in one vectorised pass: u0 (g on the boundary when asked,
+// 0 elsewhere), the KSP right-hand side b = -F(u0) = beff - J u0 and its
+// b.b.  The same values as k_initial64, k_beff64 and v_resid_zero0 in turn
+// (every point the same expressions in the same order, the norm reduced as
+// v_resid_zero0 reduces it), without the beff array.
+template <int DIM>
+__global__ void __launch_bounds__(256) v_user_start(Geom g, Slots s, Prob pb, int gbdry, double *__restrict__ u0,
+                                                    double *__restrict__ b, Reducer red, int slot, double *out) {
+  const double sd = g.scdiag;
+  // the user arrays read directly: the problem-generic accessors would carry
+  // the built-in problems' FP64 transcendentals into the loop
+  const double *__restrict__ fu = pb.f, *__restrict__ gu = pb.g;
+  auto uf = [&](int i, int j, int k) { return fu[uidx(pb, i, j, k)]; };
+  auto ug = [&](int i, int j, int k) { return gu[uidx(pb, i, j, k)]; };
+  double rr = 0.0;
+  FG_PW_BEGIN
+  V4<double> uo, bo;
+#pragma unroll
+  for (int e = 0; e < 4; e++) {
+    const int i = p.i4 + e, j = p.j;
+    double uv = 0.0, bv = 0.0;
+    if (i < g.mx) {
+      if (on_bdry<DIM>(g, i, j, k)) {
+        const double gv = ug(i, j, k);
+        uv = gbdry ? gv : 0.0;
+        bv = fma(-sd, uv, g.scdiag * gv);
+      } else {
+        double v = g.vol * uf(i, j, k);
+        if (i - 1 == 0) v = fma(g.sc[0], ug(i - 1, j, k), v);
+        if (i + 1 == g.mx - 1) v = fma(g.sc[0], ug(i + 1, j, k), v);
+        if (DIM >= 2) {
+          if (j - 1 == 0) v = fma(g.sc[1], ug(i, j - 1, k), v);
+          if (j + 1 == g.my - 1) v = fma(g.sc[1], ug(i, j + 1, k), v);
+        }
+        if (DIM >= 3) {
+          if (k - 1 == 0) v = fma(g.sc[2], ug(i, j, k - 1), v);
+          if (k + 1 == g.mz - 1) v = fma(g.sc[2], ug(i, j, k + 1), v);
+        }
+        bv = v + 0.0;
+      }
+    }
+    set_el(uo, e, uv);
+    set_el(bo, e, bv);
+  }
+  st4(u0 + n, uo);
+  st4(b + n, bo);
+  rr = fma(bo.x, bo.x, fma(bo.y, bo.y, fma(bo.z, bo.z, fma(bo.w, bo.w, rr))));
+  FG_PW_END
+  double v1[1] = {rr};
+  reduce_slots<1>(v1, red, slot, nullptr, FIN_STORE, out, s);
+}
+
 static int read_vals(fishgpu_solver *S, int n) {
   FG_CUDA(cudaMemcpyAsync(S->hval, S->dval, sizeof(double) * n, cudaMemcpyDeviceToHost, S->stream));
   FG_CUDA(cudaStreamSynchronize(S->stream));
@@ -658,22 +711,31 @@ static int solve_dim(fishgpu_solver *S, double *u, fishgpu_report *rep) {
   const Launch &L = S->Lf;
   const Geom &g = S->fine;
   FG_CUDA(cudaEventRecord(S->ev0, s));
-  S->launches = 2;  // initial state, -F(u0) with its norm
-  k_initial64<DIM><<<L.grid, L.block, 0, s>>>(g, S->dense, L.tm, S->prob, o.initial_type, o.initial_gonboundary,
-                                               o.seed, u, S->u64);
-  if (!S->beff_ready) {
-    k_beff64<DIM><<<L.grid, L.block, 0, s>>>(g, L.tm, S->prob, S->beff);
-    S->launches += 1;
-    S->beff_ready = S->o.ctx.problem != FISHGPU_USER;  // user data may change between solves
-  }
   // the KSP right-hand side is -F(u0) = beff - A u0 and its norm; it solves
   // for -y and u = u0 + (-y)
   double *F = o.precision == FISHGPU_MIXED ? S->b64 : S->r64;
-  if (o.initial_type == FISHGPU_INITIAL_ZEROS)
-    v_resid_zero0<DIM><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(g, S->sf, S->beff, S->u64, F, S->red, 1, S->dval);
-  else
-    v_resid<DIM, double, true><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(g, S->sf, nullptr, S->beff, S->u64, F,
-                                                                         S->red, 1, S->dval);
+  if (o.precision == FISHGPU_MIXED && o.ctx.problem == FISHGPU_USER && o.initial_type == FISHGPU_INITIAL_ZEROS) {
+    // user data change between solves: u0, b and ||b|| in one pass (beff is
+    // not needed by the mixed form)
+    v_user_start<DIM><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(g, S->sf, S->prob, o.initial_gonboundary, S->u64,
+                                                                  F, S->red, 1, S->dval);
+    S->launches = 1;
+  } else {
+    S->launches = 2;  // initial state, -F(u0) with its norm
+    k_initial64<DIM><<<L.grid, L.block, 0, s>>>(g, S->dense, L.tm, S->prob, o.initial_type, o.initial_gonboundary,
+                                                 o.seed, u, S->u64);
+    if (!S->beff_ready) {
+      k_beff64<DIM><<<L.grid, L.block, 0, s>>>(g, L.tm, S->prob, S->beff);
+      S->launches += 1;
+      S->beff_ready = S->o.ctx.problem != FISHGPU_USER;  // user data may change between solves
+    }
+    if (o.initial_type == FISHGPU_INITIAL_ZEROS)
+      v_resid_zero0<DIM><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(g, S->sf, S->beff, S->u64, F, S->red, 1,
+                                                                     S->dval);
+    else
+      v_resid<DIM, double, true><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(g, S->sf, nullptr, S->beff, S->u64, F,
+                                                                           S->red, 1, S->dval);
+  }
   FG_CUDA(cudaGetLastError());
   int rc = read_vals(S, 1);
   if (rc) return rc;

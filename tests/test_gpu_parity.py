@@ -343,6 +343,39 @@ def test_device_loop_matches_host_loop(cuda, args):
     assert torch.equal(u1, u0)
 
 
+@pytest.mark.parametrize("args,gb", [
+    ("-fsh_dim 3 -da_grid_x 5 -da_grid_y 3 -da_grid_z 9 -da_refine 3 -pc_type mg -ksp_rtol 1e-10", 1),
+    ("-fsh_dim 2 -fsh_problem manupoly -da_refine 6 -pc_type mg -ksp_rtol 1e-10 -fsh_cx 0.5", 1),
+    ("-fsh_dim 2 -da_refine 5 -pc_type mg -ksp_rtol 1e-10 -fsh_initial_gonboundary false", 0),
+    ("-fsh_dim 1 -da_refine 7 -pc_type mg -ksp_rtol 1e-10", 1),
+])
+def test_user_data_start_matches_the_three_kernels(cuda, args, gb):
+    """A mixed solve of user f and g from the zero state starts with one fused
+    pass (u0, b = -F(u0), its norm); the same u0 given explicitly takes the
+    initial-state, beff and stencil-residual kernels.  Histories and solutions
+    agree to the bit."""
+    import torch
+    fg = fgmod()
+    oa = fg.options(args + " -fsh_precision mixed")
+    ob = fg.options(args + " -fsh_precision mixed")
+    rng = np.random.default_rng(5)
+    f = torch.from_numpy(rng.standard_normal(tuple(oa.shape))).to(cuda)
+    gd = torch.from_numpy(rng.standard_normal(tuple(oa.shape))).to(cuda)
+    for o in (oa, ob):
+        o.ctx.problem, o.ctx.f, o.ctx.g = fg.USER, f.data_ptr(), gd.data_ptr()
+    ob.initial_type = fg.INITIAL_GIVEN
+    u0 = torch.empty(oa.shape, dtype=torch.float64, device=cuda)
+    fg.InitialState(fg.info_for(oa), fg.INITIAL_ZEROS, gb, u0, oa.ctx)
+    ua, ub = torch.empty_like(u0), u0.clone()
+    with fg.Solver(oa) as s:
+        ra = s.solve(ua)
+    with fg.Solver(ob) as s:
+        rb = s.solve(ub)
+    assert ra.reason == rb.reason == 2 and ra.its == rb.its and ra.outer_its == rb.outer_its
+    assert ra.history() == rb.history() and ra.fnorm0 == rb.fnorm0
+    assert torch.equal(ua, ub)
+
+
 def test_fp64_fma_rate_is_plausible(cuda):
     """The FP64 FMA probe used as the FP64 residual's roofline denominator:
     GB300's FP64 rate is ~1.2 TFLOP/s nominal, far below its FP32 rate."""
