@@ -575,23 +575,33 @@ static int run_ksp(fishgpu_solver *S, Hier<T> &H, KspVecs<T> v, double rtol, int
 // columns eliminated): beff = scdiag*g on boundary rows; on interior rows
 // vol*f plus sc_d*g at each neighbour on the boundary -- the reference's
 // residual (poissonfunctions.c:10-19, :43-59, :86-106) rearranged.
-template <int DIM>
+// USERP: FISHGPU_USER data, read directly (the problem-generic accessors would
+// carry the built-in problems' FP64 transcendentals into the loop)
+template <int DIM, bool USERP>
 __global__ void __launch_bounds__(256) k_beff64(Geom g, Tiles tm, Prob pb, double *__restrict__ be) {
   const Range R = full_range(g);
+  auto fa = [&](int i, int j, int k) -> double {
+    if constexpr (USERP) return pb.f[uidx(pb, i, j, k)];
+    else return f_at(pb, g, i, j, k);
+  };
+  auto ga = [&](int i, int j, int k) -> double {
+    if constexpr (USERP) return pb.g[uidx(pb, i, j, k)];
+    else return g_at(pb, g, i, j, k);
+  };
   FG_POINT_LOOP_BEGIN(R)
   if (on_bdry<DIM>(g, i, j, k)) {
-    be[n] = g.scdiag * g_at(pb, g, i, j, k);
+    be[n] = g.scdiag * ga(i, j, k);
   } else {
-    double v = g.vol * f_at(pb, g, i, j, k);
-    if (i - 1 == 0) v = fma(g.sc[0], g_at(pb, g, i - 1, j, k), v);
-    if (i + 1 == g.mx - 1) v = fma(g.sc[0], g_at(pb, g, i + 1, j, k), v);
+    double v = g.vol * fa(i, j, k);
+    if (i - 1 == 0) v = fma(g.sc[0], ga(i - 1, j, k), v);
+    if (i + 1 == g.mx - 1) v = fma(g.sc[0], ga(i + 1, j, k), v);
     if (DIM >= 2) {
-      if (j - 1 == 0) v = fma(g.sc[1], g_at(pb, g, i, j - 1, k), v);
-      if (j + 1 == g.my - 1) v = fma(g.sc[1], g_at(pb, g, i, j + 1, k), v);
+      if (j - 1 == 0) v = fma(g.sc[1], ga(i, j - 1, k), v);
+      if (j + 1 == g.my - 1) v = fma(g.sc[1], ga(i, j + 1, k), v);
     }
     if (DIM >= 3) {
-      if (k - 1 == 0) v = fma(g.sc[2], g_at(pb, g, i, j, k - 1), v);
-      if (k + 1 == g.mz - 1) v = fma(g.sc[2], g_at(pb, g, i, j, k + 1), v);
+      if (k - 1 == 0) v = fma(g.sc[2], ga(i, j, k - 1), v);
+      if (k + 1 == g.mz - 1) v = fma(g.sc[2], ga(i, j, k + 1), v);
     }
     be[n] = v;
   }
@@ -725,7 +735,10 @@ static int solve_dim(fishgpu_solver *S, double *u, fishgpu_report *rep) {
     k_initial64<DIM><<<L.grid, L.block, 0, s>>>(g, S->dense, L.tm, S->prob, o.initial_type, o.initial_gonboundary,
                                                  o.seed, u, S->u64);
     if (!S->beff_ready) {
-      k_beff64<DIM><<<L.grid, L.block, 0, s>>>(g, L.tm, S->prob, S->beff);
+      if (S->prob.problem == FISHGPU_USER)
+        k_beff64<DIM, true><<<L.grid, L.block, 0, s>>>(g, L.tm, S->prob, S->beff);
+      else
+        k_beff64<DIM, false><<<L.grid, L.block, 0, s>>>(g, L.tm, S->prob, S->beff);
       S->launches += 1;
       S->beff_ready = S->o.ctx.problem != FISHGPU_USER;  // user data may change between solves
     }
