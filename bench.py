@@ -442,7 +442,7 @@ def run_ours(args):
     batch = batch_leg(torch, fg, args.batch_instances) if args.batch_instances > 0 else None
     serving = serve_leg(fg, args.serve_requests) if args.serve_requests > 0 else None
     if serving is not None:
-        # the same stream at a rate one GB300 sustains (the 2000 req/s stream offers ~2.8x its
+        # the same stream at a rate one GB300 sustains (the 2000 req/s stream offers about twice its
         # throughput, so its latencies are mostly queueing): latency without a growing queue
         serving["at_sustainable_rate"] = serve_leg(fg, max(200, args.serve_requests // 2), rate=500.0)
     c1 = c1_leg(torch, fg)
