@@ -51,30 +51,40 @@ static Range info_range(const fishgpu_info *info) {
 
 // F on the owned range.  Boundary rows scdiag*(u - g); interior rows read g
 // at boundary neighbours (c/ch6/poissonfunctions.c:10-19, :43-59, :86-106).
-template <int DIM>
+// USERP: FISHGPU_USER f and g read directly (the problem-generic accessors
+// would carry the built-in problems' FP64 transcendentals into the loop).
+template <int DIM, bool USERP>
 __global__ void __launch_bounds__(256) k_funclocal(Geom g, Range R, Tiles tm, Prob pb,
                                                    const double *__restrict__ u,
                                                    double *__restrict__ F) {
+  auto fa = [&](int i, int j, int k) -> double {
+    if constexpr (USERP) return pb.f[uidx(pb, i, j, k)];
+    else return f_at(pb, g, i, j, k);
+  };
+  auto ga = [&](int i, int j, int k) -> double {
+    if constexpr (USERP) return pb.g[uidx(pb, i, j, k)];
+    else return g_at(pb, g, i, j, k);
+  };
   FG_POINT_LOOP_BEGIN(R)
   const double uc = u[n];
   if (on_bdry<DIM>(g, i, j, k)) {
-    double v = uc - g_at(pb, g, i, j, k);
+    double v = uc - ga(i, j, k);
     F[n] = v * g.scdiag;
   } else {
-    const double ue = (i + 1 == g.mx - 1) ? g_at(pb, g, i + 1, j, k) : u[n + 1];
-    const double uw = (i - 1 == 0) ? g_at(pb, g, i - 1, j, k) : u[n - 1];
+    const double ue = (i + 1 == g.mx - 1) ? ga(i + 1, j, k) : u[n + 1];
+    const double uw = (i - 1 == 0) ? ga(i - 1, j, k) : u[n - 1];
     if (DIM == 1) {
-      F[n] = pb.cx * (2.0 * uc - uw - ue) / g.h[0] - g.h[0] * f_at(pb, g, i, j, k);
+      F[n] = pb.cx * (2.0 * uc - uw - ue) / g.h[0] - g.h[0] * fa(i, j, k);
     } else {
-      const double un = (j + 1 == g.my - 1) ? g_at(pb, g, i, j + 1, k) : u[n + g.pitch];
-      const double us = (j - 1 == 0) ? g_at(pb, g, i, j - 1, k) : u[n - g.pitch];
+      const double un = (j + 1 == g.my - 1) ? ga(i, j + 1, k) : u[n + g.pitch];
+      const double us = (j - 1 == 0) ? ga(i, j - 1, k) : u[n - g.pitch];
       if (DIM == 2) {
-        F[n] = g.scdiag * uc - g.sc[0] * (uw + ue) - g.sc[1] * (us + un) - g.vol * f_at(pb, g, i, j, k);
+        F[n] = g.scdiag * uc - g.sc[0] * (uw + ue) - g.sc[1] * (us + un) - g.vol * fa(i, j, k);
       } else {
-        const double uu = (k + 1 == g.mz - 1) ? g_at(pb, g, i, j, k + 1) : u[n + g.plane];
-        const double ud = (k - 1 == 0) ? g_at(pb, g, i, j, k - 1) : u[n - g.plane];
+        const double uu = (k + 1 == g.mz - 1) ? ga(i, j, k + 1) : u[n + g.plane];
+        const double ud = (k - 1 == 0) ? ga(i, j, k - 1) : u[n - g.plane];
         F[n] = g.scdiag * uc - g.sc[0] * (uw + ue) - g.sc[1] * (us + un) - g.sc[2] * (uu + ud) -
-               g.vol * f_at(pb, g, i, j, k);
+               g.vol * fa(i, j, k);
       }
     }
   }
@@ -157,7 +167,10 @@ static int funclocal(const fishgpu_info *info, const double *au, double *aF, con
   pb.uplane = g.plane;
   const Range R = info_range(info);
   const Launch L = launch_box(DIM, info->xm, info->ym, info->zm);
-  k_funclocal<DIM><<<L.grid, L.block, 0, (cudaStream_t)stream>>>(g, R, L.tm, pb, au, aF);
+  if (pb.problem == FISHGPU_USER)
+    k_funclocal<DIM, true><<<L.grid, L.block, 0, (cudaStream_t)stream>>>(g, R, L.tm, pb, au, aF);
+  else
+    k_funclocal<DIM, false><<<L.grid, L.block, 0, (cudaStream_t)stream>>>(g, R, L.tm, pb, au, aF);
   return cudaGetLastError() == cudaSuccess ? FISHGPU_OK : FISHGPU_ERR_CUDA;
 }
 
