@@ -125,6 +125,18 @@ def test_default_options_are_fish_defaults(built):
     assert list(o.esteig) == [0.0, 0.1, 0.0, 1.1]
 
 
+def test_build_options_parse_and_default(built):
+    """Options of this build beside fish's: precision form, inner tolerances,
+    graph shape, device-side loop, fused post-smoother."""
+    import p4pdes_gb300 as fg
+    o = fg.options([])
+    assert o.device_loop == 1 and o.fuse_smooth == 0 and o.precision == fg.FP64
+    o = fg.options("-fsh_precision mixed -fsh_inner_rtol 1e-7 -fsh_inner_max_it 50 -fsh_outer_max_it 9 "
+                   "-fsh_graph_iters 6 -fsh_device_loop 0 -fsh_fuse_smooth 1")
+    assert o.precision == fg.MIXED and o.inner_rtol == 1e-7 and o.inner_max_it == 50 and o.outer_max_it == 9
+    assert o.graph_iters == 6 and o.device_loop == 0 and o.fuse_smooth == 1
+
+
 @pytest.mark.parametrize("args,grid,levels", [
     ("-fsh_dim 2 -da_refine 7 -pc_type mg", (257, 257, 1), 8),
     ("-fsh_dim 3 -da_refine 8", (513, 513, 513), 9),
