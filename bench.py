@@ -12,7 +12,8 @@ copied in and u copied out every step.  Every vector (1.08 GB in FP64) is far
 larger than L2, so no flush is needed between steps.
 
 --impl reference times the CPU restatement of the same solve (the oracle:
-FP64 CG + MG, OpenMP on all host cores) on a bounded sample (129^3).
+FP64 CG + MG, OpenMP on all host cores) on the same 513^3 workload, one whole
+solve per step (about 6-7 s each on 16 Arm cores); its warm-up is one solve.
 Multi-GPU: replicas only (independent solves per rank, no collective on the
 data path); value = DOFs of all ranks / max time over ranks.
 """
@@ -30,7 +31,6 @@ sys.path.insert(0, ROOT)
 METRIC = "Poisson DOF/s to 1e-10 rel. residual, mixed vs FP64 MG, HBM %peak; p99 latency"
 BASE_ARGS = ("-fsh_dim 3 -fsh_problem manupoly -da_refine {r} -pc_type mg -mg_levels_ksp_type chebyshev "
              "-mg_levels_pc_type jacobi -ksp_rtol 1e-10 -ksp_norm_type unpreconditioned")
-CPU_SAMPLE_REFINE = 7  # 257^3 for the CPU baseline sample
 
 
 def peaks():
@@ -82,11 +82,13 @@ class Clocks:
                 "reasons": reasons, "samples": len(self.rows)}
 
 
-def cpu_baseline(steps=None, budget_s=12.0):
-    """Oracle (FP64 CG+MG, OpenMP) on a 129^3 sample; returns (DOF/s, info)."""
+def cpu_baseline(refine, steps=None, budget_s=12.0):
+    """Oracle (FP64 CG+MG, OpenMP on all host cores) on the bench's workload
+    (-da_refine `refine`); `steps` whole solves, or as many as fit `budget_s`
+    (at least one, at most five).  Returns (DOF/s, info)."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import _oracle as orc
-    o = orc.options(BASE_ARGS.format(r=CPU_SAMPLE_REFINE).split())
+    o = orc.options(BASE_ARGS.format(r=refine).split())
     dofs = o.grid.mx * o.grid.my * o.grid.mz
     times = []
     t_all = time.perf_counter()
@@ -102,8 +104,9 @@ def cpu_baseline(steps=None, budget_s=12.0):
             break
     tot = sum(times)
     return dofs * n / tot, {"cores": orc.lib().or_num_threads(), "solves": n, "its": rep["its"], "dofs": dofs,
-                            "sample": "oracle FP64 CG+MG V(2,2) Chebyshev/Jacobi, 3D %d^3 manupoly, rtol 1e-10, "
-                                      "%d solve(s), %.2f s" % (o.grid.mx, n, tot)}
+                            "errinf": rep["errinf"], "s_per_solve": tot / n,
+                            "sample": "oracle FP64 CG+MG V(2,2) Chebyshev/Jacobi, 3D %d^3 manupoly, rtol 1e-10 "
+                                      "(unpreconditioned norm), %d whole solve(s), %.2f s" % (o.grid.mx, n, tot)}
 
 
 def job_rate(units_per_rank, ms_local, world, device):
@@ -136,17 +139,18 @@ def run_reference(args):
         return
     W = max(0, args.warmup)
     K = max(1, args.steps)
-    for _ in range(min(W, 1)):
-        cpu_baseline(steps=1)
-    v, info = cpu_baseline(steps=K)
+    for _ in range(min(W, 1)):  # one untimed solve warms the host (pages, threads)
+        cpu_baseline(args.refine, steps=1)
+    v, info = cpu_baseline(args.refine, steps=K)
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "DOF/s", "n_gpus": args.gpus,
             "steps": K, "warmup": W, "ms_per_step": 1e3 * info["dofs"] / v,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (manufactured manupoly problem)",
-            "config": {"workload": WORKLOAD, "dofs": 513 ** 3, "levels": 9,
+            "config": {"workload": WORKLOAD, "dofs": info["dofs"], "levels": args.refine + 1,
                        "parallelism": "host cores (OpenMP)",
-                       "measured_on": "a 257^3 sample of this workload per step (the whole 513^3 solve takes "
-                                      "minutes on the host); DOF/s of the sample",
+                       "measured_on": "the whole workload: one %d^3 solve per step, %d timed steps after %d "
+                                      "untimed solve(s)" % (round(info["dofs"] ** (1 / 3)), K, min(W, 1)),
+                       "its": info["its"], "errinf": info["errinf"],
                        "implementation": "CPU restatement (oracle) of the reference's CG + MG V(2,2) "
                                          "Chebyshev/Jacobi path, FP64; PETSc is not available to build "
                                          "the reference's own fish"},
@@ -438,7 +442,7 @@ def run_ours(args):
         traffic = tr.get(rk, {}).get("dram_bytes_per_launch")
     except Exception:
         pass
-    cpu_v, cpu_info = cpu_baseline()
+    cpu_v, cpu_info = cpu_baseline(args.refine, steps=1)  # one whole solve of the same workload
     batch = batch_leg(torch, fg, args.batch_instances) if args.batch_instances > 0 else None
     serving = serve_leg(fg, args.serve_requests) if args.serve_requests > 0 else None
     if serving is not None:
@@ -465,6 +469,10 @@ def run_ours(args):
             "fp64": {"ms": ms64, "dof_per_s": N / (ms64 * 1e-3), "its": rep_64.its,
                      "true_rel_resid": rep_64.true_rel_resid, "errinf": err_64[0], "err2h": err_64[1]},
             "mixed_over_fp64": (N / (ms / K * 1e-3)) / (N / (ms64 * 1e-3)),
+            # like for like against the oracle's FP64 solve of the same workload on the host cores
+            "fp64_over_cpu": (N / (ms64 * 1e-3)) / cpu_v,
+            "mixed_over_cpu": value / cpu_v,
+            "e2e_over_cpu": e2e / cpu_v,
             "error_ratio_mixed_over_fp64": err_mx[0] / err_64[0],
             "batch": batch,
             "serving": serving,

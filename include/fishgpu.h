@@ -92,9 +92,10 @@ int Poisson3DOperatorApply_gpu(const fishgpu_info *info, const double *p, double
    in a static device array of 4096 doubles + 256 B held by every GPU that
    loads the library.  Launches that would need more partial sums are rejected
    with FISHGPU_ERR_ARG.  All calls on a device share the array, so calls that
-   overlap on the GPU race; the first call on a device looks up the array's
-   address and should come before any stream capture.  This entry point has
-   no counterpart in the reference. */
+   overlap on the GPU race.  `stream` must belong to the current device (the
+   array's address is that device's), else FISHGPU_ERR_ARG; the first call on
+   a device may load the library's device code and should come before any
+   stream capture.  This entry point has no counterpart in the reference. */
 int PoissonOperatorApplyNoAlloc_gpu(const fishgpu_info *info, const double *p, double *q,
                                     double *pq_dot, const fishgpu_ctx *user, void *stream);
 
@@ -157,6 +158,11 @@ typedef struct {
                                graph_iters iterations per host read of the
                                stop flag (same kernels; profilers that skip
                                conditional bodies list every launch)        */
+  int loop_cap;             /* -fsh_loop_cap: bodies (graph_iters CG
+                               iterations each) the solve loop may run
+                               before it gives up with FISHGPU_ERR_TIMEOUT
+                               (0: max_it / graph_iters + 5, which a solve
+                               that stops on its own never reaches)         */
 } fishgpu_opts;
 
 #define FISHGPU_MAX_HIST 512
@@ -362,6 +368,10 @@ typedef struct {
   int mg_levels;          /* 0: down to 3x3                                  */
   int monitor_degree;     /* -ms_monitor: quadrature degree 1..3, 0 = off    */
   int snes_monitor, converged_reason, ksp_converged_reason; /* driver flags  */
+  int loop_cap;           /* -ms_loop_cap: bodies the inner BiCGStab loop may
+                             run per Newton step before the solve gives up
+                             with FISHGPU_ERR_TIMEOUT (0: ksp_max_it / iterations
+                             per body + 5, never reached by a solve that stops) */
 } fishgpu_ms_opts;
 
 #define FISHGPU_MS_MAX_GRIDS 12

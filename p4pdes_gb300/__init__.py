@@ -72,7 +72,7 @@ class Opts(ctypes.Structure):
                 ("esteig", c_double * 4), ("richardson_scale", c_double), ("precision", c_int),
                 ("inner_rtol", c_double), ("inner_max_it", c_int), ("outer_max_it", c_int),
                 ("graph_iters", c_int), ("monitor", c_int), ("converged_reason", c_int),
-                ("snes_monitor", c_int), ("fuse_smooth", c_int), ("device_loop", c_int)]
+                ("snes_monitor", c_int), ("fuse_smooth", c_int), ("device_loop", c_int), ("loop_cap", c_int)]
 
     @property
     def dofs(self):
@@ -137,7 +137,7 @@ class MsOpts(ctypes.Structure):
                 ("rtol", c_double), ("atol", c_double), ("stol", c_double), ("max_it", c_int),
                 ("line_search", c_int), ("ksp_rtol", c_double), ("ksp_max_it", c_int), ("pc_type", c_int),
                 ("mg_levels", c_int), ("monitor_degree", c_int), ("snes_monitor", c_int),
-                ("converged_reason", c_int), ("ksp_converged_reason", c_int)]
+                ("converged_reason", c_int), ("ksp_converged_reason", c_int), ("loop_cap", c_int)]
 
 
 class MsReport(ctypes.Structure):

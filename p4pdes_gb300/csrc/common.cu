@@ -214,6 +214,7 @@ extern "C" int fishgpu_opts_parse(fishgpu_opts *o, int argc, const char *const *
     else if (!strcmp(k, "-fsh_graph_iters")) { NEEDV(); o->graph_iters = atoi(v); }
     else if (!strcmp(k, "-fsh_fuse_smooth")) { NEEDV(); o->fuse_smooth = atoi(v) != 0; }
     else if (!strcmp(k, "-fsh_device_loop")) { NEEDV(); o->device_loop = atoi(v) != 0; }
+    else if (!strcmp(k, "-fsh_loop_cap")) { NEEDV(); o->loop_cap = atoi(v); }
     else if (!strcmp(k, "-da_refine")) { NEEDV(); refine = atoi(v); }
     else if (!strcmp(k, "-da_grid_x")) { NEEDV(); base[0] = atoi(v); }
     else if (!strcmp(k, "-da_grid_y")) { NEEDV(); base[1] = atoi(v); }

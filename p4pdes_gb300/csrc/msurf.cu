@@ -1076,6 +1076,7 @@ extern "C" int fishgpu_ms_opts_parse(fishgpu_ms_opts *o, int argc, const char *c
     else if (!strcmp(k, "-snes_max_it")) rc = num(a, nullptr, &o->max_it);
     else if (!strcmp(k, "-ksp_rtol")) rc = num(a, &o->ksp_rtol, nullptr);
     else if (!strcmp(k, "-ksp_max_it")) rc = num(a, nullptr, &o->ksp_max_it);
+    else if (!strcmp(k, "-ms_loop_cap")) rc = num(a, nullptr, &o->loop_cap);
     else if (!strcmp(k, "-pc_mg_levels")) rc = num(a, nullptr, &o->mg_levels);
     else if (!strcmp(k, "-pc_type")) {
       if (a + 1 >= argc) return FISHGPU_ERR_ARG;
@@ -1173,7 +1174,7 @@ extern "C" int fishgpu_ms_solver_create(const fishgpu_ms_opts *o, void *stream, 
     return FISHGPU_ERR_ARG;  // bratu2D.c:109-113
   if (o->ctx.model == FISHGPU_NL_BRATU && o->monitor_degree) return FISHGPU_ERR_ARG;
   if (!(o->rtol >= 0) || !(o->atol >= 0) || !(o->stol >= 0) || o->max_it < 0 || !(o->ksp_rtol > 0) ||
-      o->ksp_max_it < 1 || o->monitor_degree < 0 || o->monitor_degree > 3)
+      o->ksp_max_it < 1 || o->monitor_degree < 0 || o->monitor_degree > 3 || o->loop_cap < 0)
     return FISHGPU_ERR_ARG;
   if (o->pc_type != FISHGPU_PC_MG && o->pc_type != FISHGPU_PC_NONE) return FISHGPU_ERR_UNSUPPORTED;
   int ndev = 0;
@@ -1268,7 +1269,8 @@ extern "C" int fishgpu_ms_solver_create(const fishgpu_ms_opts *o, void *stream, 
     MS_FAIL(capture(S, L, true, &L.g_init));
     // the BiCGStab loop on the device (bodies of giters iterations until the
     // inner solve stops, capped); the host-polled graph if the driver refuses
-    const unsigned int cap = (unsigned int)(std::max(1, o->ksp_max_it) / L.giters + 5);
+    const unsigned int cap =
+        o->loop_cap > 0 ? (unsigned int)o->loop_cap : (unsigned int)(std::max(1, o->ksp_max_it) / L.giters + 5);
     if (!build_loop_graph(S->stream, [&] { for (int k = 0; k < L.giters; k++) enq_bicg_iter(S, L); },
                           &S->st->k.done, nullptr, 0u, &S->st->k.loops, cap, &L.g_loop, &L.n_loop))
       MS_FAIL(capture(S, L, false, &L.g_iter));

@@ -21,11 +21,14 @@
 //     wrong dot products.  The ticket is cleared before every launch; the
 //     partial sums need no clearing (each block writes its own slot before the
 //     last block reads it);
-//   * the first call on each device looks the array's device address up with
-//     cudaGetSymbolAddress, with that device current, and caches it; make that
-//     first call before any stream capture on that device.
-#include <mutex>
-
+//   * every call looks the array's device address up with
+//     cudaGetSymbolAddress on the current device (cheap, allocates nothing),
+//     so the address stays right after a device reset; the first call on a
+//     device may load the library's device code there, so make it before any
+//     stream capture on that device;
+//   * the stream must belong to the current device (the array's address is
+//     that device's); a stream of another device is rejected with
+//     FISHGPU_ERR_ARG.
 #include "common.cuh"
 
 namespace fg {
@@ -33,27 +36,32 @@ namespace fg {
 constexpr int NOALLOC_MAX_BLOCKS = 4096;
 constexpr size_t NOALLOC_TICKET_BYTES = 256;
 constexpr size_t NOALLOC_BYTES = sizeof(double) * NOALLOC_MAX_BLOCKS + NOALLOC_TICKET_BYTES;
+// launch_box caps every grid at MAX_BLOCKS blocks; the array must hold that many partial sums
+static_assert(MAX_BLOCKS <= NOALLOC_MAX_BLOCKS, "the scratch array holds fewer partial sums than a launch may need");
 
 // Host code must not use this name as an address: it is a host-side stand-in.
 static __device__ __align__(256) unsigned char g_apply_scratch[NOALLOC_BYTES];
 
-static std::mutex g_noalloc_mu;
-static void *g_noalloc_ptr[64];
-
-// Device address of g_apply_scratch on the current device (looked up once).
-static int noalloc_scratch(unsigned char **out) {
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return FISHGPU_ERR_NODEVICE;
-  std::lock_guard<std::mutex> lk(g_noalloc_mu);
-  if (!g_noalloc_ptr[dev]) {
-    void *p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_apply_scratch) != cudaSuccess || !p) {
-      cudaGetLastError();
-      return FISHGPU_ERR_CUDA;
-    }
-    g_noalloc_ptr[dev] = p;
+// Device address of g_apply_scratch on the current device, after checking
+// that `s` belongs to that device (the legacy and per-thread default streams
+// belong to whichever device is current).
+static int noalloc_scratch(cudaStream_t s, unsigned char **out) {
+  int dev = 0, sdev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return FISHGPU_ERR_NODEVICE;
   }
-  *out = (unsigned char *)g_noalloc_ptr[dev];
+  if (cudaStreamGetDevice(s, &sdev) != cudaSuccess) {
+    cudaGetLastError();
+    return FISHGPU_ERR_ARG;
+  }
+  if (sdev != dev) return FISHGPU_ERR_ARG;
+  void *p = nullptr;
+  if (cudaGetSymbolAddress(&p, g_apply_scratch) != cudaSuccess || !p) {
+    cudaGetLastError();
+    return FISHGPU_ERR_CUDA;
+  }
+  *out = (unsigned char *)p;
   return FISHGPU_OK;
 }
 
@@ -85,7 +93,7 @@ static int apply_noalloc(const fishgpu_info *info, const double *p, double *q, d
   }
   if ((int)L.grid.x > NOALLOC_MAX_BLOCKS) return FISHGPU_ERR_ARG;  // more partial sums than the array holds
   unsigned char *base = nullptr;
-  int rc = noalloc_scratch(&base);
+  int rc = noalloc_scratch(s, &base);
   if (rc) return rc;
   Reducer red;
   red.partials = (double *)base;

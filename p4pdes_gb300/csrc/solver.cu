@@ -528,7 +528,7 @@ static int run_ksp(fishgpu_solver *S, Hier<T> &H, KspVecs<T> v, double rtol, int
   cudaGraphExec_t *gi = from64 < 0 ? &S->gexec_init : &S->gexec_init64[from64 & 1];
   const double *src64 = from64 < 0 ? nullptr : from64 ? S->r64 : S->b64;
   if (!*gi && (rc = capture(S, [&] { enq_cg_init<DIM, T>(S, H, v, src64); }, gi, &S->n_init))) return rc;
-  const long long guard = (long long)max_it / S->giters + 4;
+  const long long guard = S->o.loop_cap > 0 ? (long long)S->o.loop_cap - 1 : (long long)max_it / S->giters + 4;
   // The loop on the device: one launch runs bodies of giters iterations until
   // the state says stop (or guard bodies ran).  A driver that refuses the
   // conditional node gets the host loop: a graph of giters iterations per
@@ -1023,6 +1023,7 @@ static int validate_opts(const fishgpu_opts *o) {
   if (o->pc_type < 0 || o->pc_type > FISHGPU_PC_MG) return FISHGPU_ERR_UNSUPPORTED;
   if (o->smooth_its < 1 || o->max_it < 0 || o->mg_cycles < 1 || o->mg_cycles > 2) return FISHGPU_ERR_ARG;
   if (o->precision != FISHGPU_FP64 && o->precision != FISHGPU_MIXED) return FISHGPU_ERR_ARG;
+  if (o->loop_cap < 0) return FISHGPU_ERR_ARG;
   if (o->precision == FISHGPU_MIXED && o->pc_type != FISHGPU_PC_MG) return FISHGPU_ERR_UNSUPPORTED;
   if (o->initial_type < 0 || o->initial_type > FISHGPU_INITIAL_GIVEN) return FISHGPU_ERR_ARG;
   if (!(o->rtol >= 0) || !(o->atol >= 0) || !(o->dtol > 0)) return FISHGPU_ERR_ARG;

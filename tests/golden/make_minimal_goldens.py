@@ -55,4 +55,6 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python %s <path of the p4pdes source tree>" % sys.argv[0])
+    main(sys.argv[1])

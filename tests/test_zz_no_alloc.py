@@ -3,8 +3,11 @@ apply + dot, for callers that may not allocate device memory once running.
 
 It is called through the C ABI twice in a row (the static scratch keeps the
 previous call's contents, so the second call checks that nothing stale leaks
-into the dot product) and compared with Poisson{1,2,3}DOperatorApply_gpu to
-the tolerance the other apply tests use: 1e-13 relative for q, 1e-12 for p.q.
+into the dot product) and compared with Poisson{1,2,3}DOperatorApply_gpu.  Both
+run the same kernel with the same launch shape and summing order, so q and p.q
+must be equal to the bit.  The allocating apply takes its scratch from the
+device's default memory pool (cudaMallocAsync); the pool's high-water mark,
+reset to zero before a no-alloc call, must still be zero after it.
 The file sorts last so a run that stops at the first failure has already run
 every other test.
 """
@@ -15,12 +18,33 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
+POOL_USED_MEM_HIGH = 0x8  # cudaMemPoolAttrUsedMemHigh
+
+
+def _cudart():
+    rt = ctypes.CDLL("libcudart.so.13")
+    rt.cudaDeviceGetDefaultMemPool.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int]
+    rt.cudaMemPoolSetAttribute.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+    rt.cudaMemPoolGetAttribute.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+    return rt
+
+
+def _pool_high(rt, pool, reset=False):
+    v = ctypes.c_uint64(0)
+    if reset:
+        assert rt.cudaMemPoolSetAttribute(pool, POOL_USED_MEM_HIGH, ctypes.byref(v)) == 0
+    assert rt.cudaMemPoolGetAttribute(pool, POOL_USED_MEM_HIGH, ctypes.byref(v)) == 0
+    return v.value
+
 
 @pytest.mark.parametrize("dim,m", [(1, (257, 1, 1)), (2, (129, 65, 1)), (3, (65, 33, 129))])
 def test_no_alloc_apply_matches_allocating_apply(cuda, dim, m):
     import torch
     import p4pdes_gb300 as fg
     lib = fg.load()
+    rt = _cudart()
+    pool = ctypes.c_void_p()
+    assert rt.cudaDeviceGetDefaultMemPool(ctypes.byref(pool), cuda.index or 0) == 0
     inf = fg.Info()
     inf.dim, (inf.mx, inf.my, inf.mz) = dim, m
     inf.xm, inf.ym, inf.zm = m
@@ -35,16 +59,20 @@ def test_no_alloc_apply_matches_allocating_apply(cuda, dim, m):
         p = torch.randn(shape, dtype=torch.float64, generator=gen).cuda()
         q_ref = torch.empty_like(p)
         d_ref = torch.zeros(1, dtype=torch.float64, device=cuda)
+        q = torch.full_like(p, float("nan"))
+        d = torch.full((1,), float("nan"), dtype=torch.float64, device=cuda)
+        torch.cuda.synchronize()
+        _pool_high(rt, pool, reset=True)
         rc = getattr(lib, "Poisson%dDOperatorApply_gpu" % dim)(ctypes.byref(inf), p.data_ptr(), q_ref.data_ptr(),
                                                               d_ref.data_ptr(), ctypes.byref(ctx), stream)
         assert rc == 0
-        q = torch.full_like(p, float("nan"))
-        d = torch.full((1,), float("nan"), dtype=torch.float64, device=cuda)
+        torch.cuda.synchronize()
+        assert _pool_high(rt, pool) > 0, "the allocating apply did not draw on the default pool"
+        _pool_high(rt, pool, reset=True)
         rc = lib.PoissonOperatorApplyNoAlloc_gpu(ctypes.byref(inf), p.data_ptr(), q.data_ptr(), d.data_ptr(),
                                                  ctypes.byref(ctx), stream)
         assert rc == 0, "call %d" % call
         torch.cuda.synchronize()
-        qr, qn = q_ref.cpu().numpy(), q.cpu().numpy()
-        assert np.max(np.abs(qn - qr)) <= 1e-13 * np.max(np.abs(qr)), "call %d" % call
-        dr = d_ref.item()
-        assert abs(d.item() - dr) <= 1e-12 * abs(dr), (call, d.item(), dr)
+        assert _pool_high(rt, pool) == 0, "call %d allocated from the default pool" % call
+        assert np.array_equal(q.cpu().numpy(), q_ref.cpu().numpy()), "call %d" % call
+        assert d.item() == d_ref.item(), (call, d.item(), d_ref.item())
