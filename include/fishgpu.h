@@ -163,6 +163,20 @@ typedef struct {
                                before it gives up with FISHGPU_ERR_TIMEOUT
                                (0: max_it / graph_iters + 5, which a solve
                                that stops on its own never reaches)         */
+  double first_floor_scale; /* -fsh_first_floor: mixed form, the first
+                               refinement step's inner solve stops at
+                               first_floor * kappa * pi h * 2^-24 (the FP32
+                               floor of the accurate form; default 0.3)    */
+  int inner_accurate;       /* -fsh_inner_accurate -1|0|1: mixed form, 1: the
+                               inner FP32 CG applies J in difference form and
+                               accumulates its solution in FP64, which moves
+                               the FP32 floor of a refinement step from
+                               ~kappa 2^-24 to ~kappa pi h 2^-24; 0: standard
+                               FP32 apply and FP32 correction (8 fewer bytes
+                               per node and iteration); -1 (default): 1 when
+                               the standard form's two refinement steps
+                               cannot reach rtol, that is when rtol <
+                               0.3 kappa 2^-24 inner_rtol                  */
 } fishgpu_opts;
 
 #define FISHGPU_MAX_HIST 512
@@ -235,7 +249,8 @@ int fishgpu_solve_host(const fishgpu_opts *o, const double *f_host, const double
 
 /* Times `reps` launches of one solver kernel on the finest level with the
    solver's resident data (CUDA events on the solver's stream).  Names:
-   "smooth", "smooth_first", "smooth_dots", "smooth_zero", "post2", "cgp_apply", "cg_update",
+   "smooth", "smooth_first", "smooth_dots", "smooth_zero", "post2", "cgp_apply",
+   "cgp_apply_acc" (mixed form: the accurate inner form's apply), "cg_update",
    "resid", "apply", "restrict", "prolong", "residual64".  Reports the mean ms
    per launch and the algorithmic bytes one launch moves. */
 int fishgpu_solver_time_kernel(fishgpu_solver *s, const char *name, int reps,
@@ -262,6 +277,7 @@ typedef struct {
   int mg_cycles;          /* 1 = V, 2 = W                                 */
   double esteig[4];
   int tune;               /* pick each level's block size by timing       */
+  int inner_accurate;     /* as fishgpu_opts.inner_accurate, per size group (default -1) */
 } fishgpu_batch_opts;
 
 typedef struct {

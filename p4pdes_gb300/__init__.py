@@ -72,7 +72,8 @@ class Opts(ctypes.Structure):
                 ("esteig", c_double * 4), ("richardson_scale", c_double), ("precision", c_int),
                 ("inner_rtol", c_double), ("inner_max_it", c_int), ("outer_max_it", c_int),
                 ("graph_iters", c_int), ("monitor", c_int), ("converged_reason", c_int),
-                ("snes_monitor", c_int), ("fuse_smooth", c_int), ("device_loop", c_int), ("loop_cap", c_int)]
+                ("snes_monitor", c_int), ("fuse_smooth", c_int), ("device_loop", c_int), ("loop_cap", c_int),
+                ("first_floor_scale", c_double), ("inner_accurate", c_int)]
 
     @property
     def dofs(self):
@@ -100,7 +101,7 @@ class Report(ctypes.Structure):
 class BatchOpts(ctypes.Structure):
     _fields_ = [("rtol", c_double), ("atol", c_double), ("inner_rtol", c_double), ("inner_max_it", c_int),
                 ("outer_max_it", c_int), ("smooth_its", c_int), ("mg_cycles", c_int), ("esteig", c_double * 4),
-                ("tune", c_int)]
+                ("tune", c_int), ("inner_accurate", c_int)]
 
 
 class BatchReport(ctypes.Structure):

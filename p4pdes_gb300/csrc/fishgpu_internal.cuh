@@ -68,6 +68,12 @@ struct KspState {
   unsigned int loops;  // bodies run by the device-side solve loop (graph_loop.cuh)
   double dp, rnorm0, ttol, beta, betaold, dpi, dpiold, alpha;
   double bratio;  // beta / betaold for the next direction update (one division, in the finaliser)
+  // Mixed form, solution accumulated in FP64: the inner solve's updates go
+  // straight into the outer FP64 solution as y64 += (yscale * alpha) p, with
+  // yscale the refinement step's residual norm; yfresh: y64 holds nothing yet
+  // (the first refinement step), so the first update writes it without reading
+  double yscale;
+  int yfresh;
   double acc[4];
   unsigned int *ndone;  // batches: incremented once when this instance stops
   double hist[FISHGPU_MAX_HIST];

@@ -68,6 +68,15 @@ static Geom padded(Geom g) {
   return g;
 }
 
+// Whether the inner FP32 solves of the mixed form use the accurate form
+// (v_cgp_apply's ACC): asked for (1, 0), or, by default (-1), when the
+// standard form cannot finish in two refinement steps: its first step stops
+// near 0.3 kappa 2^-24 and a second one reduces by inner_rtol at best.
+static bool inner_accurate_for(int choice, double rtol, double inner_rtol, double kappa) {
+  if (choice >= 0) return choice != 0;
+  return rtol < 0.3 * kappa * 0x1.0p-24 * inner_rtol;
+}
+
 // Exact spectrum ends of D^{-1}A for the constant-diagonal stencil:
 // 1 -+ sum_d (2 sc_d / scdiag) cos(pi/(m_d-1)); boundary rows give 1.
 static void spectrum(const Geom &g, double *lmin, double *lmax) {
@@ -424,6 +433,7 @@ static bool enq_pc(fishgpu_solver *S, Hier<T> &H, const T *r, int dots) {
 template <typename T>
 struct KspVecs {
   T *r, *p[2], *w, *y;  // p: two buffers, the direction update reads one and writes the other
+  double *y64 = nullptr;  // FP32 solves with FP64 accumulation: the outer solution the updates go to
 };
 
 // src64 (FP32 solves of the mixed form, unpreconditioned norm): the FP64
@@ -457,8 +467,24 @@ static void enq_cg_iter(fishgpu_solver *S, Hier<T> &H, KspVecs<T> v, int par) {
   bool planes = false;
   if constexpr (DIM == 2) {
     if (S->batch) {
-      v_cgp_apply<DIM, T, true><<<slot_blocks(S->sfst), S->sfst.chunk, 0, s>>>(S->fine, S->sfst, st, H.z, pold, pnew, v.w,
-                                                                       v.y, S->red, 0);
+      if constexpr (sizeof(T) == 4) {
+        if (v.y64)
+          v_cgp_apply<DIM, T, true, true><<<slot_blocks(S->sfst), S->sfst.chunk, 0, s>>>(
+              S->fine, S->sfst, st, H.z, pold, pnew, v.w, v.y64, S->red, 0);
+        else
+          v_cgp_apply<DIM, T, true><<<slot_blocks(S->sfst), S->sfst.chunk, 0, s>>>(S->fine, S->sfst, st, H.z, pold, pnew,
+                                                                           v.w, v.y, S->red, 0);
+      } else {
+        v_cgp_apply<DIM, T, true><<<slot_blocks(S->sfst), S->sfst.chunk, 0, s>>>(S->fine, S->sfst, st, H.z, pold, pnew, v.w,
+                                                                         v.y, S->red, 0);
+      }
+      planes = true;
+    }
+  }
+  if constexpr (sizeof(T) == 4) {
+    if (!planes && v.y64) {  // accurate inner form: difference-form apply, FP64 accumulation
+      v_cgp_apply<DIM, T, false, true><<<slot_blocks(S->sfst), S->sfst.chunk, 0, s>>>(
+          S->fine, S->sfst, st, H.z, pold, pnew, v.w, v.y64, S->red, 0);
       planes = true;
     }
   }
@@ -504,7 +530,8 @@ static int capture(fishgpu_solver *S, F enq, cudaGraphExec_t *exec, long long *n
   return FISHGPU_OK;
 }
 
-static void reset_state(fishgpu_solver *S, double rtol, double atol, double dtol, int max_it, int norm) {
+static void reset_state(fishgpu_solver *S, double rtol, double atol, double dtol, int max_it, int norm,
+                        double yscale = 0.0, bool yfresh = false) {
   KspState *h = S->st_h;
   memset(h, 0, sizeof(*h));
   h->rtol = rtol;
@@ -513,15 +540,19 @@ static void reset_state(fishgpu_solver *S, double rtol, double atol, double dtol
   h->max_it = max_it;
   h->norm_type = norm;
   h->betaold = 1.0;
+  h->yscale = yscale;
+  h->yfresh = yfresh ? 1 : 0;
 }
 
 // CG solve of J y = r from y = 0 (r is overwritten), on the solver's stream.
 // from64 >= 0 (FP32 solves of the mixed form): r is set up from the FP64
 // residual in b64 (0) or r64 (1), scaled by 1/||.|| from dval[0], and the
 // last deferred y += alpha p is left to the caller (v_pend_promote).
+// yscale, yfresh: the FP64 accumulation of the accurate inner form (v.y64).
 // The caller reads S->st_h for its, reason and the history.
 template <int DIM, typename T>
-static int run_ksp(fishgpu_solver *S, Hier<T> &H, KspVecs<T> v, double rtol, int max_it, int from64 = -1) {
+static int run_ksp(fishgpu_solver *S, Hier<T> &H, KspVecs<T> v, double rtol, int max_it, int from64 = -1,
+                   double yscale = 0.0, bool yfresh = false) {
   cudaStream_t s = S->stream;
   const int norm = S->ksp_norm;  // the captured graphs compute this norm
   int rc;
@@ -541,7 +572,7 @@ static int run_ksp(fishgpu_solver *S, Hier<T> &H, KspVecs<T> v, double rtol, int
       (rc = capture(S, [&] { for (int g = 0; g < S->giters; g++) enq_cg_iter<DIM, T>(S, H, v, g & 1); },
                     &S->gexec, &S->n_iter)))
     return rc;
-  reset_state(S, rtol, S->o.atol, S->o.dtol, max_it, norm);
+  reset_state(S, rtol, S->o.atol, S->o.dtol, max_it, norm, yscale, yfresh);
   FG_CUDA(cudaMemcpyAsync(S->st, S->st_h, sizeof(KspState), cudaMemcpyHostToDevice, s));
   FG_CUDA(cudaGraphLaunch(*gi, s));
   S->launches += S->n_init;
@@ -765,15 +796,24 @@ static int solve_dim(fishgpu_solver *S, double *u, fishgpu_report *rep) {
     double rn = bn;
     int reason = 0, its = 0, outer = 0, nh = 0;
     rep->hist[nh++] = rn;
-    KspVecs<float> v{S->r32, {S->p32, S->q32}, S->w32, S->y32};
-    // The first correction is smooth and carries the FP32 rounding of its
-    // storage, which J amplifies by up to its condition number: the true
-    // residual cannot drop below ~kappa * 2^-24 of ||b|| in that step, so the
-    // first inner solve stops there.  kappa is the exact ratio of the extreme
-    // eigenvalues of D^{-1}J on the fine grid.
     double lmin, lmax;
     spectrum(g, &lmin, &lmax);
-    const double first_floor = fmin(0.5, 0.3 * (lmax / fmax(lmin, 1e-300)) * 0x1.0p-24);
+    const double kappa = lmax / fmax(lmin, 1e-300);
+    const bool accurate = inner_accurate_for(o.inner_accurate, o.rtol, o.inner_rtol, kappa);
+    KspVecs<float> v{S->r32, {S->p32, S->q32}, S->w32, S->y32, accurate ? S->y64 : nullptr};
+    // The first correction is smooth and carries the FP32 rounding of its
+    // storage and of the FP32 apply's diagonal term, which J amplifies by up
+    // to its condition number: the true residual cannot drop below ~kappa *
+    // 2^-24 of ||b|| in that step, so the first inner solve stops there.  The
+    // accurate form (difference-form apply, FP64 accumulation) leaves the
+    // rounding of the differences, ~kappa * pi h * 2^-24 (h: the finest grid
+    // spacing in units of the longest side).  kappa is the exact ratio of the
+    // extreme eigenvalues of D^{-1}J on the fine grid.
+    int mmax = g.mx;
+    if (g.dim >= 2) mmax = std::max(mmax, g.my);
+    if (g.dim >= 3) mmax = std::max(mmax, g.mz);
+    const double first_floor = accurate ? fmin(0.5, o.first_floor_scale * kappa * (M_PI / (mmax - 1)) * 0x1.0p-24)
+                                        : fmin(0.5, 0.3 * kappa * 0x1.0p-24);
     while (true) {
       if (isnan(rn) || isinf(rn)) { reason = R_DIVERGED_NANORINF; break; }
       if (rn <= ttol) { reason = rn < o.atol ? R_CONVERGED_ATOL : R_CONVERGED_RTOL; break; }
@@ -784,7 +824,8 @@ static int solve_dim(fishgpu_solver *S, double *u, fishgpu_report *rep) {
       if (outer == 0) irtol = fmax(irtol, first_floor);
       if (irtol > 0.5) irtol = 0.5;
       // r32 = r / ||r|| (r: b64 in the first step, r64 after) inside the KSP set-up
-      if ((rc = run_ksp<DIM, float>(S, S->h32, v, irtol, o.inner_max_it, outer == 0 ? 0 : 1))) return rc;
+      if ((rc = run_ksp<DIM, float>(S, S->h32, v, irtol, o.inner_max_it, outer == 0 ? 0 : 1, rn, outer == 0)))
+        return rc;
       const KspState *h = S->st_h;
       its += h->its;
       if (outer < FISHGPU_MAX_OUTER) rep->inner_its[outer] = h->its;
@@ -793,10 +834,14 @@ static int solve_dim(fishgpu_solver *S, double *u, fishgpu_report *rep) {
         reason = h->reason;
         break;
       }
-      // y32 += alpha p (deferred), y64 += rn y32; y64 = 0 before the first
-      // step: that step writes it without reading
-      v_pend_promote<<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(g, S->sf, S->st, S->p32, S->q32, S->y32, rn, S->y64,
-                                                                outer == 0);
+      if (accurate) {  // the last deferred y64 += rn alpha p (the others went to y64 in the loop)
+        v_pend_acc<<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(g, S->sf, S->st, S->p32, S->q32, S->y64);
+      } else {
+        // y32 += alpha p (deferred), y64 += rn y32; y64 = 0 before the first
+        // step: that step writes it without reading
+        v_pend_promote<<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(g, S->sf, S->st, S->p32, S->q32, S->y32, rn, S->y64,
+                                                                  outer == 0);
+      }
       // FP64 true residual r = b - J y and its norm
       v_resid<DIM, double, true><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(g, S->sf, nullptr, S->b64, S->y64,
                                                                            S->r64, S->red, 1, S->dval);
@@ -862,7 +907,7 @@ static int time_kernel_dim(fishgpu_solver *S, const char *name, int reps, double
   // (beta/betaold = 1, a small alpha); p.w > 0 keeps it running, and a stop
   // (non-finite data) is reported
   KspState *tst = nullptr;
-  if (!strcmp(name, "cgp_apply") || !strcmp(name, "cg_update")) {
+  if (!strcmp(name, "cgp_apply") || !strcmp(name, "cgp_apply_acc") || !strcmp(name, "cg_update")) {
     KspState h;
     memset(&h, 0, sizeof(h));
     h.i = 2;  // a direction update that also reads y (the first one, i = 1, starts y from 0)
@@ -908,6 +953,11 @@ static int time_kernel_dim(fishgpu_solver *S, const char *name, int reps, double
       else
         v_cgp_apply<DIM, double><<<gb, sl.chunk, 0, s>>>(g, sl, tst, ld.X[0], S->p64, S->q64, S->w64, S->y64, S->red, 1);
       *bytes = 6.0 * sz * N;
+    } else if (!strcmp(name, "cgp_apply_acc")) {  // the same with the difference-form apply and y in FP64
+      if (!mixed) return FISHGPU_ERR_UNSUPPORTED;
+      v_cgp_apply<DIM, float, false, true><<<gb, sl.chunk, 0, s>>>(g, sl, tst, lf.X[0], S->p32, S->q32, S->w32, S->y64,
+                                                                 S->red, 1);
+      *bytes = (4.0 + 4.0 + 8.0 + 4.0 + 4.0 + 8.0) * N;
     } else if (!strcmp(name, "post2")) {  // both post-smoothing steps fused: reads b, x0, writes x2
       if constexpr (DIM == 3) {
         if (!mixed) return FISHGPU_ERR_UNSUPPORTED;
@@ -1023,7 +1073,8 @@ static int validate_opts(const fishgpu_opts *o) {
   if (o->pc_type < 0 || o->pc_type > FISHGPU_PC_MG) return FISHGPU_ERR_UNSUPPORTED;
   if (o->smooth_its < 1 || o->max_it < 0 || o->mg_cycles < 1 || o->mg_cycles > 2) return FISHGPU_ERR_ARG;
   if (o->precision != FISHGPU_FP64 && o->precision != FISHGPU_MIXED) return FISHGPU_ERR_ARG;
-  if (o->loop_cap < 0) return FISHGPU_ERR_ARG;
+  if (o->loop_cap < 0 || !(o->first_floor_scale > 0) || o->inner_accurate < -1 || o->inner_accurate > 1)
+    return FISHGPU_ERR_ARG;
   if (o->precision == FISHGPU_MIXED && o->pc_type != FISHGPU_PC_MG) return FISHGPU_ERR_UNSUPPORTED;
   if (o->initial_type < 0 || o->initial_type > FISHGPU_INITIAL_GIVEN) return FISHGPU_ERR_ARG;
   if (!(o->rtol >= 0) || !(o->atol >= 0) || !(o->dtol > 0)) return FISHGPU_ERR_ARG;
@@ -1530,6 +1581,7 @@ static int group_create(const fishgpu_batch_opts &bo, int n, int count, fishgpu_
   o.mg_cycles = bo.mg_cycles;
   for (int q = 0; q < 4; q++) o.esteig[q] = bo.esteig[q];
   o.graph_iters = 2;
+  o.inner_accurate = bo.inner_accurate;
   o.norm_type = FISHGPU_NORM_UNPRECONDITIONED;
   fishgpu_solver *S = new fishgpu_solver();
   S->o = o;
@@ -1640,11 +1692,16 @@ static int group_solve(fishgpu_solver *S, const double *const *f, double *const 
     bn[q] = rn[q] = sqrt(S->hval[2 * q]);
     ttol[q] = fmax(o.rtol * bn[q], o.atol);
   }
+  // the first step's FP32 floor, as in solve_dim (y64 is zero-filled above,
+  // so the accurate form's updates always read it: yfresh = 0)
   double lmin, lmax;
   spectrum(g, &lmin, &lmax);
-  const double first_floor = fmin(0.5, 0.3 * (lmax / fmax(lmin, 1e-300)) * 0x1.0p-24);
+  const double kappa = lmax / fmax(lmin, 1e-300);
+  const bool accurate = inner_accurate_for(o.inner_accurate, o.rtol, o.inner_rtol, kappa);
+  const double first_floor = accurate ? fmin(0.5, o.first_floor_scale * kappa * (M_PI / (g.mx - 1)) * 0x1.0p-24)
+                                      : fmin(0.5, 0.3 * kappa * 0x1.0p-24);
   std::vector<double> hs(count), his(count);
-  KspVecs<float> v{S->r32, {S->p32, S->q32}, S->w32, S->y32};
+  KspVecs<float> v{S->r32, {S->p32, S->q32}, S->w32, S->y32, accurate ? S->y64 : nullptr};
   for (int step = 0;; step++) {
     int nact = 0;
     for (int q = 0; q < count; q++) {
@@ -1672,6 +1729,7 @@ static int group_solve(fishgpu_solver *S, const double *const *f, double *const 
         double irtol = fmax(o.inner_rtol, 0.5 * ttol[q] / rn[q]);
         if (step == 0) irtol = fmax(irtol, first_floor);
         h->rtol = fmin(irtol, 0.5);
+        h->yscale = rn[q];
         hs[q] = rn[q];
         his[q] = 1.0 / rn[q];
       } else {
@@ -1715,12 +1773,17 @@ static int group_solve(fishgpu_solver *S, const double *const *f, double *const 
         S->launches += S->n_iter;
       }
     }
-    v_cg_pend<float><<<gb, S->sf.chunk, 0, s>>>(g, S->sf, S->st, v.p[0], v.p[1], v.y);
-    S->launches += 1;
-    FG_CUDA(cudaMemcpyAsync(S->st_h, S->st, sizeof(KspState) * count, cudaMemcpyDeviceToHost, s));
-    v_promote_add<<<gb, S->sf.chunk, 0, s>>>(g, S->sf, S->y32, S->scl, 0.0, S->y64);
+    if (accurate) {  // the last deferred y64 += scale alpha p (the others went to y64 in the loop)
+      v_pend_acc<<<gb, S->sf.chunk, 0, s>>>(g, S->sf, S->st, v.p[0], v.p[1], S->y64);
+      FG_CUDA(cudaMemcpyAsync(S->st_h, S->st, sizeof(KspState) * count, cudaMemcpyDeviceToHost, s));
+    } else {
+      v_cg_pend<float><<<gb, S->sf.chunk, 0, s>>>(g, S->sf, S->st, v.p[0], v.p[1], v.y);
+      FG_CUDA(cudaMemcpyAsync(S->st_h, S->st, sizeof(KspState) * count, cudaMemcpyDeviceToHost, s));
+      v_promote_add<<<gb, S->sf.chunk, 0, s>>>(g, S->sf, S->y32, S->scl, 0.0, S->y64);
+      S->launches += 1;
+    }
     v_resid<2, double><<<gb, S->sf.chunk, 0, s>>>(g, S->sf, nullptr, S->b64, S->y64, S->r64);
-    S->launches += 3;
+    S->launches += 2;
     if ((rc = plane_norms(S, S->r64))) return rc;  // synchronises: st_h holds the planes' states
     if (S->gloop) {
       S->launches += (long long)S->st_h[0].loops * S->n_loop;
@@ -1771,6 +1834,7 @@ extern "C" int fishgpu_batch_opts_default(fishgpu_batch_opts *o) {
   o->esteig[2] = 0.0;
   o->esteig[3] = 1.1;
   o->tune = 1;
+  o->inner_accurate = -1;
   return FISHGPU_OK;
 }
 
@@ -1784,7 +1848,8 @@ extern "C" int fishgpu_batch_destroy(fishgpu_batch *B) {
 extern "C" int fishgpu_batch_create(const fishgpu_batch_opts *o, int ninst, const int *n, fishgpu_batch **out) {
   if (!o || ninst < 1 || !n || !out) return FISHGPU_ERR_ARG;
   *out = nullptr;
-  if (!(o->rtol >= 0) || o->inner_max_it < 1 || o->smooth_its < 1 || o->mg_cycles < 1 || o->mg_cycles > 2)
+  if (!(o->rtol >= 0) || o->inner_max_it < 1 || o->smooth_its < 1 || o->mg_cycles < 1 || o->mg_cycles > 2 ||
+      o->inner_accurate < -1 || o->inner_accurate > 1)
     return FISHGPU_ERR_ARG;
   std::map<int, std::vector<int>> bysize;
   for (int q = 0; q < ninst; q++) {

@@ -51,6 +51,13 @@ template <typename T>
 __device__ __forceinline__ V4<T> add4(const V4<T> &a, const V4<T> &b) {
   return V4<T>{a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w};
 }
+// (c - a) + (c - b) per element: the y- or z-part of the operator in
+// difference form (see apply_diff_el)
+template <typename T>
+__device__ __forceinline__ V4<T> dsum4(const V4<T> &c, const V4<T> &a, const V4<T> &b) {
+  return V4<T>{(c.x - a.x) + (c.x - b.x), (c.y - a.y) + (c.y - b.y), (c.z - a.z) + (c.z - b.z),
+               (c.w - a.w) + (c.w - b.w)};
+}
 template <typename T>
 __device__ __forceinline__ T el(const V4<T> &v, int e) {
   return e == 0 ? v.x : e == 1 ? v.y : e == 2 ? v.z : v.w;
@@ -173,8 +180,8 @@ template <typename T>
 struct Nb {
   V4<T> c;   // centre values
   T l, r;    // x-neighbours of element 0 (i4-1) and element 3 (i4+4)
-  V4<T> ys;  // sum of the y-neighbours that are interior nodes
-  V4<T> zs;  // sum of the z-neighbours that are interior nodes
+  V4<T> ys;  // sum of the y-neighbours that are interior nodes (difference form: (c - s) + (c - n))
+  V4<T> zs;  // sum of the z-neighbours that are interior nodes (difference form: (c - d) + (c - u))
   bool jkb;  // the slot's row or plane is on the boundary
 };
 
@@ -201,7 +208,9 @@ struct AxpySrc {
 };
 
 // Loads everything but the z-window for plane k; shuffles need all lanes.
-template <int DIM, typename T, class Src>
+// DIFF: ys holds the difference form (c - s) + (c - n) of the y-part, with
+// neighbours that are boundary nodes taken as 0 (see apply_diff_el).
+template <int DIM, typename T, class Src, bool DIFF = false>
 __device__ __forceinline__ void load_xy(const Geom &g, const SlotPos &p, const Src &x, long long n, const V4<T> &c,
                                         Nb<T> &nb) {
   const int lane = threadIdx.x & 31;
@@ -216,7 +225,7 @@ __device__ __forceinline__ void load_xy(const Geom &g, const SlotPos &p, const S
     const bool hs = p.j - 1 > 0, hn = p.j + 1 < g.my - 1;
     V4<T> s4 = (p.in && hs) ? x.v4(n - g.pitch) : zero4<T>();
     V4<T> n4 = (p.in && hn) ? x.v4(n + g.pitch) : zero4<T>();
-    nb.ys = add4(s4, n4);
+    nb.ys = DIFF ? dsum4(c, s4, n4) : add4(s4, n4);
   } else {
     nb.ys = zero4<T>();
   }
@@ -237,6 +246,27 @@ __device__ __forceinline__ T resid_el(const Geom &g, const Wv<T> &w, const Nb<T>
   if (DIM >= 2) s = fma(w.sy, el(nb.ys, e), s);
   if (DIM >= 3) s = fma(w.sz, el(nb.zs, e), s);
   return fma(-w.sd, xc, s);
+}
+
+// (A x) at element e in difference form, from neighbour data assembled with
+// DIFF: interior rows sum_d sc_d ((x - x_-) + (x - x_+)) with neighbours on the
+// boundary taken as 0, which is A x exactly because scdiag = 2 sum_d sc_d.
+// For the smooth vectors of an inner Krylov solve the differences of nearby
+// values are exact in FP32, so the rounding error is of the order eps * h
+// |grad x| instead of eps * scdiag |x|: the FP32 apply keeps its accuracy
+// when the result is small against its terms (a smooth x, whose A x cancels
+// to O(h^2) of them).  Boundary rows: scdiag x.
+template <int DIM, typename T>
+__device__ __forceinline__ T apply_diff_el(const Geom &g, const Wv<T> &w, const Nb<T> &nb, int e, int i, bool jkb) {
+  const T xc = el(nb.c, e);
+  if (jkb || i == 0 || i == g.mx - 1) return w.sd * xc;
+  const T xl = e == 0 ? nb.l : el(nb.c, e - 1);
+  const T xr = e == 3 ? nb.r : el(nb.c, e + 1);
+  const T a = (xc - (i - 1 > 0 ? xl : T(0))) + (xc - (i + 1 < g.mx - 1 ? xr : T(0)));
+  T s = w.sx * a;
+  if (DIM >= 2) s = fma(w.sy, el(nb.ys, e), s);
+  if (DIM >= 3) s = fma(w.sz, el(nb.zs, e), s);
+  return s;
 }
 
 __device__ __forceinline__ bool ksp_done_v(const KspState *st) { return st && __ldcg(&st->done); }
@@ -319,7 +349,7 @@ __device__ __forceinline__ bool jk_bdry(const Geom &g, int dim, int j, int k) {
 // plain form, the y-neighbour rows from the register window instead of
 // loads, in the plain form's order (south + north).  Every thread runs ry
 // steps (the shuffles need all lanes); rows past the grid are skipped.
-template <typename T, class Op, class Src>
+template <typename T, bool DIFF, class Op, class Src>
 __device__ __forceinline__ void march_rows(const Geom &g, const Slots &s, const SlotPos &p, const Src &x, Op &op) {
   const int lane = threadIdx.x & 31;
   const long long base = (long long)p.k0 * g.plane + p.i4;
@@ -341,7 +371,8 @@ __device__ __forceinline__ void march_rows(const Geom &g, const Slots &s, const 
     nb.l = l;
     nb.r = r;
     const bool hs = j - 1 > 0, hn = j + 1 < g.my - 1;
-    nb.ys = add4(hs ? xs : zero4<T>(), hn ? xn : zero4<T>());
+    nb.ys = DIFF ? dsum4(xc, hs ? xs : zero4<T>(), hn ? xn : zero4<T>())
+                 : add4(hs ? xs : zero4<T>(), hn ? xn : zero4<T>());
     nb.zs = zero4<T>();
     nb.jkb = j == 0 || j == g.my - 1;
     if (valid) op(p.k0, n, nb);
@@ -350,11 +381,12 @@ __device__ __forceinline__ void march_rows(const Geom &g, const Slots &s, const 
   }
 }
 
-template <int DIM, typename T, class Op, class Src>
-__device__ __forceinline__ void march_src(const Geom &g, const Slots &s, const SlotPos &p, const Src &x, Op &op) {
+// DIFF: the y- and z-sums of the neighbour data in difference form (load_xy)
+template <int DIM, typename T, bool DIFF, class Op, class Src>
+__device__ __forceinline__ void march_core(const Geom &g, const Slots &s, const SlotPos &p, const Src &x, Op &op) {
   if constexpr (DIM == 2) {
     if (s.ry) {
-      march_rows<T>(g, s, p, x, op);
+      march_rows<T, DIFF>(g, s, p, x, op);
       return;
     }
   }
@@ -368,10 +400,11 @@ __device__ __forceinline__ void march_src(const Geom &g, const Slots &s, const S
     V4<T> zu = zero4<T>();
     if (DIM >= 3 && p.in && k + 1 < g.mz) zu = x.v4(n + g.plane);
     Nb<T> nb;
-    load_xy<DIM, T>(g, p, x, n, zc, nb);
+    load_xy<DIM, T, Src, DIFF>(g, p, x, n, zc, nb);
     if (DIM >= 3) {
       const bool hd = k - 1 > 0, hu = k + 1 < g.mz - 1;
-      nb.zs = add4(hd ? zd : zero4<T>(), hu ? zu : zero4<T>());
+      nb.zs = DIFF ? dsum4(zc, hd ? zd : zero4<T>(), hu ? zu : zero4<T>())
+                   : add4(hd ? zd : zero4<T>(), hu ? zu : zero4<T>());
     } else {
       nb.zs = zero4<T>();
     }
@@ -380,6 +413,11 @@ __device__ __forceinline__ void march_src(const Geom &g, const Slots &s, const S
     zd = zc;
     zc = zu;
   }
+}
+
+template <int DIM, typename T, class Op, class Src>
+__device__ __forceinline__ void march_src(const Geom &g, const Slots &s, const SlotPos &p, const Src &x, Op &op) {
+  march_core<DIM, T, false>(g, s, p, x, op);
 }
 
 template <int DIM, typename T, class Op>
@@ -534,18 +572,36 @@ __global__ void __launch_bounds__(256, MinBlocks<T>::value) v_apply_dot(Geom g, 
 // update costs y's read and write only, and v_cg_r no longer reads p and y.
 // alpha is still the previous iteration's: FIN_PW replaces it only after
 // every block has finished.
-template <int DIM, typename T, bool PL = false>
+// ACC (FP32 inner solves of the mixed form): w = A p in difference form
+// (apply_diff_el) and the solution update in FP64 straight into the outer
+// solution, y64 += (yscale * alpha) p_old (the state's yscale and yfresh), so
+// that neither the apply nor the FP32 storage of the correction limits the
+// true residual an inner solve reaches to ~kappa * 2^-24.
+template <typename T, bool ACC>
+struct CgY {
+  using type = T;
+};
+template <typename T>
+struct CgY<T, true> {
+  using type = double;
+};
+
+template <int DIM, typename T, bool PL = false, bool ACC = false>
 __global__ void __launch_bounds__(256, MinBlocksLean<T>::value) v_cgp_apply(Geom g, Slots s, KspState *st, const T *__restrict__ z,
                                                    const T *__restrict__ pold, T *__restrict__ pnew,
-                                                   T *__restrict__ wv, T *__restrict__ y, Reducer red, int slot) {
+                                                   T *__restrict__ wv, typename CgY<T, ACC>::type *__restrict__ y,
+                                                   Reducer red, int slot) {
+  using YT = typename CgY<T, ACC>::type;
   st = block_state_sel<PL>(st, s);
   if (ksp_done_v(st)) return;
   const SlotPos p = slot_pos_st<DIM>(g, s);
   const Wv<T> w(g);
   const bool first = !st || st->i == 0;  // no state: p = z
   const bool pend = st && st->pend && y;
-  const bool yfresh = pend && st->i == 1;  // no update has reached y yet (it is not zero-filled)
-  const T a = pend ? (T)st->alpha : T(0);
+  // no update has reached y yet (it is not zero-filled); ACC: nor has an
+  // earlier refinement step
+  const bool yfresh = pend && st->i == 1 && (!ACC || st->yfresh);
+  const YT a = pend ? (ACC ? (YT)(st->yscale * st->alpha) : (YT)st->alpha) : YT(0);
   T acc = T(0);
   auto op = [&](int k, long long n, const Nb<T> &nb) {
     const bool jkb = nb.jkb;
@@ -555,7 +611,8 @@ __global__ void __launch_bounds__(256, MinBlocksLean<T>::value) v_cgp_apply(Geom
       const int i = p.i4 + e;
       T v = T(0);
       if (i < g.mx) {
-        v = -resid_el<DIM, T>(g, w, nb, e, i, jkb, T(0));
+        if constexpr (ACC) v = apply_diff_el<DIM, T>(g, w, nb, e, i, jkb);
+        else v = -resid_el<DIM, T>(g, w, nb, e, i, jkb, T(0));
         acc = fma(el(nb.c, e), v, acc);
       }
       set_el(o, e, v);
@@ -563,14 +620,16 @@ __global__ void __launch_bounds__(256, MinBlocksLean<T>::value) v_cgp_apply(Geom
     st4(pnew + n, nb.c);
     st4(wv + n, o);
     if (pend) {  // the first update (iteration 1) starts y from 0 without reading it
-      const V4<T> pp = ld4(pold + n), yy = yfresh ? zero4<T>() : ld4(y + n);
-      st4(y + n, V4<T>{fma(a, pp.x, yy.x), fma(a, pp.y, yy.y), fma(a, pp.z, yy.z), fma(a, pp.w, yy.w)});
+      const V4<T> pp = ld4(pold + n);
+      const V4<YT> yy = yfresh ? zero4<YT>() : ld4(y + n);
+      st4(y + n, V4<YT>{fma(a, (YT)pp.x, yy.x), fma(a, (YT)pp.y, yy.y), fma(a, (YT)pp.z, yy.z),
+                        fma(a, (YT)pp.w, yy.w)});
     }
   };
   // the first iteration (p = z) and the others (p = z + beta/betaold p_old)
   // march separately, so that no load of the common case tests `first`
-  if (first) march_src<DIM, T>(g, s, p, ArraySrc<T>{z}, op);
-  else march_src<DIM, T>(g, s, p, AxpySrc<T>{z, pold, (T)st->bratio}, op);
+  if (first) march_core<DIM, T, ACC>(g, s, p, ArraySrc<T>{z}, op);
+  else march_core<DIM, T, ACC>(g, s, p, AxpySrc<T>{z, pold, (T)st->bratio}, op);
   double v1[1] = {(double)acc};
   reduce_sel<1, PL>(v1, red, slot, st, FIN_PW, nullptr, s);
 }
@@ -1050,6 +1109,32 @@ static __global__ void __launch_bounds__(256) v_demote_init(Geom g, Slots s, Ksp
   FG_PW_END
   double v1[1] = {(double)zz};
   reduce_slots<1>(v1, red, slot, st, FIN_INIT_RR, nullptr, s);
+}
+
+// The end of an inner FP32 solve whose updates accumulate in FP64 (the ACC
+// form of v_cgp_apply): the last deferred update y64 += (yscale * alpha) p.
+// y64 is read unless nothing has reached it yet (no update in this inner
+// solve and the state's yfresh: the first refinement step), in which case it
+// is written from 0.  Per plane for a batch.
+static __global__ void __launch_bounds__(256) v_pend_acc(Geom g, Slots s, const KspState *st,
+                                                  const float *__restrict__ p0, const float *__restrict__ p1,
+                                                  double *__restrict__ y) {
+  st = block_state(const_cast<KspState *>(st), s);
+  if (!st) return;
+  const bool keep = ksp_y_written(st) || !st->yfresh;
+  const int pend = st->pend;
+  if (keep && !pend) return;
+  const double a = pend ? st->yscale * st->alpha : 0.0;
+  const float *__restrict__ pv = pend == 1 ? p0 : p1;
+  FG_PW_BEGIN
+  V4<double> yy = keep ? ld4(y + n) : zero4<double>();
+  if (pend) {
+    const V4<float> pp = ld4(pv + n);
+    yy = V4<double>{fma(a, (double)pp.x, yy.x), fma(a, (double)pp.y, yy.y), fma(a, (double)pp.z, yy.z),
+                    fma(a, (double)pp.w, yy.w)};
+  }
+  st4(y + n, yy);
+  FG_PW_END
 }
 
 // r32 = (float)(r64 * inv_s); inv_s per plane for a batch (scale[plane])

@@ -164,3 +164,41 @@ def run_main(argv):
                        env=dict(os.environ, OMP_NUM_THREADS="1"))
     assert p.returncode == 0, p.stderr
     return p.stdout
+
+
+def weights(g):
+    """Stencil weights of the oracle's residual (poissonfunctions.c:35-40 in 2D,
+    :76-82 in 3D): off-diagonal sc per dimension and the diagonal 2 * sum(sc)."""
+    h = [g.Lx / (g.mx - 1), g.Ly / (g.my - 1) if g.dim >= 2 else 1.0, g.Lz / (g.mz - 1) if g.dim >= 3 else 1.0]
+    c = [g.cx, g.cy, g.cz]
+    if g.dim == 2:
+        sc = [c[0] * h[1] / h[0], c[1] * h[0] / h[1]]
+    elif g.dim == 3:
+        vol = h[0] * h[1] * h[2]
+        sc = [c[d] * vol / (h[d] * h[d]) for d in range(3)]
+    else:
+        raise ValueError("weights: 2D and 3D grids only")
+    return sc, 2.0 * sum(sc)
+
+
+def exact_solve_dst(g, b):
+    """The exact solve of or_exact_solve (sine-transform diagonalisation of the
+    Jacobian: boundary rows x = b / scdiag, interior x = S Lambda^-1 S b), with
+    scipy's orthonormal DST-I for the transforms instead of dense sine
+    matrices, so that grids of 513^3 nodes solve in seconds.  2D and 3D."""
+    from scipy import fft
+    sc, scdiag = weights(g)
+    x = b / scdiag
+    inner = (slice(1, -1), slice(1, -1), slice(1, -1)) if g.dim == 3 else (slice(None), slice(1, -1), slice(1, -1))
+    axes = (0, 1, 2) if g.dim == 3 else (1, 2)
+    a = fft.dstn(b[inner], type=1, norm="ortho", axes=axes, workers=-1)
+    lam = 0.0
+    for d in range(g.dim):  # axis of dimension d: x is the last axis
+        n = b.shape[2 - d] - 2
+        ld = sc[d] * (2.0 - 2.0 * np.cos(np.pi * np.arange(1, n + 1) / (n + 1)))
+        shp = [1, 1, 1]
+        shp[2 - d] = n
+        lam = lam + ld.reshape(shp)
+    a /= lam
+    x[inner] = fft.dstn(a, type=1, norm="ortho", axes=axes, workers=-1, overwrite_x=True)
+    return x

@@ -449,3 +449,26 @@ def test_fish_driver_replays_golden(cuda, rec):
     got = [l for l in p.stdout.splitlines() if "error |u-uexact|" in l or "SNES Function norm" in l
            or l.startswith("problem ")]
     assert got == want
+
+
+def test_accurate_inner_form_needs_fewer_refinement_steps(cuda):
+    """The accurate inner form (difference-form FP32 apply, inner solution
+    accumulated in FP64) lifts the FP32 floor of the first refinement step
+    from ~kappa 2^-24 to ~kappa pi h 2^-24: at 257^3 its first step reaches a
+    true residual below what the standard form's can, so the solve needs
+    fewer FP64 residuals; both forms keep the FP64 form's error."""
+    fg = fgmod()
+    base = ("-fsh_dim 3 -fsh_problem manupoly -da_refine 7 -pc_type mg -ksp_rtol 1e-10 "
+            "-ksp_norm_type unpreconditioned")
+    _, r64 = fg.solve(fg.options(base))
+    _, std = fg.solve(fg.options(base + " -fsh_precision mixed -fsh_inner_accurate 0"))
+    _, acc = fg.solve(fg.options(base + " -fsh_precision mixed -fsh_inner_accurate 1"))
+    # a first inner solve asked for 3e-6 of kappa pi h 2^-24 (~2e-6 here): the accurate form gets there
+    _, deep = fg.solve(fg.options(base + " -fsh_precision mixed -fsh_inner_accurate 1 -fsh_first_floor 0.1"))
+    for r in (std, acc, deep):
+        assert r.reason == 2 and r.true_rel_resid <= 1e-10
+        assert r.errinf <= 1.01 * r64.errinf and r.err2h <= 1.01 * r64.err2h
+    h_std, h_deep = std.history(), deep.history()
+    assert h_std[1] / h_std[0] > 1e-4   # the standard form's first step stops at its floor, ~kappa 2^-24
+    assert h_deep[1] / h_deep[0] < 1e-5  # measured 3.3e-7
+    assert acc.outer_its == 2 and std.outer_its == 3

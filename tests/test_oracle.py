@@ -214,3 +214,18 @@ def test_oracle_is_deterministic_across_threads():
                            env=dict(os.environ, OMP_NUM_THREADS=nt))
         outs.append(p.stdout)
     assert outs[0] == outs[1]
+
+
+@pytest.mark.parametrize("dim,m,c,L", [(2, (17, 9), (1.0, 0.5, 1.0), (1.0, 2.0, 1.0)),
+                                       (3, (9, 17, 5), (1.0, 2.0, 0.3), (1.0, 1.0, 3.0)),
+                                       (3, (33, 33, 33), (1.0, 1.0, 1.0), (1.0, 1.0, 1.0))])
+def test_fft_exact_solve_equals_the_dense_sine_transform_solve(dim, m, c, L):
+    """The FFT form of the exact solve (used for grids too large for the
+    dense transforms) gives the dense form's solution to rounding."""
+    g = orc.grid(dim, *m, problem=orc.ZERO, c=c, L=L)
+    b = np.random.default_rng(dim).standard_normal(orc.shape(g))
+    x1 = orc.exact_solve(g, b)
+    x2 = orc.exact_solve_dst(g, b)
+    assert np.max(np.abs(x1 - x2)) <= 1e-12 * np.max(np.abs(x1))
+    # and it solves the system: the oracle's operator maps it back to b
+    assert np.max(np.abs(orc.apply(g, x2) - b)) <= 1e-10 * np.max(np.abs(b))
