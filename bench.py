@@ -378,8 +378,8 @@ def run_ours(args):
     rk = args.roofline_kernel
     kms, kbytes = s_mx.time_kernel(rk, 20)
     kernel_table = {}
-    for name in ("smooth", "smooth_first", "smooth_dots", "smooth_zero", "cgp_apply", "cg_update", "resid", "restrict",
-                 "prolong", "residual64"):
+    for name in ("smooth", "smooth_first", "smooth_dots", "smooth_zero", "cgp_apply", "cgp_apply_acc", "cg_update",
+                 "resid", "restrict", "resid_restrict", "prolong", "residual64"):
         try:
             t, b = s_mx.time_kernel(name, 10)
         except fg.FishError:
@@ -500,7 +500,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--refine", type=int, default=8, help="-da_refine (8: 513^3)")
-    ap.add_argument("--roofline-kernel", default="cgp_apply")
+    ap.add_argument("--roofline-kernel", default="cgp_apply_acc")
     ap.add_argument("--batch-instances", type=int, default=4096, help="batched 2D leg (0: skip)")
     ap.add_argument("--serve-requests", type=int, default=1000, help="serving-stream leg (0: skip)")
     ap.add_argument("--minimal", type=int, default=1, help="minimal-surface leg (0: skip)")

@@ -177,6 +177,12 @@ typedef struct {
                                the standard form's two refinement steps
                                cannot reach rtol, that is when rtol <
                                0.3 kappa 2^-24 inner_rtol                  */
+  int fuse_restrict;        /* -fsh_fuse_restrict 0|1: on 3D levels the
+                               V-cycle's residual and its restriction run as
+                               one kernel that keeps the fine residual in
+                               shared memory (bit-identical to the
+                               two-kernel form; default 0: measured slower,
+                               0.51 ms against 0.27 + 0.12 ms at 513^3)    */
 } fishgpu_opts;
 
 #define FISHGPU_MAX_HIST 512
@@ -250,7 +256,7 @@ int fishgpu_solve_host(const fishgpu_opts *o, const double *f_host, const double
 /* Times `reps` launches of one solver kernel on the finest level with the
    solver's resident data (CUDA events on the solver's stream).  Names:
    "smooth", "smooth_first", "smooth_dots", "smooth_zero", "post2", "cgp_apply",
-   "cgp_apply_acc" (mixed form: the accurate inner form's apply), "cg_update",
+   "cgp_apply_acc" (mixed form: the accurate inner form's apply), "cg_update", "resid_restrict" (3D),
    "resid", "apply", "restrict", "prolong", "residual64".  Reports the mean ms
    per launch and the algorithmic bytes one launch moves. */
 int fishgpu_solver_time_kernel(fishgpu_solver *s, const char *name, int reps,

@@ -398,8 +398,13 @@ static void enq_vcycle(fishgpu_solver *S, Hier<T> &H, int l, bool from_zero, int
   }
   Level<T> &lc = H.lev[l - 1];
   enq_smooth<DIM, T>(S, lv, from_zero);
-  v_resid<DIM, T><<<slot_blocks(lv.st), lv.st.chunk, 0, s>>>(lv.g, lv.st, st, lv.b, lv.X[lv.cur], lv.r);
-  v_restrict<DIM, T><<<slot_blocks(lc.sl), lc.sl.chunk, 0, s>>>(lv.g, lc.g, lc.sl, st, lv.r, lc.b);
+  if (DIM == 3 && !S->batch && S->o.fuse_restrict) {  // b_c = P^T (b - A x) in one pass
+    const RRShape q = rr_shape(lv.g, lc.g);
+    v_resid_restrict<T><<<q.blocks(), 288, 0, s>>>(lv.g, lc.g, q, st, lv.b, lv.X[lv.cur], lc.b);
+  } else {
+    v_resid<DIM, T><<<slot_blocks(lv.st), lv.st.chunk, 0, s>>>(lv.g, lv.st, st, lv.b, lv.X[lv.cur], lv.r);
+    v_restrict<DIM, T><<<slot_blocks(lc.sl), lc.sl.chunk, 0, s>>>(lv.g, lc.g, lc.sl, st, lv.r, lc.b);
+  }
   for (int c = 0; c < S->o.mg_cycles; c++) enq_vcycle<DIM, T>(S, H, l - 1, c == 0);
   v_prolong<DIM, T><<<slot_blocks(lc.sl), lc.sl.chunk, 0, s>>>(lv.g, lc.g, lc.sl, st, lc.X[lc.cur], lv.X[lv.cur]);
   enq_smooth<DIM, T>(S, lv, false, dots);
@@ -998,6 +1003,19 @@ static int time_kernel_dim(fishgpu_solver *S, const char *name, int reps, double
       else
         v_restrict<DIM, double><<<slot_blocks(cd.sl), cd.sl.chunk, 0, s>>>(g, cd.g, cd.sl, nullptr, ld.X[0], cd.b);
       *bytes = sz * N * (1.0 + 1.0 / (1 << DIM));
+    } else if (!strcmp(name, "resid_restrict")) {  // fused: reads b, x; writes the coarse b
+      if constexpr (DIM == 3) {
+        if (mixed) {
+          const RRShape q = rr_shape(g, cf.g);
+          v_resid_restrict<float><<<q.blocks(), 288, 0, s>>>(g, cf.g, q, nullptr, S->r32, lf.X[0], cf.b);
+        } else {
+          const RRShape q = rr_shape(g, cd.g);
+          v_resid_restrict<double><<<q.blocks(), 288, 0, s>>>(g, cd.g, q, nullptr, S->r64, ld.X[0], cd.b);
+        }
+        *bytes = sz * N * (2.0 + 1.0 / 8.0);
+      } else {
+        return FISHGPU_ERR_UNSUPPORTED;
+      }
     } else if (!strcmp(name, "prolong")) {
       if (mixed)
         v_prolong<DIM, float><<<slot_blocks(cf.sl), cf.sl.chunk, 0, s>>>(g, cf.g, cf.sl, nullptr, cf.X[0], lf.X[0]);

@@ -885,6 +885,115 @@ __global__ void __launch_bounds__(256) v_restrict(Geom gf, Geom g, Slots s, KspS
   }
 }
 
+// Fused residual and restriction of a 3D level: b_c = P^T (b - A x) without
+// storing the fine residual (2s + s/8 bytes per fine node instead of the
+// 3s + s + s/8 of v_resid and v_restrict).  A block owns a tile of 31 fine
+// x-slots (124 points) by 8 fine rows and a chunk of coarse planes; its nine
+// warps compute the residual of nine fine rows (the tile's rows and the one
+// below them) on 32 slots (the tile's and the slot left of it) of one fine
+// plane at a time, exactly as v_resid does, into a shared-memory plane
+// (double-buffered: one barrier per fine plane); 248 threads, one per coarse
+// point of the tile (4 coarse rows by 62), then weight that plane in x and y
+// as v_restrict does and combine consecutive fine planes in z in registers.
+// Every residual and every weighted sum is the same operation in the same
+// order as in the two kernels, so b_c is bit-identical.
+struct RRShape {
+  int nxt, nyt, nzt, zc;  // x-tiles (31 fine slots), y-tiles (8 fine rows), coarse-plane chunks, planes per chunk
+  unsigned blocks() const { return (unsigned)nxt * (unsigned)nyt * (unsigned)nzt; }
+};
+
+inline RRShape rr_shape(const Geom &gf, const Geom &gc, int zc = 16) {
+  RRShape q;
+  q.nxt = (gf.pitch / 4 + 30) / 31;
+  q.nyt = (gc.my + 3) / 4;
+  q.zc = zc < gc.mz ? zc : gc.mz;
+  q.nzt = (gc.mz + q.zc - 1) / q.zc;
+  return q;
+}
+
+template <typename T>
+struct RRBlocks {  // FP32: 4 blocks of 288 threads per SM (56 registers); FP64: no cap
+  static constexpr int value = sizeof(T) == 4 ? 4 : 1;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(288, RRBlocks<T>::value) v_resid_restrict(Geom gf, Geom gc, RRShape q, KspState *st,
+                                                                        const T *__restrict__ b,
+                                                                        const T *__restrict__ x, T *__restrict__ bc) {
+  if (ksp_done_v(st)) return;
+  __shared__ V4<T> rs[2][9][32];  // residual of the tile's 9 fine rows x 32 slots, two fine planes
+  const int lane = threadIdx.x & 31, row = threadIdx.x >> 5;
+  const int tx = blockIdx.x % q.nxt, tr = blockIdx.x / q.nxt, ty = tr % q.nyt, tz = tr / q.nyt;
+  const int slot = 31 * tx - 1 + lane, j = 8 * ty - 1 + row, i4 = 4 * slot;
+  const bool in = slot >= 0 && i4 < gf.pitch && j >= 0 && j < gf.my;
+  const long long col = in ? (long long)j * gf.pitch + i4 : 0;
+  const int K0 = tz * q.zc, K1 = min(K0 + q.zc, gc.mz);
+  const int fbeg = max(2 * K0 - 1, 0), fend = min(2 * K1 - 1, gf.mz - 1);  // fine planes, inclusive
+  const Wv<T> w(gf);
+  const T h = T(0.5);
+  // restriction thread: coarse point (I, J) of the tile
+  const int t = threadIdx.x;
+  const bool rt = t < 248;
+  const int Jl = t / 62, Il = t - 62 * (t / 62);
+  const int J = 4 * ty + Jl, I = 62 * tx + Il;
+  const bool rst = rt && J < gc.my && I < gc.pitch;  // stores (points past mx_c are padding: 0)
+  T below = T(0), mid = T(0);
+  // z-window of the residual threads (x at planes f-1, f, f+1)
+  V4<T> zd = zero4<T>(), zc = zero4<T>();
+  if (in) {
+    if (fbeg > 0) zd = ld4(x + (long long)(fbeg - 1) * gf.plane + col);
+    zc = ld4(x + (long long)fbeg * gf.plane + col);
+  }
+  SlotPos p;
+  p.in = in;
+  p.i4 = i4;
+  p.j = j;
+  p.col = col;
+  long long n = (long long)fbeg * gf.plane + col;
+  for (int f = fbeg; f <= fend; f++, n += gf.plane) {
+    V4<T> zu = zero4<T>();
+    if (in && f + 1 < gf.mz) zu = ld4(x + n + gf.plane);
+    Nb<T> nb;
+    load_xy<3, T>(gf, p, ArraySrc<T>{x}, n, zc, nb);
+    const bool hd = f - 1 > 0, hu = f + 1 < gf.mz - 1;
+    nb.zs = add4(hd ? zd : zero4<T>(), hu ? zu : zero4<T>());
+    nb.jkb = jk_bdry(gf, 3, j, f);
+    V4<T> o = zero4<T>();
+    if (in) {
+      const V4<T> bv = ld4(b + n);
+#pragma unroll
+      for (int e = 0; e < 4; e++) {
+        const int i = i4 + e;
+        set_el(o, e, i < gf.mx ? resid_el<3, T>(gf, w, nb, e, i, nb.jkb, el(bv, e)) : T(0));
+      }
+    }
+    rs[f & 1][row][lane] = o;
+    zd = zc;
+    zc = zu;
+    __syncthreads();
+    if (rt) {
+      // fine points 2I-1, 2I, 2I+1 are elements 2Il+3 .. 2Il+5 of the row (slot 0 is the halo slot)
+      const T *r0 = reinterpret_cast<const T *>(&rs[f & 1][0][0]);
+      auto rowv = [&](int rr) -> T {
+        const T *a = r0 + rr * 128 + 2 * Il + 3;
+        return fma(h, a[0] + a[2], a[1]);
+      };
+      // fine rows 2J-1, 2J, 2J+1 are tile rows 2Jl, 2Jl+1, 2Jl+2
+      const T v = fma(h, rowv(2 * Jl) + rowv(2 * Jl + 2), rowv(2 * Jl + 1));
+      if ((f & 1) == 0) {
+        mid = v;
+        if (f + 1 >= gf.mz && rst)  // no fine plane 2K+1: the last coarse plane
+          bc[(long long)(f >> 1) * gc.plane + (long long)J * gc.pitch + I] = I < gc.mx ? fma(h, below + T(0), mid) : T(0);
+      } else {
+        const int K = f >> 1;  // coarse plane whose upper fine plane this is
+        if (f > 2 * K0 - 1 && rst)
+          bc[(long long)K * gc.plane + (long long)J * gc.pitch + I] = I < gc.mx ? fma(h, below + v, mid) : T(0);
+        below = v;
+      }
+    }
+  }
+}
+
 // x_f += P x_c (Q1 interpolation).  A thread owns a coarse slot I4..I4+3 and
 // writes the 8 fine x-points 2I4 .. 2I4+7 of fine rows 2J, 2J+1 and planes
 // 2K, 2K+1 (those inside the fine grid).  The x-interpolated coarse rows J and

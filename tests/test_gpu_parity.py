@@ -472,3 +472,26 @@ def test_accurate_inner_form_needs_fewer_refinement_steps(cuda):
     assert h_std[1] / h_std[0] > 1e-4   # the standard form's first step stops at its floor, ~kappa 2^-24
     assert h_deep[1] / h_deep[0] < 1e-5  # measured 3.3e-7
     assert acc.outer_its == 2 and std.outer_its == 3
+
+
+@pytest.mark.parametrize("args", [
+    "-fsh_dim 3 -fsh_problem manupoly -da_refine 5 -pc_type mg -ksp_rtol 1e-10",
+    "-fsh_dim 3 -fsh_problem manupoly -da_refine 5 -pc_type mg -ksp_rtol 1e-10 -fsh_precision mixed",
+    "-fsh_dim 3 -fsh_problem manupoly -da_grid_x 5 -da_grid_y 3 -da_grid_z 9 -da_refine 4 -pc_type mg "
+    "-ksp_rtol 1e-10 -fsh_cz 3",
+    "-fsh_dim 3 -da_grid_x 9 -da_grid_y 17 -da_grid_z 5 -da_refine 3 -pc_type mg -ksp_rtol 1e-10 "
+    "-fsh_precision mixed -pc_mg_cycle_type w",
+    "-fsh_dim 3 -fsh_problem manuexp -da_refine 6 -pc_type mg -ksp_rtol 1e-10 -fsh_precision mixed",
+])
+def test_fused_residual_restriction_is_bit_identical(cuda, args):
+    """The 3D levels' fused residual + restriction (v_resid_restrict) computes
+    every fine residual and weighted sum as v_resid and v_restrict do, in the
+    same order: the whole solve is identical to the two-kernel form, bit for
+    bit (tile edges in x, y and z, odd level shapes, W-cycles)."""
+    import torch
+    fg = fgmod()
+    u1, a = fg.solve(fg.options(args + " -fsh_fuse_restrict 1"))
+    u0, b = fg.solve(fg.options(args + " -fsh_fuse_restrict 0"))
+    assert a.reason == b.reason == 2 and a.its == b.its and a.outer_its == b.outer_its
+    assert a.history() == b.history()
+    assert torch.equal(u1, u0)
