@@ -21,7 +21,8 @@ BINDIR = os.path.join(PKG, "bin")
 LIB = os.path.join(LIBDIR, "libfishgpu.so")
 
 SOURCES = ["common.cu", "callbacks.cu", "solver.cu", "noalloc.cu", "server.cu", "msurf.cu", "petscbin.cu"]
-HEADERS = ["fishgpu_internal.cuh", "kernels.cuh", "common.cuh", "vkernels.cuh", "mg_hooks.cuh", "graph_loop.cuh"]
+HEADERS = ["fishgpu_internal.cuh", "kernels.cuh", "common.cuh", "vkernels.cuh", "mg_hooks.cuh", "graph_loop.cuh",
+           "tma.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -7,9 +7,43 @@
 #include <strings.h>
 
 
+#include <cudaTypedefs.h>
+
 #include "common.cuh"
+#include "tma.cuh"
 
 namespace fg {
+
+// cuTensorMapEncodeTiled, looked up once through the runtime (the library
+// links the runtime only)
+static PFN_cuTensorMapEncodeTiled_v12000 tma_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+    else
+      cudaGetLastError();
+  });
+  return fn;
+}
+
+bool tma_map_3d(CUtensorMap *map, const void *base, CUtensorMapDataType dtype, long long nx, long long ny,
+                long long nz, long long row_bytes, long long plane_bytes, int bx, int by, int bz) {
+  PFN_cuTensorMapEncodeTiled_v12000 enc = tma_encoder();
+  if (!enc) return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)nx, (cuuint64_t)ny, (cuuint64_t)nz};
+  const cuuint64_t strides[2] = {(cuuint64_t)row_bytes, (cuuint64_t)plane_bytes};
+  const cuuint32_t box[3] = {(cuuint32_t)bx, (cuuint32_t)by, (cuuint32_t)bz};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  return enc(map, dtype, 3, const_cast<void *>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+             CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) ==
+         CUDA_SUCCESS;
+}
 
 Geom make_geom_box(int dim, int mx, int my, int mz, const double xmin[3], const double xmax[3],
                    double cx, double cy, double cz) {
@@ -45,6 +79,8 @@ Geom make_geom_box(int dim, int mx, int my, int mz, const double xmin[3], const 
     g.scdiag = 2.0 * (g.sc[0] + g.sc[1] + g.sc[2]);
     g.vol = dvol;
   }
+  for (int d = 0; d < 3; d++) g.scf[d] = (float)g.sc[d];
+  g.scdiagf = (float)g.scdiag;
   return g;
 }
 

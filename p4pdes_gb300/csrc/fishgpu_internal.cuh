@@ -28,6 +28,12 @@ struct Geom {
   double sc[3];
   double scdiag;
   double vol;       // cell volume multiplying f in the residual
+  // sc and scdiag rounded to FP32 once on the host: the FP32 kernels read
+  // these instead of converting the FP64 values, a conversion the compiler
+  // may repeat inside a loop (it rematerialises kernel parameters rather than
+  // keep them in registers), and that runs on the FP64 pipe
+  float scf[3];
+  float scdiagf;
 };
 
 Geom make_geom(int dim, int mx, int my, int mz, double Lx, double Ly, double Lz,

@@ -27,8 +27,19 @@ __host__ __device__ inline Range full_range(const Geom &g) { return Range{0, 0, 
 template <typename T>
 struct Wt {
   T sx, sy, sz, sd;
-  __device__ __forceinline__ explicit Wt(const Geom &g)
-      : sx((T)g.sc[0]), sy((T)g.sc[1]), sz((T)g.sc[2]), sd((T)g.scdiag) {}
+  __device__ __forceinline__ explicit Wt(const Geom &g) {
+    if constexpr (sizeof(T) == 4) {  // FP32 weights rounded on the host (Geom::scf)
+      sx = g.scf[0];
+      sy = g.scf[1];
+      sz = g.scf[2];
+      sd = g.scdiagf;
+    } else {
+      sx = g.sc[0];
+      sy = g.sc[1];
+      sz = g.sc[2];
+      sd = g.scdiag;
+    }
+  }
 };
 
 template <int DIM>

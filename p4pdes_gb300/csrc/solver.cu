@@ -151,6 +151,7 @@ struct fishgpu_solver_s {
   std::vector<void *> allocs;
   long long bytes = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  int *fault = nullptr;  // set by a kernel whose bounded wait on a copy gave up
 };
 
 namespace fg {
@@ -261,6 +262,23 @@ static int build_hier(fishgpu_solver *S, Hier<T> &H) {
 
 // ------------------------------------------------------------------ enqueue
 static inline int third(int a, int b) { return 3 - a - b; }
+
+// b_c = P^T (b - A x) of a 3D level in one kernel (v_resid_restrict): tensor
+// maps of x and b for the kernel's ring; false if the driver refuses them.
+template <typename T>
+static bool launch_resid_restrict(fishgpu_solver *S, const Geom &gf, const Geom &gc, const T *b, const T *x, T *bc,
+                                  KspState *st) {
+  using R = RRRing<T>;
+  const CUtensorMapDataType dt = sizeof(T) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
+  CUtensorMap xm, bm;
+  const long long rb = (long long)gf.pitch * sizeof(T), pb = gf.plane * (long long)sizeof(T);
+  if (!tma_map_3d(&xm, x, dt, gf.pitch, gf.my, gf.mz, rb, pb, R::XW, R::XR, 1) ||
+      !tma_map_3d(&bm, b, dt, gf.pitch, gf.my, gf.mz, rb, pb, R::BW, R::BR, 1))
+    return false;
+  const RRShape q = rr_shape(gf, gc);
+  v_resid_restrict<T><<<q.blocks(), 320, R::SMEM, S->stream>>>(xm, bm, gf, gc, q, st, bc, S->fault);
+  return true;
+}
 
 // Level smoother, PETSc KSPCHEBYSHEV / KSPRICHARDSON with PCJACOBI, `its`
 // iterations, nonzero initial guess; from_zero: the iterate is known to be 0
@@ -398,9 +416,8 @@ static void enq_vcycle(fishgpu_solver *S, Hier<T> &H, int l, bool from_zero, int
   }
   Level<T> &lc = H.lev[l - 1];
   enq_smooth<DIM, T>(S, lv, from_zero);
-  if (DIM == 3 && !S->batch && S->o.fuse_restrict) {  // b_c = P^T (b - A x) in one pass
-    const RRShape q = rr_shape(lv.g, lc.g);
-    v_resid_restrict<T><<<q.blocks(), 288, 0, s>>>(lv.g, lc.g, q, st, lv.b, lv.X[lv.cur], lc.b);
+  if (DIM == 3 && !S->batch && S->o.fuse_restrict &&
+      launch_resid_restrict<T>(S, lv.g, lc.g, lv.b, lv.X[lv.cur], lc.b, st)) {  // b_c = P^T (b - A x) in one pass
   } else {
     v_resid<DIM, T><<<slot_blocks(lv.st), lv.st.chunk, 0, s>>>(lv.g, lv.st, st, lv.b, lv.X[lv.cur], lv.r);
     v_restrict<DIM, T><<<slot_blocks(lc.sl), lc.sl.chunk, 0, s>>>(lv.g, lc.g, lc.sl, st, lv.r, lc.b);
@@ -887,6 +904,16 @@ static int solve_dim(fishgpu_solver *S, double *u, fishgpu_report *rep) {
   FG_CUDA(cudaEventSynchronize(S->ev1));
   FG_CUDA(cudaEventElapsedTime(&ms, S->ev0, S->ev1));
   rep->solve_ms = ms;
+  if (S->fault) {  // a kernel's bounded wait on a copy gave up: its results are not to be trusted
+    FG_CUDA(cudaMemcpyAsync(S->hval + 7, S->fault, sizeof(int), cudaMemcpyDeviceToHost, s));
+    FG_CUDA(cudaStreamSynchronize(s));
+    int f = 0;
+    memcpy(&f, S->hval + 7, sizeof(int));
+    if (f) {
+      FG_CUDA(cudaMemsetAsync(S->fault, 0, sizeof(int), s));
+      return FISHGPU_ERR_TIMEOUT;
+    }
+  }
   return FISHGPU_OK;
 }
 
@@ -1005,13 +1032,9 @@ static int time_kernel_dim(fishgpu_solver *S, const char *name, int reps, double
       *bytes = sz * N * (1.0 + 1.0 / (1 << DIM));
     } else if (!strcmp(name, "resid_restrict")) {  // fused: reads b, x; writes the coarse b
       if constexpr (DIM == 3) {
-        if (mixed) {
-          const RRShape q = rr_shape(g, cf.g);
-          v_resid_restrict<float><<<q.blocks(), 288, 0, s>>>(g, cf.g, q, nullptr, S->r32, lf.X[0], cf.b);
-        } else {
-          const RRShape q = rr_shape(g, cd.g);
-          v_resid_restrict<double><<<q.blocks(), 288, 0, s>>>(g, cd.g, q, nullptr, S->r64, ld.X[0], cd.b);
-        }
+        const bool ok = mixed ? launch_resid_restrict<float>(S, g, cf.g, S->r32, lf.X[0], cf.b, nullptr)
+                              : launch_resid_restrict<double>(S, g, cd.g, S->r64, ld.X[0], cd.b, nullptr);
+        if (!ok) return FISHGPU_ERR_UNSUPPORTED;
         *bytes = sz * N * (2.0 + 1.0 / 8.0);
       } else {
         return FISHGPU_ERR_UNSUPPORTED;
@@ -1168,7 +1191,16 @@ extern "C" int fishgpu_solver_create(const fishgpu_opts *o, void *stream, fishgp
     }
   }
   CK(dalloc(S, &S->st, 1));
+  CK(dalloc(S, &S->fault, 1));
   CK(dalloc(S, &S->dval, 8));
+  if (dim == 3 &&
+      (cudaFuncSetAttribute(v_resid_restrict<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)RRRing<float>::SMEM) != cudaSuccess ||
+       cudaFuncSetAttribute(v_resid_restrict<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)RRRing<double>::SMEM) != cudaSuccess)) {
+    fishgpu_solver_destroy(S);
+    return FISHGPU_ERR_CUDA;
+  }
   CK(dalloc(S, &S->red.partials, (size_t)2 * 2 * cap));  // two slots of up to two values
   CK(dalloc(S, &S->red.tickets, 4));
   S->red.cap = cap;
@@ -1220,7 +1252,7 @@ extern "C" long long fishgpu_solver_estimate_bytes(const fishgpu_opts *o) {
   Geom d = make_geom(dim, o->mx, dim >= 2 ? o->my : 1, dim >= 3 ? o->mz : 1, 1, 1, 1, 1, 1, 1);
   Geom g = padded(d);
   const long long N = (long long)nelem(g), Nd = (long long)d.plane * d.mz;
-  long long b = rnd(sizeof(KspState)) + rnd(64);  // state, scalars
+  long long b = rnd(sizeof(KspState)) + rnd(4) + rnd(64);  // state, fault word, scalars
   const long long cap = slot_blocks(make_slots(g, ZC));
   b += rnd(8LL * 4 * cap) + rnd(16);
   b += 4 * rnd(8LL * N);                                          // u, beff, y, r

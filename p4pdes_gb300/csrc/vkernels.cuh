@@ -19,6 +19,7 @@
 #pragma once
 
 #include "fishgpu_internal.cuh"
+#include "tma.cuh"
 
 namespace fg {
 
@@ -171,8 +172,19 @@ struct MinBlocksLean {
 template <typename T>
 struct Wv {
   T sx, sy, sz, sd;
-  __device__ __forceinline__ explicit Wv(const Geom &g)
-      : sx((T)g.sc[0]), sy((T)g.sc[1]), sz((T)g.sc[2]), sd((T)g.scdiag) {}
+  __device__ __forceinline__ explicit Wv(const Geom &g) {
+    if constexpr (sizeof(T) == 4) {  // FP32 weights rounded on the host (Geom::scf)
+      sx = g.scf[0];
+      sy = g.scf[1];
+      sz = g.scf[2];
+      sd = g.scdiagf;
+    } else {
+      sx = g.sc[0];
+      sy = g.sc[1];
+      sz = g.sc[2];
+      sd = g.scdiag;
+    }
+  }
 };
 
 // Neighbour data of a slot at plane k.
@@ -888,15 +900,19 @@ __global__ void __launch_bounds__(256) v_restrict(Geom gf, Geom g, Slots s, KspS
 // Fused residual and restriction of a 3D level: b_c = P^T (b - A x) without
 // storing the fine residual (2s + s/8 bytes per fine node instead of the
 // 3s + s + s/8 of v_resid and v_restrict).  A block owns a tile of 31 fine
-// x-slots (124 points) by 8 fine rows and a chunk of coarse planes; its nine
-// warps compute the residual of nine fine rows (the tile's rows and the one
-// below them) on 32 slots (the tile's and the slot left of it) of one fine
-// plane at a time, exactly as v_resid does, into a shared-memory plane
-// (double-buffered: one barrier per fine plane); 248 threads, one per coarse
-// point of the tile (4 coarse rows by 62), then weight that plane in x and y
-// as v_restrict does and combine consecutive fine planes in z in registers.
-// Every residual and every weighted sum is the same operation in the same
-// order as in the two kernels, so b_c is bit-identical.
+// x-slots (124 points) by 8 fine rows and a chunk of coarse planes.  Its
+// producer warp streams the tile's planes of x (11 rows: the tile's, the row
+// below them and their y-neighbours) and b (9 rows) into a 4-stage
+// shared-memory ring with bulk tensor copies, one or two planes ahead; nine
+// consumer warps compute the residual of nine fine rows (the tile's rows and
+// the one below) on 32 slots (the tile's and the one left of it) of one fine
+// plane, every neighbour taken from the ring, exactly as v_resid computes it,
+// into a shared-memory plane (double-buffered: one barrier of the consumers
+// per fine plane); 248 of them, one per coarse point of the tile (4 coarse
+// rows by 62), then weight the plane in x and y as v_restrict does and
+// combine consecutive fine planes in z in registers.  Every residual and
+// every weighted sum is the same operation in the same order as in the two
+// kernels, so b_c is bit-identical.
 struct RRShape {
   int nxt, nyt, nzt, zc;  // x-tiles (31 fine slots), y-tiles (8 fine rows), coarse-plane chunks, planes per chunk
   unsigned blocks() const { return (unsigned)nxt * (unsigned)nyt * (unsigned)nzt; }
@@ -911,56 +927,98 @@ inline RRShape rr_shape(const Geom &gf, const Geom &gc, int zc = 16) {
   return q;
 }
 
+// Shared-memory layout of the ring (offsets from a 128-byte aligned base)
 template <typename T>
-struct RRBlocks {  // FP32: 4 blocks of 288 threads per SM (56 registers); FP64: no cap
-  static constexpr int value = sizeof(T) == 4 ? 4 : 1;
+struct RRRing {
+  static constexpr int NS = 4;                   // stages (planes)
+  static constexpr int XW = 136, XR = 11;        // x box: points 124 tx - 4 .. + 135, rows j0 - 2 .. j0 + 8
+  static constexpr int BW = 128, BR = 9;         // b box: points 124 tx - 4 .. + 127, rows j0 - 1 .. j0 + 7
+  static constexpr unsigned XBYTES = XW * XR * sizeof(T), BBYTES = BW * BR * sizeof(T);
+  static constexpr unsigned XSTR = (XBYTES + 127) / 128 * 128, BSTR = (BBYTES + 127) / 128 * 128;
+  static constexpr unsigned STAGE = XSTR + BSTR;
+  static constexpr unsigned RS = 2 * 9 * 32 * sizeof(V4<T>);  // the residual planes
+  static constexpr unsigned BARS = NS * STAGE + RS;            // full[NS], empty[NS]
+  static constexpr size_t SMEM = 128 + BARS + 2 * NS * sizeof(uint64_t);
 };
 
 template <typename T>
-__global__ void __launch_bounds__(288, RRBlocks<T>::value) v_resid_restrict(Geom gf, Geom gc, RRShape q, KspState *st,
-                                                                        const T *__restrict__ b,
-                                                                        const T *__restrict__ x, T *__restrict__ bc) {
+struct RRBlocks {  // FP32: 4 blocks of 320 threads per SM (51 registers); FP64: 2 (the ring's size)
+  static constexpr int value = sizeof(T) == 4 ? 4 : 2;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(320, RRBlocks<T>::value)
+    v_resid_restrict(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtensorMap bmap, Geom gf,
+                     Geom gc, RRShape q, KspState *st, T *__restrict__ bc, int *fault) {
+  using R = RRRing<T>;
   if (ksp_done_v(st)) return;
-  __shared__ V4<T> rs[2][9][32];  // residual of the tile's 9 fine rows x 32 slots, two fine planes
-  const int lane = threadIdx.x & 31, row = threadIdx.x >> 5;
+  extern __shared__ unsigned char rr_raw[];
+  unsigned char *base = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(rr_raw) + 127) & ~uintptr_t(127));
+  V4<T>(*rs)[9][32] = reinterpret_cast<V4<T>(*)[9][32]>(base + R::NS * R::STAGE);
+  uint64_t *full = reinterpret_cast<uint64_t *>(base + R::BARS), *empty = full + R::NS;
+  auto xs = [&](int s) { return reinterpret_cast<const T *>(base + s * R::STAGE); };
+  auto bs = [&](int s) { return reinterpret_cast<const T *>(base + s * R::STAGE + R::XSTR); };
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int tx = blockIdx.x % q.nxt, tr = blockIdx.x / q.nxt, ty = tr % q.nyt, tz = tr / q.nyt;
-  const int slot = 31 * tx - 1 + lane, j = 8 * ty - 1 + row, i4 = 4 * slot;
-  const bool in = slot >= 0 && i4 < gf.pitch && j >= 0 && j < gf.my;
-  const long long col = in ? (long long)j * gf.pitch + i4 : 0;
   const int K0 = tz * q.zc, K1 = min(K0 + q.zc, gc.mz);
   const int fbeg = max(2 * K0 - 1, 0), fend = min(2 * K1 - 1, gf.mz - 1);  // fine planes, inclusive
+  const int nq = fend - fbeg + 3;                                          // ring planes fbeg - 1 .. fend + 1
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < R::NS; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 9);
+    }
+    mbar_init_fence();
+  }
+  __syncthreads();
+  if (warp == 9) {  // producer
+    if (lane == 0) {
+      for (int qq = 0; qq < nq; qq++) {
+        const int s = qq % R::NS, u = qq / R::NS;
+        if (u > 0) mbar_wait(&empty[s], (u - 1) & 1, fault);  // the plane that used the stage is done
+        const int pl = fbeg - 1 + qq;
+        mbar_arrive_tx(&full[s], R::XBYTES + R::BBYTES);
+        tma_load_3d(base + s * R::STAGE, &xmap, 124 * tx - 4, 8 * ty - 2, pl, &full[s]);
+        tma_load_3d(base + s * R::STAGE + R::XSTR, &bmap, 124 * tx - 4, 8 * ty - 1, pl, &full[s]);
+      }
+      // no copy may still be in flight when the block ends
+      for (int qq = max(0, nq - R::NS); qq < nq; qq++) mbar_wait(&full[qq % R::NS], (qq / R::NS) & 1, fault, true);
+    }
+    return;
+  }
+  const int row = warp;
+  const int slot = 31 * tx - 1 + lane, j = 8 * ty - 1 + row, i4 = 4 * slot;
+  const bool in = slot >= 0 && i4 < gf.pitch && j >= 0 && j < gf.my;
+  const bool hs = j - 1 > 0, hn = j + 1 < gf.my - 1;
+  const int c0 = 4 * lane;  // box column of the slot's element 0
   const Wv<T> w(gf);
   const T h = T(0.5);
-  // restriction thread: coarse point (I, J) of the tile
   const int t = threadIdx.x;
   const bool rt = t < 248;
   const int Jl = t / 62, Il = t - 62 * (t / 62);
   const int J = 4 * ty + Jl, I = 62 * tx + Il;
   const bool rst = rt && J < gc.my && I < gc.pitch;  // stores (points past mx_c are padding: 0)
   T below = T(0), mid = T(0);
-  // z-window of the residual threads (x at planes f-1, f, f+1)
-  V4<T> zd = zero4<T>(), zc = zero4<T>();
-  if (in) {
-    if (fbeg > 0) zd = ld4(x + (long long)(fbeg - 1) * gf.plane + col);
-    zc = ld4(x + (long long)fbeg * gf.plane + col);
-  }
-  SlotPos p;
-  p.in = in;
-  p.i4 = i4;
-  p.j = j;
-  p.col = col;
-  long long n = (long long)fbeg * gf.plane + col;
-  for (int f = fbeg; f <= fend; f++, n += gf.plane) {
-    V4<T> zu = zero4<T>();
-    if (in && f + 1 < gf.mz) zu = ld4(x + n + gf.plane);
-    Nb<T> nb;
-    load_xy<3, T>(gf, p, ArraySrc<T>{x}, n, zc, nb);
-    const bool hd = f - 1 > 0, hu = f + 1 < gf.mz - 1;
-    nb.zs = add4(hd ? zd : zero4<T>(), hu ? zu : zero4<T>());
-    nb.jkb = jk_bdry(gf, 3, j, f);
+  mbar_wait(&full[0], 0, fault);  // planes fbeg - 1 and fbeg
+  mbar_wait(&full[1], 0, fault);
+  for (int f = fbeg; f <= fend; f++) {
+    const int qq = f - fbeg + 1;  // ring index of plane f
+    mbar_wait(&full[(qq + 1) % R::NS], ((qq + 1) / R::NS) & 1, fault);
+    const T *xm = xs((qq - 1) % R::NS), *xc = xs(qq % R::NS), *xp = xs((qq + 1) % R::NS);
     V4<T> o = zero4<T>();
     if (in) {
-      const V4<T> bv = ld4(b + n);
+      const int ro = (row + 1) * R::XW + c0;
+      Nb<T> nb;
+      nb.c = *reinterpret_cast<const V4<T> *>(xc + ro);
+      nb.l = xc[ro - 1];  // lane 0 (the slot left of the tile): element 0 is not used
+      nb.r = xc[ro + 4];
+      nb.ys = add4(hs ? *reinterpret_cast<const V4<T> *>(xc + ro - R::XW) : zero4<T>(),
+                   hn ? *reinterpret_cast<const V4<T> *>(xc + ro + R::XW) : zero4<T>());
+      const bool hd = f - 1 > 0, hu = f + 1 < gf.mz - 1;
+      nb.zs = add4(hd ? *reinterpret_cast<const V4<T> *>(xm + ro) : zero4<T>(),
+                   hu ? *reinterpret_cast<const V4<T> *>(xp + ro) : zero4<T>());
+      nb.jkb = jk_bdry(gf, 3, j, f);
+      const V4<T> bv = *reinterpret_cast<const V4<T> *>(bs(qq % R::NS) + row * R::BW + c0);
 #pragma unroll
       for (int e = 0; e < 4; e++) {
         const int i = i4 + e;
@@ -968,9 +1026,9 @@ __global__ void __launch_bounds__(288, RRBlocks<T>::value) v_resid_restrict(Geom
       }
     }
     rs[f & 1][row][lane] = o;
-    zd = zc;
-    zc = zu;
-    __syncthreads();
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[(qq - 1) % R::NS]);  // plane f - 1 is no longer read
+    bar_sync(1, 288);
     if (rt) {
       // fine points 2I-1, 2I, 2I+1 are elements 2Il+3 .. 2Il+5 of the row (slot 0 is the halo slot)
       const T *r0 = reinterpret_cast<const T *>(&rs[f & 1][0][0]);
