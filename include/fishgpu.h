@@ -183,6 +183,12 @@ typedef struct {
                                shared memory (bit-identical to the
                                two-kernel form; default 0: measured slower,
                                0.51 ms against 0.27 + 0.12 ms at 513^3)    */
+  int tma_apply;            /* -fsh_tma_apply 0|1: the accurate inner form's
+                               CG direction update + apply on 3D grids reads
+                               its planes from a shared-memory ring filled by
+                               bulk tensor copies (default 0: measured level
+                               with the slot march, 0.79 against 0.80 ms at
+                               513^3, and the solve no faster)             */
 } fishgpu_opts;
 
 #define FISHGPU_MAX_HIST 512
@@ -256,7 +262,8 @@ int fishgpu_solve_host(const fishgpu_opts *o, const double *f_host, const double
 /* Times `reps` launches of one solver kernel on the finest level with the
    solver's resident data (CUDA events on the solver's stream).  Names:
    "smooth", "smooth_first", "smooth_dots", "smooth_zero", "post2", "cgp_apply",
-   "cgp_apply_acc" (mixed form: the accurate inner form's apply), "cg_update", "resid_restrict" (3D),
+   "cgp_apply_acc" (mixed form: the accurate inner form's apply), "cgp_apply_tma" (the same from the
+   TMA ring, 3D), "cg_update", "resid_restrict" (3D),
    "resid", "apply", "restrict", "prolong", "residual64".  Reports the mean ms
    per launch and the algorithmic bytes one launch moves. */
 int fishgpu_solver_time_kernel(fishgpu_solver *s, const char *name, int reps,

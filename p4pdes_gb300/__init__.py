@@ -73,7 +73,8 @@ class Opts(ctypes.Structure):
                 ("inner_rtol", c_double), ("inner_max_it", c_int), ("outer_max_it", c_int),
                 ("graph_iters", c_int), ("monitor", c_int), ("converged_reason", c_int),
                 ("snes_monitor", c_int), ("fuse_smooth", c_int), ("device_loop", c_int), ("loop_cap", c_int),
-                ("first_floor_scale", c_double), ("inner_accurate", c_int), ("fuse_restrict", c_int)]
+                ("first_floor_scale", c_double), ("inner_accurate", c_int), ("fuse_restrict", c_int),
+                ("tma_apply", c_int)]
 
     @property
     def dofs(self):

@@ -191,6 +191,7 @@ extern "C" int fishgpu_opts_default(fishgpu_opts *o) {
   o->first_floor_scale = 0.3;
   o->inner_accurate = -1;
   o->fuse_restrict = 0;
+  o->tma_apply = 0;
   return FISHGPU_OK;
 }
 
@@ -256,6 +257,7 @@ extern "C" int fishgpu_opts_parse(fishgpu_opts *o, int argc, const char *const *
     else if (!strcmp(k, "-fsh_loop_cap")) { NEEDV(); o->loop_cap = atoi(v); }
     else if (!strcmp(k, "-fsh_first_floor")) { NEEDV(); o->first_floor_scale = atof(v); }
     else if (!strcmp(k, "-fsh_fuse_restrict")) { NEEDV(); o->fuse_restrict = atoi(v) != 0; }
+    else if (!strcmp(k, "-fsh_tma_apply")) { NEEDV(); o->tma_apply = atoi(v) != 0; }
     else if (!strcmp(k, "-fsh_inner_accurate")) { NEEDV(); o->inner_accurate = atoi(v) < 0 ? -1 : atoi(v) != 0; }
     else if (!strcmp(k, "-da_refine")) { NEEDV(); refine = atoi(v); }
     else if (!strcmp(k, "-da_grid_x")) { NEEDV(); base[0] = atoi(v); }

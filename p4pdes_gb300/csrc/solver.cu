@@ -263,6 +263,29 @@ static int build_hier(fishgpu_solver *S, Hier<T> &H) {
 // ------------------------------------------------------------------ enqueue
 static inline int third(int a, int b) { return 3 - a - b; }
 
+// The accurate CG direction update + apply of a 3D FP32 grid from a TMA ring
+// (v_cgp_apply_tma): false when the grid is too narrow for its tiles (less
+// than one 43-slot tile per row), the reduction scratch too small for its
+// blocks, or the driver refuses the tensor maps; the caller then launches
+// v_cgp_apply.
+static bool launch_cgp_tma(fishgpu_solver *S, const Geom &g, KspState *st, const float *z, const float *pold,
+                           float *pnew, float *w, double *y, int slot) {
+  if (g.dim != 3 || g.pitch / 4 < 43) return false;
+  const CgTile q = cg_tile_shape(g);
+  if ((int)q.blocks() > S->red.cap) return false;
+  CUtensorMap zm, pm, ym;
+  const long long rb = (long long)g.pitch * 4, pb = g.plane * 4LL;
+  if (!tma_map_3d(&zm, z, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, g.pitch, g.my, g.mz, rb, pb, CgRing::ZW, CgRing::ZR, 1) ||
+      !tma_map_3d(&pm, pold, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, g.pitch, g.my, g.mz, rb, pb, CgRing::ZW, CgRing::ZR,
+                  1) ||
+      !tma_map_3d(&ym, y, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, g.pitch, g.my, g.mz, rb * 2, pb * 2, CgRing::YW,
+                  CgRing::YR, 1))
+    return false;
+  v_cgp_apply_tma<<<q.blocks(), CgRing::THREADS, CgRing::SMEM, S->stream>>>(zm, pm, ym, g, q, st, pnew, w, y, S->red,
+                                                                            slot, S->fault);
+  return true;
+}
+
 // b_c = P^T (b - A x) of a 3D level in one kernel (v_resid_restrict): tensor
 // maps of x and b for the kernel's ring; false if the driver refuses them.
 template <typename T>
@@ -505,8 +528,9 @@ static void enq_cg_iter(fishgpu_solver *S, Hier<T> &H, KspVecs<T> v, int par) {
   }
   if constexpr (sizeof(T) == 4) {
     if (!planes && v.y64) {  // accurate inner form: difference-form apply, FP64 accumulation
-      v_cgp_apply<DIM, T, false, true><<<slot_blocks(S->sfst), S->sfst.chunk, 0, s>>>(
-          S->fine, S->sfst, st, H.z, pold, pnew, v.w, v.y64, S->red, 0);
+      if (!(DIM == 3 && S->o.tma_apply && launch_cgp_tma(S, S->fine, st, H.z, pold, pnew, v.w, v.y64, 0)))
+        v_cgp_apply<DIM, T, false, true><<<slot_blocks(S->sfst), S->sfst.chunk, 0, s>>>(
+            S->fine, S->sfst, st, H.z, pold, pnew, v.w, v.y64, S->red, 0);
       planes = true;
     }
   }
@@ -939,7 +963,8 @@ static int time_kernel_dim(fishgpu_solver *S, const char *name, int reps, double
   // (beta/betaold = 1, a small alpha); p.w > 0 keeps it running, and a stop
   // (non-finite data) is reported
   KspState *tst = nullptr;
-  if (!strcmp(name, "cgp_apply") || !strcmp(name, "cgp_apply_acc") || !strcmp(name, "cg_update")) {
+  if (!strcmp(name, "cgp_apply") || !strcmp(name, "cgp_apply_acc") || !strcmp(name, "cgp_apply_tma") ||
+      !strcmp(name, "cg_update")) {
     KspState h;
     memset(&h, 0, sizeof(h));
     h.i = 2;  // a direction update that also reads y (the first one, i = 1, starts y from 0)
@@ -989,6 +1014,10 @@ static int time_kernel_dim(fishgpu_solver *S, const char *name, int reps, double
       if (!mixed) return FISHGPU_ERR_UNSUPPORTED;
       v_cgp_apply<DIM, float, false, true><<<gb, sl.chunk, 0, s>>>(g, sl, tst, lf.X[0], S->p32, S->q32, S->w32, S->y64,
                                                                  S->red, 1);
+      *bytes = (4.0 + 4.0 + 8.0 + 4.0 + 4.0 + 8.0) * N;
+    } else if (!strcmp(name, "cgp_apply_tma")) {  // the accurate form from the TMA ring (3D)
+      if (!mixed || !launch_cgp_tma(S, g, tst, lf.X[0], S->p32, S->q32, S->w32, S->y64, 1))
+        return FISHGPU_ERR_UNSUPPORTED;
       *bytes = (4.0 + 4.0 + 8.0 + 4.0 + 4.0 + 8.0) * N;
     } else if (!strcmp(name, "post2")) {  // both post-smoothing steps fused: reads b, x0, writes x2
       if constexpr (DIM == 3) {
@@ -1194,7 +1223,9 @@ extern "C" int fishgpu_solver_create(const fishgpu_opts *o, void *stream, fishgp
   CK(dalloc(S, &S->fault, 1));
   CK(dalloc(S, &S->dval, 8));
   if (dim == 3 &&
-      (cudaFuncSetAttribute(v_resid_restrict<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+      (cudaFuncSetAttribute(v_cgp_apply_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CgRing::SMEM) !=
+           cudaSuccess ||
+       cudaFuncSetAttribute(v_resid_restrict<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                             (int)RRRing<float>::SMEM) != cudaSuccess ||
        cudaFuncSetAttribute(v_resid_restrict<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                             (int)RRRing<double>::SMEM) != cudaSuccess)) {

@@ -646,6 +646,156 @@ __global__ void __launch_bounds__(256, MinBlocksLean<T>::value) v_cgp_apply(Geom
   reduce_sel<1, PL>(v1, red, slot, st, FIN_PW, nullptr, s);
 }
 
+// The accurate form of v_cgp_apply (3D, FP32, one grid) fed by a TMA ring.
+// A block owns a tile of 43 slots (172 points) by 8 rows and a chunk of
+// planes.  Its producer warp streams each plane's tile of z and p_old (with
+// one row and one slot of halo on every side) and of y64 (the tile alone)
+// into a 3-stage shared-memory ring with bulk tensor copies; eleven consumer
+// warps (one thread per slot of the tile) form p = z + beta/betaold p_old for
+// their slot and its x- and y-neighbours from the ring, keep p of planes
+// k-1, k, k+1 of their slot in registers, and write p, w = A p (difference
+// form) and the deferred y64 += (yscale alpha) p_old, summing p.w.  No
+// consumer reads shared memory another consumer wrote, so the warps never
+// wait for one another: only for their planes to arrive.  Every value of p,
+// w and y64 is the same operation on the same operands as in v_cgp_apply;
+// p.w is summed in another order (other blocks).
+struct CgTile {
+  int ntx, nty, nzt, zc;  // x-tiles (43 slots), y-tiles (8 rows), plane chunks, planes per chunk
+  unsigned blocks() const { return (unsigned)ntx * (unsigned)nty * (unsigned)nzt; }
+};
+
+inline CgTile cg_tile_shape(const Geom &g, int zc = 32) {
+  CgTile q;
+  q.ntx = (g.pitch / 4 + 42) / 43;
+  q.nty = (g.my + 7) / 8;
+  q.zc = zc < g.mz ? zc : g.mz;
+  q.nzt = (g.mz + q.zc - 1) / q.zc;
+  return q;
+}
+
+struct CgRing {
+  static constexpr int NS = 3;
+  static constexpr int SL = 43, RY = 8;         // slots and rows of a tile
+  static constexpr int ZW = 180, ZR = 10;       // z, p_old box: points 172 tx - 4 .. + 179, rows j0 - 1 .. j0 + 8
+  static constexpr int YW = 172, YR = 8;        // y64 box: points 172 tx .. + 171, rows j0 .. j0 + 7
+  static constexpr unsigned ZBYTES = ZW * ZR * 4, YBYTES = YW * YR * 8;
+  static constexpr unsigned ZSTR = (ZBYTES + 127) / 128 * 128, YSTR = (YBYTES + 127) / 128 * 128;
+  static constexpr unsigned STAGE = 2 * ZSTR + YSTR;
+  static constexpr int CONSUMERS = 11, THREADS = 32 * (CONSUMERS + 1);
+  static constexpr size_t SMEM = 128 + NS * STAGE + 2 * NS * sizeof(uint64_t);
+};
+
+static __global__ void __launch_bounds__(CgRing::THREADS, 2)
+    v_cgp_apply_tma(const __grid_constant__ CUtensorMap zmap, const __grid_constant__ CUtensorMap pmap,
+                    const __grid_constant__ CUtensorMap ymap, Geom g, CgTile q, KspState *st,
+                    float *__restrict__ pnew, float *__restrict__ wv, double *__restrict__ y, Reducer red, int slot,
+                    int *fault) {
+  using R = CgRing;
+  if (ksp_done_v(st)) return;
+  extern __shared__ unsigned char cg_raw[];
+  unsigned char *base = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(cg_raw) + 127) & ~uintptr_t(127));
+  uint64_t *full = reinterpret_cast<uint64_t *>(base + R::NS * R::STAGE), *empty = full + R::NS;
+  auto zs = [&](int s) { return reinterpret_cast<const float *>(base + s * R::STAGE); };
+  auto ps = [&](int s) { return reinterpret_cast<const float *>(base + s * R::STAGE + R::ZSTR); };
+  auto ys = [&](int s) { return reinterpret_cast<const double *>(base + s * R::STAGE + 2 * R::ZSTR); };
+  const bool first = !st || st->i == 0;  // p = z
+  const bool pend = st && st->pend;
+  const bool yfresh = pend && st->i == 1 && st->yfresh;  // y64 written without reading
+  const bool yread = pend && !yfresh;
+  const double a = pend ? st->yscale * st->alpha : 0.0;
+  const float bb = first ? 0.f : (float)st->bratio;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int tx = blockIdx.x % q.ntx, tr = blockIdx.x / q.ntx, ty = tr % q.nty, tz = tr / q.nty;
+  const int k0 = tz * q.zc, k1 = min(k0 + q.zc, g.mz);
+  const int nq = k1 - k0 + 2;  // ring planes k0 - 1 .. k1
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < R::NS; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], R::CONSUMERS);
+    }
+    mbar_init_fence();
+  }
+  __syncthreads();
+  float acc = 0.f;
+  if (warp == R::CONSUMERS) {  // producer
+    if (lane == 0) {
+      for (int qq = 0; qq < nq; qq++) {
+        const int s = qq % R::NS, u = qq / R::NS;
+        if (u > 0) mbar_wait(&empty[s], (u - 1) & 1, fault);
+        const int pl = k0 - 1 + qq;
+        const bool yl = yread && pl >= k0 && pl < k1;
+        mbar_arrive_tx(&full[s], R::ZBYTES + (first ? 0u : R::ZBYTES) + (yl ? R::YBYTES : 0u));
+        tma_load_3d(base + s * R::STAGE, &zmap, 172 * tx - 4, 8 * ty - 1, pl, &full[s]);
+        if (!first) tma_load_3d(base + s * R::STAGE + R::ZSTR, &pmap, 172 * tx - 4, 8 * ty - 1, pl, &full[s]);
+        if (yl) tma_load_3d(base + s * R::STAGE + 2 * R::ZSTR, &ymap, 172 * tx, 8 * ty, pl, &full[s]);
+      }
+      for (int qq = max(0, nq - R::NS); qq < nq; qq++) mbar_wait(&full[qq % R::NS], (qq / R::NS) & 1, fault, true);
+    }
+  } else {  // consumers: thread t owns slot t % 43 of tile row t / 43
+    const int t = threadIdx.x, row = t / R::SL, sl = t - R::SL * (t / R::SL);
+    const int j = 8 * ty + row, i4 = 4 * (R::SL * tx + sl);
+    const bool act = t < R::SL * R::RY && j < g.my && i4 < g.pitch;
+    const int zr = (row + 1) * R::ZW + 4 * sl + 4;  // ring offset of the slot's element 0
+    const bool hs = j - 1 > 0, hn = j + 1 < g.my - 1;
+    const Wv<float> w(g);
+    auto pv4 = [&](int s, int off) -> V4<float> {  // p = z + bb p_old (p = z on the first iteration)
+      const V4<float> zz = *reinterpret_cast<const V4<float> *>(zs(s) + off);
+      if (first) return zz;
+      const V4<float> pp = *reinterpret_cast<const V4<float> *>(ps(s) + off);
+      return V4<float>{fmaf(bb, pp.x, zz.x), fmaf(bb, pp.y, zz.y), fmaf(bb, pp.z, zz.z), fmaf(bb, pp.w, zz.w)};
+    };
+    auto pv1 = [&](int s, int off) -> float { return first ? zs(s)[off] : fmaf(bb, ps(s)[off], zs(s)[off]); };
+    mbar_wait(&full[0], 0, fault);  // planes k0 - 1 and k0
+    mbar_wait(&full[1], 0, fault);
+    V4<float> pd = (act && k0 > 0) ? pv4(0, zr) : zero4<float>();
+    V4<float> pc = act ? pv4(1, zr) : zero4<float>();
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[0]);  // plane k0 - 1 is no longer read
+    for (int k = k0; k < k1; k++) {
+      const int qq = k - k0 + 1, sc = qq % R::NS, su = (qq + 1) % R::NS;
+      mbar_wait(&full[su], ((qq + 1) / R::NS) & 1, fault);
+      const V4<float> pu = (act && k + 1 < g.mz) ? pv4(su, zr) : zero4<float>();
+      if (act) {
+        Nb<float> nb;
+        nb.c = pc;
+        nb.l = pv1(sc, zr - 1);
+        nb.r = pv1(sc, zr + 4);
+        nb.ys = dsum4(pc, hs ? pv4(sc, zr - R::ZW) : zero4<float>(), hn ? pv4(sc, zr + R::ZW) : zero4<float>());
+        const bool hd = k - 1 > 0, hu = k + 1 < g.mz - 1;
+        nb.zs = dsum4(pc, hd ? pd : zero4<float>(), hu ? pu : zero4<float>());
+        nb.jkb = jk_bdry(g, 3, j, k);
+        V4<float> o;
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+          const int i = i4 + e;
+          float v = 0.f;
+          if (i < g.mx) {
+            v = apply_diff_el<3, float>(g, w, nb, e, i, nb.jkb);
+            acc = fmaf(el(pc, e), v, acc);
+          }
+          set_el(o, e, v);
+        }
+        const long long n = (long long)k * g.plane + (long long)j * g.pitch + i4;
+        st4(pnew + n, pc);
+        st4(wv + n, o);
+        if (pend) {
+          const V4<float> pp = *reinterpret_cast<const V4<float> *>(ps(sc) + zr);
+          const V4<double> yy =
+              yfresh ? zero4<double>() : *reinterpret_cast<const V4<double> *>(ys(sc) + row * R::YW + 4 * sl);
+          st4(y + n, V4<double>{fma(a, (double)pp.x, yy.x), fma(a, (double)pp.y, yy.y), fma(a, (double)pp.z, yy.z),
+                                fma(a, (double)pp.w, yy.w)});
+        }
+      }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&empty[sc]);  // plane k is no longer read
+      pd = pc;
+      pc = pu;
+    }
+  }
+  double v1[1] = {(double)acc};
+  reduce_and_finalize<1>(v1, red, slot, st, FIN_PW, nullptr);
+}
+
 // ------------------------------------------------------------------ temporally blocked smoothing
 // Two Chebyshev steps from a nonzero iterate in one pass (3D, FP32):
 //   x1 = x0 + c1 (b - A x0)
