@@ -189,6 +189,13 @@ typedef struct {
                                bulk tensor copies (default 0: measured level
                                with the slot march, 0.79 against 0.80 ms at
                                513^3, and the solve no faster)             */
+  int vtail;                /* -fsh_vtail 0|1: the V-cycle's smallest levels
+                               below the finest (up to 1200 nodes: 33^2,
+                               9^3) run in one block per grid, a barrier
+                               between phases instead of a launch (default
+                               1; bit-identical to 0)                      */
+  int vtail_points;         /* -fsh_vtail_points: largest level (nodes per
+                               grid) the tail takes (0: the limits above)  */
 } fishgpu_opts;
 
 #define FISHGPU_MAX_HIST 512

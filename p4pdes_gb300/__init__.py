@@ -74,7 +74,8 @@ class Opts(ctypes.Structure):
                 ("graph_iters", c_int), ("monitor", c_int), ("converged_reason", c_int),
                 ("snes_monitor", c_int), ("fuse_smooth", c_int), ("device_loop", c_int), ("loop_cap", c_int),
                 ("first_floor_scale", c_double), ("inner_accurate", c_int), ("fuse_restrict", c_int),
-                ("tma_apply", c_int)]
+                ("tma_apply", c_int), ("vtail", c_int),
+                ("vtail_points", c_int)]
 
     @property
     def dofs(self):

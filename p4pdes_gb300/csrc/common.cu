@@ -192,6 +192,7 @@ extern "C" int fishgpu_opts_default(fishgpu_opts *o) {
   o->inner_accurate = -1;
   o->fuse_restrict = 0;
   o->tma_apply = 0;
+  o->vtail = 1;
   return FISHGPU_OK;
 }
 
@@ -258,6 +259,8 @@ extern "C" int fishgpu_opts_parse(fishgpu_opts *o, int argc, const char *const *
     else if (!strcmp(k, "-fsh_first_floor")) { NEEDV(); o->first_floor_scale = atof(v); }
     else if (!strcmp(k, "-fsh_fuse_restrict")) { NEEDV(); o->fuse_restrict = atoi(v) != 0; }
     else if (!strcmp(k, "-fsh_tma_apply")) { NEEDV(); o->tma_apply = atoi(v) != 0; }
+    else if (!strcmp(k, "-fsh_vtail")) { NEEDV(); o->vtail = atoi(v) != 0; }
+    else if (!strcmp(k, "-fsh_vtail_points")) { NEEDV(); o->vtail_points = atoi(v); }
     else if (!strcmp(k, "-fsh_inner_accurate")) { NEEDV(); o->inner_accurate = atoi(v) < 0 ? -1 : atoi(v) != 0; }
     else if (!strcmp(k, "-da_refine")) { NEEDV(); refine = atoi(v); }
     else if (!strcmp(k, "-da_grid_x")) { NEEDV(); base[0] = atoi(v); }

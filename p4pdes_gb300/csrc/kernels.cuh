@@ -144,22 +144,13 @@ inline size_t coarse_smem_bytes(int dim, int n0, int n1, int n2) {
   return e * sizeof(T);
 }
 
+// The solve of one block: b, x already offset to the block's plane (1D/2D),
+// `sm` the block's dynamic shared memory, `work` its global work area.
 template <int DIM, typename T>
-__global__ void __launch_bounds__(1024) k_coarse(Geom g, KspState *st, int batch, const T *__restrict__ b,
-                                                 T *__restrict__ x, const T *__restrict__ S0,
-                                                 const T *__restrict__ S1, const T *__restrict__ S2,
-                                                 const T *__restrict__ ilam, T *work, int n0, int n1, int n2,
-                                                 int smem, T dinv) {
-  extern __shared__ __align__(16) unsigned char fg_coarse_sm[];
-  // 3D: one block for the grid; 1D/2D: block q solves k-plane q (a batch of
-  // independent instances when batch != 0, else the single plane)
-  const int plane = DIM < 3 ? (int)blockIdx.x : 0;
-  if (batch && st) st += plane;
-  if (ksp_done(st)) return;
-  if (DIM < 3) {
-    b += (long long)plane * g.plane;
-    x += (long long)plane * g.plane;
-  }
+__device__ __forceinline__ void coarse_solve_block(const Geom &g, const T *__restrict__ b, T *__restrict__ x,
+                                                   const T *__restrict__ S0, const T *__restrict__ S1,
+                                                   const T *__restrict__ S2, const T *__restrict__ ilam, T *work,
+                                                   int n0, int n1, int n2, int smem, T dinv, unsigned char *sm_raw) {
   const int tid = threadIdx.x, nt = blockDim.x;
   const int mzl = DIM < 3 ? 1 : g.mz;
   const int N = g.mx * g.my * mzl;
@@ -174,7 +165,7 @@ __global__ void __launch_bounds__(1024) k_coarse(Geom g, KspState *st, int batch
   const T *Sd[3] = {S0, S1, S2};
   const T *il = ilam;
   if (smem) {
-    T *sm = reinterpret_cast<T *>(fg_coarse_sm);
+    T *sm = reinterpret_cast<T *>(sm_raw);
     A = sm;
     B = A + ni;
     T *sl = B + ni, *s0 = sl + ni, *s1 = s0 + n0 * n0, *s2 = s1 + (DIM >= 2 ? n1 * n1 : 0);
@@ -225,6 +216,25 @@ __global__ void __launch_bounds__(1024) k_coarse(Geom g, KspState *st, int batch
     const int i = q % n0, j = (q / n0) % n1, k = q / (n0 * n1);
     x[gidx(g, i + 1, j + oj, k + ok)] = A[q];
   }
+}
+
+template <int DIM, typename T>
+__global__ void __launch_bounds__(1024) k_coarse(Geom g, KspState *st, int batch, const T *__restrict__ b,
+                                                 T *__restrict__ x, const T *__restrict__ S0,
+                                                 const T *__restrict__ S1, const T *__restrict__ S2,
+                                                 const T *__restrict__ ilam, T *work, int n0, int n1, int n2,
+                                                 int smem, T dinv) {
+  extern __shared__ __align__(16) unsigned char fg_coarse_sm[];
+  // 3D: one block for the grid; 1D/2D: block q solves k-plane q (a batch of
+  // independent instances when batch != 0, else the single plane)
+  const int plane = DIM < 3 ? (int)blockIdx.x : 0;
+  if (batch && st) st += plane;
+  if (ksp_done(st)) return;
+  if (DIM < 3) {
+    b += (long long)plane * g.plane;
+    x += (long long)plane * g.plane;
+  }
+  coarse_solve_block<DIM, T>(g, b, x, S0, S1, S2, ilam, work, n0, n1, n2, smem, dinv, fg_coarse_sm);
 }
 
 }  // namespace fg

@@ -54,12 +54,30 @@ struct Level {
   int n[3] = {1, 1, 1};
 };
 
+// One level of the V-cycle tail (k_vtail): the level's arrays and the
+// Chebyshev coefficients of its smoothing steps (the same values enq_smooth
+// passes to v_cheb2_zero and v_cheb).  Every tail level ends its V-cycle with
+// its iterate in X[0] (pre-smoothing writes X[1], the two post-smoothing steps
+// X[2] and X[0]), as the rotation of enq_smooth leaves it.
+template <typename T>
+struct TailLevel {
+  Geom g;
+  T *b, *r, *X[3];
+  T a0, a1;            // two steps from zero: x = a0 b - a1 (A b)
+  T c1;                // post-smoothing step 1: x1 = x0 + c1 (b - A x0)
+  T ckm1, ck, crd;     // step 2: x2 = ckm1 x0 + ck x1 + crd (b - A x1)
+};
+
 template <typename T>
 struct Hier {
   int nlev = 0;
   Level<T> lev[MAX_LEVELS];
   T *zbuf = nullptr;  // z for the Jacobi / none preconditioners
   T *z = nullptr;     // where the preconditioner leaves z (fixed per option set)
+  TailLevel<T> *tail = nullptr;  // device: levels 0 .. tail_top of the one-block V-cycle tail
+  int tail_top = 0;              // 0: no tail
+  int tail_threads = 0;
+  size_t tail_smem = 0;
 };
 
 static Geom padded(Geom g) {
@@ -182,6 +200,81 @@ static int batch_rows(const Geom &g) {
   return g.mx >= 257 ? 16 : g.mx >= 65 ? 8 : g.mx >= 33 ? 4 : 0;  // measured per size: 4096-instance batch
 }
 
+// Levels up to tail_max_points nodes (per instance) below the finest run as
+// the one-block V-cycle tail.  One SM then does the level's work, so the
+// level must be small enough that a phase costs less than a launch (about
+// one point per thread): up to 33^2 / 9^3 nodes.  Swept (limits 300, 1200,
+// 5000, 17000 nodes) on 2D 257^2 and 3D 129^3 / 513^3 solves: 1200 is best
+// or level with the best in both precisions; 17000 (129^2) took the 2D
+// FP64 solve from 2.4 to 4.0 ms (FP64 on one SM is slow on this part).
+static long long tail_max_points(const fishgpu_opts &o, size_t) {
+  return o.vtail_points > 0 ? o.vtail_points : 1200;
+}
+
+static long long level_points(const Geom &g) { return (long long)g.mx * g.my * (g.dim >= 3 ? g.mz : 1); }
+
+// The V-cycle tail of a hierarchy (k_vtail): the largest level below the
+// finest with at most TAIL_MAX_POINTS nodes per instance and everything
+// under it, for V-cycles of two Chebyshev/Jacobi steps (the default
+// smoother; other smoothers keep a launch per phase).
+template <typename T>
+static int build_tail(fishgpu_solver *S, Hier<T> &H) {
+  const fishgpu_opts &o = S->o;
+  H.tail_top = 0;
+  if (!o.vtail || o.pc_type != FISHGPU_PC_MG || o.smooth_type != FISHGPU_SMOOTH_CHEBYSHEV || o.smooth_its != 2 ||
+      o.mg_cycles != 1 || S->fine.dim < 2 || H.nlev < 3)
+    return FISHGPU_OK;
+  int top = 0;
+  for (int l = 1; l <= H.nlev - 2; l++)
+    if (level_points(H.lev[l].g) <= tail_max_points(o, sizeof(T))) top = l;
+  if (top < 1) return FISHGPU_OK;
+  std::vector<TailLevel<T>> tl(top + 1);
+  for (int l = 0; l <= top; l++) {
+    Level<T> &lv = H.lev[l];
+    TailLevel<T> &t = tl[l];
+    memset(&t, 0, sizeof(t));
+    t.g = lv.g;
+    t.b = lv.b;
+    t.r = lv.r;
+    for (int q = 0; q < 3; q++) t.X[q] = lv.X[q];
+    if (l == 0) continue;
+    // enq_smooth's Chebyshev coefficients, the same expressions
+    const double dinv = 1.0 / lv.g.scdiag;
+    const double scale = 2.0 / (lv.emax + lv.emin);
+    const double alpha = 1.0 - scale * lv.emin;
+    const double mu = 1.0 / alpha, omegaprod = 2.0 / alpha;
+    const double c1 = scale * dinv;
+    {
+      const double ckp1 = 2.0 * mu * mu - 1.0, omega = omegaprod * mu / ckp1;
+      t.a0 = (T)(2.0 * omega * c1);
+      t.a1 = (T)(omega * c1 * c1);
+    }
+    t.c1 = (T)c1;
+    {
+      const double ckm1 = 1.0, ck = mu;
+      const double ckp1 = 2.0 * mu * ck - ckm1;
+      const double omega = omegaprod * ck / ckp1;
+      t.ckm1 = (T)(1.0 - omega);
+      t.ck = (T)omega;
+      t.crd = (T)(omega * c1);
+    }
+  }
+  // the level's b of the top level is the restriction target of the level
+  // above it (allocated); levels below the finest all have r
+  int rc;
+  if ((rc = dalloc(S, &H.tail, (size_t)(top + 1)))) return rc;
+  if (cudaMemcpyAsync(H.tail, tl.data(), sizeof(TailLevel<T>) * (top + 1), cudaMemcpyHostToDevice, S->stream) !=
+      cudaSuccess)
+    return FISHGPU_ERR_CUDA;
+  const Level<T> &c = H.lev[0];
+  const long long per = level_points(H.lev[top].g);
+  H.tail_threads = (int)std::min<long long>(1024, std::max<long long>(64, (per + 31) / 32 * 32));
+  const size_t smb = coarse_smem_bytes<T>(S->fine.dim, c.n[0], c.n[1], c.n[2]);
+  H.tail_smem = (c.n[0] * c.n[1] * c.n[2] > 0 && smb <= 48 * 1024) ? smb : 0;
+  H.tail_top = top;
+  return FISHGPU_OK;
+}
+
 template <typename T>
 static int build_hier(fishgpu_solver *S, Hier<T> &H) {
   const fishgpu_opts &o = S->o;
@@ -257,7 +350,171 @@ static int build_hier(fishgpu_solver *S, Hier<T> &H) {
       return FISHGPU_ERR_CUDA;
     for (int d = c.g.dim; d < 3; d++) c.S[d] = c.S[0];  // unused
   }
-  return FISHGPU_OK;
+  return build_tail<T>(S, H);
+}
+
+// ------------------------------------------------------------------ V-cycle tail
+// The coarse end of a V-cycle in ONE block per grid (per instance of a
+// batch): levels tail_top .. 1 pre-smooth, take their residual and restrict
+// it, level 0 is solved exactly, and on the way up every level adds the
+// prolongated correction and post-smooths -- the work of ~7 launches per
+// level, each too small to fill the GPU, as phases separated by block
+// barriers.  Every point is computed by the same operations in the same
+// order as the vectorised kernels (resid_pt restates resid_el, and so on),
+// so the V-cycle is bit-identical to the launch-per-phase form.
+
+// b - A x at one point (resid_el's operations on one point)
+template <int DIM, typename T>
+__device__ __forceinline__ T resid_pt(const Geom &g, const Wv<T> &w, const T *__restrict__ x, long long n, int i, int j,
+                                      int k, T bv) {
+  const T xc = x[n];
+  const bool bd = jk_bdry(g, DIM, j, k) || i == 0 || i == g.mx - 1;
+  if (bd) return fma(-w.sd, xc, bv);
+  const T a = (i - 1 > 0 ? x[n - 1] : T(0)) + (i + 1 < g.mx - 1 ? x[n + 1] : T(0));
+  T s = fma(w.sx, a, bv);
+  if (DIM >= 2) s = fma(w.sy, (j - 1 > 0 ? x[n - g.pitch] : T(0)) + (j + 1 < g.my - 1 ? x[n + g.pitch] : T(0)), s);
+  if (DIM >= 3) s = fma(w.sz, (k - 1 > 0 ? x[n - g.plane] : T(0)) + (k + 1 < g.mz - 1 ? x[n + g.plane] : T(0)), s);
+  return fma(-w.sd, xc, s);
+}
+
+// x-interpolated coarse value at fine x-index fi of coarse row (jc, kc) (v_prolong's lo/hi)
+template <typename T>
+__device__ __forceinline__ T prolong_x(const Geom &gc, const T *__restrict__ xc, int fi, int jc, int kc) {
+  const long long m = (long long)kc * gc.plane + (long long)jc * gc.pitch;
+  const int I = fi >> 1;
+  if ((fi & 1) == 0) return xc[m + I];
+  return T(0.5) * (xc[m + I] + (I + 1 < gc.mx ? xc[m + I + 1] : T(0)));
+}
+
+// restricted row value at coarse x-index I of fine row (fj, fk) (restrict_row)
+template <typename T>
+__device__ __forceinline__ T restrict_x(const Geom &gf, const T *__restrict__ rf, int I, int fj, int fk) {
+  const long long m = (long long)fk * gf.plane + (long long)fj * gf.pitch;
+  const int fi = 2 * I;
+  const T L = fi > 0 ? rf[m + fi - 1] : T(0);
+  const T R = fi + 1 < gf.pitch ? rf[m + fi + 1] : T(0);
+  return fma(T(0.5), L + R, rf[m + fi]);
+}
+
+template <int DIM, typename T>
+__global__ void __launch_bounds__(1024) k_vtail(const TailLevel<T> *__restrict__ tl, int top, KspState *st, int batch,
+                                                const T *__restrict__ S0, const T *__restrict__ S1,
+                                                const T *__restrict__ S2, const T *__restrict__ ilam, T *work, int n0,
+                                                int n1, int n2, int smem, T dinv) {
+  extern __shared__ __align__(16) unsigned char fg_tail_sm[];
+  const int plane = (DIM < 3 && batch) ? (int)blockIdx.x : 0;  // instance of a batch
+  if (batch && st) st += plane;
+  if (ksp_done(st)) return;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const T h = T(0.5);
+  // points of level l (one plane of a batch); (i, j, k) and the element offset
+  auto npts = [&](const Geom &g) { return g.mx * g.my * (DIM < 3 ? 1 : g.mz); };
+  auto pos = [&](const Geom &g, int q, int &i, int &j, int &k) -> long long {
+    i = q % g.mx;
+    const int r = q / g.mx;
+    j = DIM >= 2 ? r % g.my : 0;
+    k = DIM >= 3 ? r / g.my : plane;
+    return (long long)k * g.plane + (long long)j * g.pitch + i;
+  };
+  for (int l = top; l >= 1; l--) {
+    const TailLevel<T> &L = tl[l];
+    const TailLevel<T> &C = tl[l - 1];
+    const Geom &g = L.g;
+    const Wv<T> w(g);
+    const int N = npts(g);
+    for (int q = tid; q < N; q += nt) {  // two Chebyshev steps from zero (v_cheb2_zero): X[1]
+      int i, j, k;
+      const long long n = pos(g, q, i, j, k);
+      const T mab = resid_pt<DIM, T>(g, w, L.b, n, i, j, k, T(0));
+      L.X[1][n] = fma(L.a1, mab, L.a0 * L.b[n]);
+    }
+    __syncthreads();
+    for (int q = tid; q < N; q += nt) {  // r = b - A x (v_resid)
+      int i, j, k;
+      const long long n = pos(g, q, i, j, k);
+      L.r[n] = resid_pt<DIM, T>(g, w, L.X[1], n, i, j, k, L.b[n]);
+    }
+    __syncthreads();
+    const Geom &gc = C.g;
+    const int Nc = npts(gc);
+    for (int q = tid; q < Nc; q += nt) {  // b_c = P^T r (v_restrict)
+      int I, J, K;
+      const long long m = pos(gc, q, I, J, K);
+      auto rowsum = [&](int fk) -> T {
+        const int fj = 2 * J;
+        const T c = restrict_x<T>(g, L.r, I, fj, fk);
+        if (DIM < 2) return c;
+        const T sr = fj - 1 >= 0 ? restrict_x<T>(g, L.r, I, fj - 1, fk) : T(0);
+        const T nr = fj + 1 < g.my ? restrict_x<T>(g, L.r, I, fj + 1, fk) : T(0);
+        return fma(h, sr + nr, c);
+      };
+      T o;
+      if (DIM >= 3) {
+        const T below = K > 0 ? rowsum(2 * K - 1) : T(0);
+        const T mid = rowsum(2 * K);
+        const T above = 2 * K + 1 < g.mz ? rowsum(2 * K + 1) : T(0);
+        o = fma(h, below + above, mid);
+      } else {
+        o = rowsum(K);  // 2D: K is the instance plane
+      }
+      C.b[m] = o;
+    }
+    __syncthreads();
+  }
+  {  // exact solve on level 0 into X[0]
+    const TailLevel<T> &C = tl[0];
+    const long long off = DIM < 3 ? (long long)plane * C.g.plane : 0;
+    coarse_solve_block<DIM, T>(C.g, C.b + off, C.X[0] + off, S0, S1, S2, ilam, work, n0, n1, n2, smem, dinv,
+                               fg_tail_sm);
+    __syncthreads();
+  }
+  for (int l = 1; l <= top; l++) {
+    const TailLevel<T> &L = tl[l];
+    const TailLevel<T> &C = tl[l - 1];
+    const Geom &g = L.g, &gc = C.g;
+    const Wv<T> w(g);
+    const int N = npts(g);
+    for (int q = tid; q < N; q += nt) {  // x += P x_c (v_prolong), x in X[1]
+      int i, j, k;
+      const long long n = pos(g, q, i, j, k);
+      const int J = j >> 1, K = DIM >= 3 ? k >> 1 : k;
+      const T a0 = prolong_x<T>(gc, C.X[0], i, J, K);
+      T v;
+      T wgt = T(1);
+      if (DIM >= 3 && (k & 1)) {
+        const T b0 = prolong_x<T>(gc, C.X[0], i, J, K + 1);
+        if (j & 1) {
+          const T a1 = prolong_x<T>(gc, C.X[0], i, J + 1, K), b1 = prolong_x<T>(gc, C.X[0], i, J + 1, K + 1);
+          v = (a0 + a1) + (b0 + b1);
+          wgt = T(0.25);
+        } else {
+          v = a0 + b0;
+          wgt = h;
+        }
+      } else if (DIM >= 2 && (j & 1)) {
+        v = a0 + prolong_x<T>(gc, C.X[0], i, J + 1, K);
+        wgt = h;
+      } else {
+        v = a0;
+      }
+      L.X[1][n] = fma(wgt, v, L.X[1][n]);
+    }
+    __syncthreads();
+    for (int q = tid; q < N; q += nt) {  // x1 = x0 + c1 (b - A x0) (v_cheb without x_{k-1}): X[2]
+      int i, j, k;
+      const long long n = pos(g, q, i, j, k);
+      const T r = resid_pt<DIM, T>(g, w, L.X[1], n, i, j, k, L.b[n]);
+      L.X[2][n] = fma(L.c1, r, T(1) * L.X[1][n]);
+    }
+    __syncthreads();
+    for (int q = tid; q < N; q += nt) {  // x2 = ckm1 x0 + ck x1 + crd (b - A x1) (v_cheb): X[0]
+      int i, j, k;
+      const long long n = pos(g, q, i, j, k);
+      const T r = resid_pt<DIM, T>(g, w, L.X[2], n, i, j, k, L.b[n]);
+      L.X[0][n] = fma(L.crd, r, fma(L.ckm1, L.X[1][n], L.ck * L.X[2][n]));
+    }
+    __syncthreads();
+  }
 }
 
 // ------------------------------------------------------------------ enqueue
@@ -423,6 +680,16 @@ static void enq_vcycle(fishgpu_solver *S, Hier<T> &H, int l, bool from_zero, int
   Level<T> &lv = H.lev[l];
   cudaStream_t s = S->stream;
   KspState *st = S->st;
+  if constexpr (DIM >= 2) {
+    if (l > 0 && l == H.tail_top && from_zero && dots < 0) {  // levels l .. 0 in one block per instance
+      const Level<T> &c = H.lev[0];
+      k_vtail<DIM, T><<<DIM < 3 && S->batch ? (unsigned)S->nplanes : 1u, H.tail_threads, H.tail_smem, s>>>(
+          H.tail, l, st, DIM < 3 ? S->batch : 0, c.S[0], c.S[1], c.S[2], c.ilam, c.work, c.n[0], c.n[1], c.n[2],
+          H.tail_smem ? 1 : 0, (T)(1.0 / c.g.scdiag));
+      for (int q = 0; q <= l; q++) H.lev[q].cur = 0;  // every tail level ends with its iterate in X[0]
+      return;
+    }
+  }
   if (l == 0) {
     lv.cur = 0;
     // a block of just enough threads (tiny coarsest grids start and synchronise
@@ -1143,7 +1410,8 @@ static int validate_opts(const fishgpu_opts *o) {
   if (o->pc_type < 0 || o->pc_type > FISHGPU_PC_MG) return FISHGPU_ERR_UNSUPPORTED;
   if (o->smooth_its < 1 || o->max_it < 0 || o->mg_cycles < 1 || o->mg_cycles > 2) return FISHGPU_ERR_ARG;
   if (o->precision != FISHGPU_FP64 && o->precision != FISHGPU_MIXED) return FISHGPU_ERR_ARG;
-  if (o->loop_cap < 0 || !(o->first_floor_scale > 0) || o->inner_accurate < -1 || o->inner_accurate > 1)
+  if (o->loop_cap < 0 || !(o->first_floor_scale > 0) || o->inner_accurate < -1 || o->inner_accurate > 1 ||
+      o->vtail_points < 0)
     return FISHGPU_ERR_ARG;
   if (o->precision == FISHGPU_MIXED && o->pc_type != FISHGPU_PC_MG) return FISHGPU_ERR_UNSUPPORTED;
   if (o->initial_type < 0 || o->initial_type > FISHGPU_INITIAL_GIVEN) return FISHGPU_ERR_ARG;
@@ -1293,7 +1561,9 @@ extern "C" long long fishgpu_solver_estimate_bytes(const fishgpu_opts *o) {
   else b += 3 * rnd(8LL * N);                                              // p q w
   if (o->pc_type != FISHGPU_PC_MG) return b + rnd((long long)es * N);
   Geom lv = g;
+  std::vector<long long> pts(o->mg_levels, 0);  // nodes per level (build_tail's choice below)
   for (int l = o->mg_levels - 1; l >= 0; l--) {
+    pts[l] = level_points(lv);
     const long long Nl = (long long)nelem(lv);
     b += 3 * rnd((long long)es * Nl) + (l > 0 ? rnd((long long)es * Nl) : 0) + (l < o->mg_levels - 1 ? rnd((long long)es * Nl) : 0);
     if (l > 0) {
@@ -1309,6 +1579,14 @@ extern "C" long long fishgpu_solver_estimate_bytes(const fishgpu_opts *o) {
       for (int q = 0; q < dim && ni > 0; q++) b += rnd((long long)es * (m[q] - 2) * (m[q] - 2));
       if (ni > 0) b += rnd((long long)es * ni) + rnd((long long)es * 2 * ni);  // 1/lambda, work area
     }
+  }
+  if (o->vtail && o->smooth_type == FISHGPU_SMOOTH_CHEBYSHEV && o->smooth_its == 2 && o->mg_cycles == 1 &&
+      dim >= 2 && o->mg_levels >= 3) {  // the V-cycle tail's level table
+    int top = 0;
+    for (int l = 1; l <= o->mg_levels - 2; l++)
+      if (pts[l] <= tail_max_points(*o, es)) top = l;
+    if (top > 0)
+      b += rnd((long long)(es == 4 ? sizeof(TailLevel<float>) : sizeof(TailLevel<double>)) * (top + 1));
   }
   return b;
 }

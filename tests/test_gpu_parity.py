@@ -525,3 +525,29 @@ def test_tma_apply_matches_the_slot_march(cuda, args):
     d = (u1 - u0).abs().max().item()
     assert d <= 1e-9 * u0.abs().max().item()
     assert abs(a.errinf - b.errinf) <= 1e-9 * u0.abs().max().item()
+
+
+@pytest.mark.parametrize("args", [
+    "-fsh_dim 2 -fsh_problem manupoly -da_refine 7 -pc_type mg -mg_levels_ksp_type chebyshev "
+    "-mg_levels_pc_type jacobi -ksp_rtol 1e-10",
+    "-fsh_dim 2 -fsh_problem manupoly -da_refine 8 -pc_type mg -ksp_rtol 1e-10 -fsh_precision mixed",
+    "-fsh_dim 2 -fsh_problem manupoly -da_grid_x 5 -da_grid_y 3 -da_refine 7 -pc_type mg -ksp_rtol 1e-10 -fsh_cy 3",
+    "-fsh_dim 3 -fsh_problem manupoly -da_refine 5 -pc_type mg -ksp_rtol 1e-10",
+    "-fsh_dim 3 -fsh_problem manuexp -da_refine 6 -pc_type mg -ksp_rtol 1e-10 -fsh_precision mixed",
+    "-fsh_dim 3 -fsh_problem manupoly -da_grid_x 3 -da_grid_y 5 -da_grid_z 9 -da_refine 3 -pc_type mg "
+    "-ksp_rtol 1e-10 -fsh_cz 2 -ksp_norm_type unpreconditioned",
+    "-fsh_dim 3 -fsh_problem manupoly -da_grid_x 3 -da_grid_y 5 -da_grid_z 9 -da_refine 3 -pc_type mg "
+    "-ksp_rtol 1e-10 -fsh_cz 2 -fsh_precision mixed",
+])
+def test_vcycle_tail_is_bit_identical(cuda, args):
+    """The V-cycle's small levels in one block (k_vtail) compute every point
+    with the operations of the per-phase kernels, in the same order: the
+    solve is identical, bit for bit, to the launch-per-phase form."""
+    import torch
+    fg = fgmod()
+    u1, a = fg.solve(fg.options(args + " -fsh_vtail 1"))
+    u0, b = fg.solve(fg.options(args + " -fsh_vtail 0"))
+    assert a.reason == b.reason == 2 and a.its == b.its and a.outer_its == b.outer_its
+    assert a.history() == b.history()
+    assert torch.equal(u1, u0)
+    assert a.launches <= b.launches  # fewer wherever a level is small enough for the tail
