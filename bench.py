@@ -270,16 +270,26 @@ def minimal_leg(fg, reps=3):
         "grid_ms": [rep.grid_ms[k] for k in range(rep.ngrids)],
         "inner_its_per_grid": [sum(rep.ksp_its[k][i] for i in range(rep.its[k])) for k in range(rep.ngrids)],
     }
-    # the oracle's Newton (exact sparse solves, one host core) on a bounded sample of the same flow
+    # the same method on the host cores: the oracle's Newton + BiCGStab + Poisson-multigrid
+    # solve (FP64, OpenMP) of the same 33^2 -> 1025^2 sequence, best of two
     try:
         sys.path.insert(0, os.path.join(ROOT, "tests"))
         import _ms_oracle as mso
-        t0 = time.perf_counter()
-        lv, g, uo, err = mso.solve(base=33, grid_sequence=2, rtol=1e-10)
-        dt = time.perf_counter() - t0
-        out["cpu_baseline"] = {"value": g.mx * g.my / dt, "unit": "DOF/s", "cores": 1, "kind": "port",
-                               "sample": "oracle Newton + sparse direct solves, 33^2 -> 129^2 (%.2f s)" % dt}
-    except Exception as e:  # scipy missing: report why
+        import _oracle as orc
+        best = None
+        for _ in range(2):
+            t0 = time.perf_counter()
+            _, nk = mso.nk_solve(base=33, grid_sequence=5, rtol=1e-10)
+            dt = time.perf_counter() - t0
+            best = dt if best is None or dt < best else best
+        m = nk.m[nk.ngrids - 1]
+        out["cpu_baseline"] = {"value": m * m / best, "unit": "DOF/s", "cores": orc.lib().or_num_threads(),
+                               "kind": "port", "newton_its": [nk.its[k] for k in range(nk.ngrids)],
+                               "inner_its_total": nk.ksp_its, "errinf": nk.errinf,
+                               "sample": "oracle Newton + BiCGStab/Poisson-MG (FP64, OpenMP), 33^2 -> %d^2 by grid "
+                                         "sequencing, snes rtol 1e-10, ksp rtol 1e-5, best of 2 (%.2f s)" % (m, best)}
+        out["gpu_over_cpu"] = out["dof_per_s"] / out["cpu_baseline"]["value"]
+    except Exception as e:  # oracle library missing: report why
         out["cpu_baseline"] = {"unavailable": str(e)[:200]}
     return out
 

@@ -604,6 +604,33 @@ static void mg_apply(mg_ctx *mg, const double *r, double *z) {
   vcopy(N, top->x, z);
 }
 
+/* The multigrid V-cycle as a preconditioner object for other oracle solvers
+   (the minimal-surface Newton-Krylov baseline): the hierarchy of o->grid with
+   o's smoother options; the options are copied. */
+typedef struct {
+  or_opts o;
+  mg_ctx mg;
+} or_mg;
+
+void *or_mg_new(const or_opts *o) {
+  or_mg *m = (or_mg *)calloc(1, sizeof(or_mg));
+  if (!m) return NULL;
+  m->o = *o;
+  if (mg_setup(&m->o, &m->mg) != 0) {
+    free(m);
+    return NULL;
+  }
+  return m;
+}
+
+void or_mg_apply(void *m, const double *r, double *z) { mg_apply(&((or_mg *)m)->mg, r, z); }
+
+void or_mg_free(void *m) {
+  if (!m) return;
+  mg_free(&((or_mg *)m)->mg);
+  free(m);
+}
+
 /* ---- ILU(0), natural ordering, on the Jacobian pattern ---- */
 typedef struct {
   or_grid g;

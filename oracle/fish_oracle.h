@@ -103,6 +103,11 @@ int or_exact_solve(const or_grid *g, const double *b, double *x);
 
 /* KSP solve J y = b from y = 0 with the selected PC; returns 0 or -1 (bad args) */
 int or_ksp_solve(const or_opts *o, const double *b, double *y, or_report *rep);
+/* one V-cycle of the multigrid preconditioner of o (pc mg, o's smoother
+   options) as an object: z = B r on o->grid */
+void *or_mg_new(const or_opts *o);
+void or_mg_apply(void *mg, const double *r, double *z);
+void or_mg_free(void *mg);
 
 /* the whole fish flow: u0, F(u0), KSP, u = u0 - y, errors.  u: output. */
 int or_fish_solve(const or_opts *o, double *u, or_report *rep);

@@ -62,6 +62,7 @@ static void neighbours(const ms_grid *g, const double *u, int i, int j, double v
 void ms_residual(const ms_grid *g, const double *u, double *F) {
   const int mx = g->mx, my = g->my;
   const double hx = 1.0 / (mx - 1), hy = 1.0 / (my - 1), hxhy = hx / hy, hyhx = hy / hx;
+#pragma omp parallel for schedule(static)
   for (int j = 0; j < my; j++)
     for (int i = 0; i < mx; i++) {
       const long n = (long)j * mx + i;
@@ -129,6 +130,28 @@ static void row_weights(const ms_grid *g, const double A[4], const double Q[4], 
   w[2] = a * Qe + b * Qs;                   /* se */
   w[6] = a * Qw + b * Qn;                   /* nw */
   w[0] = -a * Qw - b * Qs;                  /* sw */
+}
+
+/* the nine column weights of every row (ms_jv's, once per linearisation
+   point): w[9 n + (dj+1)*3 + di+1]; boundary rows get w[9n+4] = 1 and zeros */
+void ms_row_weights(const ms_grid *g, const double *u, double *w) {
+  const int mx = g->mx, my = g->my;
+#pragma omp parallel for schedule(static)
+  for (int j = 0; j < my; j++)
+    for (int i = 0; i < mx; i++) {
+      const long n = (long)j * mx + i;
+      double *wn = w + 9 * n;
+      if (on_bdry(g, i, j)) {
+        for (int q = 0; q < 9; q++) wn[q] = q == 4 ? 1.0 : 0.0;
+        continue;
+      }
+      double A[4], Q[4];
+      node_coefs(g, u, i, j, A, Q);
+      row_weights(g, A, Q, wn);
+      for (int dj = -1; dj <= 1; dj++)
+        for (int di = -1; di <= 1; di++)
+          if (on_bdry(g, i + di, j + dj)) wn[(dj + 1) * 3 + di + 1] = 0.0;
+    }
 }
 
 void ms_jv(const ms_grid *g, const double *u, const double *v, double *out) {

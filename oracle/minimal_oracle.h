@@ -29,6 +29,8 @@ void ms_initial(const ms_grid *g, double *u);
 void ms_exact(const ms_grid *g, double *u);
 /* F(u), FormFunctionLocal */
 void ms_residual(const ms_grid *g, const double *u, double *F);
+/* the row weights of J at u, 9 per node (see minimal_oracle.c) */
+void ms_row_weights(const ms_grid *g, const double *u, double *w);
 /* J v, the exact derivative of F at u applied to v */
 void ms_jv(const ms_grid *g, const double *u, const double *v, double *out);
 /* the same Jacobian in CSR form (9 entries per interior row, 1 per boundary row);

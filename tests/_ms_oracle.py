@@ -27,6 +27,12 @@ class MsGrid(ctypes.Structure):
                 ("catenoid_c", ctypes.c_double), ("tent_H", ctypes.c_double)]
 
 
+class NkReport(ctypes.Structure):
+    _fields_ = [("ngrids", ctypes.c_int), ("m", ctypes.c_int * 16), ("its", ctypes.c_int * 16),
+                ("reason", ctypes.c_int * 16), ("ksp_its", ctypes.c_longlong), ("errinf", ctypes.c_double),
+                ("fnorm_last", ctypes.c_double)]
+
+
 _bound = False
 
 
@@ -48,6 +54,8 @@ def lib():
         L.ms_area.argtypes = [P(MsGrid), dp, ctypes.c_int, P(ctypes.c_double), P(ctypes.c_double),
                               P(ctypes.c_double)]
         L.ms_interpolate.argtypes = [P(MsGrid), dp, P(MsGrid), dp]
+        L.ms_nk_solve.argtypes = [P(MsGrid), ctypes.c_int, ctypes.c_double, ctypes.c_double, dp, P(NkReport)]
+        L.ms_nk_solve.restype = ctypes.c_int
         _bound = True
     return L
 
@@ -297,3 +305,18 @@ def bratu_solve(base=3, refine=0, grid_sequence=0, lam=1.0, exact=False, rtol=1e
     u = levels[-1]["u"]
     err = float(np.max(np.abs(u - model.exact()))) if exact else None
     return levels, model, u, err
+
+
+def nk_solve(base=33, grid_sequence=5, rtol=1e-10, ksp_rtol=1e-5, problem=CATENOID, q=-0.5, c=1.1, H=1.0):
+    """The GPU library's method on the CPU (oracle/ms_nk.c): Newton with the
+    cubic line search, BiCGStab right-preconditioned with the Poisson V-cycle,
+    grid sequencing; FP64, OpenMP.  Returns (u of the last grid, report)."""
+    g = grid(base, problem, q, c, H)
+    m = base
+    for _ in range(grid_sequence):
+        m = 2 * m - 1
+    u = np.empty(m * m)
+    rep = NkReport()
+    rc = lib().ms_nk_solve(ctypes.byref(g), grid_sequence, rtol, ksp_rtol, u, ctypes.byref(rep))
+    assert rc == 0, rc
+    return u, rep

@@ -137,3 +137,14 @@ def test_bratu_jacobian_is_the_derivative():
 def test_bratu_error_is_second_order():
     errs = [ms.bratu_solve(refine=r, exact=True, rtol=1e-12)[3] for r in (3, 4, 5)]
     assert errs[0] / errs[1] > 3.5 and errs[1] / errs[2] > 3.5
+
+
+def test_newton_krylov_baseline_reaches_the_newton_solution():
+    """The CPU Newton-Krylov-multigrid solve (the minimal-surface leg's CPU
+    baseline) converges on every grid of a sequence and ends at the solution
+    of the exact-Newton oracle."""
+    u, rep = ms.nk_solve(base=9, grid_sequence=3, rtol=1e-10)
+    assert rep.ngrids == 4 and all(rep.reason[k] > 0 for k in range(4))
+    lv, g, uo, err = ms.solve(base=9, grid_sequence=3, rtol=1e-10)
+    assert np.max(np.abs(u - uo)) <= 1e-7
+    assert abs(rep.errinf - err) <= 1e-6 * err
