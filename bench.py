@@ -194,6 +194,7 @@ def batch_leg(torch, fg, n_inst, reps=3):
         if best is None or rep.solve_ms < best.solve_ms:
             best = rep
     inner, outer, rel, reason = b.results()
+    groups = b.groups()
     b.close()
     return {
         "workload": "%d 2D Poisson instances, n = 2^k+1, k ~ U{5..9} (seed 0), f ~ N(0,1) (seed 1), rtol 1e-8, "
@@ -202,6 +203,9 @@ def batch_leg(torch, fg, n_inst, reps=3):
         "dofs": best.dofs, "dof_per_s": best.dofs / (best.solve_ms * 1e-3), "groups": best.groups,
         "converged": best.converged, "max_outer": best.max_outer, "max_inner": best.max_inner,
         "max_rel_resid": max(rel), "launches": best.launches, "setup_s": setup_s,
+        "size_groups": [{"n": n, "instances": c, "smoothing_steps": sw} for n, c, sw in groups],
+        "tuning": "tiles (block size, rows per thread) per level by timing a smoothing step; smoothing steps "
+                  "per group by timing batched solves of up to 32 instances (part of setup_s)",
         "timing": "CUDA events around one batched solve, best of %d" % reps,
     }
 

@@ -296,8 +296,13 @@ typedef struct {
   int smooth_its;         /* Chebyshev/Jacobi steps per level (2: V(2,2)) */
   int mg_cycles;          /* 1 = V, 2 = W                                 */
   double esteig[4];
-  int tune;               /* pick each level's block size by timing       */
+  int tune;               /* pick each level's tiles (block size, rows per
+                             thread) by timing one smoothing step          */
   int inner_accurate;     /* as fishgpu_opts.inner_accurate, per size group (default -1) */
+  int tune_sweeps;        /* with tune: smoothing steps per level of each
+                             size group (1, 2 or 3) picked by timing batched
+                             solves of up to 32 of its instances (default 1;
+                             0: smooth_its for every group)              */
 } fishgpu_batch_opts;
 
 typedef struct {
@@ -313,6 +318,9 @@ int fishgpu_batch_opts_default(fishgpu_batch_opts *o);
 int fishgpu_batch_create(const fishgpu_batch_opts *o, int ninst, const int *n, fishgpu_batch **out);
 /* f[q], u[q]: device pointers to dense n[q] x n[q] arrays (x fastest) */
 int fishgpu_batch_solve(fishgpu_batch *b, const double *const *f, double *const *u, fishgpu_batch_report *rep);
+/* per size group g (largest first): nodes per side, instances and the
+   smoothing steps per level in use; returns the number of groups */
+int fishgpu_batch_groups(const fishgpu_batch *b, int *n, int *count, int *sweeps);
 /* per-instance results of the last solve (host arrays of ninst, any may be NULL) */
 int fishgpu_batch_results(const fishgpu_batch *b, int *inner_its, int *outer_its, double *rel_resid, int *reason);
 int fishgpu_batch_destroy(fishgpu_batch *b);

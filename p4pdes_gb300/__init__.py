@@ -103,7 +103,7 @@ class Report(ctypes.Structure):
 class BatchOpts(ctypes.Structure):
     _fields_ = [("rtol", c_double), ("atol", c_double), ("inner_rtol", c_double), ("inner_max_it", c_int),
                 ("outer_max_it", c_int), ("smooth_its", c_int), ("mg_cycles", c_int), ("esteig", c_double * 4),
-                ("tune", c_int), ("inner_accurate", c_int)]
+                ("tune", c_int), ("inner_accurate", c_int), ("tune_sweeps", c_int)]
 
 
 class BatchReport(ctypes.Structure):
@@ -211,8 +211,9 @@ def load():
     lib.fishgpu_batch_solve.argtypes = [c_void_p, _P(c_void_p), _P(c_void_p), _P(BatchReport)]
     lib.fishgpu_batch_results.argtypes = [c_void_p, _P(c_int), _P(c_int), _P(c_double), _P(c_int)]
     lib.fishgpu_batch_destroy.argtypes = [c_void_p]
+    lib.fishgpu_batch_groups.argtypes = [c_void_p, _P(c_int), _P(c_int), _P(c_int)]
     for name in ("fishgpu_batch_opts_default", "fishgpu_batch_create", "fishgpu_batch_solve",
-                 "fishgpu_batch_results", "fishgpu_batch_destroy"):
+                 "fishgpu_batch_results", "fishgpu_batch_destroy", "fishgpu_batch_groups"):
         getattr(lib, name).restype = c_int
     lib.fishgpu_solver_time_kernel.argtypes = [c_void_p, ctypes.c_char_p, c_int, _P(c_double), _P(c_double)]
     lib.fishgpu_fp64_fma_rate.argtypes = [c_int, _P(c_double)]
@@ -466,6 +467,13 @@ class Batch:
         a, b, c, d = (c_int * n)(), (c_int * n)(), (c_double * n)(), (c_int * n)()
         _check(load().fishgpu_batch_results(self._h, a, b, c, d), "fishgpu_batch_results")
         return list(a), list(b), list(c), list(d)
+
+    def groups(self):
+        """[(n, instances, smoothing steps per level)] per size group, largest first."""
+        k = len(set(self.sizes))
+        a, b, c = (c_int * k)(), (c_int * k)(), (c_int * k)()
+        ng = load().fishgpu_batch_groups(self._h, a, b, c)
+        return [(a[g], b[g], c[g]) for g in range(ng)]
 
     def close(self):
         if self._h:

@@ -23,6 +23,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <chrono>
 #include <map>
 #include <mutex>
 #include <thread>
@@ -1864,12 +1865,20 @@ __global__ void __launch_bounds__(256) k_unpack_planes(Geom g, const double *__r
 }
 
 // ---------------------------------------------------------------- autotuner
-// Picks the block size (slots per block) of each level of a group by timing
-// one Chebyshev step with each candidate; results are cached per (n, planes).
+// Tiles: the block size (slots per block) and the strip of rows a stencil
+// thread marches (ry: 0 = one slot per thread, or 4 .. 32 rows) of each level
+// of a group, by timing one Chebyshev step with each candidate pair; cached
+// per (n, planes).  Sweeps: the smoothing steps per level (V(1,1), V(2,2),
+// V(3,3)) of a group, by timing whole batched solves of up to 32 instances of
+// its size with each count (tune_sweeps); cached per n.
+struct TileChoice {
+  int chunk, ry;
+};
 static std::mutex g_tune_mu;
-static std::map<std::pair<int, int>, int> g_tune_cache;
+static std::map<std::pair<int, int>, TileChoice> g_tune_cache;
+static std::map<std::pair<int, int>, int> g_sweep_cache;
 
-static int tune_chunk(fishgpu_solver *S, Level<float> &lv) {
+static TileChoice tune_tiles(fishgpu_solver *S, Level<float> &lv) {
   const std::pair<int, int> key(lv.g.mx, lv.g.mz);
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
@@ -1877,26 +1886,32 @@ static int tune_chunk(fishgpu_solver *S, Level<float> &lv) {
     if (it != g_tune_cache.end()) return it->second;
   }
   static const int cand[3] = {64, 128, 256};
-  int best = 256;
+  static const int rows[5] = {0, 4, 8, 16, 32};
+  TileChoice best{256, batch_rows(lv.g)};
   float best_ms = 1e30f;
   cudaStream_t s = S->stream;
-  for (int c = 0; c < 3; c++) {
-    const Slots sl = make_slots(lv.g, ZC, 2432, cand[c], 1, batch_rows(lv.g));
-    const unsigned gb = slot_blocks(sl);
-    // b = the level's residual buffer, x_{k-1}, x_k, out: its three iterate buffers
-    for (int w = 0; w < 2; w++)
-      v_cheb<2, float, true><<<gb, sl.chunk, 0, s>>>(lv.g, sl, nullptr, lv.r, lv.X[0], lv.X[1], lv.X[2], 0.5f, 0.5f,
-                                                      0.1f);
-    cudaEventRecord(S->ev0, s);
-    for (int r = 0; r < 5; r++)
-      v_cheb<2, float, true><<<gb, sl.chunk, 0, s>>>(lv.g, sl, nullptr, lv.r, lv.X[0], lv.X[1], lv.X[2], 0.5f, 0.5f,
-                                                      0.1f);
-    cudaEventRecord(S->ev1, s);
-    if (cudaEventSynchronize(S->ev1) != cudaSuccess) return 256;
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, S->ev0, S->ev1);
-    if (ms < best_ms) { best_ms = ms; best = cand[c]; }
-  }
+  for (int c = 0; c < 3; c++)
+    for (int r = 0; r < 5; r++) {
+      if (rows[r] > lv.g.my) continue;
+      const Slots sl = make_slots(lv.g, ZC, 2432, cand[c], 1, rows[r]);
+      const unsigned gb = slot_blocks(sl);
+      // b = the level's residual buffer, x_{k-1}, x_k, out: its three iterate buffers
+      for (int w = 0; w < 2; w++)
+        v_cheb<2, float, true><<<gb, sl.chunk, 0, s>>>(lv.g, sl, nullptr, lv.r, lv.X[0], lv.X[1], lv.X[2], 0.5f,
+                                                        0.5f, 0.1f);
+      cudaEventRecord(S->ev0, s);
+      for (int q = 0; q < 5; q++)
+        v_cheb<2, float, true><<<gb, sl.chunk, 0, s>>>(lv.g, sl, nullptr, lv.r, lv.X[0], lv.X[1], lv.X[2], 0.5f,
+                                                        0.5f, 0.1f);
+      cudaEventRecord(S->ev1, s);
+      if (cudaEventSynchronize(S->ev1) != cudaSuccess) return best;
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, S->ev0, S->ev1);
+      if (ms < best_ms) {
+        best_ms = ms;
+        best = TileChoice{cand[c], rows[r]};
+      }
+    }
   std::lock_guard<std::mutex> lk(g_tune_mu);
   g_tune_cache[key] = best;
   return best;
@@ -1996,9 +2011,9 @@ static int group_create(const fishgpu_batch_opts &bo, int n, int count, fishgpu_
     }
     for (int l = S->h32.nlev - 1; l >= 1; l--) {
       Level<float> &lv = S->h32.lev[l];
-      const int c = tune_chunk(S, lv);
-      lv.sl = make_slots(lv.g, ZC, 2432, c, 1);
-      lv.st = make_slots(lv.g, ZC, 2432, c, 1, batch_rows(lv.g));
+      const TileChoice c = tune_tiles(S, lv);
+      lv.sl = make_slots(lv.g, ZC, 2432, c.chunk, 1);
+      lv.st = make_slots(lv.g, ZC, 2432, c.chunk, 1, c.ry);
     }
     S->sf = S->h32.lev[S->h32.nlev - 1].sl;
   }
@@ -2178,6 +2193,83 @@ static int group_solve(fishgpu_solver *S, const double *const *f, double *const 
 
 }  // namespace fg
 
+namespace fg {
+
+// a deterministic right-hand side for the sweep tuner: uniform in [-1, 1)
+static __global__ void k_fill_rhs(double *__restrict__ f, long long n, unsigned long long seed) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    unsigned long long x = (seed ^ (unsigned long long)t) + 0x9E3779B97F4A7C15ULL;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBULL;
+    x ^= x >> 31;
+    f[t] = (double)(x >> 11) * 0x1.0p-52 - 1.0;
+  }
+}
+
+// Smoothing steps per level for a group of n x n instances: the count among
+// 1, 2, 3 whose batched solve of min(count, 32) instances (a fixed random
+// right-hand side, the batch's tolerances) takes least time, every instance
+// converged; the batch's own count when no candidate does better.
+static int tune_sweeps(const fishgpu_batch_opts &bo, int n, int count) {
+  const int q = std::min(count, 32);
+  const std::pair<int, int> key(n, q);
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_sweep_cache.find(key);
+    if (it != g_sweep_cache.end()) return it->second;
+  }
+  const long long per = (long long)n * n;
+  double *f = nullptr, *u = nullptr;
+  double **fp = nullptr, **up = nullptr;
+  int best = bo.smooth_its;
+  if (cudaMalloc((void **)&f, sizeof(double) * per * q) != cudaSuccess ||
+      cudaMalloc((void **)&u, sizeof(double) * per * q) != cudaSuccess ||
+      cudaMalloc((void **)&fp, sizeof(double *) * q) != cudaSuccess ||
+      cudaMalloc((void **)&up, sizeof(double *) * q) != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(f); cudaFree(u); cudaFree(fp); cudaFree(up);
+    return best;
+  }
+  std::vector<double *> hf(q), hu(q);
+  for (int p = 0; p < q; p++) {
+    hf[p] = f + per * p;
+    hu[p] = u + per * p;
+  }
+  cudaMemcpy(fp, hf.data(), sizeof(double *) * q, cudaMemcpyHostToDevice);
+  cudaMemcpy(up, hu.data(), sizeof(double *) * q, cudaMemcpyHostToDevice);
+  k_fill_rhs<<<256, 256>>>(f, per * q, 12345ULL);
+  cudaDeviceSynchronize();
+  std::vector<int> its(q), outer(q), reason(q);
+  std::vector<double> rel(q);
+  double best_s = 1e30;
+  for (int sw = 1; sw <= 3; sw++) {
+    fishgpu_batch_opts b2 = bo;
+    b2.smooth_its = sw;
+    b2.tune_sweeps = 0;
+    fishgpu_solver *S = nullptr;
+    if (group_create(b2, n, q, &S) != FISHGPU_OK) continue;
+    double dt = 1e30;
+    bool ok = true;
+    for (int rep = 0; rep < 2 && ok; rep++) {  // the first builds the graphs
+      const auto t0 = std::chrono::steady_clock::now();
+      ok = group_solve(S, fp, up, its.data(), outer.data(), rel.data(), reason.data()) == FISHGPU_OK;
+      dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+      for (int p = 0; p < q && ok; p++) ok = reason[p] > 0;
+    }
+    fishgpu_solver_destroy(S);
+    if (ok && dt < best_s) {
+      best_s = dt;
+      best = sw;
+    }
+  }
+  cudaFree(f); cudaFree(u); cudaFree(fp); cudaFree(up);
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_sweep_cache[key] = best;
+  return best;
+}
+
+}  // namespace fg
+
 extern "C" int fishgpu_batch_opts_default(fishgpu_batch_opts *o) {
   if (!o) return FISHGPU_ERR_ARG;
   memset(o, 0, sizeof(*o));
@@ -2194,6 +2286,7 @@ extern "C" int fishgpu_batch_opts_default(fishgpu_batch_opts *o) {
   o->esteig[3] = 1.1;
   o->tune = 1;
   o->inner_accurate = -1;
+  o->tune_sweeps = 1;
   return FISHGPU_OK;
 }
 
@@ -2228,7 +2321,9 @@ extern "C" int fishgpu_batch_create(const fishgpu_batch_opts *o, int ninst, cons
   B->n.assign(n, n + ninst);
   for (auto it = bysize.rbegin(); it != bysize.rend(); ++it) {  // largest first
     fishgpu_solver *S = nullptr;
-    int rc = group_create(*o, it->first, (int)it->second.size(), &S);
+    fishgpu_batch_opts go = *o;
+    if (o->tune && o->tune_sweeps) go.smooth_its = tune_sweeps(*o, it->first, (int)it->second.size());
+    int rc = group_create(go, it->first, (int)it->second.size(), &S);
     if (rc) {
       fishgpu_batch_destroy(B);
       return rc;
@@ -2332,6 +2427,17 @@ extern "C" int fishgpu_batch_solve(fishgpu_batch *B, const double *const *f, dou
     }
   }
   return rep->converged == B->ninst ? FISHGPU_OK : FISHGPU_ERR_NOT_CONVERGED;
+}
+
+extern "C" int fishgpu_batch_groups(const fishgpu_batch *B, int *n, int *count, int *sweeps) {
+  if (!B) return FISHGPU_ERR_ARG;
+  for (size_t g = 0; g < B->groups.size(); g++) {
+    const fishgpu_solver *S = B->groups[g];
+    if (n) n[g] = S->fine.mx;
+    if (count) count[g] = S->nplanes;
+    if (sweeps) sweeps[g] = S->o.smooth_its;
+  }
+  return (int)B->groups.size();
 }
 
 extern "C" int fishgpu_batch_results(const fishgpu_batch *B, int *inner_its, int *outer_its, double *rel_resid,

@@ -83,3 +83,28 @@ def test_batch_rejects_sizes_that_do_not_coarsen(built):
         pytest.skip("needs a device")
     with pytest.raises(fg.FishError):
         fg.Batch([33, 34])
+
+
+def test_autotuner_picks_sweeps_per_group_and_every_instance_converges(cuda):
+    """With tuning on, the smoothing steps of every size group are chosen by
+    timing batched solves (1, 2 or 3 per level); the tuned batch still meets
+    rtol on every instance, checked by the oracle.  Without sweep tuning every
+    group keeps the batch's own count."""
+    import torch
+    import p4pdes_gb300 as fg
+    sizes = [65, 33, 129, 65, 17, 33]
+    fs = make_f(sizes, 5)
+    ft = [torch.from_numpy(f).cuda() for f in fs]
+    ut = [torch.full_like(f, float("nan")) for f in ft]
+    with fg.Batch(sizes, rtol=1e-8, tune=True) as b:
+        groups = b.groups()
+        rep = b.solve(ft, ut)
+    assert sorted(n for n, _, _ in groups) == sorted(set(sizes))
+    assert all(sw in (1, 2, 3) for _, _, sw in groups)
+    assert sum(c for _, c, _ in groups) == len(sizes)
+    assert rep.converged == len(sizes)
+    for f, u in zip(fs, ut):
+        relres, _ = oracle_check(f, u.cpu().numpy(), 1e-8)
+        assert relres <= 2e-8
+    with fg.Batch(sizes, rtol=1e-8, tune=True, tune_sweeps=0) as b:
+        assert all(sw == 2 for _, _, sw in b.groups())
