@@ -416,6 +416,9 @@ typedef struct {
                              run per Newton step before the solve gives up
                              with FISHGPU_ERR_TIMEOUT (0: ksp_max_it / iterations
                              per body + 5, never reached by a solve that stops) */
+  int inner_block;        /* -ms_inner_block 0|1: on grids of up to 4096 nodes whose
+                             preconditioner is one exact coarse solve, the whole
+                             inner BiCGStab runs in one block (default 1)    */
 } fishgpu_ms_opts;
 
 #define FISHGPU_MS_MAX_GRIDS 12

@@ -140,7 +140,8 @@ class MsOpts(ctypes.Structure):
                 ("rtol", c_double), ("atol", c_double), ("stol", c_double), ("max_it", c_int),
                 ("line_search", c_int), ("ksp_rtol", c_double), ("ksp_max_it", c_int), ("pc_type", c_int),
                 ("mg_levels", c_int), ("monitor_degree", c_int), ("snes_monitor", c_int),
-                ("converged_reason", c_int), ("ksp_converged_reason", c_int), ("loop_cap", c_int)]
+                ("converged_reason", c_int), ("ksp_converged_reason", c_int), ("loop_cap", c_int),
+                ("inner_block", c_int)]
 
 
 class MsReport(ctypes.Structure):

@@ -20,4 +20,18 @@ cudaStream_t solver_stream(const fishgpu_solver_s *S);
 // when the solver is not a 2D mixed-form multigrid solver.
 const float *solver_vcycle32(fishgpu_solver_s *S, const float *r, KspState *st);
 
+// The exact coarse solve that is the whole V-cycle of a 2D mixed-form
+// solver with one multigrid level: its geometry, sine-transform tables,
+// work area, shared-memory bytes (0: use `work`) and output buffer.
+struct CoarseView {
+  Geom g;
+  const float *S0, *S1, *ilam;
+  float *work, *x;
+  int n0, n1;
+  size_t smem;
+  float dinv;
+};
+// False unless the solver is a 2D mixed-form multigrid solver with one level.
+bool solver_coarse32(const fishgpu_solver_s *S, CoarseView *c);
+
 }  // namespace fg

@@ -516,6 +516,124 @@ __global__ void __launch_bounds__(256) k_bi_xr(Geom g, MsKsp *st, const float *_
   ms_reduce<2>(v2, red, XrFin{st});
 }
 
+// The whole BiCGStab solve of a small grid in ONE block: the iteration of
+// k_bi_p .. k_bi_xr above, each kernel a phase of the block (same operations
+// on every node), the preconditioner the exact coarse solve that is the whole
+// Poisson V-cycle of a grid with one multigrid level (coarse_solve_block), the
+// dot products summed over the block's threads in a fixed order.  The inner
+// solve of such a grid is ~20 launches per iteration of almost no work each;
+// here it is one launch.  Same finalisers, so the state the host reads (its,
+// reason) means the same; the dot products are summed in another order than
+// the multi-block kernels', so iterates differ from theirs by rounding.
+struct BiCoarse {
+  Geom g;
+  const float *S0, *S1, *ilam;
+  float *work, *z;
+  int n0, n1, smem;
+  float dinv;
+};
+
+__global__ void __launch_bounds__(1024) k_bi_block(Geom g, int model, float a, float b, const float4 *__restrict__ C1,
+                                                   const float4 *__restrict__ C2, const float *__restrict__ bv,
+                                                   float *__restrict__ r, float *__restrict__ rh, float *__restrict__ p,
+                                                   float *__restrict__ v, float *__restrict__ s, float *__restrict__ t,
+                                                   float *__restrict__ x, float *__restrict__ ph, float *__restrict__ sh,
+                                                   MsKsp *st, BiCoarse pc, int use_pc, int max_iters) {
+  extern __shared__ __align__(16) unsigned char bi_sm[];
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int N = g.pitch * g.my;  // every element of the padded grid, as the node kernels cover it
+  auto done = [&]() { return *(volatile int *)&st->k.done != 0; };
+  // z = M in into out (k_bi_pcout): the Poisson solve inside, `in` elsewhere
+  auto precondition = [&](const float *in, float *out) {
+    if (use_pc) {
+      coarse_solve_block<2, float>(pc.g, in, pc.z, pc.S0, pc.S1, pc.S1, pc.ilam, pc.work, pc.n0, pc.n1, 1,
+                                   pc.smem, pc.dinv, bi_sm);
+      __syncthreads();
+    }
+    for (int q = tid; q < N; q += nt) {
+      const int i = q % g.pitch, j = q / g.pitch;
+      const bool node = i < g.mx;
+      bool use_z;
+      if (model == FISHGPU_NL_OBSTACLE) use_z = node && use_pc && C1[q].x == 0.f;
+      else use_z = node && use_pc && !ms_bdry(g, i, j);
+      out[q] = use_z ? pc.z[q] : in[q];
+    }
+    __syncthreads();
+  };
+  {  // k_bi_init: r = b, rhat = b, x = p = v = 0; rho = b.b
+    double acc[1] = {0.0};
+    for (int q = tid; q < N; q += nt) {
+      const float bb = bv[q];
+      r[q] = bb;
+      rh[q] = bb;
+      x[q] = 0.f;
+      p[q] = 0.f;
+      v[q] = 0.f;
+      acc[0] += (double)bb * bb;
+    }
+    block_sum<1>(acc);
+    if (tid == 0) InitFin{st}(acc);
+    __syncthreads();
+  }
+  // max_iters: the iterations the device loop's cap would allow; a solve
+  // still running then ends with its state not done (the host reports it)
+  for (int iter = 0; !done() && iter < max_iters; iter++) {
+    {  // k_bi_p
+      const bool first = *(volatile int *)&st->first != 0;
+      const float be = (float)*(volatile double *)&st->beta, om = (float)*(volatile double *)&st->omega;
+      for (int q = tid; q < N; q += nt) p[q] = first ? r[q] : fmaf(be, fmaf(-om, v[q], p[q]), r[q]);
+      __syncthreads();
+    }
+    precondition(p, ph);
+    {  // k_bi_jv1: v = J ph, rhat.v -> alpha
+      double acc[1] = {0.0};
+      for (int q = tid; q < N; q += nt) {
+        const int i = q % g.pitch, j = q / g.pitch;
+        const float o = i < g.mx ? ms_jv_node(g, model, i, j, q, a, b, C1, C2, ph) : 0.f;
+        v[q] = o;
+        acc[0] += (double)rh[q] * o;
+      }
+      block_sum<1>(acc);
+      if (tid == 0) AlphaFin{st}(acc);
+      __syncthreads();
+    }
+    if (done()) break;
+    {  // k_bi_s
+      const float al = (float)*(volatile double *)&st->alpha;
+      for (int q = tid; q < N; q += nt) s[q] = fmaf(-al, v[q], r[q]);
+      __syncthreads();
+    }
+    precondition(s, sh);
+    {  // k_bi_jv2: t = J sh; t.s, t.t -> omega
+      double acc[2] = {0.0, 0.0};
+      for (int q = tid; q < N; q += nt) {
+        const int i = q % g.pitch, j = q / g.pitch;
+        const float o = i < g.mx ? ms_jv_node(g, model, i, j, q, a, b, C1, C2, sh) : 0.f;
+        t[q] = o;
+        acc[0] += (double)o * s[q];
+        acc[1] += (double)o * o;
+      }
+      block_sum<2>(acc);
+      if (tid == 0) OmegaFin{st}(acc);
+      __syncthreads();
+    }
+    {  // k_bi_xr: x += alpha ph + omega sh; r = s - omega t; r.r, rhat.r
+      const float al = (float)*(volatile double *)&st->alpha, om = (float)*(volatile double *)&st->omega;
+      double acc[2] = {0.0, 0.0};
+      for (int q = tid; q < N; q += nt) {
+        x[q] = fmaf(om, sh[q], fmaf(al, ph[q], x[q]));
+        const float rn = fmaf(-om, t[q], s[q]);
+        r[q] = rn;
+        acc[0] += (double)rn * rn;
+        acc[1] += (double)rh[q] * rn;
+      }
+      block_sum<2>(acc);
+      if (tid == 0) XrFin{st}(acc);
+      __syncthreads();
+    }
+  }
+}
+
 // ------------------------------------------------------------------ Newton helpers
 // b = F / fnorm (FP32); 0 on the active set of the obstacle problem (C1.x)
 __global__ void __launch_bounds__(256) k_ms_demote(Geom g, int model, const float4 *__restrict__ C1,
@@ -738,6 +856,10 @@ struct MsLevel {
   cudaGraphExec_t g_loop = nullptr;  // g_iter's body repeated on the device until the inner solve stops
   long long n_loop = 0;
   int giters = 2;
+  bool block1 = false;  // the inner solve is one launch of k_bi_block
+  BiCoarse bc{};
+  int use_pc = 0;
+  int max_iters = 0;
 };
 
 }  // namespace
@@ -900,9 +1022,20 @@ static int newton(fishgpu_ms_solver *S, MsLevel &L, int k, fishgpu_ms_report *re
     k_ms_coef<<<L.grid, L.block, 0, s>>>(g, level_params(S, L), L.u, L.F, L.C1, L.C2);
     k_ms_demote<<<L.grid, L.block, 0, s>>>(g, S->P.model, L.C1, L.F, 1.0 / fnorm, L.b);
     MS_CK(cudaGetLastError());
-    MS_CK(cudaGraphLaunch(L.g_init, s));
     int kits = 0, kreason = 0;
-    if (L.g_loop) MS_CK(cudaGraphLaunch(L.g_loop, s));
+    if (L.block1) {
+      const float ja = (float)(g.h[1] / g.h[0]), jb = (float)(g.h[0] / g.h[1]);
+      k_bi_block<<<1, 1024, L.use_pc ? (size_t)L.bc.smem : 0, s>>>(
+          g, S->P.model, ja, jb, L.C1, L.C2, L.b, L.r, L.rh, L.p, L.v, L.s, L.t, L.x, L.ph, L.sh, S->st, L.bc,
+          L.use_pc, L.max_iters);
+      MS_CK(cudaGetLastError());
+      MS_CK(cudaMemcpyAsync(S->st_h, S->st, sizeof(MsKsp), cudaMemcpyDeviceToHost, s));
+      MS_CK(cudaStreamSynchronize(s));
+      if (!S->st_h->k.done) return FISHGPU_ERR_TIMEOUT;  // the iteration cap ended it unfinished
+    } else {
+      MS_CK(cudaGraphLaunch(L.g_init, s));
+      if (L.g_loop) MS_CK(cudaGraphLaunch(L.g_loop, s));
+    }
     for (;;) {
       MS_CK(cudaMemcpyAsync(S->st_h, S->st, sizeof(MsKsp), cudaMemcpyDeviceToHost, s));
       MS_CK(cudaStreamSynchronize(s));
@@ -1002,6 +1135,7 @@ extern "C" int fishgpu_ms_opts_default(fishgpu_ms_opts *o) {
   o->line_search = 1;
   o->ksp_rtol = 1e-5;
   o->ksp_max_it = 10000;
+  o->inner_block = 1;
   o->pc_type = FISHGPU_PC_MG;
   return FISHGPU_OK;
 }
@@ -1077,6 +1211,7 @@ extern "C" int fishgpu_ms_opts_parse(fishgpu_ms_opts *o, int argc, const char *c
     else if (!strcmp(k, "-ksp_rtol")) rc = num(a, &o->ksp_rtol, nullptr);
     else if (!strcmp(k, "-ksp_max_it")) rc = num(a, nullptr, &o->ksp_max_it);
     else if (!strcmp(k, "-ms_loop_cap")) rc = num(a, nullptr, &o->loop_cap);
+    else if (!strcmp(k, "-ms_inner_block")) rc = num(a, nullptr, &o->inner_block);
     else if (!strcmp(k, "-pc_mg_levels")) rc = num(a, nullptr, &o->mg_levels);
     else if (!strcmp(k, "-pc_type")) {
       if (a + 1 >= argc) return FISHGPU_ERR_ARG;
@@ -1246,6 +1381,19 @@ extern "C" int fishgpu_ms_solver_create(const fishgpu_ms_opts *o, void *stream, 
     float **vs[10] = {&L.b, &L.r, &L.rh, &L.p, &L.v, &L.s, &L.t, &L.x, &L.ph, &L.sh};
     for (float **q : vs) MS_FAIL(ms_alloc(S, q, L.N));
     L.giters = L.N >= (1LL << 20) ? 1 : 2;
+    {  // grids of up to 4096 nodes whose preconditioner is one exact coarse solve: one-block inner solves
+      CoarseView cv;
+      const bool one_level = o->pc_type == FISHGPU_PC_MG && solver_coarse32(L.P, &cv);
+      if (o->inner_block && (long long)L.g.mx * L.g.my <= 4096 && (o->pc_type != FISHGPU_PC_MG || one_level)) {
+        L.block1 = true;
+        L.use_pc = one_level ? 1 : 0;
+        if (one_level)
+          L.bc = BiCoarse{cv.g, cv.S0, cv.S1, cv.ilam, cv.work, cv.x, cv.n0, cv.n1, (int)cv.smem, cv.dinv};
+        const long long cap =
+            o->loop_cap > 0 ? o->loop_cap : (long long)std::max(1, o->ksp_max_it) / L.giters + 5;
+        L.max_iters = (int)std::min<long long>(cap * L.giters, 1 << 30);
+      }
+    }
     if (S->P.model != FISHGPU_NL_OBSTACLE) {
       L.gtm = std::max(L.g.mx, L.g.my);
       MS_FAIL(ms_alloc(S, &L.gt, 16LL * L.gtm));

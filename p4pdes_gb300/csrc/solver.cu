@@ -31,6 +31,7 @@
 
 #include "common.cuh"
 #include "graph_loop.cuh"
+#include "mg_hooks.cuh"
 #include "vkernels.cuh"
 
 namespace fg {
@@ -1368,6 +1369,24 @@ static int time_kernel_dim(fishgpu_solver *S, const char *name, int reps, double
 const Geom &solver_fine(const fishgpu_solver *S) { return S->fine; }
 const Slots &solver_slots(const fishgpu_solver *S) { return S->sf; }
 cudaStream_t solver_stream(const fishgpu_solver *S) { return S->stream; }
+
+bool solver_coarse32(const fishgpu_solver *S, CoarseView *c) {
+  if (S->o.ctx.dim != 2 || S->o.precision != FISHGPU_MIXED || S->o.pc_type != FISHGPU_PC_MG || S->h32.nlev != 1)
+    return false;
+  const Level<float> &lv = S->h32.lev[0];
+  c->g = lv.g;
+  c->S0 = lv.S[0];
+  c->S1 = lv.S[1];
+  c->ilam = lv.ilam;
+  c->work = lv.work;
+  c->x = lv.X[0];
+  c->n0 = lv.n[0];
+  c->n1 = lv.n[1];
+  const size_t smb = coarse_smem_bytes<float>(2, lv.n[0], lv.n[1], 1);
+  c->smem = (lv.n[0] * lv.n[1] > 0 && smb <= 48 * 1024) ? smb : 0;
+  c->dinv = (float)(1.0 / lv.g.scdiag);
+  return true;
+}
 
 const float *solver_vcycle32(fishgpu_solver *S, const float *r, KspState *st) {
   if (S->o.ctx.dim != 2 || S->o.precision != FISHGPU_MIXED || S->o.pc_type != FISHGPU_PC_MG) return nullptr;

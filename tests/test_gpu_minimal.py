@@ -192,3 +192,22 @@ def test_drivers_write_the_solution_as_petsc_binary(cuda, tmp_path):
     import _oracle as orc
     uref, ref = orc.fish_solve(orc.options(args))
     assert np.max(np.abs(fg.petsc_vec_read(f2) - uref.ravel())) <= 1e-9 * np.max(np.abs(uref))
+
+
+@pytest.mark.parametrize("args", ["-da_grid_x 33 -da_grid_y 33 -snes_grid_sequence 2 -snes_rtol 1e-10",
+                                  "-da_refine 4 -ms_problem tent -ms_tent_H 0.5 -snes_rtol 1e-10",
+                                  "-da_refine 3 -pc_type none -snes_rtol 1e-10"])
+def test_one_block_inner_solve_matches_the_launch_per_phase_form(cuda, args):
+    """On grids of up to 4096 nodes whose preconditioner is one exact coarse
+    solve the inner BiCGStab runs as one block (k_bi_block): the same
+    iteration and finalisers, dot products summed in another order, so the
+    Newton solve takes the same steps and ends at the same solution to the
+    Newton tolerance."""
+    import p4pdes_gb300 as fg
+    o1, u1, r1 = run(args + " -ms_inner_block 1")
+    o0, u0, r0 = run(args + " -ms_inner_block 0")
+    assert r1.ngrids == r0.ngrids
+    for k in range(r0.ngrids):
+        assert r1.reason[k] > 0 and r0.reason[k] > 0
+        assert r1.its[k] == r0.its[k]
+    assert np.max(np.abs(u1 - u0)) <= 1e-8 * np.max(np.abs(u0))
