@@ -196,6 +196,20 @@ typedef struct {
                                1; bit-identical to 0)                      */
   int vtail_points;         /* -fsh_vtail_points: largest level (nodes per
                                grid) the tail takes (0: the limits above)  */
+  int persist;              /* -fsh_persist -1|0|1: each CG solve (its
+                               set-up, iterations and V-cycles) as ONE
+                               cooperative launch with a grid-wide barrier
+                               between phases, for grids too small to fill
+                               the GPU with a launch per phase (2D/3D, MG
+                               with two Chebyshev steps, V-cycles, the
+                               device loop); -1 (default): when the finest
+                               grid has at most persist_points nodes      */
+  int persist_points;       /* -fsh_persist_points: that limit (0: 2.5e6
+                               for the FP64 form, 1.5e5 for the mixed
+                               form's FP32 inner solves)                  */
+  int persist_tail;         /* -fsh_persist_tail: largest level (nodes) the
+                               persistent solve runs in its block 0 (0:
+                               300 in FP64, 1200 in FP32)                  */
 } fishgpu_opts;
 
 #define FISHGPU_MAX_HIST 512
@@ -270,7 +284,8 @@ int fishgpu_solve_host(const fishgpu_opts *o, const double *f_host, const double
    solver's resident data (CUDA events on the solver's stream).  Names:
    "smooth", "smooth_first", "smooth_dots", "smooth_zero", "post2", "cgp_apply",
    "cgp_apply_acc" (mixed form: the accurate inner form's apply), "cgp_apply_tma" (the same from the
-   TMA ring, 3D), "cg_update", "resid_restrict" (3D),
+   TMA ring, 3D), "cg_update", "resid_restrict" (3D), "grid_sync" (one grid-wide barrier of the
+   persistent solve; bytes 0),
    "resid", "apply", "restrict", "prolong", "residual64".  Reports the mean ms
    per launch and the algorithmic bytes one launch moves. */
 int fishgpu_solver_time_kernel(fishgpu_solver *s, const char *name, int reps,

@@ -75,7 +75,8 @@ class Opts(ctypes.Structure):
                 ("snes_monitor", c_int), ("fuse_smooth", c_int), ("device_loop", c_int), ("loop_cap", c_int),
                 ("first_floor_scale", c_double), ("inner_accurate", c_int), ("fuse_restrict", c_int),
                 ("tma_apply", c_int), ("vtail", c_int),
-                ("vtail_points", c_int)]
+                ("vtail_points", c_int), ("persist", c_int), ("persist_points", c_int),
+                ("persist_tail", c_int)]
 
     @property
     def dofs(self):

@@ -32,6 +32,7 @@
 #include "common.cuh"
 #include "graph_loop.cuh"
 #include "mg_hooks.cuh"
+#include "vblock.cuh"
 #include "vkernels.cuh"
 
 namespace fg {
@@ -56,20 +57,6 @@ struct Level {
   int n[3] = {1, 1, 1};
 };
 
-// One level of the V-cycle tail (k_vtail): the level's arrays and the
-// Chebyshev coefficients of its smoothing steps (the same values enq_smooth
-// passes to v_cheb2_zero and v_cheb).  Every tail level ends its V-cycle with
-// its iterate in X[0] (pre-smoothing writes X[1], the two post-smoothing steps
-// X[2] and X[0]), as the rotation of enq_smooth leaves it.
-template <typename T>
-struct TailLevel {
-  Geom g;
-  T *b, *r, *X[3];
-  T a0, a1;            // two steps from zero: x = a0 b - a1 (A b)
-  T c1;                // post-smoothing step 1: x1 = x0 + c1 (b - A x0)
-  T ckm1, ck, crd;     // step 2: x2 = ckm1 x0 + ck x1 + crd (b - A x1)
-};
-
 template <typename T>
 struct Hier {
   int nlev = 0;
@@ -80,7 +67,19 @@ struct Hier {
   int tail_top = 0;              // 0: no tail
   int tail_threads = 0;
   size_t tail_smem = 0;
+  // the persistent solve (k_ksp_persist): every level, the fine one's b the KSP residual
+  TailLevel<T> *plev = nullptr;  // device, levels 0 .. nlev-1; null: no persistent solve
+  int pbtop = 0;                 // levels pbtop .. 0 in block 0
+  size_t psmem = 0;              // dynamic shared memory of the coarse solve (0: its work area)
 };
+
+// Threads per block of the slot kernels of a level: 128 on 2D grids (twice
+// the blocks of 256, spreading the FP64 kernels of a 257^2 .. 1025^2 grid over
+// more SMs: measured 1.50 -> 1.35 ms at 257^2, 3.33 -> 3.13 ms at 1025^2 for
+// the FP64 solve, the mixed form unchanged; 64 and 32 were no better)
+static int level_chunk(const Geom &g, int batch) {
+  return g.dim == 2 && !batch ? 128 : 256;
+}
 
 static Geom padded(Geom g) {
   g.pitch = (g.mx + 3) / 4 * 4;
@@ -172,6 +171,10 @@ struct fishgpu_solver_s {
   long long bytes = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   int *fault = nullptr;  // set by a kernel whose bounded wait on a copy gave up
+  // persistent solve: grid barrier, partial sums, blocks (one per SM at most)
+  unsigned *pbar = nullptr;
+  double *ppart = nullptr;
+  int pblocks = 0;
 };
 
 namespace fg {
@@ -215,6 +218,39 @@ static long long tail_max_points(const fishgpu_opts &o, size_t) {
 
 static long long level_points(const Geom &g) { return (long long)g.mx * g.my * (g.dim >= 3 ? g.mz : 1); }
 
+// A level's arrays and enq_smooth's Chebyshev coefficients (the same
+// expressions) for the block-level V-cycle code.
+template <typename T>
+static TailLevel<T> tail_level(const Level<T> &lv, bool smoothed) {
+  TailLevel<T> t;
+  memset(&t, 0, sizeof(t));
+  t.g = lv.g;
+  t.b = lv.b;
+  t.r = lv.r;
+  for (int q = 0; q < 3; q++) t.X[q] = lv.X[q];
+  if (!smoothed) return t;
+  const double dinv = 1.0 / lv.g.scdiag;
+  const double scale = 2.0 / (lv.emax + lv.emin);
+  const double alpha = 1.0 - scale * lv.emin;
+  const double mu = 1.0 / alpha, omegaprod = 2.0 / alpha;
+  const double c1 = scale * dinv;
+  {
+    const double ckp1 = 2.0 * mu * mu - 1.0, omega = omegaprod * mu / ckp1;
+    t.a0 = (T)(2.0 * omega * c1);
+    t.a1 = (T)(omega * c1 * c1);
+  }
+  t.c1 = (T)c1;
+  {
+    const double ckm1 = 1.0, ck = mu;
+    const double ckp1 = 2.0 * mu * ck - ckm1;
+    const double omega = omegaprod * ck / ckp1;
+    t.ckm1 = (T)(1.0 - omega);
+    t.ck = (T)omega;
+    t.crd = (T)(omega * c1);
+  }
+  return t;
+}
+
 // The V-cycle tail of a hierarchy (k_vtail): the largest level below the
 // finest with at most TAIL_MAX_POINTS nodes per instance and everything
 // under it, for V-cycles of two Chebyshev/Jacobi steps (the default
@@ -231,36 +267,7 @@ static int build_tail(fishgpu_solver *S, Hier<T> &H) {
     if (level_points(H.lev[l].g) <= tail_max_points(o, sizeof(T))) top = l;
   if (top < 1) return FISHGPU_OK;
   std::vector<TailLevel<T>> tl(top + 1);
-  for (int l = 0; l <= top; l++) {
-    Level<T> &lv = H.lev[l];
-    TailLevel<T> &t = tl[l];
-    memset(&t, 0, sizeof(t));
-    t.g = lv.g;
-    t.b = lv.b;
-    t.r = lv.r;
-    for (int q = 0; q < 3; q++) t.X[q] = lv.X[q];
-    if (l == 0) continue;
-    // enq_smooth's Chebyshev coefficients, the same expressions
-    const double dinv = 1.0 / lv.g.scdiag;
-    const double scale = 2.0 / (lv.emax + lv.emin);
-    const double alpha = 1.0 - scale * lv.emin;
-    const double mu = 1.0 / alpha, omegaprod = 2.0 / alpha;
-    const double c1 = scale * dinv;
-    {
-      const double ckp1 = 2.0 * mu * mu - 1.0, omega = omegaprod * mu / ckp1;
-      t.a0 = (T)(2.0 * omega * c1);
-      t.a1 = (T)(omega * c1 * c1);
-    }
-    t.c1 = (T)c1;
-    {
-      const double ckm1 = 1.0, ck = mu;
-      const double ckp1 = 2.0 * mu * ck - ckm1;
-      const double omega = omegaprod * ck / ckp1;
-      t.ckm1 = (T)(1.0 - omega);
-      t.ck = (T)omega;
-      t.crd = (T)(omega * c1);
-    }
-  }
+  for (int l = 0; l <= top; l++) tl[l] = tail_level<T>(H.lev[l], l > 0);
   // the level's b of the top level is the restriction target of the level
   // above it (allocated); levels below the finest all have r
   int rc;
@@ -274,6 +281,81 @@ static int build_tail(fishgpu_solver *S, Hier<T> &H) {
   const size_t smb = coarse_smem_bytes<T>(S->fine.dim, c.n[0], c.n[1], c.n[2]);
   H.tail_smem = (c.n[0] * c.n[1] * c.n[2] > 0 && smb <= 48 * 1024) ? smb : 0;
   H.tail_top = top;
+  return FISHGPU_OK;
+}
+
+// Whether a solve's CG loop runs as one persistent launch (k_ksp_persist):
+// CG + MG with two Chebyshev/Jacobi steps, V-cycles, a 2D or 3D single grid,
+// the device loop, and (default) a finest grid of at most persist_points
+// nodes (by default 2.5e6 in FP64, 1.5e5 in FP32).  The levels of at most persist_tail nodes run in block 0 between
+// two grid barriers (*btop: the largest of them, >= 1): one SM's FP64 rate
+// is 1/152 of the GPU's, so in FP64 only the smallest levels stay there.
+// pts: nodes per level (0 .. nlev-1); psmem: the coarse solve's dynamic
+// shared memory.  Returns the blocks of the launch (one of 512 threads per
+// SM at most, fewer for fewer fine points), 0 for no persistent solve; *nsm:
+// the device's SMs (the partial sums' capacity).
+template <typename T>
+static int persist_shape(const fishgpu_opts &o, int dim, bool batch, int nlev, const long long *pts, size_t psmem,
+                         int *btop, int *nsm) {
+  if (!o.persist || !o.device_loop || batch || o.pc_type != FISHGPU_PC_MG ||
+      o.smooth_type != FISHGPU_SMOOTH_CHEBYSHEV || o.smooth_its != 2 || o.mg_cycles != 1 || dim < 2 || nlev < 3 ||
+      nlev > kMaxPersistLevels)
+    return 0;
+  const long long fine_pts = pts[nlev - 1];
+  // measured against the launch-per-phase solve (2D 257^2 .. 1025^2, 3D 33^3 .. 129^3): the FP64 form
+  // gains at every size (its kernels are FP64-bound there, the launch overhead is not hidden), the
+  // FP32 inner solves of the mixed form up to ~1e5 nodes and break even near 2.7e5
+  const long long lim = o.persist_points > 0 ? o.persist_points : sizeof(T) == 8 ? 2500000 : 150000;
+  if (o.persist < 0 && fine_pts > lim) return 0;
+  const long long tmax = o.persist_tail > 0 ? o.persist_tail : sizeof(T) == 8 ? 300 : 1200;
+  *btop = 0;
+  for (int l = 1; l <= nlev - 2; l++)
+    if (pts[l] <= tmax) *btop = l;
+  if (*btop < 1) return 0;
+  int dev = 0, coop = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || !coop || *nsm < 1) {
+    cudaGetLastError();
+    return 0;
+  }
+  const void *fn = dim == 2 ? (const void *)k_ksp_persist<2, T, false> : (const void *)k_ksp_persist<3, T, false>;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 512, psmem) != cudaSuccess || per_sm < 1) {
+    cudaGetLastError();
+    return 0;
+  }
+  int blocks = (int)std::max<long long>(1, std::min<long long>(*nsm, (fine_pts + 511) / 512));
+  return blocks;
+}
+
+// the coarse solve's dynamic shared memory (0: its work area in global memory)
+template <typename T>
+static size_t coarse_psmem(int dim, const int *n) {
+  const size_t smb = coarse_smem_bytes<T>(dim, n[0], n[1], n[2]);
+  return (n[0] * n[1] * n[2] > 0 && smb <= 48 * 1024) ? smb : 0;
+}
+
+template <typename T>
+static int build_persist(fishgpu_solver *S, Hier<T> &H) {
+  H.plev = nullptr;
+  std::vector<long long> pts(H.nlev);
+  for (int l = 0; l < H.nlev; l++) pts[l] = level_points(H.lev[l].g);
+  const size_t psmem = coarse_psmem<T>(S->fine.dim, H.lev[0].n);
+  int btop = 0, nsm = 0;
+  const int blocks = persist_shape<T>(S->o, S->fine.dim, S->batch != 0, H.nlev, pts.data(), psmem, &btop, &nsm);
+  if (!blocks) return FISHGPU_OK;
+  std::vector<TailLevel<T>> tl(H.nlev);
+  for (int l = 0; l < H.nlev; l++) tl[l] = tail_level<T>(H.lev[l], l > 0);
+  tl[H.nlev - 1].b = sizeof(T) == 8 ? (T *)(void *)S->r64 : (T *)(void *)S->r32;  // the KSP residual
+  int rc;
+  if ((rc = dalloc(S, &H.plev, (size_t)H.nlev))) return rc;
+  if (cudaMemcpyAsync(H.plev, tl.data(), sizeof(TailLevel<T>) * H.nlev, cudaMemcpyHostToDevice, S->stream) !=
+      cudaSuccess)
+    return FISHGPU_ERR_CUDA;
+  if (!S->pbar && ((rc = dalloc(S, &S->pbar, 2)) || (rc = dalloc(S, &S->ppart, (size_t)4 * nsm)))) return rc;
+  H.pbtop = btop;
+  H.psmem = psmem;
+  S->pblocks = blocks;
   return FISHGPU_OK;
 }
 
@@ -295,7 +377,7 @@ static int build_hier(fishgpu_solver *S, Hier<T> &H) {
     Level<T> &lv = H.lev[l];
     if (S->batch) g.mz = S->nplanes;  // a batch keeps its instances as planes on every level
     lv.g = g;
-    lv.sl = make_slots(g, ZC, 2432, 256, S->batch);
+    lv.sl = make_slots(g, ZC, 2432, level_chunk(g, S->batch), S->batch);
     lv.st = S->batch ? make_slots(g, ZC, 2432, 256, 1, batch_rows(g)) : lv.sl;
     if (g.dim == 3) lv.pz = post2z_shape(g);
     double lmin, lmax;
@@ -352,52 +434,14 @@ static int build_hier(fishgpu_solver *S, Hier<T> &H) {
       return FISHGPU_ERR_CUDA;
     for (int d = c.g.dim; d < 3; d++) c.S[d] = c.S[0];  // unused
   }
-  return build_tail<T>(S, H);
+  if ((rc = build_tail<T>(S, H))) return rc;
+  return build_persist<T>(S, H);
 }
 
 // ------------------------------------------------------------------ V-cycle tail
 // The coarse end of a V-cycle in ONE block per grid (per instance of a
-// batch): levels tail_top .. 1 pre-smooth, take their residual and restrict
-// it, level 0 is solved exactly, and on the way up every level adds the
-// prolongated correction and post-smooths -- the work of ~7 launches per
-// level, each too small to fill the GPU, as phases separated by block
-// barriers.  Every point is computed by the same operations in the same
-// order as the vectorised kernels (resid_pt restates resid_el, and so on),
-// so the V-cycle is bit-identical to the launch-per-phase form.
-
-// b - A x at one point (resid_el's operations on one point)
-template <int DIM, typename T>
-__device__ __forceinline__ T resid_pt(const Geom &g, const Wv<T> &w, const T *__restrict__ x, long long n, int i, int j,
-                                      int k, T bv) {
-  const T xc = x[n];
-  const bool bd = jk_bdry(g, DIM, j, k) || i == 0 || i == g.mx - 1;
-  if (bd) return fma(-w.sd, xc, bv);
-  const T a = (i - 1 > 0 ? x[n - 1] : T(0)) + (i + 1 < g.mx - 1 ? x[n + 1] : T(0));
-  T s = fma(w.sx, a, bv);
-  if (DIM >= 2) s = fma(w.sy, (j - 1 > 0 ? x[n - g.pitch] : T(0)) + (j + 1 < g.my - 1 ? x[n + g.pitch] : T(0)), s);
-  if (DIM >= 3) s = fma(w.sz, (k - 1 > 0 ? x[n - g.plane] : T(0)) + (k + 1 < g.mz - 1 ? x[n + g.plane] : T(0)), s);
-  return fma(-w.sd, xc, s);
-}
-
-// x-interpolated coarse value at fine x-index fi of coarse row (jc, kc) (v_prolong's lo/hi)
-template <typename T>
-__device__ __forceinline__ T prolong_x(const Geom &gc, const T *__restrict__ xc, int fi, int jc, int kc) {
-  const long long m = (long long)kc * gc.plane + (long long)jc * gc.pitch;
-  const int I = fi >> 1;
-  if ((fi & 1) == 0) return xc[m + I];
-  return T(0.5) * (xc[m + I] + (I + 1 < gc.mx ? xc[m + I + 1] : T(0)));
-}
-
-// restricted row value at coarse x-index I of fine row (fj, fk) (restrict_row)
-template <typename T>
-__device__ __forceinline__ T restrict_x(const Geom &gf, const T *__restrict__ rf, int I, int fj, int fk) {
-  const long long m = (long long)fk * gf.plane + (long long)fj * gf.pitch;
-  const int fi = 2 * I;
-  const T L = fi > 0 ? rf[m + fi - 1] : T(0);
-  const T R = fi + 1 < gf.pitch ? rf[m + fi + 1] : T(0);
-  return fma(T(0.5), L + R, rf[m + fi]);
-}
-
+// batch): vtail_body's phases, a block barrier between them instead of a
+// launch each; bit-identical to the launch-per-phase form.
 template <int DIM, typename T>
 __global__ void __launch_bounds__(1024) k_vtail(const TailLevel<T> *__restrict__ tl, int top, KspState *st, int batch,
                                                 const T *__restrict__ S0, const T *__restrict__ S1,
@@ -407,116 +451,7 @@ __global__ void __launch_bounds__(1024) k_vtail(const TailLevel<T> *__restrict__
   const int plane = (DIM < 3 && batch) ? (int)blockIdx.x : 0;  // instance of a batch
   if (batch && st) st += plane;
   if (ksp_done(st)) return;
-  const int tid = threadIdx.x, nt = blockDim.x;
-  const T h = T(0.5);
-  // points of level l (one plane of a batch); (i, j, k) and the element offset
-  auto npts = [&](const Geom &g) { return g.mx * g.my * (DIM < 3 ? 1 : g.mz); };
-  auto pos = [&](const Geom &g, int q, int &i, int &j, int &k) -> long long {
-    i = q % g.mx;
-    const int r = q / g.mx;
-    j = DIM >= 2 ? r % g.my : 0;
-    k = DIM >= 3 ? r / g.my : plane;
-    return (long long)k * g.plane + (long long)j * g.pitch + i;
-  };
-  for (int l = top; l >= 1; l--) {
-    const TailLevel<T> &L = tl[l];
-    const TailLevel<T> &C = tl[l - 1];
-    const Geom &g = L.g;
-    const Wv<T> w(g);
-    const int N = npts(g);
-    for (int q = tid; q < N; q += nt) {  // two Chebyshev steps from zero (v_cheb2_zero): X[1]
-      int i, j, k;
-      const long long n = pos(g, q, i, j, k);
-      const T mab = resid_pt<DIM, T>(g, w, L.b, n, i, j, k, T(0));
-      L.X[1][n] = fma(L.a1, mab, L.a0 * L.b[n]);
-    }
-    __syncthreads();
-    for (int q = tid; q < N; q += nt) {  // r = b - A x (v_resid)
-      int i, j, k;
-      const long long n = pos(g, q, i, j, k);
-      L.r[n] = resid_pt<DIM, T>(g, w, L.X[1], n, i, j, k, L.b[n]);
-    }
-    __syncthreads();
-    const Geom &gc = C.g;
-    const int Nc = npts(gc);
-    for (int q = tid; q < Nc; q += nt) {  // b_c = P^T r (v_restrict)
-      int I, J, K;
-      const long long m = pos(gc, q, I, J, K);
-      auto rowsum = [&](int fk) -> T {
-        const int fj = 2 * J;
-        const T c = restrict_x<T>(g, L.r, I, fj, fk);
-        if (DIM < 2) return c;
-        const T sr = fj - 1 >= 0 ? restrict_x<T>(g, L.r, I, fj - 1, fk) : T(0);
-        const T nr = fj + 1 < g.my ? restrict_x<T>(g, L.r, I, fj + 1, fk) : T(0);
-        return fma(h, sr + nr, c);
-      };
-      T o;
-      if (DIM >= 3) {
-        const T below = K > 0 ? rowsum(2 * K - 1) : T(0);
-        const T mid = rowsum(2 * K);
-        const T above = 2 * K + 1 < g.mz ? rowsum(2 * K + 1) : T(0);
-        o = fma(h, below + above, mid);
-      } else {
-        o = rowsum(K);  // 2D: K is the instance plane
-      }
-      C.b[m] = o;
-    }
-    __syncthreads();
-  }
-  {  // exact solve on level 0 into X[0]
-    const TailLevel<T> &C = tl[0];
-    const long long off = DIM < 3 ? (long long)plane * C.g.plane : 0;
-    coarse_solve_block<DIM, T>(C.g, C.b + off, C.X[0] + off, S0, S1, S2, ilam, work, n0, n1, n2, smem, dinv,
-                               fg_tail_sm);
-    __syncthreads();
-  }
-  for (int l = 1; l <= top; l++) {
-    const TailLevel<T> &L = tl[l];
-    const TailLevel<T> &C = tl[l - 1];
-    const Geom &g = L.g, &gc = C.g;
-    const Wv<T> w(g);
-    const int N = npts(g);
-    for (int q = tid; q < N; q += nt) {  // x += P x_c (v_prolong), x in X[1]
-      int i, j, k;
-      const long long n = pos(g, q, i, j, k);
-      const int J = j >> 1, K = DIM >= 3 ? k >> 1 : k;
-      const T a0 = prolong_x<T>(gc, C.X[0], i, J, K);
-      T v;
-      T wgt = T(1);
-      if (DIM >= 3 && (k & 1)) {
-        const T b0 = prolong_x<T>(gc, C.X[0], i, J, K + 1);
-        if (j & 1) {
-          const T a1 = prolong_x<T>(gc, C.X[0], i, J + 1, K), b1 = prolong_x<T>(gc, C.X[0], i, J + 1, K + 1);
-          v = (a0 + a1) + (b0 + b1);
-          wgt = T(0.25);
-        } else {
-          v = a0 + b0;
-          wgt = h;
-        }
-      } else if (DIM >= 2 && (j & 1)) {
-        v = a0 + prolong_x<T>(gc, C.X[0], i, J + 1, K);
-        wgt = h;
-      } else {
-        v = a0;
-      }
-      L.X[1][n] = fma(wgt, v, L.X[1][n]);
-    }
-    __syncthreads();
-    for (int q = tid; q < N; q += nt) {  // x1 = x0 + c1 (b - A x0) (v_cheb without x_{k-1}): X[2]
-      int i, j, k;
-      const long long n = pos(g, q, i, j, k);
-      const T r = resid_pt<DIM, T>(g, w, L.X[1], n, i, j, k, L.b[n]);
-      L.X[2][n] = fma(L.c1, r, T(1) * L.X[1][n]);
-    }
-    __syncthreads();
-    for (int q = tid; q < N; q += nt) {  // x2 = ckm1 x0 + ck x1 + crd (b - A x1) (v_cheb): X[0]
-      int i, j, k;
-      const long long n = pos(g, q, i, j, k);
-      const T r = resid_pt<DIM, T>(g, w, L.X[2], n, i, j, k, L.b[n]);
-      L.X[0][n] = fma(L.crd, r, fma(L.ckm1, L.X[1][n], L.ck * L.X[2][n]));
-    }
-    __syncthreads();
-  }
+  vtail_body<DIM, T>(tl, top, plane, S0, S1, S2, ilam, work, n0, n1, n2, smem, dinv, fg_tail_sm);
 }
 
 // ------------------------------------------------------------------ enqueue
@@ -865,9 +800,67 @@ static void reset_state(fishgpu_solver *S, double rtol, double atol, double dtol
 // last deferred y += alpha p is left to the caller (v_pend_promote).
 // yscale, yfresh: the FP64 accumulation of the accurate inner form (v.y64).
 // The caller reads S->st_h for its, reason and the history.
+// run_ksp as one cooperative launch of k_ksp_persist (build_persist chose it)
+template <int DIM, typename T>
+static int run_ksp_persist(fishgpu_solver *S, Hier<T> &H, KspVecs<T> v, double rtol, int max_it, int from64,
+                           double yscale, bool yfresh) {
+  cudaStream_t s = S->stream;
+  reset_state(S, rtol, S->o.atol, S->o.dtol, max_it, S->ksp_norm, yscale, yfresh);
+  FG_CUDA(cudaMemcpyAsync(S->st, S->st_h, sizeof(KspState), cudaMemcpyHostToDevice, s));
+  FG_CUDA(cudaMemsetAsync(S->pbar, 0, 2 * sizeof(unsigned), s));
+  PersistArgs<T> a;
+  memset(&a, 0, sizeof(a));
+  a.lv = H.plev;
+  a.top = H.nlev - 1;
+  a.btop = H.pbtop;
+  a.r = v.r;
+  a.p[0] = v.p[0];
+  a.p[1] = v.p[1];
+  a.w = v.w;
+  a.y = v.y;
+  a.y64 = v.y64;
+  a.src64 = from64 < 0 ? nullptr : from64 ? S->r64 : S->b64;
+  a.rr64 = S->dval;
+  a.unprec = S->ksp_norm == FISHGPU_NORM_UNPRECONDITIONED;
+  a.do_pend = from64 < 0;
+  // the device loop's cap: loop_cap bodies of giters iterations
+  a.max_iters = S->o.loop_cap > 0 ? S->o.loop_cap * S->giters : max_it + 8;
+  a.st = S->st;
+  a.part = S->ppart;
+  a.bar = S->pbar;
+  a.fault = S->fault;
+  const Level<T> &c = H.lev[0];
+  a.S0 = c.S[0];
+  a.S1 = c.S[1];
+  a.S2 = c.S[2];
+  a.ilam = c.ilam;
+  a.work = c.work;
+  a.n0 = c.n[0];
+  a.n1 = c.n[1];
+  a.n2 = c.n[2];
+  a.smem = H.psmem ? 1 : 0;
+  a.dinv = (T)(1.0 / c.g.scdiag);
+  void *args[] = {&a};
+  const void *fn;
+  if constexpr (sizeof(T) == 4) {
+    fn = v.y64 ? (const void *)k_ksp_persist<DIM, T, true> : (const void *)k_ksp_persist<DIM, T, false>;
+  } else {
+    fn = (const void *)k_ksp_persist<DIM, T, false>;
+  }
+  FG_CUDA(cudaLaunchCooperativeKernel(fn, dim3(S->pblocks), dim3(512), args, H.psmem, s));
+  S->launches += 1;
+  FG_CUDA(cudaMemcpyAsync(S->st_h, S->st, sizeof(KspState), cudaMemcpyDeviceToHost, s));
+  FG_CUDA(cudaStreamSynchronize(s));
+  if (!S->st_h->done) return FISHGPU_ERR_TIMEOUT;
+  return FISHGPU_OK;
+}
+
 template <int DIM, typename T>
 static int run_ksp(fishgpu_solver *S, Hier<T> &H, KspVecs<T> v, double rtol, int max_it, int from64 = -1,
                    double yscale = 0.0, bool yfresh = false) {
+  if constexpr (DIM >= 2) {
+    if (H.plev) return run_ksp_persist<DIM, T>(S, H, v, rtol, max_it, from64, yscale, yfresh);
+  }
   cudaStream_t s = S->stream;
   const int norm = S->ksp_norm;  // the captured graphs compute this norm
   int rc;
@@ -1232,8 +1225,7 @@ static int time_kernel_dim(fishgpu_solver *S, const char *name, int reps, double
   // (beta/betaold = 1, a small alpha); p.w > 0 keeps it running, and a stop
   // (non-finite data) is reported
   KspState *tst = nullptr;
-  if (!strcmp(name, "cgp_apply") || !strcmp(name, "cgp_apply_acc") || !strcmp(name, "cgp_apply_tma") ||
-      !strcmp(name, "cg_update")) {
+  if (!strncmp(name, "cgp_apply", 9) || !strcmp(name, "cg_update")) {
     KspState h;
     memset(&h, 0, sizeof(h));
     h.i = 2;  // a direction update that also reads y (the first one, i = 1, starts y from 0)
@@ -1251,6 +1243,24 @@ static int time_kernel_dim(fishgpu_solver *S, const char *name, int reps, double
     KspState *p;
     ~Free() { if (p) cudaFree(p); }
   } free_tst{tst};
+  if (!strcmp(name, "grid_sync")) {  // one barrier of the persistent solve (launches of 100)
+    if (!S->pbar || S->pblocks < 1) return FISHGPU_ERR_UNSUPPORTED;
+    int nb = 100;
+    void *args[] = {&S->pbar, &S->fault, &nb};
+    FG_CUDA(cudaMemsetAsync(S->pbar, 0, 2 * sizeof(unsigned), s));
+    FG_CUDA(cudaLaunchCooperativeKernel((const void *)k_grid_sync_probe, dim3(S->pblocks), dim3(512), args, 0, s));
+    FG_CUDA(cudaEventRecord(S->ev0, s));
+    for (int q = 0; q < reps; q++) {
+      FG_CUDA(cudaMemsetAsync(S->pbar, 0, 2 * sizeof(unsigned), s));
+      FG_CUDA(cudaLaunchCooperativeKernel((const void *)k_grid_sync_probe, dim3(S->pblocks), dim3(512), args, 0, s));
+    }
+    FG_CUDA(cudaEventRecord(S->ev1, s));
+    FG_CUDA(cudaEventSynchronize(S->ev1));
+    FG_CUDA(cudaEventElapsedTime(&t, S->ev0, S->ev1));
+    *ms = (double)t / (reps * (double)nb);
+    *bytes = 0.0;
+    return FISHGPU_OK;
+  }
   FG_CUDA(cudaEventRecord(S->ev0, s));
   for (int q = 0; q < reps; q++) {
     if (!strcmp(name, "smooth")) {  // one Chebyshev step with x_{k-1}: reads b, x_{k-1}, x_k, writes x_{k+1}
@@ -1466,7 +1476,7 @@ extern "C" int fishgpu_solver_create(const fishgpu_opts *o, void *stream, fishgp
   S->dense = make_geom(dim, o->mx, dim >= 2 ? o->my : 1, dim >= 3 ? o->mz : 1, o->ctx.Lx, o->ctx.Ly, o->ctx.Lz,
                        o->ctx.cx, o->ctx.cy, o->ctx.cz);
   S->fine = padded(S->dense);
-  S->sf = make_slots(S->fine, ZC);
+  S->sf = make_slots(S->fine, ZC, 2432, level_chunk(S->fine, 0));
   S->sfst = S->sf;
   S->Lf = launch_for(S->fine);
   S->gfl = flat_grid(S->sf.tot4);
@@ -1572,7 +1582,7 @@ extern "C" long long fishgpu_solver_estimate_bytes(const fishgpu_opts *o) {
   Geom g = padded(d);
   const long long N = (long long)nelem(g), Nd = (long long)d.plane * d.mz;
   long long b = rnd(sizeof(KspState)) + rnd(4) + rnd(64);  // state, fault word, scalars
-  const long long cap = slot_blocks(make_slots(g, ZC));
+  const long long cap = slot_blocks(make_slots(g, ZC, 2432, level_chunk(g, 0)));
   b += rnd(8LL * 4 * cap) + rnd(16);
   b += 4 * rnd(8LL * N);                                          // u, beff, y, r
   if (o->ctx.problem == FISHGPU_USER && !o->ctx.f) b += 3 * rnd(8LL * Nd);  // f, g, u (host-array form)
@@ -1607,6 +1617,16 @@ extern "C" long long fishgpu_solver_estimate_bytes(const fishgpu_opts *o) {
       if (pts[l] <= tail_max_points(*o, es)) top = l;
     if (top > 0)
       b += rnd((long long)(es == 4 ? sizeof(TailLevel<float>) : sizeof(TailLevel<double>)) * (top + 1));
+  }
+  {  // the persistent solve's level table, grid barrier and partial sums
+    int n[3] = {1, 1, 1}, btop = 0, nsm = 0;
+    for (int q = 0; q < dim; q++) n[q] = (q == 0 ? lv.mx : q == 1 ? lv.my : lv.mz) - 2;
+    const int L = o->mg_levels;
+    const int blocks = es == 4 ? persist_shape<float>(*o, dim, false, L, pts.data(), coarse_psmem<float>(dim, n), &btop, &nsm)
+                               : persist_shape<double>(*o, dim, false, L, pts.data(), coarse_psmem<double>(dim, n), &btop, &nsm);
+    if (blocks)
+      b += rnd((long long)(es == 4 ? sizeof(TailLevel<float>) : sizeof(TailLevel<double>)) * L) + rnd(8) +
+           rnd(8LL * 4 * nsm);
   }
   return b;
 }

@@ -589,6 +589,21 @@ __global__ void __launch_bounds__(256, MinBlocks<T>::value) v_apply_dot(Geom g, 
 // solution, y64 += (yscale * alpha) p_old (the state's yscale and yfresh), so
 // that neither the apply nor the FP32 storage of the correction limits the
 // true residual an inner solve reaches to ~kappa * 2^-24.
+// float -> double by integer operations, exact: the same value as (double)f.
+// On this part the conversion instruction runs on the FP64 pipe (1/64 of the
+// FP32 rate) beside the FP64 FMAs; normal numbers need only a rebased
+// exponent and a shifted mantissa (the integer pipe), the rest take the branch.
+__device__ __forceinline__ double f2d_bits(float f) {
+  const unsigned u = __float_as_uint(f), a = u & 0x7FFFFFFFu;
+  if (a - 0x00800000u >= 0x7F000000u) return a == 0u ? __hiloint2double((int)(u & 0x80000000u), 0) : (double)f;
+  return __hiloint2double((int)(((a >> 3) + (896u << 20)) | (u & 0x80000000u)), (int)(u << 29));
+}
+template <typename YT, typename T>
+__device__ __forceinline__ YT to_y(T v) {
+  if constexpr (sizeof(YT) == 8 && sizeof(T) == 4) return f2d_bits(v);
+  else return (YT)v;
+}
+
 template <typename T, bool ACC>
 struct CgY {
   using type = T;
@@ -634,8 +649,8 @@ __global__ void __launch_bounds__(256, MinBlocksLean<T>::value) v_cgp_apply(Geom
     if (pend) {  // the first update (iteration 1) starts y from 0 without reading it
       const V4<T> pp = ld4(pold + n);
       const V4<YT> yy = yfresh ? zero4<YT>() : ld4(y + n);
-      st4(y + n, V4<YT>{fma(a, (YT)pp.x, yy.x), fma(a, (YT)pp.y, yy.y), fma(a, (YT)pp.z, yy.z),
-                        fma(a, (YT)pp.w, yy.w)});
+      st4(y + n, V4<YT>{fma(a, to_y<YT>(pp.x), yy.x), fma(a, to_y<YT>(pp.y), yy.y), fma(a, to_y<YT>(pp.z), yy.z),
+                        fma(a, to_y<YT>(pp.w), yy.w)});
     }
   };
   // the first iteration (p = z) and the others (p = z + beta/betaold p_old)
@@ -782,8 +797,8 @@ static __global__ void __launch_bounds__(CgRing::THREADS, 2)
           const V4<float> pp = *reinterpret_cast<const V4<float> *>(ps(sc) + zr);
           const V4<double> yy =
               yfresh ? zero4<double>() : *reinterpret_cast<const V4<double> *>(ys(sc) + row * R::YW + 4 * sl);
-          st4(y + n, V4<double>{fma(a, (double)pp.x, yy.x), fma(a, (double)pp.y, yy.y), fma(a, (double)pp.z, yy.z),
-                                fma(a, (double)pp.w, yy.w)});
+          st4(y + n, V4<double>{fma(a, f2d_bits(pp.x), yy.x), fma(a, f2d_bits(pp.y), yy.y), fma(a, f2d_bits(pp.z), yy.z),
+                                fma(a, f2d_bits(pp.w), yy.w)});
         }
       }
       __syncwarp();
@@ -1447,8 +1462,8 @@ static __global__ void __launch_bounds__(256) v_pend_acc(Geom g, Slots s, const 
   V4<double> yy = keep ? ld4(y + n) : zero4<double>();
   if (pend) {
     const V4<float> pp = ld4(pv + n);
-    yy = V4<double>{fma(a, (double)pp.x, yy.x), fma(a, (double)pp.y, yy.y), fma(a, (double)pp.z, yy.z),
-                    fma(a, (double)pp.w, yy.w)};
+    yy = V4<double>{fma(a, f2d_bits(pp.x), yy.x), fma(a, f2d_bits(pp.y), yy.y), fma(a, f2d_bits(pp.z), yy.z),
+                    fma(a, f2d_bits(pp.w), yy.w)};
   }
   st4(y + n, yy);
   FG_PW_END

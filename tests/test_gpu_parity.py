@@ -251,8 +251,9 @@ def test_fused_post_smoother_matches_two_steps(cuda, args):
     operations of the two separate Chebyshev steps: same iteration counts,
     the same solution to FP32 rounding of the fused dot products."""
     fg = fgmod()
-    u1, a = fg.solve(fg.options(args + " -fsh_precision mixed -fsh_fuse_smooth 1"))
-    u0, b = fg.solve(fg.options(args + " -fsh_precision mixed -fsh_fuse_smooth 0"))
+    # the launch-per-phase solve (the persistent one has no fused post-smoother)
+    u1, a = fg.solve(fg.options(args + " -fsh_precision mixed -fsh_fuse_smooth 1 -fsh_persist 0"))
+    u0, b = fg.solve(fg.options(args + " -fsh_precision mixed -fsh_fuse_smooth 0 -fsh_persist 0"))
     assert a.reason == b.reason == 2 and a.its == b.its and a.outer_its == b.outer_its
     h0 = b.history()[0]
     assert a.history()[0] == h0  # the FP64 residual before any V-cycle
@@ -335,8 +336,8 @@ def test_device_loop_matches_host_loop(cuda, args):
     runs the same kernels as the host-polled graphs: identical histories and
     solutions."""
     fg = fgmod()
-    u1, a = fg.solve(fg.options(args + " -fsh_device_loop 1"))
-    u0, b = fg.solve(fg.options(args + " -fsh_device_loop 0"))
+    u1, a = fg.solve(fg.options(args + " -fsh_device_loop 1 -fsh_persist 0"))
+    u0, b = fg.solve(fg.options(args + " -fsh_device_loop 0 -fsh_persist 0"))
     assert a.reason == b.reason == 2 and a.its == b.its and a.outer_its == b.outer_its
     assert a.history() == b.history()
     import torch
@@ -490,8 +491,8 @@ def test_fused_residual_restriction_is_bit_identical(cuda, args):
     bit (tile edges in x, y and z, odd level shapes, W-cycles)."""
     import torch
     fg = fgmod()
-    u1, a = fg.solve(fg.options(args + " -fsh_fuse_restrict 1"))
-    u0, b = fg.solve(fg.options(args + " -fsh_fuse_restrict 0"))
+    u1, a = fg.solve(fg.options(args + " -fsh_fuse_restrict 1 -fsh_persist 0"))
+    u0, b = fg.solve(fg.options(args + " -fsh_fuse_restrict 0 -fsh_persist 0"))
     assert a.reason == b.reason == 2 and a.its == b.its and a.outer_its == b.outer_its
     assert a.history() == b.history()
     assert torch.equal(u1, u0)
@@ -511,8 +512,8 @@ def test_tma_apply_matches_the_slot_march(cuda, args):
     meet rtol, solutions agree to 1e-9 relative (tile edges in x, y and z at
     uneven grid shapes, first iteration, fresh and accumulated y64)."""
     fg = fgmod()
-    u1, a = fg.solve(fg.options(args + " -fsh_tma_apply 1"))
-    u0, b = fg.solve(fg.options(args + " -fsh_tma_apply 0"))
+    u1, a = fg.solve(fg.options(args + " -fsh_tma_apply 1 -fsh_persist 0"))
+    u0, b = fg.solve(fg.options(args + " -fsh_tma_apply 0 -fsh_persist 0"))
     assert a.reason == b.reason == 2 and a.its == b.its and a.outer_its == b.outer_its
     # the outer FP64 residual after a refinement step is what the FP32 inner
     # solve reached, which the other summation order of p.w perturbs at the
@@ -545,9 +546,86 @@ def test_vcycle_tail_is_bit_identical(cuda, args):
     solve is identical, bit for bit, to the launch-per-phase form."""
     import torch
     fg = fgmod()
-    u1, a = fg.solve(fg.options(args + " -fsh_vtail 1"))
-    u0, b = fg.solve(fg.options(args + " -fsh_vtail 0"))
+    u1, a = fg.solve(fg.options(args + " -fsh_vtail 1 -fsh_persist 0"))
+    u0, b = fg.solve(fg.options(args + " -fsh_vtail 0 -fsh_persist 0"))
     assert a.reason == b.reason == 2 and a.its == b.its and a.outer_its == b.outer_its
     assert a.history() == b.history()
     assert torch.equal(u1, u0)
     assert a.launches <= b.launches  # fewer wherever a level is small enough for the tail
+
+
+PERSIST_CASES = [
+    # fish's 2D case (preconditioned norm), FP64 and mixed
+    "-fsh_dim 2 -fsh_problem manupoly -da_refine 7 -pc_type mg -mg_levels_ksp_type chebyshev "
+    "-mg_levels_pc_type jacobi -ksp_rtol 1e-10",
+    "-fsh_dim 2 -fsh_problem manupoly -da_refine 7 -pc_type mg -ksp_rtol 1e-10 -fsh_precision mixed",
+    # uneven anisotropic 2D grid, unpreconditioned norm
+    "-fsh_dim 2 -fsh_problem manupoly -da_grid_x 5 -da_grid_y 3 -da_refine 6 -pc_type mg -ksp_rtol 1e-10 -fsh_cy 3 "
+    "-ksp_norm_type unpreconditioned",
+    # 3D, both forms, the accurate inner form forced on and off
+    "-fsh_dim 3 -fsh_problem manupoly -da_refine 5 -pc_type mg -ksp_rtol 1e-10",
+    "-fsh_dim 3 -fsh_problem manuexp -da_grid_x 5 -da_grid_y 3 -da_grid_z 9 -da_refine 3 -pc_type mg -ksp_rtol 1e-10 "
+    "-fsh_precision mixed -fsh_inner_accurate 1",
+    "-fsh_dim 3 -fsh_problem manupoly -da_refine 5 -pc_type mg -ksp_rtol 1e-10 -fsh_precision mixed "
+    "-fsh_inner_accurate 0",
+    # the whole hierarchy but the coarsest level in the grid-wide part
+    "-fsh_dim 2 -fsh_problem manupoly -da_refine 6 -pc_type mg -ksp_rtol 1e-10 -fsh_persist_tail 25",
+    # random initial state (a nonzero initial iterate)
+    "-fsh_dim 3 -fsh_problem manupoly -da_refine 4 -pc_type mg -fsh_initial_type random -fsh_seed 77 -ksp_rtol 1e-10",
+]
+
+
+@pytest.mark.parametrize("args", PERSIST_CASES)
+def test_persistent_solve_matches_the_launch_per_phase_solve(cuda, args):
+    """The whole CG + MG solve as one cooperative launch (k_ksp_persist) runs
+    every point with the per-phase kernels' operations; only the dot
+    products are summed in another order.  FP64: the same iterations and the
+    history to 1e-10 relative; mixed: the same refinement steps, both meet
+    rtol, solutions to 1e-9 relative of max|u|."""
+    fg = fgmod()
+    u1, a = fg.solve(fg.options(args + " -fsh_persist 1"))
+    u0, b = fg.solve(fg.options(args + " -fsh_persist 0"))
+    assert a.reason == b.reason == 2 and a.outer_its == b.outer_its
+    assert a.launches < b.launches  # the persistent path was taken
+    scale = u0.abs().max().item()
+    if "mixed" in args:
+        assert abs(a.its - b.its) <= 1
+        assert a.true_rel_resid <= 1e-10 and b.true_rel_resid <= 1e-10
+        assert a.history()[0] == b.history()[0]
+        d = (u1 - u0).abs().max().item()
+        assert d <= 1e-9 * scale, d
+    else:
+        assert a.its == b.its
+        ha, hb = a.history(), b.history()
+        assert len(ha) == len(hb)
+        for x, y in zip(ha, hb):
+            assert abs(x - y) <= 1e-10 * abs(y) + 1e-14 * hb[0]
+        d = (u1 - u0).abs().max().item()
+        assert d <= 1e-10 * scale, d
+    assert abs(a.errinf - b.errinf) <= 1e-8 * scale
+
+
+@pytest.mark.parametrize("args", [PERSIST_CASES[0], PERSIST_CASES[2], PERSIST_CASES[3]])
+def test_persistent_solve_matches_oracle(cuda, args):
+    """The persistent FP64 solve against the CPU oracle, as the launch-per-phase
+    solves are compared (compare_runs: iterations, reason, history to 1e-8,
+    errors), and the solution within 1e-9 of max|u|."""
+    fg = fgmod()
+    u, rep = fg.solve(fg.options(args + " -fsh_persist 1"))
+    uref, ref = orc.fish_solve(orc.options(args.split()))
+    compare_runs(args.split(), rep, ref)
+    diff = np.max(np.abs(u.cpu().numpy() - uref))
+    assert diff <= 1e-9 * max(1e-300, np.max(np.abs(uref)))
+
+
+def test_persistent_solve_is_deterministic_and_reusable(cuda):
+    import torch
+    fg = fgmod()
+    o = fg.options(PERSIST_CASES[1] + " -fsh_persist 1")
+    with fg.Solver(o) as s:
+        u1 = torch.empty(o.shape, dtype=torch.float64, device=cuda)
+        u2 = torch.empty_like(u1)
+        r1 = s.solve(u1)
+        r2 = s.solve(u2)
+    assert r1.its == r2.its and r2.launches < 12  # one launch per inner solve, a few around them
+    assert torch.equal(u1, u2) and r1.history() == r2.history()
