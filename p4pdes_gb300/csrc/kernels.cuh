@@ -144,6 +144,23 @@ inline size_t coarse_smem_bytes(int dim, int n0, int n1, int n2) {
   return e * sizeof(T);
 }
 
+// Stages 1/Lambda and the transform matrices in the shared-memory layout of
+// coarse_solve_block (after its two work arrays).  No barrier.
+template <int DIM, typename T>
+__device__ __forceinline__ void coarse_stage(const T *S0, const T *S1, const T *S2, const T *ilam, int n0, int n1,
+                                             int n2, unsigned char *sm_raw) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int ni = n0 * n1 * n2;
+  T *sl = reinterpret_cast<T *>(sm_raw) + 2 * ni, *s0 = sl + ni, *s1 = s0 + n0 * n0;
+  T *s2 = s1 + (DIM >= 2 ? n1 * n1 : 0);
+  for (int q = tid; q < ni; q += nt) sl[q] = ilam[q];
+  for (int q = tid; q < n0 * n0; q += nt) s0[q] = S0[q];
+  if (DIM >= 2)
+    for (int q = tid; q < n1 * n1; q += nt) s1[q] = S1[q];
+  if (DIM >= 3)
+    for (int q = tid; q < n2 * n2; q += nt) s2[q] = S2[q];
+}
+
 // The solve of one block: b, x already offset to the block's plane (1D/2D),
 // `sm` the block's dynamic shared memory, `work` its global work area.
 template <int DIM, typename T>
@@ -169,12 +186,7 @@ __device__ __forceinline__ void coarse_solve_block(const Geom &g, const T *__res
     A = sm;
     B = A + ni;
     T *sl = B + ni, *s0 = sl + ni, *s1 = s0 + n0 * n0, *s2 = s1 + (DIM >= 2 ? n1 * n1 : 0);
-    for (int q = tid; q < ni; q += nt) sl[q] = ilam[q];
-    for (int q = tid; q < n0 * n0; q += nt) s0[q] = S0[q];
-    if (DIM >= 2)
-      for (int q = tid; q < n1 * n1; q += nt) s1[q] = S1[q];
-    if (DIM >= 3)
-      for (int q = tid; q < n2 * n2; q += nt) s2[q] = S2[q];
+    if (smem != 2) coarse_stage<DIM, T>(S0, S1, S2, ilam, n0, n1, n2, sm_raw);  // 2: staged by the caller
     Sd[0] = s0;
     Sd[1] = s1;
     Sd[2] = s2;

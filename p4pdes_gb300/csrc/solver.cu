@@ -66,11 +66,15 @@ struct Hier {
   TailLevel<T> *tail = nullptr;  // device: levels 0 .. tail_top of the one-block V-cycle tail
   int tail_top = 0;              // 0: no tail
   int tail_threads = 0;
-  size_t tail_smem = 0;
+  size_t tail_smem = 0;    // dynamic shared memory of k_vtail: the coarse solve's scratch and the tail's copy
+  size_t tail_coarse = 0;  // the coarse solve's scratch (0: its work area in global memory)
+  int tail_copy = -1;      // offset of the tail's copy (-1: the tail works in global memory)
   // the persistent solve (k_ksp_persist): every level, the fine one's b the KSP residual
   TailLevel<T> *plev = nullptr;  // device, levels 0 .. nlev-1; null: no persistent solve
   int pbtop = 0;                 // levels pbtop .. 0 in block 0
-  size_t psmem = 0;              // dynamic shared memory of the coarse solve (0: its work area)
+  size_t psmem = 0;              // dynamic shared memory of the persistent solve (coarse scratch, tail copy)
+  size_t pcoarse = 0;            // the coarse solve's scratch (0: its work area in global memory)
+  int pcopy = -1;                // offset of block 0's tail copy (-1: none)
 };
 
 // Threads per block of the slot kernels of a level: 128 on 2D grids (twice
@@ -251,6 +255,56 @@ static TailLevel<T> tail_level(const Level<T> &lv, bool smoothed) {
   return t;
 }
 
+// ------------------------------------------------------------------ V-cycle tail
+// The coarse end of a V-cycle in ONE block per grid (per instance of a
+// batch): vtail_body's phases, a block barrier between them instead of a
+// launch each; bit-identical to the launch-per-phase form.
+template <int DIM, typename T>
+__global__ void __launch_bounds__(1024) k_vtail(const TailLevel<T> *__restrict__ tl, int top, KspState *st, int batch,
+                                                const T *__restrict__ S0, const T *__restrict__ S1,
+                                                const T *__restrict__ S2, const T *__restrict__ ilam, T *work, int n0,
+                                                int n1, int n2, int smem, T dinv, int copy_off) {
+  extern __shared__ __align__(16) unsigned char fg_tail_sm[];
+  __shared__ TailLevel<T> sv[MAX_LEVELS];
+  const int plane = (DIM < 3 && batch) ? (int)blockIdx.x : 0;  // instance of a batch
+  if (batch && st) st += plane;
+  if (ksp_done(st)) return;
+  if (copy_off >= 0) {
+    vtail_prepare<DIM, T>(tl, top, fg_tail_sm, copy_off, sv);
+    __syncthreads();
+  }
+  vtail_run<DIM, T>(tl, top, plane, S0, S1, S2, ilam, work, n0, n1, n2, smem, dinv, fg_tail_sm, copy_off, sv);
+}
+
+// Dynamic shared memory of a block-level V-cycle over levels 0..top with
+// pts[l] nodes per grid: the coarse solve's scratch (when it fits 48 KB) and
+// the copy of the tail's arrays (when the whole fits kTailSmemMax).
+constexpr size_t kTailSmemMax = 160 * 1024;
+static void tail_smem_plan(int dim, const int *n, size_t es, int top, const long long *pts, size_t *coarse,
+                           int *copy_off, size_t *total) {
+  const size_t smb = es * (size_t)(3 * (size_t)n[0] * n[1] * n[2] + (size_t)n[0] * n[0] +
+                                   (dim >= 2 ? (size_t)n[1] * n[1] : 0) + (dim >= 3 ? (size_t)n[2] * n[2] : 0));
+  *coarse = ((long long)n[0] * n[1] * n[2] > 0 && smb <= 48 * 1024) ? smb : 0;
+  const size_t off = (*coarse + 15) / 16 * 16;
+  size_t copy = 0;
+  for (int l = 0; l <= top; l++) copy += (size_t)tail_copy_elems(l, pts[l]) * es;
+  if (off + copy <= kTailSmemMax) {
+    *copy_off = (int)off;
+    *total = off + copy;
+  } else {
+    *copy_off = -1;
+    *total = *coarse;
+  }
+}
+
+// Lets `fn` take `bytes` of dynamic shared memory; false if the device refuses.
+static bool allow_smem(const void *fn, size_t bytes) {
+  if (bytes <= 48 * 1024) return true;
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) == cudaSuccess) return true;
+  cudaGetLastError();
+  return false;
+}
+
 // The V-cycle tail of a hierarchy (k_vtail): the largest level below the
 // finest with at most TAIL_MAX_POINTS nodes per instance and everything
 // under it, for V-cycles of two Chebyshev/Jacobi steps (the default
@@ -275,11 +329,16 @@ static int build_tail(fishgpu_solver *S, Hier<T> &H) {
   if (cudaMemcpyAsync(H.tail, tl.data(), sizeof(TailLevel<T>) * (top + 1), cudaMemcpyHostToDevice, S->stream) !=
       cudaSuccess)
     return FISHGPU_ERR_CUDA;
-  const Level<T> &c = H.lev[0];
   const long long per = level_points(H.lev[top].g);
   H.tail_threads = (int)std::min<long long>(1024, std::max<long long>(64, (per + 31) / 32 * 32));
-  const size_t smb = coarse_smem_bytes<T>(S->fine.dim, c.n[0], c.n[1], c.n[2]);
-  H.tail_smem = (c.n[0] * c.n[1] * c.n[2] > 0 && smb <= 48 * 1024) ? smb : 0;
+  std::vector<long long> pts(top + 1);
+  for (int l = 0; l <= top; l++) pts[l] = level_points(H.lev[l].g);
+  tail_smem_plan(S->fine.dim, H.lev[0].n, sizeof(T), top, pts.data(), &H.tail_coarse, &H.tail_copy, &H.tail_smem);
+  const void *fn = S->fine.dim == 2 ? (const void *)k_vtail<2, T> : (const void *)k_vtail<3, T>;
+  if (!allow_smem(fn, H.tail_smem)) {
+    H.tail_copy = -1;
+    H.tail_smem = H.tail_coarse;
+  }
   H.tail_top = top;
   return FISHGPU_OK;
 }
@@ -295,8 +354,8 @@ static int build_tail(fishgpu_solver *S, Hier<T> &H) {
 // SM at most, fewer for fewer fine points), 0 for no persistent solve; *nsm:
 // the device's SMs (the partial sums' capacity).
 template <typename T>
-static int persist_shape(const fishgpu_opts &o, int dim, bool batch, int nlev, const long long *pts, size_t psmem,
-                         int *btop, int *nsm) {
+static int persist_shape(const fishgpu_opts &o, int dim, bool batch, int nlev, const long long *pts, const int *cn,
+                         int *btop, int *nsm, size_t *coarse, int *copy_off, size_t *psmem) {
   if (!o.persist || !o.device_loop || batch || o.pc_type != FISHGPU_PC_MG ||
       o.smooth_type != FISHGPU_SMOOTH_CHEBYSHEV || o.smooth_its != 2 || o.mg_cycles != 1 || dim < 2 || nlev < 3 ||
       nlev > kMaxPersistLevels)
@@ -319,8 +378,14 @@ static int persist_shape(const fishgpu_opts &o, int dim, bool batch, int nlev, c
     cudaGetLastError();
     return 0;
   }
-  const void *fn = dim == 2 ? (const void *)k_ksp_persist<2, T, false> : (const void *)k_ksp_persist<3, T, false>;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 512, psmem) != cudaSuccess || per_sm < 1) {
+  tail_smem_plan(dim, cn, sizeof(T), *btop, pts, coarse, copy_off, psmem);
+  const void *fns[2] = {dim == 2 ? (const void *)k_ksp_persist<2, T, false> : (const void *)k_ksp_persist<3, T, false>,
+                        dim == 2 ? (const void *)k_ksp_persist<2, T, true> : (const void *)k_ksp_persist<3, T, true>};
+  if (!allow_smem(fns[0], *psmem) || (sizeof(T) == 4 && !allow_smem(fns[1], *psmem))) {
+    *copy_off = -1;
+    *psmem = *coarse;
+  }
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fns[0], 512, *psmem) != cudaSuccess || per_sm < 1) {
     cudaGetLastError();
     return 0;
   }
@@ -328,21 +393,15 @@ static int persist_shape(const fishgpu_opts &o, int dim, bool batch, int nlev, c
   return blocks;
 }
 
-// the coarse solve's dynamic shared memory (0: its work area in global memory)
-template <typename T>
-static size_t coarse_psmem(int dim, const int *n) {
-  const size_t smb = coarse_smem_bytes<T>(dim, n[0], n[1], n[2]);
-  return (n[0] * n[1] * n[2] > 0 && smb <= 48 * 1024) ? smb : 0;
-}
-
 template <typename T>
 static int build_persist(fishgpu_solver *S, Hier<T> &H) {
   H.plev = nullptr;
   std::vector<long long> pts(H.nlev);
   for (int l = 0; l < H.nlev; l++) pts[l] = level_points(H.lev[l].g);
-  const size_t psmem = coarse_psmem<T>(S->fine.dim, H.lev[0].n);
-  int btop = 0, nsm = 0;
-  const int blocks = persist_shape<T>(S->o, S->fine.dim, S->batch != 0, H.nlev, pts.data(), psmem, &btop, &nsm);
+  int btop = 0, nsm = 0, copy_off = -1;
+  size_t coarse = 0, psmem = 0;
+  const int blocks = persist_shape<T>(S->o, S->fine.dim, S->batch != 0, H.nlev, pts.data(), H.lev[0].n, &btop, &nsm,
+                                      &coarse, &copy_off, &psmem);
   if (!blocks) return FISHGPU_OK;
   std::vector<TailLevel<T>> tl(H.nlev);
   for (int l = 0; l < H.nlev; l++) tl[l] = tail_level<T>(H.lev[l], l > 0);
@@ -355,6 +414,8 @@ static int build_persist(fishgpu_solver *S, Hier<T> &H) {
   if (!S->pbar && ((rc = dalloc(S, &S->pbar, 2)) || (rc = dalloc(S, &S->ppart, (size_t)4 * nsm)))) return rc;
   H.pbtop = btop;
   H.psmem = psmem;
+  H.pcoarse = coarse;
+  H.pcopy = copy_off;
   S->pblocks = blocks;
   return FISHGPU_OK;
 }
@@ -436,22 +497,6 @@ static int build_hier(fishgpu_solver *S, Hier<T> &H) {
   }
   if ((rc = build_tail<T>(S, H))) return rc;
   return build_persist<T>(S, H);
-}
-
-// ------------------------------------------------------------------ V-cycle tail
-// The coarse end of a V-cycle in ONE block per grid (per instance of a
-// batch): vtail_body's phases, a block barrier between them instead of a
-// launch each; bit-identical to the launch-per-phase form.
-template <int DIM, typename T>
-__global__ void __launch_bounds__(1024) k_vtail(const TailLevel<T> *__restrict__ tl, int top, KspState *st, int batch,
-                                                const T *__restrict__ S0, const T *__restrict__ S1,
-                                                const T *__restrict__ S2, const T *__restrict__ ilam, T *work, int n0,
-                                                int n1, int n2, int smem, T dinv) {
-  extern __shared__ __align__(16) unsigned char fg_tail_sm[];
-  const int plane = (DIM < 3 && batch) ? (int)blockIdx.x : 0;  // instance of a batch
-  if (batch && st) st += plane;
-  if (ksp_done(st)) return;
-  vtail_body<DIM, T>(tl, top, plane, S0, S1, S2, ilam, work, n0, n1, n2, smem, dinv, fg_tail_sm);
 }
 
 // ------------------------------------------------------------------ enqueue
@@ -622,7 +667,7 @@ static void enq_vcycle(fishgpu_solver *S, Hier<T> &H, int l, bool from_zero, int
       const Level<T> &c = H.lev[0];
       k_vtail<DIM, T><<<DIM < 3 && S->batch ? (unsigned)S->nplanes : 1u, H.tail_threads, H.tail_smem, s>>>(
           H.tail, l, st, DIM < 3 ? S->batch : 0, c.S[0], c.S[1], c.S[2], c.ilam, c.work, c.n[0], c.n[1], c.n[2],
-          H.tail_smem ? 1 : 0, (T)(1.0 / c.g.scdiag));
+          H.tail_coarse ? 1 : 0, (T)(1.0 / c.g.scdiag), H.tail_copy);
       for (int q = 0; q <= l; q++) H.lev[q].cur = 0;  // every tail level ends with its iterate in X[0]
       return;
     }
@@ -838,8 +883,9 @@ static int run_ksp_persist(fishgpu_solver *S, Hier<T> &H, KspVecs<T> v, double r
   a.n0 = c.n[0];
   a.n1 = c.n[1];
   a.n2 = c.n[2];
-  a.smem = H.psmem ? 1 : 0;
+  a.smem = H.pcoarse ? 1 : 0;
   a.dinv = (T)(1.0 / c.g.scdiag);
+  a.copy_off = H.pcopy;
   void *args[] = {&a};
   const void *fn;
   if constexpr (sizeof(T) == 4) {
@@ -1619,11 +1665,13 @@ extern "C" long long fishgpu_solver_estimate_bytes(const fishgpu_opts *o) {
       b += rnd((long long)(es == 4 ? sizeof(TailLevel<float>) : sizeof(TailLevel<double>)) * (top + 1));
   }
   {  // the persistent solve's level table, grid barrier and partial sums
-    int n[3] = {1, 1, 1}, btop = 0, nsm = 0;
+    int n[3] = {1, 1, 1}, btop = 0, nsm = 0, copy_off = -1;
+    size_t coarse = 0, psmem = 0;
     for (int q = 0; q < dim; q++) n[q] = (q == 0 ? lv.mx : q == 1 ? lv.my : lv.mz) - 2;
     const int L = o->mg_levels;
-    const int blocks = es == 4 ? persist_shape<float>(*o, dim, false, L, pts.data(), coarse_psmem<float>(dim, n), &btop, &nsm)
-                               : persist_shape<double>(*o, dim, false, L, pts.data(), coarse_psmem<double>(dim, n), &btop, &nsm);
+    const int blocks =
+        es == 4 ? persist_shape<float>(*o, dim, false, L, pts.data(), n, &btop, &nsm, &coarse, &copy_off, &psmem)
+                : persist_shape<double>(*o, dim, false, L, pts.data(), n, &btop, &nsm, &coarse, &copy_off, &psmem);
     if (blocks)
       b += rnd((long long)(es == 4 ? sizeof(TailLevel<float>) : sizeof(TailLevel<double>)) * L) + rnd(8) +
            rnd(8LL * 4 * nsm);

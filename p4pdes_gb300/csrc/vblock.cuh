@@ -162,12 +162,41 @@ __device__ __forceinline__ long long level_pos(const Geom &g, int q, int plane, 
   return (long long)k * g.plane + (long long)j * g.pitch + i;
 }
 
+// level_pos without integer division, for q < 2^24 (exact in FP32): q * (1/m)
+// rounded twice is within one of q / m, and one comparison each way corrects
+// it.  rx = 1/mx, ry = 1/my in FP32.
+__device__ __forceinline__ int div_small(int q, int m, float rm) {
+  int r = __float2int_rz(__int2float_rn(q) * rm);
+  if (r * m > q) r--;
+  else if ((r + 1) * m <= q) r++;
+  return r;
+}
+struct LevelDiv {
+  float rx, ry;
+  __device__ __forceinline__ explicit LevelDiv(const Geom &g) : rx(1.0f / g.mx), ry(1.0f / g.my) {}
+};
+template <int DIM>
+__device__ __forceinline__ long long level_pos_f(const Geom &g, const LevelDiv &d, int q, int plane, int &i, int &j,
+                                                 int &k) {
+  const int r = DIM >= 2 ? div_small(q, g.mx, d.rx) : 0;
+  i = q - r * g.mx;
+  if (DIM >= 3) {
+    k = div_small(r, g.my, d.ry);
+    j = r - k * g.my;
+  } else {
+    j = r;
+    k = plane;
+  }
+  return (long long)k * g.plane + (long long)j * g.pitch + i;
+}
+
 // ------------------------------------------------------------------ the one-block tail
 // Levels top .. 1 pre-smooth, take their residual and restrict it, level 0
 // is solved exactly, and on the way up every level adds the prolongated
 // correction and post-smooths: the work of ~7 launches per level as phases
 // of one block separated by block barriers.  `plane`: the instance of a 2D
-// batch (0 otherwise).
+// batch (0 otherwise).  Tail levels have far fewer than 2^24 nodes
+// (level_pos_f).
 template <int DIM, typename T>
 __device__ void vtail_body(const TailLevel<T> *tl, int top, int plane, const T *S0, const T *S1, const T *S2,
                            const T *ilam, T *work, int n0, int n1, int n2, int smem, T dinv, unsigned char *sm_raw) {
@@ -177,17 +206,18 @@ __device__ void vtail_body(const TailLevel<T> *tl, int top, int plane, const T *
     const TailLevel<T> &C = tl[l - 1];
     const Geom &g = L.g;
     const Wv<T> w(g);
+    const LevelDiv dv(g), dvc(C.g);
     const int N = level_npts<DIM>(g);
     for (int q = tid; q < N; q += nt) {  // two Chebyshev steps from zero (v_cheb2_zero): X[1]
       int i, j, k;
-      const long long n = level_pos<DIM>(g, q, plane, i, j, k);
+      const long long n = level_pos_f<DIM>(g, dv, q, plane, i, j, k);
       const T mab = resid_pt<DIM, T>(g, w, L.b, n, i, j, k, T(0));
       L.X[1][n] = fma(L.a1, mab, L.a0 * L.b[n]);
     }
     __syncthreads();
     for (int q = tid; q < N; q += nt) {  // r = b - A x (v_resid)
       int i, j, k;
-      const long long n = level_pos<DIM>(g, q, plane, i, j, k);
+      const long long n = level_pos_f<DIM>(g, dv, q, plane, i, j, k);
       L.r[n] = resid_pt<DIM, T>(g, w, L.X[1], n, i, j, k, L.b[n]);
     }
     __syncthreads();
@@ -195,7 +225,7 @@ __device__ void vtail_body(const TailLevel<T> *tl, int top, int plane, const T *
     const int Nc = level_npts<DIM>(gc);
     for (int q = tid; q < Nc; q += nt) {  // b_c = P^T r (v_restrict)
       int I, J, K;
-      const long long m = level_pos<DIM>(gc, q, plane, I, J, K);
+      const long long m = level_pos_f<DIM>(gc, dvc, q, plane, I, J, K);
       C.b[m] = restrict_pt<DIM, T>(g, L.r, I, J, K);
     }
     __syncthreads();
@@ -211,28 +241,99 @@ __device__ void vtail_body(const TailLevel<T> *tl, int top, int plane, const T *
     const TailLevel<T> &C = tl[l - 1];
     const Geom &g = L.g, &gc = C.g;
     const Wv<T> w(g);
+    const LevelDiv dv(g);
     const int N = level_npts<DIM>(g);
     for (int q = tid; q < N; q += nt) {  // x += P x_c (v_prolong), x in X[1]
       int i, j, k;
-      const long long n = level_pos<DIM>(g, q, plane, i, j, k);
+      const long long n = level_pos_f<DIM>(g, dv, q, plane, i, j, k);
       L.X[1][n] = prolong_add<DIM, T>(gc, C.X[0], i, j, k, L.X[1][n]);
     }
     __syncthreads();
     for (int q = tid; q < N; q += nt) {  // x1 = x0 + c1 (b - A x0) (v_cheb without x_{k-1}): X[2]
       int i, j, k;
-      const long long n = level_pos<DIM>(g, q, plane, i, j, k);
+      const long long n = level_pos_f<DIM>(g, dv, q, plane, i, j, k);
       const T r = resid_pt<DIM, T>(g, w, L.X[1], n, i, j, k, L.b[n]);
       L.X[2][n] = fma(L.c1, r, T(1) * L.X[1][n]);
     }
     __syncthreads();
     for (int q = tid; q < N; q += nt) {  // x2 = ckm1 x0 + ck x1 + crd (b - A x1) (v_cheb): X[0]
       int i, j, k;
-      const long long n = level_pos<DIM>(g, q, plane, i, j, k);
+      const long long n = level_pos_f<DIM>(g, dv, q, plane, i, j, k);
       const T r = resid_pt<DIM, T>(g, w, L.X[2], n, i, j, k, L.b[n]);
       L.X[0][n] = fma(L.crd, r, fma(L.ckm1, L.X[1][n], L.ck * L.X[2][n]));
     }
     __syncthreads();
   }
+}
+
+// ------------------------------------------------------------------ the tail in shared memory
+// The tail levels' arrays copied into shared memory, compact (pitch mx): a
+// tail phase then waits on shared memory instead of an L2 round trip (~25
+// phases per V-cycle).  Level 0 keeps b and X[0], the others b, r, X[0..2].
+// Only the top level's b comes in and its X[0] goes out: every other tail
+// array is written before it is read within the tail, and nothing outside
+// the tail reads them.  The compact layout gives the same values: the
+// padded layout's extra points are zero and enter no sum (restrict_x reads
+// one as 0, where the compact row ends).
+__host__ __device__ inline Geom compact_geom(Geom g) {
+  g.pitch = g.mx;
+  g.plane = (long long)g.mx * g.my;
+  return g;
+}
+
+// elements of the copy of level l with `pts` nodes per grid
+__host__ __device__ inline long long tail_copy_elems(int l, long long pts) { return (l == 0 ? 2 : 5) * pts; }
+
+// The table of the shared-memory copy (sv): level l's entry built by thread
+// l (a level's offset is the sum of the sizes below it).  Needs a block
+// barrier before use.
+template <int DIM, typename T>
+__device__ void vtail_prepare(const TailLevel<T> *tl, int top, unsigned char *sm_raw, int copy_off, TailLevel<T> *sv) {
+  const int l = threadIdx.x;
+  if (l > top) return;
+  long long off = 0;
+  for (int q = 0; q < l; q++) off += tail_copy_elems(q, level_npts<DIM>(compact_geom(tl[q].g)));
+  T *p = reinterpret_cast<T *>(sm_raw + copy_off) + off;
+  TailLevel<T> t = tl[l];
+  t.g = compact_geom(t.g);
+  const long long n = level_npts<DIM>(t.g);
+  t.b = p;
+  t.X[0] = p + n;
+  if (l > 0) {
+    t.r = p + 2 * n;
+    t.X[1] = p + 3 * n;
+    t.X[2] = p + 4 * n;
+  }
+  sv[l] = t;
+}
+
+// The tail from a prepared shared-memory table sv (copy_off >= 0), or in
+// global memory (copy_off < 0): the top level's b in, vtail_body, its X[0]
+// out.  `smem` as coarse_solve_block takes it.
+template <int DIM, typename T>
+__device__ void vtail_run(const TailLevel<T> *tl, int top, int plane, const T *S0, const T *S1, const T *S2,
+                          const T *ilam, T *work, int n0, int n1, int n2, int smem, T dinv, unsigned char *sm_raw,
+                          int copy_off, const TailLevel<T> *sv) {
+  if (copy_off < 0) {  // the arrays stay in global memory
+    vtail_body<DIM, T>(tl, top, plane, S0, S1, S2, ilam, work, n0, n1, n2, smem, dinv, sm_raw);
+    return;
+  }
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const TailLevel<T> &G = tl[top];
+  const TailLevel<T> &C = sv[top];
+  const int N = level_npts<DIM>(G.g);
+  const LevelDiv dv(G.g);
+  for (int q = tid; q < N; q += nt) {
+    int i, j, k;
+    C.b[q] = G.b[level_pos_f<DIM>(G.g, dv, q, plane, i, j, k)];
+  }
+  __syncthreads();
+  vtail_body<DIM, T>(sv, top, 0, S0, S1, S2, ilam, work, n0, n1, n2, smem, dinv, sm_raw);
+  for (int q = tid; q < N; q += nt) {
+    int i, j, k;
+    G.X[0][level_pos_f<DIM>(G.g, dv, q, plane, i, j, k)] = C.X[0][q];
+  }
+  __syncthreads();
 }
 
 // ------------------------------------------------------------------ grid barrier
@@ -313,6 +414,7 @@ struct PersistArgs {
   T *work;
   int n0, n1, n2, smem;
   T dinv;
+  int copy_off;            // offset of the tail's shared-memory copy in the dynamic shared memory (-1: none)
 };
 
 // Per-thread partial sums -> one partial per block -> barrier -> every block
@@ -409,6 +511,7 @@ __global__ void __launch_bounds__(512, 1) k_ksp_persist(PersistArgs<T> a) {
   __shared__ KspState ks;
   __shared__ GridBar gb;
   __shared__ TailLevel<T> lv[kMaxPersistLevels];  // the level table, read at every phase
+  __shared__ TailLevel<T> sv[kMaxPersistLevels];  // block 0: the tail's shared-memory copy
   const int tid = threadIdx.x;
   if (tid == 0) {
     ks = *a.st;
@@ -418,6 +521,11 @@ __global__ void __launch_bounds__(512, 1) k_ksp_persist(PersistArgs<T> a) {
   for (int l = tid; l <= a.top; l += blockDim.x) lv[l] = a.lv[l];
   __syncthreads();
   if (ks.done) return;  // every block sees the same state
+  if (blockIdx.x == 0) {  // block 0's tail: its shared-memory table and the coarse solve's tables, once
+    if (a.copy_off >= 0) vtail_prepare<DIM, T>(lv, a.btop, fg_tail_sm, a.copy_off, sv);
+    if (a.smem) coarse_stage<DIM, T>(a.S0, a.S1, a.S2, a.ilam, a.n0, a.n1, a.n2, fg_tail_sm);
+    __syncthreads();
+  }
   // points are dealt to the blocks in warp-sized runs, round robin: a small
   // level's points spread over all SMs (FP64 work on one SM is slow) and
   // every warp still reads consecutive points
@@ -427,10 +535,19 @@ __global__ void __launch_bounds__(512, 1) k_ksp_persist(PersistArgs<T> a) {
   auto sync = [&]() { return grid_sync(&gb); };
   auto each = [&](const Geom &g, auto &&f) {
     const int N = level_npts<DIM>(g);
-    for (long long q = gt; q < N; q += G) {
-      int i, j, k;
-      const long long n = level_pos<DIM>(g, (int)q, 0, i, j, k);
-      f(n, i, j, k);
+    if (N < (1 << 24)) {
+      const LevelDiv dv(g);
+      for (long long q = gt; q < N; q += G) {
+        int i, j, k;
+        const long long n = level_pos_f<DIM>(g, dv, (int)q, 0, i, j, k);
+        f(n, i, j, k);
+      }
+    } else {
+      for (long long q = gt; q < N; q += G) {
+        int i, j, k;
+        const long long n = level_pos<DIM>(g, (int)q, 0, i, j, k);
+        f(n, i, j, k);
+      }
     }
   };
   const TailLevel<T> &F = lv[a.top];
@@ -497,9 +614,9 @@ __global__ void __launch_bounds__(512, 1) k_ksp_persist(PersistArgs<T> a) {
       }
       if (!sync()) return false;
     }
-    if (blockIdx.x == 0)
-      vtail_body<DIM, T>(lv, a.btop, 0, a.S0, a.S1, a.S2, a.ilam, a.work, a.n0, a.n1, a.n2, a.smem, a.dinv,
-                         fg_tail_sm);
+    if (blockIdx.x == 0)  // smem 2: the coarse tables are staged
+      vtail_run<DIM, T>(lv, a.btop, 0, a.S0, a.S1, a.S2, a.ilam, a.work, a.n0, a.n1, a.n2, a.smem ? 2 : 0, a.dinv,
+                        fg_tail_sm, a.copy_off, sv);
     if (!sync()) return false;
     for (int l = a.btop + 1; l <= a.top; l++) {
       const TailLevel<T> &L = lv[l];
