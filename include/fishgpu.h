@@ -340,6 +340,23 @@ int fishgpu_batch_groups(const fishgpu_batch *b, int *n, int *count, int *sweeps
 int fishgpu_batch_results(const fishgpu_batch *b, int *inner_its, int *outer_its, double *rel_resid, int *reason);
 int fishgpu_batch_destroy(fishgpu_batch *b);
 
+/* ---- same-size groups: `count` n x n instances solved together ----------
+   One size group of a batch on its own stream (no device-wide
+   synchronisation): the server's unit of merged 2D requests.  A solve takes
+   k <= count host arrays (n*n doubles each); instances k .. count-1 are
+   empty (f = 0: converged at once, their planes skip every kernel).  Every
+   instance's result is independent of the others and of count (per-plane
+   reductions, fixed tiles with o->tune = 0): bit-identical to the same
+   instance in a group of one. */
+typedef struct fishgpu_group_s fishgpu_group;
+int fishgpu_group_create(const fishgpu_batch_opts *o, int n, int count, fishgpu_group **out);
+long long fishgpu_group_bytes(const fishgpu_group *g);
+/* per instance q < k: inner (summed) and outer iterations, FP64 true
+   relative residual; returns the solve's status */
+int fishgpu_group_solve_host(fishgpu_group *g, int k, const double *const *f_host, double *const *u_host, int *its,
+                             int *outer_its, double *rel_resid);
+int fishgpu_group_destroy(fishgpu_group *g);
+
 /* ---- server: continuous batching of independent solves ----------------
    Each request is -Laplace(u) = f (fish's operator, cx = cy = cz = 1) on the
    unit square/cube with u = 0 on the boundary, n nodes per side (2^k + 1),
@@ -355,6 +372,12 @@ typedef struct {
   double rtol;                /* true relative residual per request          */
   int precision;              /* FISHGPU_MIXED (default) or FISHGPU_FP64     */
   int fifo;                   /* 1: a request waits for every earlier one    */
+  int batch_max;              /* mixed form: 2D requests of one size queued
+                                 together are merged, up to batch_max, into
+                                 one group solve
+                                 (fishgpu_group; groups of 1, 2, 4, ... up to
+                                 batch_max instances are pooled); 1: every
+                                 request its own solver (default 16)        */
 } fishgpu_server_opts;
 
 typedef struct {
@@ -374,6 +397,8 @@ int fishgpu_server_submit(fishgpu_server *s, int dim, int n, const double *f_hos
 int fishgpu_server_wait(fishgpu_server *s, long long ticket, double timeout_ms, fishgpu_server_result *res);
 int fishgpu_server_stats(fishgpu_server *s, long long *pooled_bytes, int *pooled_solvers, long long *created,
                          long long *evicted);
+/* group solves run and the requests they served */
+int fishgpu_server_group_stats(fishgpu_server *s, long long *group_solves, long long *grouped_requests);
 int fishgpu_server_destroy(fishgpu_server *s);
 
 /* ---- minimal-surface equation (c/ch7/minimal.c) -------------------------

@@ -115,7 +115,7 @@ class BatchReport(ctypes.Structure):
 
 class ServerOpts(ctypes.Structure):
     _fields_ = [("hbm_budget_bytes", c_ll), ("workers", c_int), ("rtol", c_double), ("precision", c_int),
-                ("fifo", c_int)]
+                ("fifo", c_int), ("batch_max", c_int)]
 
 
 class ServerResult(ctypes.Structure):
@@ -217,6 +217,15 @@ def load():
     for name in ("fishgpu_batch_opts_default", "fishgpu_batch_create", "fishgpu_batch_solve",
                  "fishgpu_batch_results", "fishgpu_batch_destroy", "fishgpu_batch_groups"):
         getattr(lib, name).restype = c_int
+    lib.fishgpu_group_create.argtypes = [_P(BatchOpts), c_int, c_int, _P(c_void_p)]
+    lib.fishgpu_group_create.restype = c_int
+    lib.fishgpu_group_bytes.argtypes = [c_void_p]
+    lib.fishgpu_group_bytes.restype = c_ll
+    lib.fishgpu_group_solve_host.argtypes = [c_void_p, c_int, _P(c_void_p), _P(c_void_p), _P(c_int), _P(c_int),
+                                             _P(c_double)]
+    lib.fishgpu_group_solve_host.restype = c_int
+    lib.fishgpu_group_destroy.argtypes = [c_void_p]
+    lib.fishgpu_group_destroy.restype = c_int
     lib.fishgpu_solver_time_kernel.argtypes = [c_void_p, ctypes.c_char_p, c_int, _P(c_double), _P(c_double)]
     lib.fishgpu_fp64_fma_rate.argtypes = [c_int, _P(c_double)]
     lib.fishgpu_fp64_fma_rate.restype = c_int
@@ -256,6 +265,8 @@ def load():
     lib.fishgpu_server_submit.argtypes = [c_void_p, c_int, c_int, c_void_p, c_void_p, _P(c_ll)]
     lib.fishgpu_server_wait.argtypes = [c_void_p, c_ll, c_double, _P(ServerResult)]
     lib.fishgpu_server_stats.argtypes = [c_void_p, _P(c_ll), _P(c_int), _P(c_ll), _P(c_ll)]
+    lib.fishgpu_server_group_stats.argtypes = [c_void_p, _P(c_ll), _P(c_ll)]
+    lib.fishgpu_server_group_stats.restype = c_int
     lib.fishgpu_server_destroy.argtypes = [c_void_p]
     for name in ("fishgpu_server_opts_default", "fishgpu_server_create", "fishgpu_server_submit",
                  "fishgpu_server_wait", "fishgpu_server_stats", "fishgpu_server_destroy"):
@@ -495,6 +506,56 @@ class Batch:
             pass
 
 
+class Group:
+    """`count` same-size 2D problems (n x n, n = 2^k + 1) solved together with the
+    batch's kernels on one stream; solve_host takes up to `count` host arrays
+    (the rest of the group is empty).  An instance's result does not depend on
+    the group it is solved in (tune = 0)."""
+
+    def __init__(self, n, count, rtol=1e-8, **kw):
+        o = BatchOpts()
+        _check(load().fishgpu_batch_opts_default(ctypes.byref(o)), "fishgpu_batch_opts_default")
+        o.rtol = rtol
+        o.tune = 0
+        o.tune_sweeps = 0
+        for k, v in kw.items():
+            setattr(o, k, v)
+        self.n, self.count = int(n), int(count)
+        self._h = c_void_p()
+        _check(load().fishgpu_group_create(ctypes.byref(o), self.n, self.count, ctypes.byref(self._h)),
+               "fishgpu_group_create")
+
+    @property
+    def device_bytes(self):
+        return load().fishgpu_group_bytes(self._h)
+
+    def solve_host(self, fs, us):
+        """fs, us: host float64 arrays (n, n); returns [(its, outer_its, rel_resid)] per instance."""
+        k = len(fs)
+        fa = (c_void_p * k)(*[_host_addr(f) for f in fs])
+        ua = (c_void_p * k)(*[_host_addr(u) for u in us])
+        its, outer, rel = (c_int * k)(), (c_int * k)(), (c_double * k)()
+        _check(load().fishgpu_group_solve_host(self._h, k, fa, ua, its, outer, rel), "fishgpu_group_solve_host")
+        return [(its[q], outer[q], rel[q]) for q in range(k)]
+
+    def close(self):
+        if self._h:
+            load().fishgpu_group_destroy(self._h)
+            self._h = c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def fp64_fma_rate(reps=5):
     """FP64 FMA throughput of the current device in TFLOP/s (FMA = 2 flops)."""
     t = c_double()
@@ -518,7 +579,8 @@ class Server:
     f and u are host float64 arrays (numpy or CPU tensors, pinned for speed)
     that must stay alive until wait() returns."""
 
-    def __init__(self, hbm_budget_bytes=120 << 30, workers=8, rtol=1e-8, precision=MIXED, fifo=False):
+    def __init__(self, hbm_budget_bytes=120 << 30, workers=8, rtol=1e-8, precision=MIXED, fifo=False,
+                 batch_max=16):
         o = ServerOpts()
         _check(load().fishgpu_server_opts_default(ctypes.byref(o)), "fishgpu_server_opts_default")
         o.hbm_budget_bytes = int(hbm_budget_bytes)
@@ -526,6 +588,7 @@ class Server:
         o.rtol = rtol
         o.precision = precision
         o.fifo = int(bool(fifo))
+        o.batch_max = int(batch_max)
         self._h = c_void_p()
         self._keep = {}
         _check(load().fishgpu_server_create(ctypes.byref(o), ctypes.byref(self._h)), "fishgpu_server_create")
@@ -547,7 +610,11 @@ class Server:
         b, n, c, e = c_ll(), c_int(), c_ll(), c_ll()
         _check(load().fishgpu_server_stats(self._h, ctypes.byref(b), ctypes.byref(n), ctypes.byref(c),
                                            ctypes.byref(e)), "fishgpu_server_stats")
-        return {"pooled_bytes": b.value, "pooled_solvers": n.value, "created": c.value, "evicted": e.value}
+        gs, gr = c_ll(), c_ll()
+        _check(load().fishgpu_server_group_stats(self._h, ctypes.byref(gs), ctypes.byref(gr)),
+               "fishgpu_server_group_stats")
+        return {"pooled_bytes": b.value, "pooled_solvers": n.value, "created": c.value, "evicted": e.value,
+                "group_solves": gs.value, "grouped_requests": gr.value}
 
     def close(self):
         if self._h:
@@ -585,6 +652,7 @@ def server_request_opts(dim, n, rtol=1e-8, precision=MIXED):
     o.precision = precision
     o.rtol = rtol
     o.norm_type = NORM_UNPRECONDITIONED
+    o.persist = 0
     return o
 
 

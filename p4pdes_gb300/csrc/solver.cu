@@ -2538,3 +2538,89 @@ extern "C" int fishgpu_batch_results(const fishgpu_batch *B, int *inner_its, int
   }
   return FISHGPU_OK;
 }
+
+// ------------------------------------------------------------------ same-size groups
+struct fishgpu_group_s {
+  fishgpu_solver *S = nullptr;
+  int n = 0, count = 0;
+  double *fbuf = nullptr, *ubuf = nullptr;  // count dense n x n arrays each
+  const double **fptr = nullptr;            // device: fbuf + q n^2
+  double **uptr = nullptr;
+  long long bytes = 0;
+};
+
+extern "C" int fishgpu_group_destroy(fishgpu_group *G) {
+  if (!G) return FISHGPU_OK;
+  if (G->S) fishgpu_solver_destroy(G->S);
+  cudaFree(G->fbuf);
+  cudaFree(G->ubuf);
+  cudaFree(G->fptr);
+  cudaFree(G->uptr);
+  delete G;
+  return FISHGPU_OK;
+}
+
+extern "C" int fishgpu_group_create(const fishgpu_batch_opts *o, int n, int count, fishgpu_group **out) {
+  if (!o || !out || n < 3 || ((n - 1) & (n - 2)) != 0 || count < 1 || count > 65535) return FISHGPU_ERR_ARG;
+  *out = nullptr;
+  fishgpu_group *G = new fishgpu_group();
+  G->n = n;
+  G->count = count;
+  int rc = fg::group_create(*o, n, count, &G->S);
+  const size_t nn = (size_t)n * n;
+  if (!rc) {
+    if (cudaMalloc((void **)&G->fbuf, sizeof(double) * nn * count) != cudaSuccess ||
+        cudaMalloc((void **)&G->ubuf, sizeof(double) * nn * count) != cudaSuccess ||
+        cudaMalloc((void **)&G->fptr, sizeof(double *) * count) != cudaSuccess ||
+        cudaMalloc((void **)&G->uptr, sizeof(double *) * count) != cudaSuccess) {
+      cudaGetLastError();
+      rc = FISHGPU_ERR_NOMEM;
+    }
+  }
+  if (!rc) {
+    std::vector<const double *> hf(count);
+    std::vector<double *> hu(count);
+    for (int q = 0; q < count; q++) {
+      hf[q] = G->fbuf + nn * q;
+      hu[q] = G->ubuf + nn * q;
+    }
+    if (cudaMemcpy(G->fptr, hf.data(), sizeof(double *) * count, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(G->uptr, hu.data(), sizeof(double *) * count, cudaMemcpyHostToDevice) != cudaSuccess)
+      rc = FISHGPU_ERR_CUDA;
+  }
+  if (rc) {
+    fishgpu_group_destroy(G);
+    return rc;
+  }
+  G->bytes = G->S->bytes + (long long)(2 * nn * count * sizeof(double) + 2 * count * sizeof(double *));
+  *out = G;
+  return FISHGPU_OK;
+}
+
+extern "C" long long fishgpu_group_bytes(const fishgpu_group *G) { return G ? G->bytes : 0; }
+
+extern "C" int fishgpu_group_solve_host(fishgpu_group *G, int k, const double *const *f_host, double *const *u_host,
+                                        int *its, int *outer_its, double *rel_resid) {
+  if (!G || k < 1 || k > G->count || !f_host || !u_host) return FISHGPU_ERR_ARG;
+  for (int q = 0; q < k; q++)
+    if (!f_host[q] || !u_host[q]) return FISHGPU_ERR_ARG;
+  fishgpu_solver *S = G->S;
+  cudaStream_t s = S->stream;
+  const size_t nn = (size_t)G->n * G->n;
+  for (int q = 0; q < k; q++)
+    FG_CUDA(cudaMemcpyAsync(G->fbuf + nn * q, f_host[q], sizeof(double) * nn, cudaMemcpyHostToDevice, s));
+  if (k < G->count) FG_CUDA(cudaMemsetAsync(G->fbuf + nn * k, 0, sizeof(double) * nn * (G->count - k), s));
+  std::vector<int> vi(G->count), vo(G->count), vr(G->count);
+  std::vector<double> vrel(G->count);
+  int rc = fg::group_solve(S, G->fptr, G->uptr, vi.data(), vo.data(), vrel.data(), vr.data());
+  if (rc) return rc;
+  for (int q = 0; q < k; q++)
+    FG_CUDA(cudaMemcpyAsync(u_host[q], G->ubuf + nn * q, sizeof(double) * nn, cudaMemcpyDeviceToHost, s));
+  FG_CUDA(cudaStreamSynchronize(s));
+  for (int q = 0; q < k; q++) {
+    if (its) its[q] = vi[q];
+    if (outer_its) outer_its[q] = vo[q];
+    if (rel_resid) rel_resid[q] = vrel[q];
+  }
+  return FISHGPU_OK;
+}

@@ -56,8 +56,10 @@ def run_server(reqs, **kw):
 
 
 def test_mixed_stream_equals_each_request_alone(cuda):
+    """Every request its own solver (batch_max 1): bit-identical to a fresh
+    solver."""
     reqs = requests()
-    us, res, stats = run_server(reqs, workers=6)
+    us, res, stats = run_server(reqs, workers=6, batch_max=1)
     assert stats["created"] >= len({(d, n) for d, n, _ in reqs})
     for (d, n, f), u, r in zip(reqs, us, res):
         assert r.status == 0 and r.rel_resid <= 1e-8, (d, n, r.status, r.rel_resid)
@@ -72,7 +74,7 @@ def test_small_budget_evicts_and_still_completes(cuda):
     import p4pdes_gb300 as fg
     reqs = requests(5)[:8]
     need = max(fg.estimate_bytes(fg.server_request_opts(d, n)) for d, n, _ in reqs)
-    us, res, stats = run_server(reqs, workers=4, hbm_budget_bytes=need + need // 4)
+    us, res, stats = run_server(reqs, workers=4, hbm_budget_bytes=need + need // 4, batch_max=1)
     assert stats["evicted"] > 0 and stats["pooled_bytes"] <= need + need // 4
     for (d, n, f), u, r in zip(reqs, us, res):
         assert r.status == 0
@@ -103,3 +105,47 @@ def test_estimate_equals_allocation(cuda, dim, n, prec):
     with fg.Solver(o) as s:
         s.solve_host(f, None, u)
         assert s.device_bytes == est
+
+
+def test_same_size_2d_requests_are_merged_into_group_solves(cuda):
+    """2D requests of one size queued together run as one group solve (the
+    batch's plane-stacked kernels); each result is bit-identical to the same
+    request solved alone in a group of one, meets rtol on the FP64 residual
+    recomputed on the CPU, and 3D requests keep their own solvers."""
+    import p4pdes_gb300 as fg
+    rng = np.random.default_rng(11)
+    sizes = [(2, 65)] * 6 + [(2, 129)] * 5 + [(3, 17)] * 2 + [(2, 33)] * 3
+    reqs = [(d, n, rng.standard_normal((n,) * d)) for d, n in sizes]
+    # one worker: everything queues behind the first request and is merged
+    us, res, stats = run_server(reqs, workers=1, batch_max=4)
+    assert stats["group_solves"] >= 1 and stats["grouped_requests"] > stats["group_solves"]
+    assert stats["grouped_requests"] == sum(1 for d, _, _ in reqs if d == 2)
+    for (d, n, f), u, r in zip(reqs, us, res):
+        assert r.status == 0 and r.rel_resid <= 1e-8, (d, n, r.status, r.rel_resid)
+        assert relres_cpu(d, n, f, u) <= 2e-8
+        if d == 2:
+            ua = np.full_like(f, np.nan)
+            with fg.Group(n, 1) as g:
+                (its, outer, rel), = g.solve_host([f], [ua])
+            assert np.array_equal(u, ua), (n, np.max(np.abs(u - ua)))
+            assert its == r.its and outer == r.outer_its
+        else:
+            ua, rep = solve_alone(d, n, f)
+            assert np.array_equal(u, ua)
+
+
+def test_group_instances_do_not_depend_on_the_group(cuda):
+    """One instance in groups of 1, 3 (padded to 4) and 8: identical results."""
+    import p4pdes_gb300 as fg
+    rng = np.random.default_rng(3)
+    fs = [rng.standard_normal((129, 129)) for _ in range(8)]
+    outs = {}
+    for count, k in ((1, 1), (4, 3), (8, 8)):
+        us = [np.full_like(f, np.nan) for f in fs[:k]]
+        with fg.Group(129, count) as g:
+            r = g.solve_host(fs[:k], us)
+        outs[count] = (us[0], r[0])
+    for count in (4, 8):
+        assert np.array_equal(outs[count][0], outs[1][0])
+        assert outs[count][1] == outs[1][1]
+    assert outs[1][1][2] <= 1e-8
