@@ -896,8 +896,17 @@ static int run_ksp_persist(fishgpu_solver *S, Hier<T> &H, KspVecs<T> v, double r
   FG_CUDA(cudaLaunchCooperativeKernel(fn, dim3(S->pblocks), dim3(512), args, H.psmem, s));
   S->launches += 1;
   FG_CUDA(cudaMemcpyAsync(S->st_h, S->st, sizeof(KspState), cudaMemcpyDeviceToHost, s));
+  FG_CUDA(cudaMemcpyAsync(S->hval + 7, S->fault, sizeof(int), cudaMemcpyDeviceToHost, s));
   FG_CUDA(cudaStreamSynchronize(s));
-  if (!S->st_h->done) return FISHGPU_ERR_TIMEOUT;
+  int fault = 0;
+  memcpy(&fault, S->hval + 7, sizeof(int));
+  if (fault || !S->st_h->done) {  // a barrier gave up, or the iteration cap ran out
+    if (fault) {  // the next solve starts clean
+      FG_CUDA(cudaMemsetAsync(S->fault, 0, sizeof(int), s));
+      FG_CUDA(cudaStreamSynchronize(s));
+    }
+    return FISHGPU_ERR_TIMEOUT;
+  }
   return FISHGPU_OK;
 }
 
@@ -1106,6 +1115,8 @@ static int solve_dim(fishgpu_solver *S, double *u, fishgpu_report *rep) {
   const Launch &L = S->Lf;
   const Geom &g = S->fine;
   FG_CUDA(cudaEventRecord(S->ev0, s));
+  // a solve that ended early on an error may have left the fault word set
+  if (S->fault) FG_CUDA(cudaMemsetAsync(S->fault, 0, sizeof(int), s));
   // the KSP right-hand side is -F(u0) = beff - A u0 and its norm; it solves
   // for -y and u = u0 + (-y)
   double *F = o.precision == FISHGPU_MIXED ? S->b64 : S->r64;
