@@ -291,6 +291,14 @@ int fishgpu_solve_host(const fishgpu_opts *o, const double *f_host, const double
 int fishgpu_solver_time_kernel(fishgpu_solver *s, const char *name, int reps,
                                double *ms_per_launch, double *bytes_per_launch);
 
+/* Self-test of the persistent solve's grid barrier and its time limit: one
+   barrier over the solve's blocks, with block 0 leaving without arriving
+   when `missing` is nonzero.  Returns FISHGPU_ERR_TIMEOUT when the other
+   blocks' bounded waits ran out (expected with missing, after ~0.2 s),
+   FISHGPU_OK when the barrier completed; FISHGPU_ERR_UNSUPPORTED when the
+   solver has no persistent solve.  The device stays usable either way. */
+int fishgpu_solver_barrier_selftest(fishgpu_solver *s, int missing);
+
 /* Measures the current device's FP64 FMA throughput in TFLOP/s (an FMA is 2
    flops): `reps` timed launches of a kernel of independent FMA chains on
    every SM, after one warm-up launch; the best launch counts.  The

@@ -266,6 +266,8 @@ def load():
     lib.fishgpu_server_wait.argtypes = [c_void_p, c_ll, c_double, _P(ServerResult)]
     lib.fishgpu_server_stats.argtypes = [c_void_p, _P(c_ll), _P(c_int), _P(c_ll), _P(c_ll)]
     lib.fishgpu_server_group_stats.argtypes = [c_void_p, _P(c_ll), _P(c_ll)]
+    lib.fishgpu_solver_barrier_selftest.argtypes = [c_void_p, c_int]
+    lib.fishgpu_solver_barrier_selftest.restype = c_int
     lib.fishgpu_server_group_stats.restype = c_int
     lib.fishgpu_server_destroy.argtypes = [c_void_p]
     for name in ("fishgpu_server_opts_default", "fishgpu_server_create", "fishgpu_server_submit",
@@ -413,6 +415,10 @@ class Solver:
         if rc not in (0, 4):
             raise FishError(rc, "fishgpu_solver_solve_host")
         return rep
+
+    def barrier_selftest(self, missing):
+        """The persistent solve's grid barrier with block 0 absent (missing) or not: the status."""
+        return load().fishgpu_solver_barrier_selftest(self._h, int(missing))
 
     def host_bytes_in(self, g=None):
         """Bytes solve_host moves to the device for f and g."""

@@ -1302,8 +1302,8 @@ static int time_kernel_dim(fishgpu_solver *S, const char *name, int reps, double
   } free_tst{tst};
   if (!strcmp(name, "grid_sync")) {  // one barrier of the persistent solve (launches of 100)
     if (!S->pbar || S->pblocks < 1) return FISHGPU_ERR_UNSUPPORTED;
-    int nb = 100;
-    void *args[] = {&S->pbar, &S->fault, &nb};
+    int nb = 100, absent = -1;
+    void *args[] = {&S->pbar, &S->fault, &nb, &absent};
     FG_CUDA(cudaMemsetAsync(S->pbar, 0, 2 * sizeof(unsigned), s));
     FG_CUDA(cudaLaunchCooperativeKernel((const void *)k_grid_sync_probe, dim3(S->pblocks), dim3(512), args, 0, s));
     FG_CUDA(cudaEventRecord(S->ev0, s));
@@ -2634,4 +2634,28 @@ extern "C" int fishgpu_group_solve_host(fishgpu_group *G, int k, const double *c
     if (rel_resid) rel_resid[q] = vrel[q];
   }
   return FISHGPU_OK;
+}
+
+// The grid barrier's time limit, exercised: one barrier over the persistent
+// solve's blocks with block 0 absent (missing = 1) must end with the fault
+// word set (FISHGPU_ERR_TIMEOUT, after ~0.2 s), with every block present
+// (missing = 0) without it.  The fault word and the barrier are cleared
+// afterwards.
+extern "C" int fishgpu_solver_barrier_selftest(fishgpu_solver *S, int missing) {
+  if (!S) return FISHGPU_ERR_ARG;
+  if (!S->pbar || S->pblocks < 1 || (missing && S->pblocks < 2)) return FISHGPU_ERR_UNSUPPORTED;
+  cudaStream_t s = S->stream;
+  int nb = 1, absent = missing ? 0 : -1;
+  void *args[] = {&S->pbar, &S->fault, &nb, &absent};
+  FG_CUDA(cudaMemsetAsync(S->pbar, 0, 2 * sizeof(unsigned), s));
+  FG_CUDA(cudaMemsetAsync(S->fault, 0, sizeof(int), s));
+  FG_CUDA(cudaLaunchCooperativeKernel((const void *)fg::k_grid_sync_probe, dim3(S->pblocks), dim3(512), args, 0, s));
+  FG_CUDA(cudaMemcpyAsync(S->hval + 7, S->fault, sizeof(int), cudaMemcpyDeviceToHost, s));
+  FG_CUDA(cudaStreamSynchronize(s));
+  int fault = 0;
+  memcpy(&fault, S->hval + 7, sizeof(int));
+  FG_CUDA(cudaMemsetAsync(S->fault, 0, sizeof(int), s));
+  FG_CUDA(cudaMemsetAsync(S->pbar, 0, 2 * sizeof(unsigned), s));
+  FG_CUDA(cudaStreamSynchronize(s));
+  return fault ? FISHGPU_ERR_TIMEOUT : FISHGPU_OK;
 }

@@ -383,9 +383,12 @@ __device__ __forceinline__ bool grid_sync(GridBar *gb) {
   return !gb->fail;
 }
 
-// n grid barriers and nothing else (the timer's measure of one barrier)
-static __global__ void __launch_bounds__(512, 1) k_grid_sync_probe(unsigned *bar, int *fault, int n) {
+// n grid barriers and nothing else (the timer's measure of one barrier).
+// absent >= 0 (the barrier's self-test): that block leaves without
+// arriving, so the others' waits run out and set the fault word.
+static __global__ void __launch_bounds__(512, 1) k_grid_sync_probe(unsigned *bar, int *fault, int n, int absent) {
   __shared__ GridBar gb;
+  if ((int)blockIdx.x == absent) return;
   if (threadIdx.x == 0) gb = GridBar{bar, fault, 0u, 0};
   __syncthreads();
   for (int q = 0; q < n; q++)

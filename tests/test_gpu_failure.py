@@ -80,3 +80,21 @@ def test_server_wait_gives_up_on_an_unfinished_request(cuda):
         r2 = srv.wait(t2, -1.0)
     assert r1.status == 0 and r2.status == 0
     assert r2.rel_resid <= 1e-8 and np.all(np.isfinite(u2))
+
+
+def test_persistent_grid_barrier_gives_up_and_the_device_stays_usable(cuda):
+    """The persistent solve's grid barrier waits at most ~0.2 s: with one block
+    absent (a flag nothing sets) the others give up, the fault word reports
+    it, and the same solver then solves normally."""
+    import time
+    import torch
+    import p4pdes_gb300 as fg
+    o = fg.options("-fsh_dim 2 -fsh_problem manupoly -da_refine 7 -pc_type mg -ksp_rtol 1e-10 -fsh_persist 1")
+    u = torch.empty(o.shape, dtype=torch.float64, device=cuda)
+    with fg.Solver(o) as s:
+        assert s.barrier_selftest(False) == 0
+        t0 = time.perf_counter()
+        assert s.barrier_selftest(True) == TIMEOUT
+        assert time.perf_counter() - t0 < 5.0
+        rep = s.solve(u)
+        assert rep.reason == 2 and rep.launches < 12
