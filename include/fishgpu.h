@@ -210,6 +210,13 @@ typedef struct {
   int persist_tail;         /* -fsh_persist_tail: largest level (nodes) the
                                persistent solve runs in its block 0 (0:
                                300 in FP64, 1200 in FP32)                  */
+  int fuse_cgr;             /* -fsh_fuse_cgr 0|1: the mixed form's inner CG
+                               iterations run their residual update
+                               r -= alpha w inside the V-cycle's first
+                               smoothing pass (one pass over r and w
+                               instead of two, a second r buffer; MG with
+                               two Chebyshev steps; default 1,
+                               bit-identical to 0)                        */
 } fishgpu_opts;
 
 #define FISHGPU_MAX_HIST 512

@@ -156,6 +156,7 @@ struct fishgpu_solver_s {
   bool beff_ready = false;   // built-in problems: computed once
   // FP32 inner KSP vectors (mixed form)
   float *r32 = nullptr, *p32 = nullptr, *q32 = nullptr, *w32 = nullptr, *y32 = nullptr;
+  float *r32b = nullptr;   // second CG residual buffer of the FP32 inner solves (fuse_cgr_ok)
   cudaGraphExec_t gexec = nullptr;       // giters CG iterations
   cudaGraphExec_t gloop = nullptr;       // the same repeated on the device until the solve stops
   bool loop_refused = false;             // the driver refused the device loop: poll from the host
@@ -564,8 +565,18 @@ static void launch_cheb_dots(fishgpu_solver *S, Level<T> &lv, const T *xkm1, con
                                                                        ck, crd, S->red, 0, fin);
 }
 
+// The CG residual update of an iteration, r_new = r - alpha w, carried into
+// the first smoothing pass of its V-cycle (v_cheb2_zero's RUPD form): the
+// finest level's b is r_new, formed from r and w and stored there.
+template <typename T>
+struct RUpd {
+  const T *r, *w;
+  bool rr;  // unpreconditioned norm: r_new.r_new and FIN_RR
+};
+
 template <int DIM, typename T>
-static void enq_smooth(fishgpu_solver *S, Level<T> &lv, bool from_zero, int dots = -1) {
+static void enq_smooth(fishgpu_solver *S, Level<T> &lv, bool from_zero, int dots = -1,
+                       const RUpd<T> *ru = nullptr) {
   const fishgpu_opts &o = S->o;
   const Fin fin = (Fin)(dots < 0 ? 0 : dots);
   const double dinv = 1.0 / lv.g.scdiag;
@@ -599,8 +610,17 @@ static void enq_smooth(fishgpu_solver *S, Level<T> &lv, bool from_zero, int dots
     // x1 = c1 b; x2 = omega x1 + omega c1 (b - A x1) = 2 omega c1 b - omega c1^2 (A b)
     const double ckp1 = 2.0 * mu * mu - 1.0, omega = omegaprod * mu / ckp1;
     const int nxt = (lv.cur + 1) % 3;
-    v_cheb2_zero<DIM, T><<<gbs, lv.st.chunk, 0, s>>>(lv.g, lv.st, st, lv.b, lv.X[nxt], (T)(2.0 * omega * c1),
-                                            (T)(omega * c1 * c1));
+    if (ru && ru->rr)
+      v_cheb2_zero<DIM, T, true, true><<<gbs, lv.st.chunk, 0, s>>>(lv.g, lv.st, st, ru->r, lv.X[nxt],
+                                                                   (T)(2.0 * omega * c1), (T)(omega * c1 * c1),
+                                                                   ru->w, lv.b, S->red, 0);
+    else if (ru)
+      v_cheb2_zero<DIM, T, true, false><<<gbs, lv.st.chunk, 0, s>>>(lv.g, lv.st, st, ru->r, lv.X[nxt],
+                                                                    (T)(2.0 * omega * c1), (T)(omega * c1 * c1),
+                                                                    ru->w, lv.b, S->red, 0);
+    else
+      v_cheb2_zero<DIM, T><<<gbs, lv.st.chunk, 0, s>>>(lv.g, lv.st, st, lv.b, lv.X[nxt], (T)(2.0 * omega * c1),
+                                              (T)(omega * c1 * c1));
     lv.cur = nxt;
     return;
   }
@@ -658,7 +678,8 @@ static void enq_smooth(fishgpu_solver *S, Level<T> &lv, bool from_zero, int dots
 }
 
 template <int DIM, typename T>
-static void enq_vcycle(fishgpu_solver *S, Hier<T> &H, int l, bool from_zero, int dots = -1) {
+static void enq_vcycle(fishgpu_solver *S, Hier<T> &H, int l, bool from_zero, int dots = -1,
+                       const RUpd<T> *ru = nullptr) {
   Level<T> &lv = H.lev[l];
   cudaStream_t s = S->stream;
   KspState *st = S->st;
@@ -687,7 +708,7 @@ static void enq_vcycle(fishgpu_solver *S, Hier<T> &H, int l, bool from_zero, int
     return;
   }
   Level<T> &lc = H.lev[l - 1];
-  enq_smooth<DIM, T>(S, lv, from_zero);
+  enq_smooth<DIM, T>(S, lv, from_zero, -1, ru);
   if (DIM == 3 && !S->batch && S->o.fuse_restrict &&
       launch_resid_restrict<T>(S, lv.g, lc.g, lv.b, lv.X[lv.cur], lc.b, st)) {  // b_c = P^T (b - A x) in one pass
   } else {
@@ -703,7 +724,7 @@ static void enq_vcycle(fishgpu_solver *S, Hier<T> &H, int l, bool from_zero, int
 // Returns true when z.z and z.r were reduced (and Fin(dots) run) by the last
 // smoothing step, false when the caller still has to reduce them.
 template <int DIM, typename T>
-static bool enq_pc(fishgpu_solver *S, Hier<T> &H, const T *r, int dots) {
+static bool enq_pc(fishgpu_solver *S, Hier<T> &H, const T *r, int dots, const RUpd<T> *ru = nullptr) {
   const fishgpu_opts &o = S->o;
   if (o.pc_type == FISHGPU_PC_NONE) {
     v_scale<T><<<slot_blocks(S->sf), S->sf.chunk, 0, S->stream>>>(S->fine, S->sf, S->st, r, T(1), H.zbuf);
@@ -719,7 +740,7 @@ static bool enq_pc(fishgpu_solver *S, Hier<T> &H, const T *r, int dots) {
   Level<T> &top = H.lev[H.nlev - 1];
   top.b = const_cast<T *>(r);
   const bool fused = H.nlev > 1;  // a single level ends with the coarse solve, no smoother
-  enq_vcycle<DIM, T>(S, H, H.nlev - 1, true, fused ? dots : -1);
+  enq_vcycle<DIM, T>(S, H, H.nlev - 1, true, fused ? dots : -1, ru);
   H.z = top.X[top.cur];
   return fused;
 }
@@ -728,7 +749,21 @@ template <typename T>
 struct KspVecs {
   T *r, *p[2], *w, *y;  // p: two buffers, the direction update reads one and writes the other
   double *y64 = nullptr;  // FP32 solves with FP64 accumulation: the outer solution the updates go to
+  T *r2 = nullptr;        // a second residual buffer: the residual update goes into the V-cycle's first
+                          // pass (RUpd), which reads r and writes r_new; iteration i reads r from
+                          // {r, r2}[i & 1] and writes the other
 };
+
+// Whether CG iterations carry their residual update into the V-cycle's first
+// smoothing pass (v_cheb2_zero's RUPD form): the mixed form's FP32 inner
+// solves of a single grid, MG with two Chebyshev/Jacobi steps from zero on
+// the finest level.  Not the FP64 form: forming r - alpha w at every stencil
+// point adds FP64 FMAs to an FP64-bound pass (513^3: 231 -> 241 ms; the mixed
+// form 46.9 -> 46.3 ms).
+static bool fuse_cgr_ok(const fishgpu_opts &o, int batch, int nlev) {
+  return o.fuse_cgr && o.precision == FISHGPU_MIXED && !batch && o.pc_type == FISHGPU_PC_MG && nlev > 1 &&
+         o.smooth_type == FISHGPU_SMOOTH_CHEBYSHEV && o.smooth_its == 2;
+}
 
 // src64 (FP32 solves of the mixed form, unpreconditioned norm): the FP64
 // residual the right-hand side is demoted from, its r.r in dval[0]
@@ -786,7 +821,16 @@ static void enq_cg_iter(fishgpu_solver *S, Hier<T> &H, KspVecs<T> v, int par) {
   if (!planes)
     v_cgp_apply<DIM, T, false><<<slot_blocks(S->sfst), S->sfst.chunk, 0, s>>>(S->fine, S->sfst, st, H.z, pold, pnew, v.w,
                                                                       v.y, S->red, 0);
-  if (S->ksp_norm == FISHGPU_NORM_UNPRECONDITIONED)
+  const bool unprec = S->ksp_norm == FISHGPU_NORM_UNPRECONDITIONED;
+  if (v.r2 && fuse_cgr_ok(S->o, S->batch, H.nlev)) {  // r -= alpha w inside the V-cycle's first pass
+    T *rcur = par ? v.r2 : v.r, *rnext = par ? v.r : v.r2;
+    const RUpd<T> ru{rcur, v.w, unprec};
+    if (!enq_pc<DIM, T>(S, H, rnext, FIN_ZZZR, &ru))
+      v_dots<T><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(S->fine, S->sf, st, H.z, rnext, S->red, 0, FIN_ZZZR,
+                                                           nullptr);
+    return;
+  }
+  if (unprec)
     v_cg_r<T, true><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(S->fine, S->sf, st, v.w, v.r, S->red, 0);
   else
     v_cg_r<T, false><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(S->fine, S->sf, st, v.w, v.r, S->red, 0);
@@ -1165,7 +1209,7 @@ static int solve_dim(fishgpu_solver *S, double *u, fishgpu_report *rep) {
     spectrum(g, &lmin, &lmax);
     const double kappa = lmax / fmax(lmin, 1e-300);
     const bool accurate = inner_accurate_for(o.inner_accurate, o.rtol, o.inner_rtol, kappa);
-    KspVecs<float> v{S->r32, {S->p32, S->q32}, S->w32, S->y32, accurate ? S->y64 : nullptr};
+    KspVecs<float> v{S->r32, {S->p32, S->q32}, S->w32, S->y32, accurate ? S->y64 : nullptr, S->r32b};
     // The first correction is smooth and carries the FP32 rounding of its
     // storage and of the FP32 apply's diagonal term, which J amplifies by up
     // to its condition number: the true residual cannot drop below ~kappa *
@@ -1604,6 +1648,7 @@ extern "C" int fishgpu_solver_create(const fishgpu_opts *o, void *stream, fishgp
     S->o.ctx.f = S->f_own;
     S->o.ctx.g = S->g_own;
   }
+  const bool fuse_r = fuse_cgr_ok(*o, 0, o->pc_type == FISHGPU_PC_MG ? o->mg_levels : 1);
   if (o->precision == FISHGPU_FP64) {
     CK(dalloc(S, &S->p64, N));
     CK(dalloc(S, &S->q64, N));
@@ -1616,6 +1661,7 @@ extern "C" int fishgpu_solver_create(const fishgpu_opts *o, void *stream, fishgp
     CK(dalloc(S, &S->q32, N));
     CK(dalloc(S, &S->w32, N));
     CK(dalloc(S, &S->y32, N));
+    if (fuse_r) CK(dalloc(S, &S->r32b, N));
     CK(build_hier<float>(S, S->h32));
   }
 #undef CK
@@ -1646,6 +1692,7 @@ extern "C" long long fishgpu_solver_estimate_bytes(const fishgpu_opts *o) {
   const int es = o->precision == FISHGPU_MIXED ? 4 : 8;
   if (o->precision == FISHGPU_MIXED) b += rnd(8LL * N) + 5 * rnd(4LL * N);  // b64; r p q w y (FP32)
   else b += 3 * rnd(8LL * N);                                              // p q w
+  if (fuse_cgr_ok(*o, 0, o->pc_type == FISHGPU_PC_MG ? o->mg_levels : 1)) b += rnd((long long)es * N);  // r2
   if (o->pc_type != FISHGPU_PC_MG) return b + rnd((long long)es * N);
   Geom lv = g;
   std::vector<long long> pts(o->mg_levels, 0);  // nodes per level (build_tail's choice below)

@@ -489,13 +489,22 @@ __global__ void __launch_bounds__(256, ((DOTS || HAS_KM1) ? MinBlocks<T>::value 
 // Two Chebyshev steps from a zero iterate in one pass over b:
 //   x1 = c1 b,  x2 = omega x1 + omega c1 (b - A x1) = a0 b - a1 (A b)
 // with a0 = 2 omega c1, a1 = omega c1^2 (c1 = scale/scdiag).
-template <int DIM, typename T>
+// RUPD (the finest level of a CG iteration's V-cycle): b is the CG residual
+// after this iteration's update, r_new = r - alpha w, formed on the fly from
+// r (`b`) and w exactly as v_cg_r forms it and stored to rnew (another
+// buffer: neighbours still read r); RR: r_new.r_new reduced as v_cg_r
+// reduces it (same slots, same order) and finalised as FIN_RR.  Replaces
+// v_cg_r + v_cheb2_zero, bit-identical.
+template <int DIM, typename T, bool RUPD = false, bool RR = false>
 __global__ void __launch_bounds__(256, MinBlocksLean<T>::value) v_cheb2_zero(Geom g, Slots s, KspState *st, const T *__restrict__ b,
-                                                    T *__restrict__ out, T a0, T a1) {
+                                                    T *__restrict__ out, T a0, T a1,
+                                                    const T *__restrict__ wv = nullptr, T *__restrict__ rnew = nullptr,
+                                                    Reducer red = Reducer{}, int slot = 0) {
   st = block_state(st, s);
   if (ksp_done_v(st)) return;
   const SlotPos p = slot_pos_st<DIM>(g, s);
   const Wv<T> w(g);
+  T acc = T(0);
   auto op = [&](int k, long long n, const Nb<T> &nb) {
     const bool jkb = nb.jkb;
     V4<T> o;
@@ -511,8 +520,22 @@ __global__ void __launch_bounds__(256, MinBlocksLean<T>::value) v_cheb2_zero(Geo
       set_el(o, e, v);
     }
     st4(out + n, o);
+    if constexpr (RUPD) {
+      const V4<T> &rn = nb.c;
+      st4(rnew + n, rn);
+      if (RR) acc = fma(rn.x, rn.x, fma(rn.y, rn.y, fma(rn.z, rn.z, fma(rn.w, rn.w, acc))));
+    }
   };
-  march<DIM, T>(g, s, p, b, op);
+  if constexpr (RUPD) {
+    const T a = st ? (T)st->alpha : T(0);  // no state: alpha = 0
+    march_src<DIM, T>(g, s, p, AxpySrc<T>{b, wv, -a}, op);
+    if (RR) {
+      double v1[1] = {(double)acc};
+      reduce_slots<1>(v1, red, slot, st, FIN_RR, nullptr, s);
+    }
+  } else {
+    march<DIM, T>(g, s, p, b, op);
+  }
 }
 
 // r = b - A x; NORM: r.r reduced into *out as v_dots(r, r) reduces it (same

@@ -629,3 +629,28 @@ def test_persistent_solve_is_deterministic_and_reusable(cuda):
         r2 = s.solve(u2)
     assert r1.its == r2.its and r2.launches < 12  # one launch per inner solve, a few around them
     assert torch.equal(u1, u2) and r1.history() == r2.history()
+
+
+@pytest.mark.parametrize("args", [
+    "-fsh_dim 3 -fsh_problem manupoly -da_refine 5 -pc_type mg -ksp_rtol 1e-10 -fsh_precision mixed",
+    "-fsh_dim 3 -fsh_problem manuexp -da_refine 4 -pc_type mg -ksp_rtol 1e-10 -fsh_precision mixed "
+    "-fsh_inner_accurate 0",
+    "-fsh_dim 2 -fsh_problem manupoly -da_grid_x 5 -da_grid_y 3 -da_refine 6 -pc_type mg -ksp_rtol 1e-10 "
+    "-fsh_cy 3 -fsh_precision mixed",
+    "-fsh_dim 3 -fsh_problem manupoly -da_grid_x 3 -da_grid_y 5 -da_grid_z 9 -da_refine 3 -pc_type mg "
+    "-pc_mg_cycle_type w -ksp_rtol 1e-10 -fsh_precision mixed -fsh_inner_accurate 1",
+    "-fsh_dim 1 -fsh_problem manupoly -da_refine 8 -pc_type mg -ksp_rtol 1e-10 -fsh_precision mixed",
+])
+def test_fused_residual_update_is_bit_identical(cuda, args):
+    """r -= alpha w carried into the V-cycle's first smoothing pass (the
+    residual formed on the fly as v_cg_r forms it, r.r reduced over the same
+    slots in the same order): the solve is identical, bit for bit, to the
+    separate update, with one launch fewer per iteration."""
+    import torch
+    fg = fgmod()
+    u1, a = fg.solve(fg.options(args + " -fsh_fuse_cgr 1 -fsh_persist 0"))
+    u0, b = fg.solve(fg.options(args + " -fsh_fuse_cgr 0 -fsh_persist 0"))
+    assert a.reason == b.reason == 2 and a.its == b.its and a.outer_its == b.outer_its
+    assert a.history() == b.history()
+    assert torch.equal(u1, u0)
+    assert a.launches < b.launches
