@@ -533,21 +533,42 @@ struct BiCoarse {
   float dinv;
 };
 
+// vsm_off >= 0: the ten work vectors (and the preconditioner's output z)
+// live in the dynamic shared memory from that offset for the whole solve,
+// so every phase waits on shared memory instead of an L2 round trip; x is
+// copied out at the end (the only vector the Newton step reads).  The
+// coarse solve's tables are staged in shared memory once per launch.
 __global__ void __launch_bounds__(1024) k_bi_block(Geom g, int model, float a, float b, const float4 *__restrict__ C1,
                                                    const float4 *__restrict__ C2, const float *__restrict__ bv,
-                                                   float *__restrict__ r, float *__restrict__ rh, float *__restrict__ p,
-                                                   float *__restrict__ v, float *__restrict__ s, float *__restrict__ t,
-                                                   float *__restrict__ x, float *__restrict__ ph, float *__restrict__ sh,
-                                                   MsKsp *st, BiCoarse pc, int use_pc, int max_iters) {
+                                                   float *r, float *rh, float *p, float *v, float *s, float *t,
+                                                   float *x_out, float *ph, float *sh, MsKsp *st, BiCoarse pc,
+                                                   int use_pc, int max_iters, int vsm_off) {
   extern __shared__ __align__(16) unsigned char bi_sm[];
   const int tid = threadIdx.x, nt = blockDim.x;
   const int N = g.pitch * g.my;  // every element of the padded grid, as the node kernels cover it
+  float *x = x_out, *zc = pc.z;
+  if (vsm_off >= 0) {
+    float *q0 = reinterpret_cast<float *>(bi_sm + vsm_off);
+    r = q0;
+    rh = q0 + N;
+    p = q0 + 2 * N;
+    v = q0 + 3 * N;
+    s = q0 + 4 * N;
+    t = q0 + 5 * N;
+    x = q0 + 6 * N;
+    ph = q0 + 7 * N;
+    sh = q0 + 8 * N;
+    zc = q0 + 9 * N;
+    for (int q = tid; q < N; q += nt) zc[q] = 0.f;  // the coarse solve writes z's interior and boundary nodes
+  }
+  if (use_pc && pc.smem) coarse_stage<2, float>(pc.S0, pc.S1, pc.S1, pc.ilam, pc.n0, pc.n1, 1, bi_sm);
+  __syncthreads();
   auto done = [&]() { return *(volatile int *)&st->k.done != 0; };
   // z = M in into out (k_bi_pcout): the Poisson solve inside, `in` elsewhere
   auto precondition = [&](const float *in, float *out) {
-    if (use_pc) {
-      coarse_solve_block<2, float>(pc.g, in, pc.z, pc.S0, pc.S1, pc.S1, pc.ilam, pc.work, pc.n0, pc.n1, 1,
-                                   pc.smem, pc.dinv, bi_sm);
+    if (use_pc) {  // smem 2: the tables were staged at the start
+      coarse_solve_block<2, float>(pc.g, in, zc, pc.S0, pc.S1, pc.S1, pc.ilam, pc.work, pc.n0, pc.n1, 1,
+                                   pc.smem ? 2 : 0, pc.dinv, bi_sm);
       __syncthreads();
     }
     for (int q = tid; q < N; q += nt) {
@@ -556,7 +577,7 @@ __global__ void __launch_bounds__(1024) k_bi_block(Geom g, int model, float a, f
       bool use_z;
       if (model == FISHGPU_NL_OBSTACLE) use_z = node && use_pc && C1[q].x == 0.f;
       else use_z = node && use_pc && !ms_bdry(g, i, j);
-      out[q] = use_z ? pc.z[q] : in[q];
+      out[q] = use_z ? zc[q] : in[q];
     }
     __syncthreads();
   };
@@ -631,6 +652,10 @@ __global__ void __launch_bounds__(1024) k_bi_block(Geom g, int model, float a, f
       if (tid == 0) XrFin{st}(acc);
       __syncthreads();
     }
+  }
+  if (vsm_off >= 0) {  // the Newton step reads x
+    __syncthreads();
+    for (int q = tid; q < N; q += nt) x_out[q] = x[q];
   }
 }
 
@@ -860,6 +885,8 @@ struct MsLevel {
   BiCoarse bc{};
   int use_pc = 0;
   int max_iters = 0;
+  size_t bsm = 0;    // its dynamic shared memory
+  int vsm_off = -1;  // offset of its vectors there (-1: in global memory)
 };
 
 }  // namespace
@@ -1025,9 +1052,8 @@ static int newton(fishgpu_ms_solver *S, MsLevel &L, int k, fishgpu_ms_report *re
     int kits = 0, kreason = 0;
     if (L.block1) {
       const float ja = (float)(g.h[1] / g.h[0]), jb = (float)(g.h[0] / g.h[1]);
-      k_bi_block<<<1, 1024, L.use_pc ? (size_t)L.bc.smem : 0, s>>>(
-          g, S->P.model, ja, jb, L.C1, L.C2, L.b, L.r, L.rh, L.p, L.v, L.s, L.t, L.x, L.ph, L.sh, S->st, L.bc,
-          L.use_pc, L.max_iters);
+      k_bi_block<<<1, 1024, L.bsm, s>>>(g, S->P.model, ja, jb, L.C1, L.C2, L.b, L.r, L.rh, L.p, L.v, L.s, L.t,
+                                        L.x, L.ph, L.sh, S->st, L.bc, L.use_pc, L.max_iters, L.vsm_off);
       MS_CK(cudaGetLastError());
       MS_CK(cudaMemcpyAsync(S->st_h, S->st, sizeof(MsKsp), cudaMemcpyDeviceToHost, s));
       MS_CK(cudaStreamSynchronize(s));
@@ -1392,6 +1418,17 @@ extern "C" int fishgpu_ms_solver_create(const fishgpu_ms_opts *o, void *stream, 
         const long long cap =
             o->loop_cap > 0 ? o->loop_cap : (long long)std::max(1, o->ksp_max_it) / L.giters + 5;
         L.max_iters = (int)std::min<long long>(cap * L.giters, 1 << 30);
+        // the work vectors in shared memory when they fit beside the coarse solve's tables
+        const size_t coarse = L.use_pc ? (size_t)L.bc.smem : 0;
+        const size_t off = (coarse + 15) / 16 * 16;
+        const size_t need = off + 10 * sizeof(float) * (size_t)L.g.pitch * L.g.my;
+        L.bsm = coarse;
+        if (need <= 200 * 1024 &&
+            cudaFuncSetAttribute(k_bi_block, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need) == cudaSuccess) {
+          L.bsm = need;
+          L.vsm_off = (int)off;
+        }
+        cudaGetLastError();
       }
     }
     if (S->P.model != FISHGPU_NL_OBSTACLE) {
