@@ -146,6 +146,7 @@ static bool pick(fishgpu_server_s *S, Job *job) {
       for (size_t qk = qi + 1; qk < S->queue.size() && (int)at.size() < S->o.batch_max; qk++) {
         const Req &o = S->reqs[S->queue[qk]];
         if (o.dim == 2 && o.n == r.n) at.push_back(qk);
+        else if (S->o.fifo) break;  // strict order: only the run of equal requests behind this one
       }
       int c = 1;
       while (c < (int)at.size()) c *= 2;
