@@ -533,6 +533,54 @@ struct BiCoarse {
   float dinv;
 };
 
+// Compensated FP32 dot products for the one-block BiCGStab (Ogita, Rump and
+// Oishi, "Accurate sum and dot product", 2005: TwoProduct by FMA, Knuth's
+// TwoSum): each partial is a pair (s, c) whose sum carries about twice the
+// FP32 precision, close to the FP64 accumulation it replaces.  On one SM an
+// FP64 warp instruction takes ~17 issue cycles, so the FP64 accumulation and
+// shuffle tree cost microseconds per dot product (ncu: FP64 pipe 31% busy);
+// plain FP32 sums instead cost the obstacle problem 4% more inner
+// iterations.  The _rn intrinsics keep the compiler from contracting the
+// error terms into FMAs.
+__device__ __forceinline__ void two_sum_acc(float &s, float &c, float x) {
+  const float t = __fadd_rn(s, x);
+  const float bp = __fsub_rn(t, s);
+  c = __fadd_rn(c, __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(x, bp)));
+  s = t;
+}
+__device__ __forceinline__ void dot2_acc(float &s, float &c, float a, float b) {
+  const float p = __fmul_rn(a, b);
+  two_sum_acc(s, c, p);
+  c = __fadd_rn(c, fmaf(a, b, -p));
+}
+
+// Block sum of the pairs: the warp tree combines pairs (TwoSum), each warp's
+// s + c enters FP64, the warps are summed in FP64 in warp order
+// (deterministic); the result in thread 0.
+template <int NV>
+__device__ __forceinline__ void bi_block_sum(float (&s)[NV], float (&c)[NV], double (&out)[NV]) {
+  __shared__ double red_f[NV][32];
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+    for (int q = 0; q < NV; q++) {
+      const float s2 = __shfl_down_sync(0xffffffffu, s[q], o), c2 = __shfl_down_sync(0xffffffffu, c[q], o);
+      two_sum_acc(s[q], c[q], s2);
+      c[q] = __fadd_rn(c[q], c2);
+    }
+  if (lane == 0)
+#pragma unroll
+    for (int q = 0; q < NV; q++) red_f[q][wid] = (double)s[q] + (double)c[q];
+  __syncthreads();
+  if (wid == 0) {
+#pragma unroll
+    for (int q = 0; q < NV; q++) out[q] = lane < nw ? red_f[q][lane] : 0.0;
+    warp_sum<NV>(out);
+  }
+  __syncthreads();
+}
+
 // vsm_off >= 0: the ten work vectors (and the preconditioner's output z)
 // live in the dynamic shared memory from that offset for the whole solve,
 // so every phase waits on shared memory instead of an L2 round trip; x is
@@ -582,7 +630,8 @@ __global__ void __launch_bounds__(1024) k_bi_block(Geom g, int model, float a, f
     __syncthreads();
   };
   {  // k_bi_init: r = b, rhat = b, x = p = v = 0; rho = b.b
-    double acc[1] = {0.0};
+    float as[1] = {0.f}, ac[1] = {0.f};
+    double acc[1];
     for (int q = tid; q < N; q += nt) {
       const float bb = bv[q];
       r[q] = bb;
@@ -590,9 +639,9 @@ __global__ void __launch_bounds__(1024) k_bi_block(Geom g, int model, float a, f
       x[q] = 0.f;
       p[q] = 0.f;
       v[q] = 0.f;
-      acc[0] += (double)bb * bb;
+      dot2_acc(as[0], ac[0], bb, bb);
     }
-    block_sum<1>(acc);
+    bi_block_sum<1>(as, ac, acc);
     if (tid == 0) InitFin{st}(acc);
     __syncthreads();
   }
@@ -607,14 +656,15 @@ __global__ void __launch_bounds__(1024) k_bi_block(Geom g, int model, float a, f
     }
     precondition(p, ph);
     {  // k_bi_jv1: v = J ph, rhat.v -> alpha
-      double acc[1] = {0.0};
+      float as[1] = {0.f}, ac[1] = {0.f};
+      double acc[1];
       for (int q = tid; q < N; q += nt) {
         const int i = q % g.pitch, j = q / g.pitch;
         const float o = i < g.mx ? ms_jv_node(g, model, i, j, q, a, b, C1, C2, ph) : 0.f;
         v[q] = o;
-        acc[0] += (double)rh[q] * o;
+        dot2_acc(as[0], ac[0], rh[q], o);
       }
-      block_sum<1>(acc);
+      bi_block_sum<1>(as, ac, acc);
       if (tid == 0) AlphaFin{st}(acc);
       __syncthreads();
     }
@@ -626,29 +676,31 @@ __global__ void __launch_bounds__(1024) k_bi_block(Geom g, int model, float a, f
     }
     precondition(s, sh);
     {  // k_bi_jv2: t = J sh; t.s, t.t -> omega
-      double acc[2] = {0.0, 0.0};
+      float as[2] = {0.f, 0.f}, ac[2] = {0.f, 0.f};
+      double acc[2];
       for (int q = tid; q < N; q += nt) {
         const int i = q % g.pitch, j = q / g.pitch;
         const float o = i < g.mx ? ms_jv_node(g, model, i, j, q, a, b, C1, C2, sh) : 0.f;
         t[q] = o;
-        acc[0] += (double)o * s[q];
-        acc[1] += (double)o * o;
+        dot2_acc(as[0], ac[0], o, s[q]);
+        dot2_acc(as[1], ac[1], o, o);
       }
-      block_sum<2>(acc);
+      bi_block_sum<2>(as, ac, acc);
       if (tid == 0) OmegaFin{st}(acc);
       __syncthreads();
     }
     {  // k_bi_xr: x += alpha ph + omega sh; r = s - omega t; r.r, rhat.r
       const float al = (float)*(volatile double *)&st->alpha, om = (float)*(volatile double *)&st->omega;
-      double acc[2] = {0.0, 0.0};
+      float as[2] = {0.f, 0.f}, ac[2] = {0.f, 0.f};
+      double acc[2];
       for (int q = tid; q < N; q += nt) {
         x[q] = fmaf(om, sh[q], fmaf(al, ph[q], x[q]));
         const float rn = fmaf(-om, t[q], s[q]);
         r[q] = rn;
-        acc[0] += (double)rn * rn;
-        acc[1] += (double)rh[q] * rn;
+        dot2_acc(as[0], ac[0], rn, rn);
+        dot2_acc(as[1], ac[1], rh[q], rn);
       }
-      block_sum<2>(acc);
+      bi_block_sum<2>(as, ac, acc);
       if (tid == 0) XrFin{st}(acc);
       __syncthreads();
     }
