@@ -393,7 +393,7 @@ def run_ours(args):
     kms, kbytes = s_mx.time_kernel(rk, 20)
     kernel_table = {}
     for name in ("smooth", "smooth_first", "smooth_dots", "smooth_zero", "cgp_apply", "cgp_apply_acc", "cg_update",
-                 "resid", "restrict", "resid_restrict", "prolong", "residual64"):
+                 "resid", "restrict", "resid_restrict", "prolong", "demote", "residual64"):
         try:
             t, b = s_mx.time_kernel(name, 10)
         except fg.FishError:

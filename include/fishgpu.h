@@ -292,7 +292,7 @@ int fishgpu_solve_host(const fishgpu_opts *o, const double *f_host, const double
    "smooth", "smooth_first", "smooth_dots", "smooth_zero", "post2", "cgp_apply",
    "cgp_apply_acc" (mixed form: the accurate inner form's apply), "cgp_apply_tma" (the same from the
    TMA ring, 3D), "cg_update", "resid_restrict" (3D), "grid_sync" (one grid-wide barrier of the
-   persistent solve; bytes 0),
+   persistent solve; bytes 0), "demote" (mixed form: an inner solve's set-up from the FP64 residual),
    "resid", "apply", "restrict", "prolong", "residual64".  Reports the mean ms
    per launch and the algorithmic bytes one launch moves. */
 int fishgpu_solver_time_kernel(fishgpu_solver *s, const char *name, int reps,

@@ -22,7 +22,7 @@ LIB = os.path.join(LIBDIR, "libfishgpu.so")
 
 SOURCES = ["common.cu", "callbacks.cu", "solver.cu", "noalloc.cu", "server.cu", "msurf.cu", "petscbin.cu"]
 HEADERS = ["fishgpu_internal.cuh", "kernels.cuh", "common.cuh", "vkernels.cuh", "mg_hooks.cuh", "graph_loop.cuh",
-           "tma.cuh", "vblock.cuh"]
+           "tma.cuh", "vblock.cuh", "bitconv.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

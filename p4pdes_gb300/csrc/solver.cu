@@ -1326,7 +1326,7 @@ static int time_kernel_dim(fishgpu_solver *S, const char *name, int reps, double
   // (beta/betaold = 1, a small alpha); p.w > 0 keeps it running, and a stop
   // (non-finite data) is reported
   KspState *tst = nullptr;
-  if (!strncmp(name, "cgp_apply", 9) || !strcmp(name, "cg_update")) {
+  if (!strncmp(name, "cgp_apply", 9) || !strcmp(name, "cg_update") || !strcmp(name, "demote")) {
     KspState h;
     memset(&h, 0, sizeof(h));
     h.i = 2;  // a direction update that also reads y (the first one, i = 1, starts y from 0)
@@ -1433,6 +1433,10 @@ static int time_kernel_dim(fishgpu_solver *S, const char *name, int reps, double
       else
         v_cg_r<double, false><<<gb, sl.chunk, 0, s>>>(g, sl, tst, S->w64, S->r64, S->red, 1);
       *bytes = 3.0 * sz * N;
+    } else if (!strcmp(name, "demote")) {  // an inner solve's set-up: r32 = r64 / ||r64||, r32.r32
+      if (!mixed) return FISHGPU_ERR_UNSUPPORTED;
+      v_demote_init<<<gb, sl.chunk, 0, s>>>(g, sl, tst, S->r64, S->dval, S->r32, S->red, 1);
+      *bytes = (8.0 + 4.0) * N;
     } else if (!strcmp(name, "restrict")) {
       if (mixed)
         v_restrict<DIM, float><<<slot_blocks(cf.sl), cf.sl.chunk, 0, s>>>(g, cf.g, cf.sl, nullptr, lf.X[0], cf.b);

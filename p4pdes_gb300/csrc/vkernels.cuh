@@ -18,6 +18,7 @@
 // with the rows j-1, j, j+1 in registers (march_rows).
 #pragma once
 
+#include "bitconv.cuh"
 #include "fishgpu_internal.cuh"
 #include "tma.cuh"
 
@@ -612,15 +613,7 @@ __global__ void __launch_bounds__(256, MinBlocks<T>::value) v_apply_dot(Geom g, 
 // solution, y64 += (yscale * alpha) p_old (the state's yscale and yfresh), so
 // that neither the apply nor the FP32 storage of the correction limits the
 // true residual an inner solve reaches to ~kappa * 2^-24.
-// float -> double by integer operations, exact: the same value as (double)f.
-// On this part the conversion instruction runs on the FP64 pipe (1/64 of the
-// FP32 rate) beside the FP64 FMAs; normal numbers need only a rebased
-// exponent and a shifted mantissa (the integer pipe), the rest take the branch.
-__device__ __forceinline__ double f2d_bits(float f) {
-  const unsigned u = __float_as_uint(f), a = u & 0x7FFFFFFFu;
-  if (a - 0x00800000u >= 0x7F000000u) return a == 0u ? __hiloint2double((int)(u & 0x80000000u), 0) : (double)f;
-  return __hiloint2double((int)(((a >> 3) + (896u << 20)) | (u & 0x80000000u)), (int)(u << 29));
-}
+// float -> double on the integer pipe (bitconv.cuh: the cast's value)
 template <typename YT, typename T>
 __device__ __forceinline__ YT to_y(T v) {
   if constexpr (sizeof(YT) == 8 && sizeof(T) == 4) return f2d_bits(v);
