@@ -772,7 +772,8 @@ static void enq_cg_init(fishgpu_solver *S, Hier<T> &H, KspVecs<T> v, const doubl
   cudaStream_t s = S->stream;
   if constexpr (sizeof(T) == 4) {
     if (src64) {
-      v_demote_init<<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(S->fine, S->sf, S->st, src64, S->dval, v.r, S->red,
+      k_inv_norm<<<1, 1, 0, s>>>(S->dval, S->dval + 6);
+      v_demote_init<<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(S->fine, S->sf, S->st, src64, S->dval + 6, v.r, S->red,
                                                                0);
       if (!enq_pc<DIM, T>(S, H, v.r, FIN_INIT_ZZZR))
         v_dots<T><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(S->fine, S->sf, S->st, H.z, v.r, S->red, 0, FIN_INIT_ZZZR,
@@ -1435,7 +1436,8 @@ static int time_kernel_dim(fishgpu_solver *S, const char *name, int reps, double
       *bytes = 3.0 * sz * N;
     } else if (!strcmp(name, "demote")) {  // an inner solve's set-up: r32 = r64 / ||r64||, r32.r32
       if (!mixed) return FISHGPU_ERR_UNSUPPORTED;
-      v_demote_init<<<gb, sl.chunk, 0, s>>>(g, sl, tst, S->r64, S->dval, S->r32, S->red, 1);
+      if (q == 0) k_inv_norm<<<1, 1, 0, s>>>(S->dval, S->dval + 6);
+      v_demote_init<<<gb, sl.chunk, 0, s>>>(g, sl, tst, S->r64, S->dval + 6, S->r32, S->red, 1);
       *bytes = (8.0 + 4.0) * N;
     } else if (!strcmp(name, "restrict")) {
       if (mixed)

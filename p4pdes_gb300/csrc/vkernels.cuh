@@ -1433,21 +1433,21 @@ __global__ void __launch_bounds__(256) v_resid_zero0(Geom g, Slots s, const doub
   reduce_slots<1>(v1, red, slot, nullptr, FIN_STORE, out, s);
 }
 
+// is[0] = 1 / sqrt(rr[0]) (one thread: the FP64 square root and division
+// once per inner solve instead of once per block of v_demote_init)
+static __global__ void k_inv_norm(const double *__restrict__ rr, double *__restrict__ is) { *is = 1.0 / sqrt(*rr); }
+
 // The set-up of an inner FP32 solve from an FP64 residual in one pass:
-// r32 = (float)(r64 * (1 / sqrt(rr))) with rr = r64.r64 as stored by the
-// residual kernel (the host's 1.0 / ||r|| to the bit: sqrt and the division
-// are correctly rounded) and r32.r32 reduced as v_dots<float> reduces it,
-// finalised as FIN_INIT_RR.  Replaces v_demote and v_dots (y32 is not
-// zero-filled: see v_cg_pend).
+// r32 = (float)(r64 * is) with is = 1 / sqrt(rr), rr = r64.r64 as stored by
+// the residual kernel (k_inv_norm: the host's 1.0 / ||r|| to the bit, sqrt
+// and the division are correctly rounded) and r32.r32 reduced as
+// v_dots<float> reduces it, finalised as FIN_INIT_RR.  Replaces v_demote and
+// v_dots (y32 is not zero-filled: see v_cg_pend).
 static __global__ void __launch_bounds__(256) v_demote_init(Geom g, Slots s, KspState *st, const double *__restrict__ r,
-                                                     const double *__restrict__ rr, float *__restrict__ r32,
+                                                     const double *__restrict__ isp, float *__restrict__ r32,
                                                      Reducer red, int slot) {
   if (ksp_done_v(st)) return;
-  // one sqrt and division per block (FP64 is slow on this part), shared
-  __shared__ double s_is;
-  if (threadIdx.x == 0) s_is = 1.0 / sqrt(*rr);
-  __syncthreads();
-  const double is = s_is;
+  const double is = *isp;
   float zz = 0.f;
   FG_PW_BEGIN
   const V4<double> a = ld4(r + n);
