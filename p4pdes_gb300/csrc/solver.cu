@@ -347,13 +347,15 @@ static int build_tail(fishgpu_solver *S, Hier<T> &H) {
 // Whether a solve's CG loop runs as one persistent launch (k_ksp_persist):
 // CG + MG with two Chebyshev/Jacobi steps, V-cycles, a 2D or 3D single grid,
 // the device loop, and (default) a finest grid of at most persist_points
-// nodes (by default 2.5e6 in FP64, 1.5e5 in FP32).  The levels of at most persist_tail nodes run in block 0 between
-// two grid barriers (*btop: the largest of them, >= 1): one SM's FP64 rate
-// is 1/152 of the GPU's, so in FP64 only the smallest levels stay there.
-// pts: nodes per level (0 .. nlev-1); psmem: the coarse solve's dynamic
-// shared memory.  Returns the blocks of the launch (one of 512 threads per
-// SM at most, fewer for fewer fine points), 0 for no persistent solve; *nsm:
-// the device's SMs (the partial sums' capacity).
+// nodes (by default 2.5e6 in FP64, 1.5e5 in FP32).  The levels of at most
+// persist_tail nodes run in block 0 between two grid barriers (*btop: the
+// largest of them, >= 1): one SM's FP64 rate is 1/152 of the GPU's, so in
+// FP64 only the smallest levels stay there.  pts: nodes per level
+// (0 .. nlev-1); cn: the coarsest level's interior sizes.  Returns the
+// blocks of the launch (one of 512 threads per SM at most, fewer for fewer
+// fine points), 0 for no persistent solve; *nsm: the device's SMs (the
+// partial sums' capacity); *coarse, *copy_off, *psmem: the dynamic shared
+// memory plan (tail_smem_plan) for block 0's tail.
 template <typename T>
 static int persist_shape(const fishgpu_opts &o, int dim, bool batch, int nlev, const long long *pts, const int *cn,
                          int *btop, int *nsm, size_t *coarse, int *copy_off, size_t *psmem) {
