@@ -654,3 +654,35 @@ def test_fused_residual_update_is_bit_identical(cuda, args):
     assert a.history() == b.history()
     assert torch.equal(u1, u0)
     assert a.launches < b.launches
+
+
+def test_persistent_solves_on_concurrent_streams(cuda):
+    """Two persistent solves launched on two streams at once (cooperative
+    launches that each want every SM): both complete with the results of the
+    same solves run alone."""
+    import threading
+    import torch
+    fg = fgmod()
+    args = [PERSIST_CASES[0] + " -fsh_persist 1", PERSIST_CASES[3] + " -fsh_persist 1"]
+    alone = [fg.solve(fg.options(a)) for a in args]
+    streams = [torch.cuda.Stream(device=cuda) for _ in args]
+    opts = [fg.options(a) for a in args]
+    solvers = [fg.Solver(o, stream=st.cuda_stream) for o, st in zip(opts, streams)]
+    us = [torch.empty(o.shape, dtype=torch.float64, device=cuda) for o in opts]
+    reps = [None, None]
+
+    def run(q):
+        for _ in range(3):
+            reps[q] = solvers[q].solve(us[q])
+
+    th = [threading.Thread(target=run, args=(q,)) for q in range(2)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    torch.cuda.synchronize()
+    for q in range(2):
+        ua, ra = alone[q]
+        assert reps[q].reason == ra.reason == 2 and reps[q].its == ra.its
+        assert torch.equal(us[q], ua)
+        solvers[q].close()
