@@ -180,6 +180,8 @@ struct fishgpu_solver_s {
   unsigned *pbar = nullptr;
   double *ppart = nullptr;
   int pblocks = 0;
+  // the mixed solve in one launch (k_mixed_persist): its report, device and pinned host
+  fg::MixedOut *mout = nullptr, *mout_h = nullptr;
 };
 
 namespace fg {
@@ -382,16 +384,26 @@ static int persist_shape(const fishgpu_opts &o, int dim, bool batch, int nlev, c
     return 0;
   }
   tail_smem_plan(dim, cn, sizeof(T), *btop, pts, coarse, copy_off, psmem);
-  const void *fns[2] = {dim == 2 ? (const void *)k_ksp_persist<2, T, false> : (const void *)k_ksp_persist<3, T, false>,
-                        dim == 2 ? (const void *)k_ksp_persist<2, T, true> : (const void *)k_ksp_persist<3, T, true>};
-  if (!allow_smem(fns[0], *psmem) || (sizeof(T) == 4 && !allow_smem(fns[1], *psmem))) {
+  // every kernel that may run the plan: the CG solve, and in FP32 its accurate
+  // form and the whole mixed solve in both forms
+  std::vector<const void *> fns{dim == 2 ? (const void *)k_ksp_persist<2, T, false>
+                                         : (const void *)k_ksp_persist<3, T, false>};
+  if constexpr (sizeof(T) == 4) {
+    fns.push_back(dim == 2 ? (const void *)k_ksp_persist<2, T, true> : (const void *)k_ksp_persist<3, T, true>);
+    fns.push_back(dim == 2 ? (const void *)k_mixed_persist<2, true> : (const void *)k_mixed_persist<3, true>);
+    fns.push_back(dim == 2 ? (const void *)k_mixed_persist<2, false> : (const void *)k_mixed_persist<3, false>);
+  }
+  bool ok = true;
+  for (const void *fn : fns) ok = ok && allow_smem(fn, *psmem);
+  if (!ok) {
     *copy_off = -1;
     *psmem = *coarse;
   }
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fns[0], 512, *psmem) != cudaSuccess || per_sm < 1) {
-    cudaGetLastError();
-    return 0;
-  }
+  for (const void *fn : fns)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 512, *psmem) != cudaSuccess || per_sm < 1) {
+      cudaGetLastError();
+      return 0;
+    }
   int blocks = (int)std::max<long long>(1, std::min<long long>(*nsm, (fine_pts + 511) / 512));
   return blocks;
 }
@@ -415,6 +427,10 @@ static int build_persist(fishgpu_solver *S, Hier<T> &H) {
       cudaSuccess)
     return FISHGPU_ERR_CUDA;
   if (!S->pbar && ((rc = dalloc(S, &S->pbar, 2)) || (rc = dalloc(S, &S->ppart, (size_t)4 * nsm)))) return rc;
+  if (sizeof(T) == 4 && S->o.precision == FISHGPU_MIXED && !S->mout) {  // the whole mixed solve in one launch
+    if ((rc = dalloc(S, &S->mout, 1))) return rc;
+    if (cudaMallocHost((void **)&S->mout_h, sizeof(MixedOut)) != cudaSuccess) return FISHGPU_ERR_NOMEM;
+  }
   H.pbtop = btop;
   H.psmem = psmem;
   H.pcoarse = coarse;
@@ -895,7 +911,7 @@ static void reset_state(fishgpu_solver *S, double rtol, double atol, double dtol
 // run_ksp as one cooperative launch of k_ksp_persist (build_persist chose it)
 template <int DIM, typename T>
 static int run_ksp_persist(fishgpu_solver *S, Hier<T> &H, KspVecs<T> v, double rtol, int max_it, int from64,
-                           double yscale, bool yfresh) {
+                           double yscale, bool yfresh, bool read_back = true) {
   cudaStream_t s = S->stream;
   reset_state(S, rtol, S->o.atol, S->o.dtol, max_it, S->ksp_norm, yscale, yfresh);
   FG_CUDA(cudaMemcpyAsync(S->st, S->st_h, sizeof(KspState), cudaMemcpyHostToDevice, s));
@@ -942,6 +958,7 @@ static int run_ksp_persist(fishgpu_solver *S, Hier<T> &H, KspVecs<T> v, double r
   }
   FG_CUDA(cudaLaunchCooperativeKernel(fn, dim3(S->pblocks), dim3(512), args, H.psmem, s));
   S->launches += 1;
+  if (!read_back) return FISHGPU_OK;  // the caller reads the state and the fault word
   FG_CUDA(cudaMemcpyAsync(S->st_h, S->st, sizeof(KspState), cudaMemcpyDeviceToHost, s));
   FG_CUDA(cudaMemcpyAsync(S->hval + 7, S->fault, sizeof(int), cudaMemcpyDeviceToHost, s));
   FG_CUDA(cudaStreamSynchronize(s));
@@ -1155,6 +1172,152 @@ static void fill_from_state(const KspState *h, fishgpu_report *rep) {
   for (int q = 0; q < n; q++) rep->hist[q] = h->hist[q];
 }
 
+// The mixed form's refinement loop as one launch (k_mixed_persist): the
+// right-hand side b64 and its b.b (dval[0]) are on the device already; the
+// report comes back in one read at the end.
+// The FP64 form's solve as one persistent launch followed by the unpacking
+// and F(u), with ONE read of the results at the end (the initial norm, the
+// KSP state, F(u)'s norm and the fault word), instead of a host round trip
+// before and after the KSP.
+template <int DIM>
+static int solve_fp64_persist(fishgpu_solver *S, double *u, fishgpu_report *rep) {
+  const fishgpu_opts &o = S->o;
+  cudaStream_t s = S->stream;
+  const Geom &g = S->fine;
+  const Launch &L = S->Lf;
+  KspVecs<double> v{S->r64, {S->p64, S->q64}, S->w64, S->y64};
+  int rc = run_ksp_persist<DIM, double>(S, S->h64, v, o.rtol, o.max_it, -1, 0.0, false, false);
+  if (rc) return rc;
+  k_unpack_add64<DIM><<<L.grid, L.block, 0, s>>>(g, S->dense, L.tm, S->u64, S->y64, u, true);
+  // F(u) for the final SNES norm (r64 is free now)
+  v_resid<DIM, double, true><<<slot_blocks(S->sf), S->sf.chunk, 0, s>>>(g, S->sf, nullptr, S->beff, S->u64, S->r64,
+                                                                       S->red, 1, S->dval + 1);
+  S->launches += 2;
+  FG_CUDA(cudaEventRecord(S->ev1, s));
+  FG_CUDA(cudaGetLastError());
+  FG_CUDA(cudaMemcpyAsync(S->st_h, S->st, sizeof(KspState), cudaMemcpyDeviceToHost, s));
+  FG_CUDA(cudaMemcpyAsync(S->hval, S->dval, sizeof(double) * 2, cudaMemcpyDeviceToHost, s));
+  FG_CUDA(cudaMemcpyAsync(S->hval + 7, S->fault, sizeof(int), cudaMemcpyDeviceToHost, s));
+  FG_CUDA(cudaStreamSynchronize(s));
+  int fault = 0;
+  memcpy(&fault, S->hval + 7, sizeof(int));
+  if (fault || !S->st_h->done) {  // a barrier gave up, or the iteration cap ran out
+    if (fault) {
+      FG_CUDA(cudaMemsetAsync(S->fault, 0, sizeof(int), s));
+      FG_CUDA(cudaStreamSynchronize(s));
+    }
+    return FISHGPU_ERR_TIMEOUT;
+  }
+  const double bn = sqrt(S->hval[0]);
+  rep->fnorm0 = bn;
+  fill_from_state(S->st_h, rep);
+  rep->outer_its = 0;
+  rep->fnorm1 = sqrt(S->hval[1]);
+  rep->true_rel_resid = bn > 0.0 ? rep->fnorm1 / bn : 0.0;
+  float ms = 0.f;
+  FG_CUDA(cudaEventElapsedTime(&ms, S->ev0, S->ev1));
+  rep->solve_ms = ms;
+  return FISHGPU_OK;
+}
+
+template <int DIM>
+static int solve_mixed_persist(fishgpu_solver *S, double *u, fishgpu_report *rep) {
+  const fishgpu_opts &o = S->o;
+  cudaStream_t s = S->stream;
+  const Geom &g = S->fine;
+  const Launch &L = S->Lf;
+  Hier<float> &H = S->h32;
+  double lmin, lmax;
+  spectrum(g, &lmin, &lmax);
+  const double kappa = lmax / fmax(lmin, 1e-300);
+  const bool accurate = inner_accurate_for(o.inner_accurate, o.rtol, o.inner_rtol, kappa);
+  int mmax = g.mx;
+  if (g.dim >= 2) mmax = std::max(mmax, g.my);
+  if (g.dim >= 3) mmax = std::max(mmax, g.mz);
+  // the first step's floor, as in solve_dim
+  const double first_floor = accurate ? fmin(0.5, o.first_floor_scale * kappa * (M_PI / (mmax - 1)) * 0x1.0p-24)
+                                      : fmin(0.5, 0.3 * kappa * 0x1.0p-24);
+  PersistArgs<float> a;
+  memset(&a, 0, sizeof(a));
+  a.lv = H.plev;
+  a.top = H.nlev - 1;
+  a.btop = H.pbtop;
+  a.r = S->r32;
+  a.p[0] = S->p32;
+  a.p[1] = S->q32;
+  a.w = S->w32;
+  a.y = S->y32;
+  a.y64 = accurate ? S->y64 : nullptr;
+  a.unprec = 1;
+  a.do_pend = 0;
+  a.max_iters = o.loop_cap > 0 ? o.loop_cap * S->giters : o.inner_max_it + 8;
+  a.st = S->st;
+  a.part = S->ppart;
+  a.bar = S->pbar;
+  a.fault = S->fault;
+  const Level<float> &c = H.lev[0];
+  a.S0 = c.S[0];
+  a.S1 = c.S[1];
+  a.S2 = c.S[2];
+  a.ilam = c.ilam;
+  a.work = c.work;
+  a.n0 = c.n[0];
+  a.n1 = c.n[1];
+  a.n2 = c.n[2];
+  a.smem = H.pcoarse ? 1 : 0;
+  a.dinv = (float)(1.0 / c.g.scdiag);
+  a.copy_off = H.pcopy;
+  MixedArgs m;
+  m.b64 = S->b64;
+  m.y64 = S->y64;
+  m.r64 = S->r64;
+  m.y32 = S->y32;
+  m.bb = S->dval;
+  m.rtol = o.rtol;
+  m.atol = o.atol;
+  m.inner_rtol = o.inner_rtol;
+  m.first_floor = first_floor;
+  m.outer_max_it = o.outer_max_it;
+  m.max_it = o.max_it;
+  m.inner_max_it = o.inner_max_it;
+  m.dtol = o.dtol;
+  m.out = S->mout;
+  FG_CUDA(cudaMemsetAsync(S->pbar, 0, 2 * sizeof(unsigned), s));
+  void *args[] = {&a, &m};
+  const void *fn = accurate ? (const void *)k_mixed_persist<DIM, true> : (const void *)k_mixed_persist<DIM, false>;
+  FG_CUDA(cudaLaunchCooperativeKernel(fn, dim3(S->pblocks), dim3(512), args, H.psmem, s));
+  // u = u0 + y (the kernel leaves y64 = 0 when no refinement step ran)
+  k_unpack_add64<DIM><<<L.grid, L.block, 0, s>>>(g, S->dense, L.tm, S->u64, S->y64, u, false);
+  S->launches += 2;
+  FG_CUDA(cudaEventRecord(S->ev1, s));
+  FG_CUDA(cudaMemcpyAsync(S->mout_h, S->mout, sizeof(MixedOut), cudaMemcpyDeviceToHost, s));
+  FG_CUDA(cudaMemcpyAsync(S->hval + 7, S->fault, sizeof(int), cudaMemcpyDeviceToHost, s));
+  FG_CUDA(cudaStreamSynchronize(s));
+  int fault = 0;
+  memcpy(&fault, S->hval + 7, sizeof(int));
+  const MixedOut &mo = *S->mout_h;
+  if (fault || mo.status) {
+    if (fault) {
+      FG_CUDA(cudaMemsetAsync(S->fault, 0, sizeof(int), s));
+      FG_CUDA(cudaStreamSynchronize(s));
+    }
+    return FISHGPU_ERR_TIMEOUT;
+  }
+  rep->fnorm0 = mo.bn;
+  rep->its = mo.its;
+  rep->reason = mo.reason;
+  rep->outer_its = mo.outer;
+  rep->nhist = mo.nhist;
+  for (int q = 0; q < std::min(mo.nhist, FISHGPU_MAX_HIST); q++) rep->hist[q] = mo.hist[q];
+  for (int q = 0; q < std::min(mo.outer, FISHGPU_MAX_OUTER); q++) rep->inner_its[q] = mo.inner_its[q];
+  rep->fnorm1 = mo.nhist > 0 ? mo.hist[std::min(mo.nhist, FISHGPU_MAX_HIST) - 1] : mo.bn;
+  rep->true_rel_resid = mo.bn > 0.0 ? rep->fnorm1 / mo.bn : 0.0;
+  float ms = 0.f;
+  FG_CUDA(cudaEventElapsedTime(&ms, S->ev0, S->ev1));
+  rep->solve_ms = ms;
+  return FISHGPU_OK;
+}
+
 template <int DIM>
 static int solve_dim(fishgpu_solver *S, double *u, fishgpu_report *rep) {
   const fishgpu_opts &o = S->o;
@@ -1193,6 +1356,10 @@ static int solve_dim(fishgpu_solver *S, double *u, fishgpu_report *rep) {
                                                                            S->red, 1, S->dval);
   }
   FG_CUDA(cudaGetLastError());
+  if constexpr (DIM >= 2) {
+    if (o.precision == FISHGPU_MIXED && S->h32.plev && S->mout) return solve_mixed_persist<DIM>(S, u, rep);
+    if (o.precision == FISHGPU_FP64 && S->h64.plev) return solve_fp64_persist<DIM>(S, u, rep);
+  }
   int rc = read_vals(S, 1);
   if (rc) return rc;
   const double bn = sqrt(S->hval[0]);
@@ -1530,6 +1697,7 @@ extern "C" int fishgpu_solver_destroy(fishgpu_solver *S) {
   for (void *p : S->allocs) cudaFree(p);
   if (S->st_h) cudaFreeHost(S->st_h);
   if (S->hval) cudaFreeHost(S->hval);
+  if (S->mout_h) cudaFreeHost(S->mout_h);
   if (S->ev0) cudaEventDestroy(S->ev0);
   if (S->ev1) cudaEventDestroy(S->ev1);
   if (S->own_stream && S->stream) cudaStreamDestroy(S->stream);
@@ -1740,7 +1908,7 @@ extern "C" long long fishgpu_solver_estimate_bytes(const fishgpu_opts *o) {
                 : persist_shape<double>(*o, dim, false, L, pts.data(), n, &btop, &nsm, &coarse, &copy_off, &psmem);
     if (blocks)
       b += rnd((long long)(es == 4 ? sizeof(TailLevel<float>) : sizeof(TailLevel<double>)) * L) + rnd(8) +
-           rnd(8LL * 4 * nsm);
+           rnd(8LL * 4 * nsm) + (es == 4 ? rnd((long long)sizeof(MixedOut)) : 0);
   }
   return b;
 }

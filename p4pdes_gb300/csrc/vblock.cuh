@@ -425,7 +425,7 @@ struct PersistArgs {
 // the KSP state.  Returns false when a barrier gave up.
 template <int NV>
 __device__ __forceinline__ bool grid_reduce(double (&v)[NV], double *part, int &slot, GridBar *gb, KspState *ks,
-                                            Fin fin) {
+                                            Fin fin, double *out = nullptr) {
   block_sum<NV>(v);
   const int nb = gridDim.x;
   if (threadIdx.x == 0)
@@ -440,7 +440,7 @@ __device__ __forceinline__ bool grid_reduce(double (&v)[NV], double *part, int &
       for (int b = threadIdx.x; b < nb; b += 32) s[q] += __ldcg(&part[(slot * 2 + q) * nb + b]);
     }
     warp_sum<NV>(s);
-    if (threadIdx.x == 0) ksp_finalize(ks, fin, s, NV, nullptr);
+    if (threadIdx.x == 0) ksp_finalize(ks, fin, s, NV, out);
   }
   __syncthreads();
   slot ^= 1;  // the next reduction writes the other slot: no block still reads this one after the next barrier
@@ -508,33 +508,47 @@ constexpr int kMaxPersistLevels = 24;
 // the same operations as their stored forms, so every point's value is the
 // launch-per-phase form's.  A phase never writes an array that another point
 // of the same phase reads.
-template <int DIM, typename T, bool ACC>
-__global__ void __launch_bounds__(512, 1) k_ksp_persist(PersistArgs<T> a) {
-  extern __shared__ __align__(16) unsigned char fg_tail_sm[];
-  __shared__ KspState ks;
-  __shared__ GridBar gb;
-  __shared__ TailLevel<T> lv[kMaxPersistLevels];  // the level table, read at every phase
-  __shared__ TailLevel<T> sv[kMaxPersistLevels];  // block 0: the tail's shared-memory copy
+// The shared state of a persistent launch's blocks.
+template <typename T>
+struct PersistShared {
+  KspState ks;                           // this block's copy of the KSP state
+  GridBar gb;
+  TailLevel<T> lv[kMaxPersistLevels];  // the level table, read at every phase
+  TailLevel<T> sv[kMaxPersistLevels];  // block 0: the tail's shared-memory copy
+};
+
+// The barrier, the level table, and block 0's tail tables (once per launch).
+template <int DIM, typename T>
+__device__ void persist_setup(const PersistArgs<T> &a, PersistShared<T> &sh, unsigned char *fg_tail_sm) {
   const int tid = threadIdx.x;
-  if (tid == 0) {
-    ks = *a.st;
-    ks.ndone = nullptr;
-    gb = GridBar{a.bar, a.fault, 0u, 0};
-  }
-  for (int l = tid; l <= a.top; l += blockDim.x) lv[l] = a.lv[l];
+  if (tid == 0) sh.gb = GridBar{a.bar, a.fault, 0u, 0};
+  for (int l = tid; l <= a.top; l += blockDim.x) sh.lv[l] = a.lv[l];
   __syncthreads();
-  if (ks.done) return;  // every block sees the same state
-  if (blockIdx.x == 0) {  // block 0's tail: its shared-memory table and the coarse solve's tables, once
-    if (a.copy_off >= 0) vtail_prepare<DIM, T>(lv, a.btop, fg_tail_sm, a.copy_off, sv);
+  if (blockIdx.x == 0) {
+    if (a.copy_off >= 0) vtail_prepare<DIM, T>(sh.lv, a.btop, fg_tail_sm, a.copy_off, sh.sv);
     if (a.smem) coarse_stage<DIM, T>(a.S0, a.S1, a.S2, a.ilam, a.n0, a.n1, a.n2, fg_tail_sm);
     __syncthreads();
   }
+}
+
+// One CG solve (run_ksp's work) on the state in sh.ks: the set-up from r (or
+// from src64 scaled by 1/sqrt(*rr64), when src64 is given), the iterations
+// until the state stops (or a.max_iters ran: false in *it_out's count), and
+// with a.do_pend the last deferred update.  Returns false when a barrier gave
+// up.  Every block runs it with identical state.
+template <int DIM, typename T, bool ACC>
+__device__ bool persist_cg(const PersistArgs<T> &a, const double *src64, const double *rr64, PersistShared<T> &sh,
+                           int &slot, unsigned char *fg_tail_sm) {
+  const int tid = threadIdx.x;
+  KspState &ks = sh.ks;
+  GridBar &gb = sh.gb;
+  const TailLevel<T> *lv = sh.lv;
+  const TailLevel<T> *sv = sh.sv;
   // points are dealt to the blocks in warp-sized runs, round robin: a small
   // level's points spread over all SMs (FP64 work on one SM is slow) and
   // every warp still reads consecutive points
   const long long gt = ((long long)(tid >> 5) * gridDim.x + blockIdx.x) * 32 + (tid & 31);
   const long long G = (long long)gridDim.x * blockDim.x;
-  int slot = 0;
   auto sync = [&]() { return grid_sync(&gb); };
   auto each = [&](const Geom &g, auto &&f) {
     const int N = level_npts<DIM>(g);
@@ -679,11 +693,11 @@ __global__ void __launch_bounds__(512, 1) k_ksp_persist(PersistArgs<T> a) {
 
   // ---- set-up (enq_cg_init)
   bool ok = true;
-  if (a.src64) {  // r = (T)(r64 / ||r64||), r.r (v_demote_init)
-    const double is = 1.0 / sqrt(*a.rr64);
+  if (src64) {  // r = (T)(r64 / ||r64||), r.r (v_demote_init)
+    const double is = 1.0 / sqrt(*rr64);
     T rr = T(0);
     each(gf, [&](long long n, int, int, int) {
-      const T o = (T)(a.src64[n] * is);
+      const T o = (T)(src64[n] * is);
       a.r[n] = o;
       rr = fma(o, o, rr);
     });
@@ -770,10 +784,174 @@ __global__ void __launch_bounds__(512, 1) k_ksp_persist(PersistArgs<T> a) {
       });
     }
   }
-  if (blockIdx.x == 0 && tid == 0) {
-    ks.ndone = a.st->ndone;
-    ks.loops = (unsigned)it;
-    *a.st = ks;
+  __syncthreads();
+  if (tid == 0) ks.loops = (unsigned)it;
+  __syncthreads();
+  return ok;
+}
+
+// The whole CG solve of run_ksp in one cooperative launch (one block per SM
+// at most): the state read from a.st at the start, written back by block 0.
+template <int DIM, typename T, bool ACC>
+__global__ void __launch_bounds__(512, 1) k_ksp_persist(PersistArgs<T> a) {
+  extern __shared__ __align__(16) unsigned char fg_tail_sm[];
+  __shared__ PersistShared<T> sh;
+  if (threadIdx.x == 0) {
+    sh.ks = *a.st;
+    sh.ks.ndone = nullptr;
+  }
+  persist_setup<DIM, T>(a, sh, fg_tail_sm);
+  if (sh.ks.done) return;  // every block sees the same state
+  int slot = 0;
+  persist_cg<DIM, T, ACC>(a, a.src64, a.rr64, sh, slot, fg_tail_sm);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    sh.ks.ndone = a.st->ndone;
+    *a.st = sh.ks;
+  }
+}
+
+// ------------------------------------------------------------------ the mixed solve in one launch
+// FP64 iterative refinement around the FP32 inner CG (solve_dim's mixed
+// loop), all on the device: the stop tests and inner tolerances in every
+// block from identical values, the inner solves by persist_cg, the last
+// deferred update of each (v_pend_acc / v_pend_promote) and the FP64 true
+// residual r64 = b64 - A y64 with its norm as grid phases.  What the host
+// learns at the end is in MixedOut.
+struct MixedArgs {
+  const double *b64;  // the right-hand side of J y = b
+  double *y64, *r64;  // the solution (zeroed here if no step runs) and the FP64 residual
+  float *y32;         // the standard inner form's correction (not ACC)
+  const double *bb;   // b64.b64, stored by the kernel that formed b64
+  double rtol, atol, inner_rtol, first_floor;
+  int outer_max_it, max_it, inner_max_it;
+  double dtol;
+  struct MixedOut *out;
+};
+
+struct MixedOut {
+  int status;  // 0, or FISHGPU_ERR_TIMEOUT when an inner solve's iteration cap ran out
+  int its, outer, reason, nhist;
+  int inner_its[FISHGPU_MAX_OUTER];
+  double bn;
+  double hist[FISHGPU_MAX_HIST];
+};
+
+template <int DIM, bool ACC>
+__global__ void __launch_bounds__(512, 1) k_mixed_persist(PersistArgs<float> a, MixedArgs m) {
+  extern __shared__ __align__(16) unsigned char fg_tail_sm[];
+  __shared__ PersistShared<float> sh;
+  __shared__ double s_rr, s_sum;
+  persist_setup<DIM, float>(a, sh, fg_tail_sm);
+  const int tid = threadIdx.x;
+  const long long gt = ((long long)(tid >> 5) * gridDim.x + blockIdx.x) * 32 + (tid & 31);
+  const long long G = (long long)gridDim.x * blockDim.x;
+  const Geom &gf = sh.lv[a.top].g;
+  const int N = level_npts<DIM>(gf);
+  const LevelDiv dv(gf);
+  auto each = [&](auto &&f) {
+    for (long long q = gt; q < N; q += G) {
+      int i, j, k;
+      const long long n = N < (1 << 24) ? level_pos_f<DIM>(gf, dv, (int)q, 0, i, j, k)
+                                         : level_pos<DIM>(gf, (int)q, 0, i, j, k);
+      f(n, i, j, k);
+    }
+  };
+  MixedOut *out = m.out;
+  const bool b0 = blockIdx.x == 0 && tid == 0;
+  const double bn = sqrt(*m.bb);
+  const double ttol = fmax(m.rtol * bn, m.atol);
+  double rn = bn;
+  int reason = 0, its = 0, outer = 0, nh = 0, status = 0, slot = 0;
+  if (b0) {
+    out->bn = bn;
+    out->hist[nh] = rn;
+  }
+  nh++;
+  bool ok = true;
+  while (ok) {
+    if (isnan(rn) || isinf(rn)) { reason = R_DIVERGED_NANORINF; break; }
+    if (rn <= ttol) { reason = rn < m.atol ? R_CONVERGED_ATOL : R_CONVERGED_RTOL; break; }
+    if (outer >= m.outer_max_it || its >= m.max_it) { reason = R_DIVERGED_ITS; break; }
+    double irtol = fmax(m.inner_rtol, 0.5 * ttol / rn);
+    if (outer == 0) irtol = fmax(irtol, m.first_floor);
+    if (irtol > 0.5) irtol = 0.5;
+    if (tid == 0) {  // the inner solve's fresh state (reset_state)
+      memset(&sh.ks, 0, sizeof(sh.ks));
+      sh.ks.rtol = irtol;
+      sh.ks.atol = m.atol;
+      sh.ks.dtol = m.dtol;
+      sh.ks.max_it = m.inner_max_it;
+      sh.ks.norm_type = FISHGPU_NORM_UNPRECONDITIONED;
+      sh.ks.betaold = 1.0;
+      sh.ks.yscale = rn;
+      sh.ks.yfresh = outer == 0 ? 1 : 0;
+      s_rr = outer == 0 ? *m.bb : s_sum;
+    }
+    __syncthreads();
+    // r32 = r / ||r|| (r: b64 in the first step, r64 after) inside the set-up
+    if (!(ok = persist_cg<DIM, float, ACC>(a, outer == 0 ? m.b64 : m.r64, &s_rr, sh, slot, fg_tail_sm))) break;
+    const KspState &ks = sh.ks;
+    if (!ks.done) {  // the inner iteration cap ran out (the device loop's cap)
+      status = FISHGPU_ERR_TIMEOUT;
+      break;
+    }
+    its += ks.its;
+    if (b0 && outer < FISHGPU_MAX_OUTER) out->inner_its[outer] = ks.its;
+    if (ks.reason == R_DIVERGED_NANORINF || ks.reason == R_DIVERGED_INDEFINITE_MAT ||
+        ks.reason == R_DIVERGED_INDEFINITE_PC) {
+      reason = ks.reason;
+      break;
+    }
+    {  // the last deferred update into y64 (v_pend_acc / v_pend_promote)
+      const int pend = ks.pend;
+      if constexpr (ACC) {
+        const bool keep = ksp_y_written(&ks) || !ks.yfresh;
+        if (!keep || pend) {
+          const double ya = pend ? ks.yscale * ks.alpha : 0.0;
+          const float *pv = pend == 1 ? a.p[0] : a.p[1];
+          each([&](long long n, int, int, int) {
+            const double yy = keep ? m.y64[n] : 0.0;
+            m.y64[n] = pend ? fma(ya, f2d_bits(pv[n]), yy) : yy;
+          });
+        }
+      } else {
+        const bool written = ksp_y_written(&ks);
+        const float al = pend ? (float)ks.alpha : 0.f;
+        const float *pv = pend == 1 ? a.p[0] : a.p[1];
+        const bool fresh = outer == 0;
+        each([&](long long n, int, int, int) {
+          float ev = written ? m.y32[n] : 0.f;
+          if (pend) ev = fmaf(al, pv[n], ev);
+          m.y64[n] = fma(rn, (double)ev, fresh ? 0.0 : m.y64[n]);
+        });
+      }
+    }
+    if (!(ok = grid_sync(&sh.gb))) break;
+    {  // r64 = b64 - A y64 and its norm (v_resid<double, NORM>)
+      const Wv<double> w(gf);
+      double rr = 0.0;
+      each([&](long long n, int i, int j, int k) {
+        const double v = resid_pt<DIM, double>(gf, w, m.y64, n, i, j, k, m.b64[n]);
+        m.r64[n] = v;
+        rr = fma(v, v, rr);
+      });
+      double v1[1] = {rr};
+      if (!(ok = grid_reduce<1>(v1, a.part, slot, &sh.gb, &sh.ks, FIN_STORE, &s_sum))) break;
+    }
+    rn = sqrt(s_sum);
+    outer++;
+    if (b0 && nh < FISHGPU_MAX_HIST) out->hist[nh] = rn;
+    nh++;
+  }
+  if (ok && outer == 0) {  // no step ran: the correction is zero
+    each([&](long long n, int, int, int) { m.y64[n] = 0.0; });
+  }
+  if (b0) {
+    out->status = ok ? status : FISHGPU_ERR_TIMEOUT;
+    out->its = its;
+    out->outer = outer;
+    out->reason = reason;
+    out->nhist = nh;
   }
 }
 
