@@ -205,8 +205,8 @@ typedef struct {
                                device loop); -1 (default): when the finest
                                grid has at most persist_points nodes      */
   int persist_points;       /* -fsh_persist_points: that limit (0: 2.5e6
-                               for the FP64 form, 1.5e5 for the mixed
-                               form's FP32 inner solves)                  */
+                               for the FP64 form, 5e5 for the mixed
+                               form)                                      */
   int persist_tail;         /* -fsh_persist_tail: largest level (nodes) the
                                persistent solve runs in its block 0 (0:
                                300 in FP64, 1200 in FP32)                  */

@@ -349,7 +349,7 @@ static int build_tail(fishgpu_solver *S, Hier<T> &H) {
 // Whether a solve's CG loop runs as one persistent launch (k_ksp_persist):
 // CG + MG with two Chebyshev/Jacobi steps, V-cycles, a 2D or 3D single grid,
 // the device loop, and (default) a finest grid of at most persist_points
-// nodes (by default 2.5e6 in FP64, 1.5e5 in FP32).  The levels of at most
+// nodes (by default 2.5e6 in FP64, 5e5 in FP32).  The levels of at most
 // persist_tail nodes run in block 0 between two grid barriers (*btop: the
 // largest of them, >= 1): one SM's FP64 rate is 1/152 of the GPU's, so in
 // FP64 only the smallest levels stay there.  pts: nodes per level
@@ -366,10 +366,11 @@ static int persist_shape(const fishgpu_opts &o, int dim, bool batch, int nlev, c
       nlev > kMaxPersistLevels)
     return 0;
   const long long fine_pts = pts[nlev - 1];
-  // measured against the launch-per-phase solve (2D 257^2 .. 1025^2, 3D 33^3 .. 129^3): the FP64 form
-  // gains at every size (its kernels are FP64-bound there, the launch overhead is not hidden), the
-  // FP32 inner solves of the mixed form up to ~1e5 nodes and break even near 2.7e5
-  const long long lim = o.persist_points > 0 ? o.persist_points : sizeof(T) == 8 ? 2500000 : 150000;
+  // measured against the launch-per-phase solve (2D 257^2 .. 2049^2, 3D 33^3 .. 129^3): the FP64 form
+  // gains at every size up to 2.1e6 nodes (its kernels are FP64-bound there, the launch overhead is not
+  // hidden); the mixed form, its refinement loop in the same launch, up to 2.7e5 nodes and loses from
+  // 1.05e6 (2D 1025^2: 2.78 against 2.64 ms)
+  const long long lim = o.persist_points > 0 ? o.persist_points : sizeof(T) == 8 ? 2500000 : 500000;
   if (o.persist < 0 && fine_pts > lim) return 0;
   const long long tmax = o.persist_tail > 0 ? o.persist_tail : sizeof(T) == 8 ? 300 : 1200;
   *btop = 0;
