@@ -1434,6 +1434,10 @@ extern "C" int fishgpu_ms_solver_create(const fishgpu_ms_opts *o, void *stream, 
     po.mz = 1;
     po.pc_type = FISHGPU_PC_MG;
     po.precision = FISHGPU_MIXED;
+    // only the hierarchy and its V-cycle are used here (never the fish
+    // solver's CG): no persistent-solve tables, no second residual buffer
+    po.persist = 0;
+    po.fuse_cgr = 0;
     // default hierarchy: coarsen only down to about 33 x 33 and solve that
     // grid exactly (one block, sine transform): the V-cycle of these 2D grids
     // is launch-bound, and the deepest levels cost launches, not work
