@@ -686,3 +686,36 @@ def test_persistent_solves_on_concurrent_streams(cuda):
         assert reps[q].reason == ra.reason == 2 and reps[q].its == ra.its
         assert torch.equal(us[q], ua)
         solvers[q].close()
+
+
+@pytest.mark.parametrize("args", [
+    # the iteration cap stops the FP64 CG (DIVERGED_ITS), mid-V-cycle state left behind
+    "-fsh_dim 2 -fsh_problem manupoly -da_refine 6 -pc_type mg -ksp_rtol 1e-12 -ksp_max_it 3",
+    # the mixed form's outer cap and inner cap
+    "-fsh_dim 3 -fsh_problem manupoly -da_refine 4 -pc_type mg -ksp_rtol 1e-12 -fsh_precision mixed "
+    "-fsh_outer_max_it 1",
+    "-fsh_dim 2 -fsh_problem manupoly -da_refine 6 -pc_type mg -ksp_rtol 1e-12 -fsh_precision mixed "
+    "-fsh_inner_max_it 2",
+    # a zero right-hand side: converged before any iteration
+    "-fsh_dim 3 -fsh_problem zero -da_refine 4 -pc_type mg -ksp_rtol 1e-10 -fsh_precision mixed",
+])
+def test_persistent_solve_stops_as_the_launch_per_phase_solve(cuda, args):
+    """The persistent solves stop for the same reasons as the launch-per-phase
+    solves (caps, a zero right-hand side), with the same reports: FP64 the
+    same iterations and history to 1e-10; mixed the same refinement steps,
+    inner iterations within one per step (an FP32 dot product summed in
+    another order can move a stop by one iteration), history to 1e-3."""
+    fg = fgmod()
+    u1, a = fg.solve(fg.options(args + " -fsh_persist 1"))
+    u0, b = fg.solve(fg.options(args + " -fsh_persist 0"))
+    mixed = "mixed" in args
+    assert a.reason == b.reason and a.outer_its == b.outer_its, (a.reason, b.reason, a.outer_its, b.outer_its)
+    assert abs(a.its - b.its) <= (max(1, b.outer_its) if mixed else 0), (a.its, b.its)
+    assert a.launches < b.launches or b.launches <= 6
+    ha, hb = a.history(), b.history()
+    assert len(ha) == len(hb)
+    tol = 1e-3 if mixed else 1e-10
+    for x, y in zip(ha, hb):
+        assert abs(x - y) <= tol * abs(y) + 1e-14 * max(hb[0], 1e-300), (x, y)
+    scale = max(u0.abs().max().item(), 1e-300)
+    assert (u1 - u0).abs().max().item() <= (1e-3 if mixed else 1e-10) * scale
