@@ -1,16 +1,15 @@
-// bitconv.cuh -- the exact FP32 -> FP64 conversion by integer operations,
-// for host and device.
+// bitconv.cuh -- FP32 <-> FP64 conversions by integer operations, for host
+// and device.
 //
 // On this GPU the conversion instructions run on the FP64 pipe (1/64 of the
 // FP32 rate), beside the FP64 arithmetic of the kernels that need them; the
-// same result built from the operand's bits uses the integer pipe.  Normal
-// numbers and zeros take the integer path; subnormals, infinities and NaNs
-// take the hardware conversion.  It returns exactly what the C cast returns (the
-// conversion is exact), checked on the host against numpy on random bit
-// patterns of every exponent and on the special values.
-// (The other direction, rounded to nearest even from the bits, measured no
-// faster in the inner solves' set-up kernel, whose time the FP64 scaling
-// multiply and the memory traffic set.)
+// same results built from the operand's bits use the integer pipe.  Normal
+// numbers and zeros take the integer path; subnormals, infinities, NaNs and
+// (for FP64 -> FP32) values outside the float range take the hardware
+// conversion.  Both return exactly what the C cast returns (FP32 -> FP64 is
+// exact, FP64 -> FP32 rounds to nearest, ties to even), checked on the host
+// against numpy on random bit patterns of every exponent, on rounding ties
+// and on the special values.
 #pragma once
 
 #include <stdint.h>
@@ -53,6 +52,29 @@ FG_HD double f2d_bits(float f) {
     return a == 0u ? bits_to_double((uint64_t)(u & 0x80000000u) << 32) : (double)f;
   const uint64_t hi = (uint64_t)(((a >> 3) + (896u << 20)) | (u & 0x80000000u));
   return bits_to_double((hi << 32) | (uint64_t)(uint32_t)(u << 29));
+}
+
+// (float)d: the exponent rebased by -896, the top 23 of the 52 mantissa bits
+// kept and the 29 dropped ones rounded to nearest, ties to even (a carry out
+// of the mantissa moves into the exponent, as the rounding must); biased
+// exponents 897 .. 1150 give normal floats (or infinity after rounding up
+// the largest), everything else takes the cast -- in a function of its own
+// on the device, so that the compiler does not evaluate the cast for every
+// element and select (the cast is the FP64-pipe instruction this avoids).
+#ifdef __CUDACC__
+static __host__ __device__ __noinline__ float d2f_cast(double d) { return (float)d; }
+#else
+inline float d2f_cast(double d) { return (float)d; }
+#endif
+FG_HD float d2f_bits(double d) {
+  const uint64_t u = double_bits(d);
+  const uint32_t e = (uint32_t)(u >> 52) & 0x7FFu;
+  if (e < 897u || e > 1150u) return d2f_cast(d);
+  const uint64_t m = u & 0xFFFFFFFFFFFFFull;
+  const uint32_t keep = (uint32_t)(m >> 29), rest = (uint32_t)(m & 0x1FFFFFFFull);
+  uint32_t r = ((e - 896u) << 23) | keep;
+  if (rest > 0x10000000u || (rest == 0x10000000u && (keep & 1u))) r += 1u;
+  return bits_to_float(r | ((uint32_t)(u >> 32) & 0x80000000u));
 }
 
 }  // namespace fg

@@ -693,11 +693,13 @@ __device__ bool persist_cg(const PersistArgs<T> &a, const double *src64, const d
 
   // ---- set-up (enq_cg_init)
   bool ok = true;
-  if (src64) {  // r = (T)(r64 / ||r64||), r.r (v_demote_init)
+  if (src64) {  // r = r64 / ||r64|| rounded to T as v_demote_init rounds it, r.r
     const double is = 1.0 / sqrt(*rr64);
     T rr = T(0);
     each(gf, [&](long long n, int, int, int) {
-      const T o = (T)(src64[n] * is);
+      T o;
+      if constexpr (sizeof(T) == 4) o = d2f_bits(src64[n]) * (float)is;
+      else o = (T)(src64[n] * is);
       a.r[n] = o;
       rr = fma(o, o, rr);
     });

@@ -1438,20 +1438,23 @@ __global__ void __launch_bounds__(256) v_resid_zero0(Geom g, Slots s, const doub
 static __global__ void k_inv_norm(const double *__restrict__ rr, double *__restrict__ is) { *is = 1.0 / sqrt(*rr); }
 
 // The set-up of an inner FP32 solve from an FP64 residual in one pass:
-// r32 = (float)(r64 * is) with is = 1 / sqrt(rr), rr = r64.r64 as stored by
-// the residual kernel (k_inv_norm: the host's 1.0 / ||r|| to the bit, sqrt
-// and the division are correctly rounded) and r32.r32 reduced as
-// v_dots<float> reduces it, finalised as FIN_INIT_RR.  Replaces v_demote and
-// v_dots (y32 is not zero-filled: see v_cg_pend).
+// r32 = (float)r64 * (float)is with is = 1 / sqrt(rr), rr = r64.r64 as
+// stored by the residual kernel (k_inv_norm, once), and r32.r32 reduced as
+// v_dots<float> reduces it, finalised as FIN_INIT_RR.  The scaling is done
+// in FP32 after rounding r64 to FP32 on the integer pipe (d2f_bits): the
+// FP64 multiply and conversion per element made the pass FP64-bound (ncu:
+// FP64 pipe 87%, 0.53 ms at 513^3); the inner solve only needs r32 close to
+// unit norm, and its own norm is the one it starts from.  Replaces v_demote
+// and v_dots (y32 is not zero-filled: see v_cg_pend).
 static __global__ void __launch_bounds__(256) v_demote_init(Geom g, Slots s, KspState *st, const double *__restrict__ r,
                                                      const double *__restrict__ isp, float *__restrict__ r32,
                                                      Reducer red, int slot) {
   if (ksp_done_v(st)) return;
-  const double is = *isp;
+  const float is = (float)*isp;
   float zz = 0.f;
   FG_PW_BEGIN
   const V4<double> a = ld4(r + n);
-  const V4<float> o{(float)(a.x * is), (float)(a.y * is), (float)(a.z * is), (float)(a.w * is)};
+  const V4<float> o{d2f_bits(a.x) * is, d2f_bits(a.y) * is, d2f_bits(a.z) * is, d2f_bits(a.w) * is};
   st4(r32 + n, o);
   zz = fmaf(o.x, o.x, fmaf(o.y, o.y, fmaf(o.z, o.z, fmaf(o.w, o.w, zz))));
   FG_PW_END
@@ -1485,13 +1488,14 @@ static __global__ void __launch_bounds__(256) v_pend_acc(Geom g, Slots s, const 
   FG_PW_END
 }
 
-// r32 = (float)(r64 * inv_s); inv_s per plane for a batch (scale[plane])
+// r32 = (float)r64 * (float)inv_s, rounded as v_demote_init rounds; inv_s
+// per plane for a batch (scale[plane])
 static __global__ void __launch_bounds__(256) v_demote(Geom g, Slots s, const double *__restrict__ r, const double *scale,
                                                 double inv_s, float *__restrict__ r32) {
   FG_PW_BEGIN
-  const double is = scale ? scale[k] : inv_s;
+  const float is = (float)(scale ? scale[k] : inv_s);
   const V4<double> a = ld4(r + n);
-  st4(r32 + n, V4<float>{(float)(a.x * is), (float)(a.y * is), (float)(a.z * is), (float)(a.w * is)});
+  st4(r32 + n, V4<float>{d2f_bits(a.x) * is, d2f_bits(a.y) * is, d2f_bits(a.z) * is, d2f_bits(a.w) * is});
   FG_PW_END
 }
 
