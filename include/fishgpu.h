@@ -474,7 +474,16 @@ typedef struct {
   int inner_block;        /* -ms_inner_block 0|1: on grids of up to 4096 nodes whose
                              preconditioner is one exact coarse solve, the whole
                              inner BiCGStab runs in one block (default 1)    */
+  int inner_persist;      /* -ms_inner_persist N: on multigrid grids of up to N
+                             nodes the whole inner BiCGStab solve runs as one
+                             cooperative launch (0: never; default -1: the
+                             measured limit, FISHGPU_MS_PERSIST_POINTS)       */
+  int vtail_points;       /* -ms_vtail_points N: the Poisson V-cycle's levels of
+                             at most N nodes run in one block (the coarsest
+                             always; 0: the fish solver's default)           */
 } fishgpu_ms_opts;
+
+#define FISHGPU_MS_PERSIST_POINTS 600000
 
 #define FISHGPU_MS_MAX_GRIDS 12
 #define FISHGPU_MS_MAX_ITS   64
@@ -497,6 +506,9 @@ typedef struct {
   double err1;                                 /* obstacle: mean |u - u_exact|    */
   double active_area_err;                      /* obstacle: |area(A) - pi a^2| / pi a^2 */
   long long n_active;                          /* obstacle: nodes of the active set */
+  int inner_form[FISHGPU_MS_MAX_GRIDS];        /* how each grid's inner solves ran:
+                                                  0 launch-per-phase graphs, 1 one
+                                                  block, 2 one cooperative launch */
 } fishgpu_ms_report;
 
 int fishgpu_ms_opts_default(fishgpu_ms_opts *o);

@@ -142,7 +142,7 @@ class MsOpts(ctypes.Structure):
                 ("line_search", c_int), ("ksp_rtol", c_double), ("ksp_max_it", c_int), ("pc_type", c_int),
                 ("mg_levels", c_int), ("monitor_degree", c_int), ("snes_monitor", c_int),
                 ("converged_reason", c_int), ("ksp_converged_reason", c_int), ("loop_cap", c_int),
-                ("inner_block", c_int)]
+                ("inner_block", c_int), ("inner_persist", c_int), ("vtail_points", c_int)]
 
 
 class MsReport(ctypes.Structure):
@@ -153,7 +153,7 @@ class MsReport(ctypes.Structure):
                 ("area", ((c_double * 3) * (MS_MAX_ITS + 1)) * MS_MAX_GRIDS),
                 ("errinf", c_double), ("solve_ms", c_double), ("dofs", c_ll), ("total_ksp_its", c_ll),
                 ("nfuncs", c_ll), ("grid_ms", c_double * MS_MAX_GRIDS), ("err1", c_double),
-                ("active_area_err", c_double), ("n_active", c_ll)]
+                ("active_area_err", c_double), ("n_active", c_ll), ("inner_form", c_int * MS_MAX_GRIDS)]
 
     def fnorms(self, k):
         return [self.fnorm[k][i] for i in range(self.its[k] + 1)]

@@ -5,7 +5,7 @@
 #pragma once
 
 #include "common.cuh"
-#include "vkernels.cuh"
+#include "vblock.cuh"
 
 struct fishgpu_solver_s;
 
@@ -33,5 +33,16 @@ struct CoarseView {
 };
 // False unless the solver is a 2D mixed-form multigrid solver with one level.
 bool solver_coarse32(const fishgpu_solver_s *S, CoarseView *c);
+
+// The V-cycle of a 2D mixed-form multigrid solver (two Chebyshev/Jacobi
+// steps per level) for a persistent cooperative kernel (persist_vcycle):
+// fills the level table, the coarse solve, the grid barrier (zero it before
+// each launch), the partial sums and the fault word of *a; levels of at most
+// tail_pts nodes (the coarsest always) run in block 0.  *blocks and *smem:
+// the launch's blocks of 512 threads (one per SM at most) and its dynamic
+// shared memory.  False when the solver has no such V-cycle or the kernel
+// cannot be launched so.
+bool solver_persist32(fishgpu_solver_s *S, const void *kernel, long long tail_pts, PersistArgs<float> *a,
+                      int *blocks, size_t *smem);
 
 }  // namespace fg

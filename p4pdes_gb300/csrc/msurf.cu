@@ -231,10 +231,6 @@ __device__ __forceinline__ void ms_reduce(double (&v)[NV], const Reducer &red, F
   }
 }
 
-struct StoreFin {
-  double *out;
-  __device__ void operator()(const double *s) const { out[0] = s[0]; }
-};
 struct Store2Fin {
   double *out;
   __device__ void operator()(const double *s) const { out[0] = s[0]; out[1] = s[1]; }
@@ -248,11 +244,14 @@ struct Store2Fin {
   const bool node = in_ && i < g.mx;                              \
   (void)node;
 
-// F(u) everywhere (boundary rows u - g, padding 0) and ||F||^2 -> out[0]
+// F(u) everywhere (boundary rows u - g, padding 0), ||F||^2 -> out[0] and
+// ||u||^2 -> out[1] (the Newton step's ||x||; ms_reduce sums each component
+// on its own, in the order of a reduction of that component alone)
 __global__ void __launch_bounds__(256) k_ms_resid(Geom g, MsP P, const double *__restrict__ u,
                                                   double *__restrict__ F, Reducer red, double *out) {
   MS_NODE_BEGIN
   double acc = 0.0;
+  const double uu = node ? u[n] : 0.0;
   if (in_) {
     double f = 0.0;
     if (node && P.model == FISHGPU_NL_OBSTACLE) {
@@ -268,8 +267,8 @@ __global__ void __launch_bounds__(256) k_ms_resid(Geom g, MsP P, const double *_
     }
     F[n] = f;
   }
-  double v1[1] = {acc};
-  ms_reduce<1>(v1, red, StoreFin{out});
+  double v2[2] = {acc, uu * uu};
+  ms_reduce<2>(v2, red, Store2Fin{out});
 }
 
 // Linearisation of one half-point flux D(W) d (d the normal difference):
@@ -711,6 +710,129 @@ __global__ void __launch_bounds__(1024) k_bi_block(Geom g, int model, float a, f
   }
 }
 
+// The whole BiCGStab solve of a multigrid grid in ONE cooperative launch (one
+// block of 512 threads per SM at most): the iteration of k_bi_p .. k_bi_xr,
+// each kernel a phase ended by a grid barrier, the preconditioner the fish
+// solver's FP32 V-cycle run by persist_vcycle (the launch-per-phase
+// V-cycle's values).  Two fusions save a phase each: p = r + beta (p - omega
+// v) (k_bi_p) and s = r - alpha v (k_bi_s) are formed on the fly as the
+// V-cycle's fine right-hand side and stored by its last pass, which also
+// stores ph = M p and sh = M s (k_bi_pcout).  Every block sums the dot
+// products' block partials in the same order and runs the same finalisers on
+// its own copy of the state (block 0 writes it back), so the iteration is
+// the launch-per-phase one up to the order of the dot products' sums; each
+// point runs the same operations.  Grids whose V-cycle kernels are too small
+// to hide a launch each (the inner iteration is ~60 launches) take this form.
+struct BiPersist {
+  Geom g;  // the fine grid, the fish solver's padded layout
+  int model;
+  float ja, jb;
+  const float4 *C1, *C2;
+  const float *b;
+  float *r, *rh, *p, *v, *s, *t, *x, *ph, *sh;
+  MsKsp *st;
+  int max_iters;  // iterations before the launch gives up (the host reports a timeout)
+};
+
+__global__ void __launch_bounds__(512, 1) k_bi_persist(PersistArgs<float> a, BiPersist q) {
+  extern __shared__ __align__(16) unsigned char fg_tail_sm[];
+  __shared__ PersistShared<float> ps;
+  __shared__ MsKsp mk;
+  const int tid = threadIdx.x;
+  if (tid == 0) mk = *q.st;
+  persist_setup<2, float>(a, ps, fg_tail_sm);
+  const Geom &g = q.g;
+  int slot = 0;
+  auto each = [&](auto &&f) { persist_each<2>(g, f); };
+  auto sync = [&]() { return grid_sync(&ps.gb); };
+  // M in = the V-cycle's value inside, in itself on boundary rows (k_bi_pcout)
+  auto use_z = [&](long long n, int i, int j) -> bool {
+    return q.model == FISHGPU_NL_OBSTACLE ? q.C1[n].x == 0.f : !ms_bdry(g, i, j);
+  };
+  auto sync_first = [&](float) -> int { return sync() ? 1 : 0; };
+  bool ok = true;
+  {  // k_bi_init: r = b, rhat = b, x = p = v = 0; rho = b.b.  Every vector's padding is zeroed
+     // here and never written again (the node kernels keep it at 0).
+    const long long tot = (long long)g.plane;
+    const long long G = (long long)gridDim.x * blockDim.x;
+    for (long long e = (long long)blockIdx.x * blockDim.x + tid; e < tot; e += G)
+      if ((int)(e % g.pitch) >= g.mx) {
+        q.r[e] = q.rh[e] = q.p[e] = q.v[e] = q.s[e] = q.t[e] = q.x[e] = q.ph[e] = q.sh[e] = 0.f;
+      }
+    double acc = 0.0;
+    each([&](long long n, int, int, int) {
+      const float bb = q.b[n];
+      q.r[n] = bb;
+      q.rh[n] = bb;
+      q.x[n] = 0.f;
+      q.p[n] = 0.f;
+      q.v[n] = 0.f;
+      acc += (double)bb * bb;
+    });
+    double v1[1] = {acc};
+    ok = grid_reduce_fn<1>(v1, a.part, slot, &ps.gb, [&](double *t) { InitFin{&mk}(t); });
+  }
+  int it = 0;
+  while (ok && !mk.k.done && it < q.max_iters) {
+    it++;
+    {  // p (k_bi_p) formed on the fly; ph = M p (k_bi_pcout)
+      const bool first = mk.first != 0;
+      const float be = (float)mk.beta, om = (float)mk.omega;
+      auto pf = [&](long long m) -> float { return first ? q.r[m] : fmaf(be, fmaf(-om, q.v[m], q.p[m]), q.r[m]); };
+      auto last = [&](long long n, int i, int j, int, float z, float bv) {
+        q.p[n] = bv;
+        q.ph[n] = use_z(n, i, j) ? z : bv;
+      };
+      if (!(ok = persist_vcycle<2, float>(a, ps, fg_tail_sm, pf, sync_first, last, sync))) break;
+    }
+    {  // k_bi_jv1: v = J ph; rhat.v -> alpha
+      double acc = 0.0;
+      each([&](long long n, int i, int j, int) {
+        const float o = ms_jv_node(g, q.model, i, j, n, q.ja, q.jb, q.C1, q.C2, q.ph);
+        q.v[n] = o;
+        acc += (double)q.rh[n] * o;
+      });
+      double v1[1] = {acc};
+      if (!(ok = grid_reduce_fn<1>(v1, a.part, slot, &ps.gb, [&](double *t) { AlphaFin{&mk}(t); }))) break;
+    }
+    if (mk.k.done) break;
+    {  // s = r - alpha v (k_bi_s) formed on the fly; sh = M s
+      const float al = (float)mk.alpha;
+      auto sf = [&](long long m) -> float { return fmaf(-al, q.v[m], q.r[m]); };
+      auto last = [&](long long n, int i, int j, int, float z, float bv) {
+        q.s[n] = bv;
+        q.sh[n] = use_z(n, i, j) ? z : bv;
+      };
+      if (!(ok = persist_vcycle<2, float>(a, ps, fg_tail_sm, sf, sync_first, last, sync))) break;
+    }
+    {  // k_bi_jv2: t = J sh; t.s, t.t -> omega
+      double ts = 0.0, tt = 0.0;
+      each([&](long long n, int i, int j, int) {
+        const float o = ms_jv_node(g, q.model, i, j, n, q.ja, q.jb, q.C1, q.C2, q.sh);
+        q.t[n] = o;
+        ts += (double)o * q.s[n];
+        tt += (double)o * o;
+      });
+      double v2[2] = {ts, tt};
+      if (!(ok = grid_reduce_fn<2>(v2, a.part, slot, &ps.gb, [&](double *t) { OmegaFin{&mk}(t); }))) break;
+    }
+    {  // k_bi_xr: x += alpha ph + omega sh; r = s - omega t; r.r, rhat.r
+      const float al = (float)mk.alpha, om = (float)mk.omega;
+      double rr = 0.0, hr = 0.0;
+      each([&](long long n, int, int, int) {
+        q.x[n] = fmaf(om, q.sh[n], fmaf(al, q.ph[n], q.x[n]));
+        const float rn = fmaf(-om, q.t[n], q.s[n]);
+        q.r[n] = rn;
+        rr += (double)rn * rn;
+        hr += (double)q.rh[n] * rn;
+      });
+      double v2[2] = {rr, hr};
+      if (!(ok = grid_reduce_fn<2>(v2, a.part, slot, &ps.gb, [&](double *t) { XrFin{&mk}(t); }))) break;
+    }
+  }
+  if (blockIdx.x == 0 && tid == 0) *q.st = mk;  // not done: the iteration cap (or a barrier) ended it
+}
+
 // ------------------------------------------------------------------ Newton helpers
 // b = F / fnorm (FP32); 0 on the active set of the obstacle problem (C1.x)
 __global__ void __launch_bounds__(256) k_ms_demote(Geom g, int model, const float4 *__restrict__ C1,
@@ -754,14 +876,6 @@ __global__ void __launch_bounds__(256) k_obs_project(Geom g, double *__restrict_
 // active nodes (sel 1: u <= psi + zerotol and F > 0, obstacle.c:184-213)
 __global__ void __launch_bounds__(256) k_obs_report(Geom g, int sel, const double *__restrict__ u,
                                                     const double *__restrict__ F, double *part, int cap);
-
-// u.u -> out[0]
-__global__ void __launch_bounds__(256) k_ms_norm2(Geom g, const double *__restrict__ u, Reducer red, double *out) {
-  MS_NODE_BEGIN
-  const double a = node ? u[n] : 0.0;
-  double v1[1] = {a * a};
-  ms_reduce<1>(v1, red, StoreFin{out});
-}
 
 // mode 0: u = g on the boundary and 0 inside (InitialState ZEROS with g,
 // minimal.c:155-157); 1: g everywhere (FormExactFromG, minimal.c:193-208);
@@ -934,6 +1048,10 @@ struct MsLevel {
   long long n_loop = 0;
   int giters = 2;
   bool block1 = false;  // the inner solve is one launch of k_bi_block
+  bool persist = false;  // the inner solve is one cooperative launch of k_bi_persist
+  PersistArgs<float> pa{};
+  int pblocks = 0;
+  size_t psmem = 0;
   BiCoarse bc{};
   int use_pc = 0;
   int max_iters = 0;
@@ -1042,13 +1160,16 @@ static int read_vals(fishgpu_ms_solver *S, int n) {
   return FISHGPU_OK;
 }
 
-static int residual(fishgpu_ms_solver *S, MsLevel &L, const double *u, double *F, double *fnorm) {
+// F = F(u) and ||F||; ||u||^2 into *unorm2 when asked (the same launch)
+static int residual(fishgpu_ms_solver *S, MsLevel &L, const double *u, double *F, double *fnorm,
+                    double *unorm2 = nullptr) {
   S->nfuncs++;
   k_ms_resid<<<L.grid, L.block, 0, S->stream>>>(L.g, level_params(S, L), u, F, S->red, S->dval);
   MS_CK(cudaGetLastError());
-  int rc = read_vals(S, 1);
+  int rc = read_vals(S, 2);
   if (rc) return rc;
   *fnorm = sqrt(S->hval[0]);
+  if (unorm2) *unorm2 = S->hval[1];
   return FISHGPU_OK;
 }
 
@@ -1102,36 +1223,65 @@ static int newton(fishgpu_ms_solver *S, MsLevel &L, int k, fishgpu_ms_report *re
     k_ms_demote<<<L.grid, L.block, 0, s>>>(g, S->P.model, L.C1, L.F, 1.0 / fnorm, L.b);
     MS_CK(cudaGetLastError());
     int kits = 0, kreason = 0;
+    // the inner solve, then at once the slope's dot products (k_ms_slope): the
+    // host reads them with the solver state in one round trip
+    auto enq_slope = [&]() -> int {
+      k_ms_slope<<<L.grid, L.block, 0, s>>>(g, S->P.model, a, b, L.C1, L.C2, L.x, L.F, S->red, S->dval);
+      MS_CK(cudaGetLastError());
+      MS_CK(cudaMemcpyAsync(S->hval, S->dval, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
+      return FISHGPU_OK;
+    };
     if (L.block1) {
       const float ja = (float)(g.h[1] / g.h[0]), jb = (float)(g.h[0] / g.h[1]);
       k_bi_block<<<1, 1024, L.bsm, s>>>(g, S->P.model, ja, jb, L.C1, L.C2, L.b, L.r, L.rh, L.p, L.v, L.s, L.t,
                                         L.x, L.ph, L.sh, S->st, L.bc, L.use_pc, L.max_iters, L.vsm_off);
       MS_CK(cudaGetLastError());
+      if ((rc = enq_slope())) return rc;
       MS_CK(cudaMemcpyAsync(S->st_h, S->st, sizeof(MsKsp), cudaMemcpyDeviceToHost, s));
       MS_CK(cudaStreamSynchronize(s));
       if (!S->st_h->k.done) return FISHGPU_ERR_TIMEOUT;  // the iteration cap ended it unfinished
-    } else {
+    } else if (L.persist) {
+      MS_CK(cudaMemsetAsync(L.pa.bar, 0, 2 * sizeof(unsigned), s));
+      BiPersist q{g, S->P.model, a, b, L.C1, L.C2, L.b, L.r, L.rh, L.p, L.v, L.s, L.t, L.x, L.ph, L.sh, S->st,
+                  L.max_iters};
+      void *args[] = {&L.pa, &q};
+      MS_CK(cudaLaunchCooperativeKernel((const void *)k_bi_persist, dim3(L.pblocks), dim3(512), args, L.psmem, s));
+      if ((rc = enq_slope())) return rc;
+      MS_CK(cudaMemcpyAsync(S->st_h, S->st, sizeof(MsKsp), cudaMemcpyDeviceToHost, s));
+      MS_CK(cudaMemcpyAsync(S->hval + 7, L.pa.fault, sizeof(int), cudaMemcpyDeviceToHost, s));
+      MS_CK(cudaStreamSynchronize(s));
+      int fault = 0;
+      memcpy(&fault, S->hval + 7, sizeof(int));
+      if (fault) {  // a grid barrier gave up: the state is void; the next solve starts clean
+        MS_CK(cudaMemsetAsync(L.pa.fault, 0, sizeof(int), s));
+        MS_CK(cudaStreamSynchronize(s));
+        return FISHGPU_ERR_TIMEOUT;
+      }
+      if (!S->st_h->k.done) return FISHGPU_ERR_TIMEOUT;  // the iteration cap ended it unfinished
+    } else if (L.g_loop) {
       MS_CK(cudaGraphLaunch(L.g_init, s));
-      if (L.g_loop) MS_CK(cudaGraphLaunch(L.g_loop, s));
-    }
-    for (;;) {
+      MS_CK(cudaGraphLaunch(L.g_loop, s));
+      if ((rc = enq_slope())) return rc;
       MS_CK(cudaMemcpyAsync(S->st_h, S->st, sizeof(MsKsp), cudaMemcpyDeviceToHost, s));
       MS_CK(cudaStreamSynchronize(s));
-      if (S->st_h->k.done) {
-        kits = S->st_h->its;
-        kreason = S->st_h->reason;
-        break;
+      if (!S->st_h->k.done) return FISHGPU_ERR_TIMEOUT;  // the capped device loop ended unfinished
+    } else {  // the host-polled graph
+      MS_CK(cudaGraphLaunch(L.g_init, s));
+      for (;;) {
+        MS_CK(cudaMemcpyAsync(S->st_h, S->st, sizeof(MsKsp), cudaMemcpyDeviceToHost, s));
+        MS_CK(cudaStreamSynchronize(s));
+        if (S->st_h->k.done) break;
+        MS_CK(cudaGraphLaunch(L.g_iter, s));
       }
-      if (L.g_loop) return FISHGPU_ERR_TIMEOUT;  // the capped device loop ended unfinished
-      MS_CK(cudaGraphLaunch(L.g_iter, s));
+      if ((rc = enq_slope())) return rc;
+      MS_CK(cudaStreamSynchronize(s));
     }
+    kits = S->st_h->its;
+    kreason = S->st_h->reason;
     rep->ksp_its[k][its] = kits;
     rep->ksp_reason[k][its] = kreason;
     rep->total_ksp_its += kits;
-    // slope of ||F||^2/2 along -Y: -(F, J Y) = -||F|| (F, J x); ||Y|| = ||F|| ||x||
-    k_ms_slope<<<L.grid, L.block, 0, s>>>(g, S->P.model, a, b, L.C1, L.C2, L.x, L.F, S->red, S->dval);
-    MS_CK(cudaGetLastError());
-    if ((rc = read_vals(S, 2))) return rc;
+    // slope of ||F||^2/2 along -Y: -(F, J Y) = -||F|| (F, J x); ||Y|| = ||F|| ||x|| (read above)
     double initslope = -fnorm * S->hval[0];
     double ynorm = fnorm * sqrt(S->hval[1]);
     if (initslope > 0.0) initslope = -initslope;
@@ -1142,12 +1292,12 @@ static int newton(fishgpu_ms_solver *S, MsLevel &L, int k, fishgpu_ms_report *re
       ynorm = 1e8;
     }
     // line search: lambda = 1, then cubic backtracking (Dennis & Schnabel A6.3.1)
-    double lam = 1.0, gnorm = 0.0, lamprev = 1.0, gprev = 0.0;
+    double lam = 1.0, gnorm = 0.0, lamprev = 1.0, gprev = 0.0, wnorm2 = 0.0;
     bool ok = false;
     const double alpha = 1e-4;
     for (int ls = 0; ls < 41; ls++) {
       k_ms_trial<<<L.grid, L.block, 0, s>>>(g, S->P.model, L.u, lam * scale, L.x, L.W);
-      if ((rc = residual(S, L, L.W, L.G, &gnorm))) return rc;
+      if ((rc = residual(S, L, L.W, L.G, &gnorm, &wnorm2))) return rc;
       if (!o.line_search || 0.5 * gnorm * gnorm <= 0.5 * fnorm * fnorm + lam * alpha * initslope) {
         ok = true;
         break;
@@ -1180,10 +1330,8 @@ static int newton(fishgpu_ms_solver *S, MsLevel &L, int k, fishgpu_ms_report *re
     fnorm = gnorm;
     rep->fnorm[k][its] = fnorm;
     if (o.monitor_degree > 0 && (rc = area(S, L, L.u, rep->area[k][its]))) return rc;
-    k_ms_norm2<<<L.grid, L.block, 0, s>>>(g, L.u, S->red, S->dval);
-    MS_CK(cudaGetLastError());
-    if ((rc = read_vals(S, 1))) return rc;
-    const double xnorm = sqrt(S->hval[0]), snorm = lam * ynorm;
+    // ||u|| of the accepted trial, reduced by its residual evaluation
+    const double xnorm = sqrt(wnorm2), snorm = lam * ynorm;
     if (fnorm != fnorm) reason = SN_DIVERGED_FNORM_NAN;
     else if (fnorm < o.atol) reason = SN_CONVERGED_FNORM_ABS;
     else if (fnorm <= ttol) reason = SN_CONVERGED_FNORM_RELATIVE;
@@ -1193,6 +1341,7 @@ static int newton(fishgpu_ms_solver *S, MsLevel &L, int k, fishgpu_ms_report *re
   rep->its[k] = its;
   rep->reason[k] = reason;
   rep->m[k] = g.mx;
+  rep->inner_form[k] = L.block1 ? 1 : L.persist ? 2 : 0;
   return FISHGPU_OK;
 }
 
@@ -1214,6 +1363,7 @@ extern "C" int fishgpu_ms_opts_default(fishgpu_ms_opts *o) {
   o->ksp_rtol = 1e-5;
   o->ksp_max_it = 10000;
   o->inner_block = 1;
+  o->inner_persist = -1;
   o->pc_type = FISHGPU_PC_MG;
   return FISHGPU_OK;
 }
@@ -1290,6 +1440,8 @@ extern "C" int fishgpu_ms_opts_parse(fishgpu_ms_opts *o, int argc, const char *c
     else if (!strcmp(k, "-ksp_max_it")) rc = num(a, nullptr, &o->ksp_max_it);
     else if (!strcmp(k, "-ms_loop_cap")) rc = num(a, nullptr, &o->loop_cap);
     else if (!strcmp(k, "-ms_inner_block")) rc = num(a, nullptr, &o->inner_block);
+    else if (!strcmp(k, "-ms_inner_persist")) rc = num(a, nullptr, &o->inner_persist);
+    else if (!strcmp(k, "-ms_vtail_points")) rc = num(a, nullptr, &o->vtail_points);
     else if (!strcmp(k, "-pc_mg_levels")) rc = num(a, nullptr, &o->mg_levels);
     else if (!strcmp(k, "-pc_type")) {
       if (a + 1 >= argc) return FISHGPU_ERR_ARG;
@@ -1438,6 +1590,7 @@ extern "C" int fishgpu_ms_solver_create(const fishgpu_ms_opts *o, void *stream, 
     // solver's CG): no persistent-solve tables, no second residual buffer
     po.persist = 0;
     po.fuse_cgr = 0;
+    if (o->vtail_points > 0) po.vtail_points = o->vtail_points;
     // default hierarchy: coarsen only down to about 33 x 33 and solve that
     // grid exactly (one block, sine transform): the V-cycle of these 2D grids
     // is launch-bound, and the deepest levels cost launches, not work
@@ -1485,6 +1638,16 @@ extern "C" int fishgpu_ms_solver_create(const fishgpu_ms_opts *o, void *stream, 
           L.vsm_off = (int)off;
         }
         cudaGetLastError();
+      }
+      // larger multigrid grids: one cooperative launch per inner solve (the
+      // V-cycle's coarse solve in block 0)
+      const long long plim = o->inner_persist < 0 ? FISHGPU_MS_PERSIST_POINTS : o->inner_persist;
+      if (!L.block1 && o->pc_type == FISHGPU_PC_MG && (long long)L.g.mx * L.g.my <= plim &&
+          solver_persist32(L.P, (const void *)k_bi_persist, o->vtail_points, &L.pa, &L.pblocks, &L.psmem)) {
+        L.persist = true;
+        const long long cap =
+            o->loop_cap > 0 ? o->loop_cap : (long long)std::max(1, o->ksp_max_it) / L.giters + 5;
+        L.max_iters = (int)std::min<long long>(cap * L.giters, 1 << 30);
       }
     }
     if (S->P.model != FISHGPU_NL_OBSTACLE) {

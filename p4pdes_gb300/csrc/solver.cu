@@ -182,6 +182,8 @@ struct fishgpu_solver_s {
   int pblocks = 0;
   // the mixed solve in one launch (k_mixed_persist): its report, device and pinned host
   fg::MixedOut *mout = nullptr, *mout_h = nullptr;
+  // another solver's persistent kernel on this hierarchy (solver_persist32): its level table
+  fg::TailLevel<float> *hplev = nullptr;
 };
 
 namespace fg {
@@ -1672,6 +1674,72 @@ bool solver_coarse32(const fishgpu_solver *S, CoarseView *c) {
   const size_t smb = coarse_smem_bytes<float>(2, lv.n[0], lv.n[1], 1);
   c->smem = (lv.n[0] * lv.n[1] > 0 && smb <= 48 * 1024) ? smb : 0;
   c->dinv = (float)(1.0 / lv.g.scdiag);
+  return true;
+}
+
+bool solver_persist32(fishgpu_solver *S, const void *kernel, long long tail_pts, PersistArgs<float> *a,
+                      int *blocks, size_t *smem) {
+  const fishgpu_opts &o = S->o;
+  Hier<float> &H = S->h32;
+  if (o.ctx.dim != 2 || o.precision != FISHGPU_MIXED || o.pc_type != FISHGPU_PC_MG ||
+      o.smooth_type != FISHGPU_SMOOTH_CHEBYSHEV || o.smooth_its != 2 || o.mg_cycles != 1 || H.nlev < 2 ||
+      H.nlev > kMaxPersistLevels)
+    return false;
+  std::vector<long long> pts(H.nlev);
+  for (int l = 0; l < H.nlev; l++) pts[l] = level_points(H.lev[l].g);
+  int btop = 0;
+  for (int l = 1; l <= H.nlev - 2; l++)
+    if (pts[l] <= tail_pts) btop = l;
+  int dev = 0, coop = 0, nsm = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || !coop || nsm < 1) {
+    cudaGetLastError();
+    return false;
+  }
+  size_t coarse = 0, psmem = 0;
+  int copy_off = -1;
+  tail_smem_plan(2, H.lev[0].n, sizeof(float), btop, pts.data(), &coarse, &copy_off, &psmem);
+  if (!allow_smem(kernel, psmem)) {
+    copy_off = -1;
+    psmem = coarse;
+  }
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 512, psmem) != cudaSuccess || per_sm < 1) {
+    cudaGetLastError();
+    return false;
+  }
+  if (!S->hplev) {  // the fine level's b is the caller's right-hand side (formed on the fly)
+    std::vector<TailLevel<float>> tl(H.nlev);
+    for (int l = 0; l < H.nlev; l++) tl[l] = tail_level<float>(H.lev[l], l > 0);
+    if (dalloc(S, &S->hplev, (size_t)H.nlev) ||
+        cudaMemcpyAsync(S->hplev, tl.data(), sizeof(TailLevel<float>) * H.nlev, cudaMemcpyHostToDevice, S->stream) !=
+            cudaSuccess) {
+      cudaGetLastError();
+      S->hplev = nullptr;
+      return false;
+    }
+  }
+  if (!S->pbar && (dalloc(S, &S->pbar, 2) || dalloc(S, &S->ppart, (size_t)4 * nsm))) return false;
+  memset(a, 0, sizeof(*a));
+  a->lv = S->hplev;
+  a->top = H.nlev - 1;
+  a->btop = btop;
+  a->part = S->ppart;
+  a->bar = S->pbar;
+  a->fault = S->fault;
+  const Level<float> &c = H.lev[0];
+  a->S0 = c.S[0];
+  a->S1 = c.S[1];
+  a->S2 = c.S[2];
+  a->ilam = c.ilam;
+  a->work = c.work;
+  a->n0 = c.n[0];
+  a->n1 = c.n[1];
+  a->n2 = c.n[2];
+  a->smem = coarse ? 1 : 0;
+  a->dinv = (float)(1.0 / c.g.scdiag);
+  a->copy_off = copy_off;
+  *blocks = (int)std::max<long long>(1, std::min<long long>(nsm, (pts[H.nlev - 1] + 511) / 512));
+  *smem = psmem;
   return true;
 }
 

@@ -421,11 +421,10 @@ struct PersistArgs {
 };
 
 // Per-thread partial sums -> one partial per block -> barrier -> every block
-// sums the partials in the same order and runs the finaliser on its copy of
-// the KSP state.  Returns false when a barrier gave up.
-template <int NV>
-__device__ __forceinline__ bool grid_reduce(double (&v)[NV], double *part, int &slot, GridBar *gb, KspState *ks,
-                                            Fin fin, double *out = nullptr) {
+// sums the partials in the same order and thread 0 calls fin(sums) (on the
+// block's copy of the solver state).  Returns false when a barrier gave up.
+template <int NV, class FN>
+__device__ __forceinline__ bool grid_reduce_fn(double (&v)[NV], double *part, int &slot, GridBar *gb, const FN &fin) {
   block_sum<NV>(v);
   const int nb = gridDim.x;
   if (threadIdx.x == 0)
@@ -440,11 +439,18 @@ __device__ __forceinline__ bool grid_reduce(double (&v)[NV], double *part, int &
       for (int b = threadIdx.x; b < nb; b += 32) s[q] += __ldcg(&part[(slot * 2 + q) * nb + b]);
     }
     warp_sum<NV>(s);
-    if (threadIdx.x == 0) ksp_finalize(ks, fin, s, NV, out);
+    if (threadIdx.x == 0) fin(s);
   }
   __syncthreads();
   slot ^= 1;  // the next reduction writes the other slot: no block still reads this one after the next barrier
   return true;
+}
+
+// grid_reduce_fn with a KSP finaliser on the block's copy of the KSP state
+template <int NV>
+__device__ __forceinline__ bool grid_reduce(double (&v)[NV], double *part, int &slot, GridBar *gb, KspState *ks,
+                                            Fin fin, double *out = nullptr) {
+  return grid_reduce_fn<NV>(v, part, slot, gb, [&](double *t) { ksp_finalize(ks, fin, t, NV, out); });
 }
 
 // b - A x at (i, j, k) from values by coordinates (resid_at's operations;
@@ -531,6 +537,148 @@ __device__ void persist_setup(const PersistArgs<T> &a, PersistShared<T> &sh, uns
   }
 }
 
+// Calls f(n, i, j, k) for this thread's points of a level: points are dealt
+// to the blocks of a persistent launch in warp-sized runs, round robin, so a
+// small level's points spread over all SMs (FP64 work on one SM is slow) and
+// every warp still reads consecutive points.
+template <int DIM, class F>
+__device__ __forceinline__ void persist_each(const Geom &g, F &&f) {
+  const int tid = threadIdx.x;
+  const long long gt = ((long long)(tid >> 5) * gridDim.x + blockIdx.x) * 32 + (tid & 31);
+  const long long G = (long long)gridDim.x * blockDim.x;
+  const int N = level_npts<DIM>(g);
+  if (N < (1 << 24)) {
+    const LevelDiv dv(g);
+    for (long long q = gt; q < N; q += G) {
+      int i, j, k;
+      const long long n = level_pos_f<DIM>(g, dv, (int)q, 0, i, j, k);
+      f(n, i, j, k);
+    }
+  } else {
+    for (long long q = gt; q < N; q += G) {
+      int i, j, k;
+      const long long n = level_pos<DIM>(g, (int)q, 0, i, j, k);
+      f(n, i, j, k);
+    }
+  }
+}
+
+// The V-cycle from zero of a persistent launch (enq_pc's V-cycle, two
+// Chebyshev/Jacobi steps per level) into lv[top].X[0], on the fine
+// right-hand side bfin(m): an array, or values formed on the fly (bfin is
+// read at the points and their neighbours in the finest level's passes, so
+// what it reads may change only in its last pass, at the point itself).
+//   first(rr) runs after the first pass of the finest level (rr: this
+//     thread's sum of bfin^2 there); it ends that phase and returns 0 when a
+//     barrier gave up, 1 to go on, 2 when the rest is not needed;
+//   last(n, i, j, k, v, bv) runs for every fine point in the last pass (v the
+//     V-cycle's value, bv = bfin(n)); end() ends that phase (a reduction or a
+//     barrier) and returns false when a barrier gave up.
+// Returns false when a barrier gave up, true at the end or when first
+// returned 2.  Levels btop .. 0 run in block 0 (vtail_run); FUSE_RR fuses the
+// residual with its restriction, FUSE_PC the prolongation with the first
+// post-smoothing step (FP32 2D only: their 3D forms repeat 27 and 7 point
+// evaluations and measured slower).  Values formed on the fly are the same
+// operations as their stored forms, so every point's value is the
+// launch-per-phase V-cycle's.
+template <int DIM, typename T, class BF, class FIRST, class LAST, class END>
+__device__ bool persist_vcycle(const PersistArgs<T> &a, PersistShared<T> &sh, unsigned char *fg_tail_sm,
+                               const BF &bfin, const FIRST &first, const LAST &last, const END &end) {
+  constexpr bool FUSE_RR = sizeof(T) == 4 && DIM == 2, FUSE_PC = FUSE_RR;
+  const TailLevel<T> *lv = sh.lv;
+  auto sync = [&]() { return grid_sync(&sh.gb); };
+  for (int l = a.top; l > a.btop; l--) {
+    const TailLevel<T> &L = lv[l];
+    const TailLevel<T> &C = lv[l - 1];
+    const Geom &g = L.g;
+    const Wv<T> w(g);
+    const bool fine = l == a.top;
+    auto bval = [&](long long m) -> T { return fine ? bfin(m) : L.b[m]; };
+    T rr = T(0);
+    persist_each<DIM>(g, [&](long long n, int i, int j, int k) {  // x1 = a0 b - a1 A b (v_cheb2_zero)
+      const T bc = bval(n);
+      T mab;
+      if (fine) mab = resid_at<DIM, T>(g, w, bfin, n, i, j, k, T(0));
+      else mab = resid_pt<DIM, T>(g, w, L.b, n, i, j, k, T(0));
+      L.X[1][n] = fma(L.a1, mab, L.a0 * bc);
+      rr = fma(bc, bc, rr);
+    });
+    if (fine) {
+      const int f = first(rr);
+      if (f != 1) return f == 2;
+    } else if (!sync()) {
+      return false;
+    }
+    if constexpr (FUSE_RR) {
+      auto rf = [&](int ii, int jj, int kk) -> T {  // the fine residual b - A x1 (v_resid)
+        if (ii >= g.mx) return T(0);
+        const long long m = (long long)kk * g.plane + (long long)jj * g.pitch + ii;
+        return resid_pt<DIM, T>(g, w, L.X[1], m, ii, jj, kk, bval(m));
+      };
+      persist_each<DIM>(C.g, [&](long long m, int I, int J, int K) { C.b[m] = restrict_ijk<DIM, T>(g, rf, I, J, K); });
+    } else {
+      persist_each<DIM>(g, [&](long long n, int i, int j, int k) {  // r = b - A x1 (v_resid)
+        L.r[n] = resid_pt<DIM, T>(g, w, L.X[1], n, i, j, k, bval(n));
+      });
+      if (!sync()) return false;
+      persist_each<DIM>(C.g, [&](long long m, int I, int J, int K) { C.b[m] = restrict_pt<DIM, T>(g, L.r, I, J, K); });
+    }
+    if (!sync()) return false;
+  }
+  if (blockIdx.x == 0)  // smem 2: the coarse tables are staged
+    vtail_run<DIM, T>(lv, a.btop, 0, a.S0, a.S1, a.S2, a.ilam, a.work, a.n0, a.n1, a.n2, a.smem ? 2 : 0, a.dinv,
+                      fg_tail_sm, a.copy_off, sh.sv);
+  if (!sync()) return false;
+  for (int l = a.btop + 1; l <= a.top; l++) {
+    const TailLevel<T> &L = lv[l];
+    const TailLevel<T> &C = lv[l - 1];
+    const Geom &g = L.g;
+    const Wv<T> w(g);
+    const bool fine = l == a.top;
+    auto bval = [&](long long m) -> T { return fine ? bfin(m) : L.b[m]; };
+    // x1' = x1 + P x_c and x2 = x1' + c1 (b - A x1'); x1' ends in xs
+    T *xs;
+    if constexpr (FUSE_PC) {
+      // x1' formed at the neighbours too, kept in X[0] (X[1] is still read there)
+      auto x1p = [&](int ii, int jj, int kk) -> T {
+        const long long m = (long long)(DIM >= 3 ? kk : 0) * g.plane + (long long)jj * g.pitch + ii;
+        return prolong_add<DIM, T>(C.g, C.X[0], ii, jj, kk, L.X[1][m]);
+      };
+      persist_each<DIM>(g, [&](long long n, int i, int j, int k) {
+        const T xc = x1p(i, j, k);
+        const T r = resid_ijk<DIM, T>(g, w, x1p, i, j, k, bval(n));
+        L.X[0][n] = xc;
+        L.X[2][n] = fma(L.c1, r, T(1) * xc);
+      });
+      xs = L.X[0];
+    } else {
+      persist_each<DIM>(g, [&](long long n, int i, int j, int k) {  // v_prolong, in place
+        L.X[1][n] = prolong_add<DIM, T>(C.g, C.X[0], i, j, k, L.X[1][n]);
+      });
+      if (!sync()) return false;
+      persist_each<DIM>(g, [&](long long n, int i, int j, int k) {  // v_cheb without x_{k-1}
+        const T r = resid_pt<DIM, T>(g, w, L.X[1], n, i, j, k, bval(n));
+        L.X[2][n] = fma(L.c1, r, T(1) * L.X[1][n]);
+      });
+      xs = L.X[1];
+    }
+    if (!sync()) return false;
+    persist_each<DIM>(g, [&](long long n, int i, int j, int k) {  // x0 = ckm1 x1' + ck x2 + crd (b - A x2)
+      const T bv = bval(n);
+      const T r = resid_pt<DIM, T>(g, w, L.X[2], n, i, j, k, bv);
+      const T v = fma(L.crd, r, fma(L.ckm1, xs[n], L.ck * L.X[2][n]));
+      L.X[0][n] = v;
+      if (fine) last(n, i, j, k, v, bv);
+    });
+    if (fine) {
+      if (!end()) return false;
+    } else if (!sync()) {
+      return false;
+    }
+  }
+  return true;
+}
+
 // One CG solve (run_ksp's work) on the state in sh.ks: the set-up from r (or
 // from src64 scaled by 1/sqrt(*rr64), when src64 is given), the iterations
 // until the state stops (or a.max_iters ran: false in *it_out's count), and
@@ -543,44 +691,17 @@ __device__ bool persist_cg(const PersistArgs<T> &a, const double *src64, const d
   KspState &ks = sh.ks;
   GridBar &gb = sh.gb;
   const TailLevel<T> *lv = sh.lv;
-  const TailLevel<T> *sv = sh.sv;
-  // points are dealt to the blocks in warp-sized runs, round robin: a small
-  // level's points spread over all SMs (FP64 work on one SM is slow) and
-  // every warp still reads consecutive points
-  const long long gt = ((long long)(tid >> 5) * gridDim.x + blockIdx.x) * 32 + (tid & 31);
-  const long long G = (long long)gridDim.x * blockDim.x;
   auto sync = [&]() { return grid_sync(&gb); };
-  auto each = [&](const Geom &g, auto &&f) {
-    const int N = level_npts<DIM>(g);
-    if (N < (1 << 24)) {
-      const LevelDiv dv(g);
-      for (long long q = gt; q < N; q += G) {
-        int i, j, k;
-        const long long n = level_pos_f<DIM>(g, dv, (int)q, 0, i, j, k);
-        f(n, i, j, k);
-      }
-    } else {
-      for (long long q = gt; q < N; q += G) {
-        int i, j, k;
-        const long long n = level_pos<DIM>(g, (int)q, 0, i, j, k);
-        f(n, i, j, k);
-      }
-    }
-  };
+  auto each = [&](const Geom &g, auto &&f) { persist_each<DIM>(g, f); };
   const TailLevel<T> &F = lv[a.top];
   const Geom &gf = F.g;
   const Wv<T> wf(gf);
   T *z = F.X[0];
 
-  // Fusions that save a barrier by forming values on the fly.  They repeat
-  // arithmetic (a neighbour's value is formed by every point that reads it),
-  // which pays in FP32 only: FP64 throughput on this part is 1/64 of FP32's.
-  // FUSE_R: the CG residual update r - alpha w inside the first smoothing
-  // pass; FUSE_RR: residual + restriction, FUSE_PC: prolongation + first
-  // post-smoothing step (2D only: their 3D forms repeat 27 and 7 point
-  // evaluations and measured slower).
+  // FUSE_R: the CG residual update r - alpha w inside the first smoothing pass
+  // of the V-cycle (FP32 only: a neighbour's value is formed by every point
+  // that reads it, and FP64 throughput on this part is 1/64 of FP32's).
   constexpr bool FUSE_R = sizeof(T) == 4;
-  constexpr bool FUSE_RR = FUSE_R && DIM == 2, FUSE_PC = FUSE_R && DIM == 2;
 
   // V-cycle from zero into z on r.  upd (FUSE_R): on r - al w, the CG
   // residual update of this iteration, stored by the last pass; unprec: its
@@ -589,106 +710,29 @@ __device__ bool persist_cg(const PersistArgs<T> &a, const double *src64, const d
   // barrier gave up; true early when FIN_RR stopped the solve.
   auto vcycle = [&](Fin fin, bool upd, T al, bool unprec) -> bool {
     auto bfin = [&](long long m) -> T { return upd ? fma(-al, a.w[m], a.r[m]) : a.r[m]; };
-    for (int l = a.top; l > a.btop; l--) {
-      const TailLevel<T> &L = lv[l];
-      const TailLevel<T> &C = lv[l - 1];
-      const Geom &g = L.g;
-      const Wv<T> w(g);
-      const bool fine = l == a.top;
-      auto bval = [&](long long m) -> T { return fine ? bfin(m) : L.b[m]; };
-      T rr = T(0);
-      each(g, [&](long long n, int i, int j, int k) {  // x1 = a0 b - a1 A b (v_cheb2_zero)
-        const T bc = bval(n);
-        T mab;
-        if (fine) mab = resid_at<DIM, T>(g, w, bfin, n, i, j, k, T(0));
-        else mab = resid_pt<DIM, T>(g, w, L.b, n, i, j, k, T(0));
-        L.X[1][n] = fma(L.a1, mab, L.a0 * bc);
-        rr = fma(bc, bc, rr);
-      });
-      if (fine && upd && unprec) {
+    auto first = [&](T rr) -> int {
+      if (upd && unprec) {
         double v1[1] = {(double)rr};
-        if (!grid_reduce<1>(v1, a.part, slot, &gb, &ks, FIN_RR)) return false;
+        if (!grid_reduce<1>(v1, a.part, slot, &gb, &ks, FIN_RR)) return 0;
         if (ks.done) {  // r stored; the rest of the V-cycle is not needed
-          each(g, [&](long long n, int, int, int) { a.r[n] = bfin(n); });
-          return true;
+          each(gf, [&](long long n, int, int, int) { a.r[n] = bfin(n); });
+          return 2;
         }
-      } else if (!sync()) {
-        return false;
+        return 1;
       }
-      if constexpr (FUSE_RR) {
-        auto rf = [&](int ii, int jj, int kk) -> T {  // the fine residual b - A x1 (v_resid)
-          if (ii >= g.mx) return T(0);
-          const long long m = (long long)kk * g.plane + (long long)jj * g.pitch + ii;
-          return resid_pt<DIM, T>(g, w, L.X[1], m, ii, jj, kk, bval(m));
-        };
-        each(C.g, [&](long long m, int I, int J, int K) { C.b[m] = restrict_ijk<DIM, T>(g, rf, I, J, K); });
-      } else {
-        each(g, [&](long long n, int i, int j, int k) {  // r = b - A x1 (v_resid)
-          L.r[n] = resid_pt<DIM, T>(g, w, L.X[1], n, i, j, k, bval(n));
-        });
-        if (!sync()) return false;
-        each(C.g, [&](long long m, int I, int J, int K) { C.b[m] = restrict_pt<DIM, T>(g, L.r, I, J, K); });
-      }
-      if (!sync()) return false;
-    }
-    if (blockIdx.x == 0)  // smem 2: the coarse tables are staged
-      vtail_run<DIM, T>(lv, a.btop, 0, a.S0, a.S1, a.S2, a.ilam, a.work, a.n0, a.n1, a.n2, a.smem ? 2 : 0, a.dinv,
-                        fg_tail_sm, a.copy_off, sv);
-    if (!sync()) return false;
-    for (int l = a.btop + 1; l <= a.top; l++) {
-      const TailLevel<T> &L = lv[l];
-      const TailLevel<T> &C = lv[l - 1];
-      const Geom &g = L.g;
-      const Wv<T> w(g);
-      const bool fine = l == a.top;
-      auto bval = [&](long long m) -> T { return fine ? bfin(m) : L.b[m]; };
-      // x1' = x1 + P x_c and x2 = x1' + c1 (b - A x1'); x1' ends in xs
-      T *xs;
-      if constexpr (FUSE_PC) {
-        // x1' formed at the neighbours too, kept in X[0] (X[1] is still read there)
-        auto x1p = [&](int ii, int jj, int kk) -> T {
-          const long long m = (long long)(DIM >= 3 ? kk : 0) * g.plane + (long long)jj * g.pitch + ii;
-          return prolong_add<DIM, T>(C.g, C.X[0], ii, jj, kk, L.X[1][m]);
-        };
-        each(g, [&](long long n, int i, int j, int k) {
-          const T xc = x1p(i, j, k);
-          const T r = resid_ijk<DIM, T>(g, w, x1p, i, j, k, bval(n));
-          L.X[0][n] = xc;
-          L.X[2][n] = fma(L.c1, r, T(1) * xc);
-        });
-        xs = L.X[0];
-      } else {
-        each(g, [&](long long n, int i, int j, int k) {  // v_prolong, in place
-          L.X[1][n] = prolong_add<DIM, T>(C.g, C.X[0], i, j, k, L.X[1][n]);
-        });
-        if (!sync()) return false;
-        each(g, [&](long long n, int i, int j, int k) {  // v_cheb without x_{k-1}
-          const T r = resid_pt<DIM, T>(g, w, L.X[1], n, i, j, k, bval(n));
-          L.X[2][n] = fma(L.c1, r, T(1) * L.X[1][n]);
-        });
-        xs = L.X[1];
-      }
-      if (!sync()) return false;
-      T zz = T(0), zr = T(0);
-      each(g, [&](long long n, int i, int j, int k) {  // x0 = ckm1 x1' + ck x2 + crd (b - A x2)
-        const T bv = bval(n);
-        const T r = resid_pt<DIM, T>(g, w, L.X[2], n, i, j, k, bv);
-        const T v = fma(L.crd, r, fma(L.ckm1, xs[n], L.ck * L.X[2][n]));
-        L.X[0][n] = v;
-        if (fine) {
-          zz = fma(v, v, zz);
-          zr = fma(v, bv, zr);
-          if (upd) a.r[n] = bv;
-        }
-      });
-      if (fine) {
-        double v2[2] = {(double)zz, (double)zr};
-        if (!grid_reduce<2>(v2, a.part, slot, &gb, &ks, fin)) return false;
-      } else if (!sync()) {
-        return false;
-      }
-    }
-    return true;
+      return sync() ? 1 : 0;
+    };
+    T zz = T(0), zr = T(0);
+    auto last = [&](long long n, int, int, int, T v, T bv) {
+      zz = fma(v, v, zz);
+      zr = fma(v, bv, zr);
+      if (upd) a.r[n] = bv;
+    };
+    auto end = [&]() -> bool {
+      double v2[2] = {(double)zz, (double)zr};
+      return grid_reduce<2>(v2, a.part, slot, &gb, &ks, fin);
+    };
+    return persist_vcycle<DIM, T>(a, sh, fg_tail_sm, bfin, first, last, end);
   };
 
   // ---- set-up (enq_cg_init)

@@ -211,3 +211,33 @@ def test_one_block_inner_solve_matches_the_launch_per_phase_form(cuda, args):
         assert r1.reason[k] > 0 and r0.reason[k] > 0
         assert r1.its[k] == r0.its[k]
     assert np.max(np.abs(u1 - u0)) <= 1e-8 * np.max(np.abs(u0))
+
+
+@pytest.mark.parametrize("kind,args", [
+    ("minimal", "-da_grid_x 33 -da_grid_y 33 -snes_grid_sequence 3 -snes_rtol 1e-10"),
+    ("minimal", "-da_refine 2 -snes_grid_sequence 4 -ms_problem tent -ms_tent_H 0.5 -snes_rtol 1e-10"),
+    ("bratu", "-da_refine 7 -snes_rtol 1e-10"),
+    ("obstacle", "-da_refine 2 -snes_grid_sequence 5"),
+])
+def test_persistent_inner_solve_matches_the_launch_per_phase_form(cuda, kind, args):
+    """On multigrid grids the inner BiCGStab solve runs as one cooperative
+    launch (k_bi_persist, the default up to FISHGPU_MS_PERSIST_POINTS nodes):
+    the same iteration, V-cycle values and finalisers as the launch-per-phase
+    graphs, the dot products summed in another order, so every grid takes the
+    same Newton steps and ends at the same solution to the Newton tolerance."""
+    import p4pdes_gb300 as fg
+    opts = {"minimal": fg.ms_options, "bratu": fg.bratu_options, "obstacle": fg.obstacle_options}[kind]
+    r1 = fg.ms_solve(opts(args))
+    r0 = fg.ms_solve(opts(args + " -ms_inner_persist 0"))
+    (u1, rep1), (u0, rep0) = r1, r0
+    assert rep1.ngrids == rep0.ngrids
+    for k in range(rep0.ngrids):
+        assert rep1.reason[k] > 0 and rep0.reason[k] > 0
+        assert rep1.its[k] == rep0.its[k]
+        small = rep0.m[k] ** 2 <= 4096 and rep0.inner_form[k] == 1  # one block (k_bi_block) either way
+        assert rep0.inner_form[k] == (1 if small else 0)
+        assert rep1.inner_form[k] == (1 if small else 2)
+    assert any(rep1.inner_form[k] == 2 for k in range(rep1.ngrids))
+    inner1, inner0 = rep1.total_ksp_its, rep0.total_ksp_its
+    assert abs(inner1 - inner0) <= max(2, inner0 // 20)
+    assert np.max(np.abs(u1 - u0)) <= 1e-8 * np.max(np.abs(u0))
