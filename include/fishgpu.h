@@ -217,7 +217,18 @@ typedef struct {
                                instead of two, a second r buffer; MG with
                                two Chebyshev steps; default 1,
                                bit-identical to 0)                        */
+  int coop_tail;            /* -fsh_coop_tail N: in launch-per-phase solves
+                               of a single grid, the V-cycle's levels from
+                               the largest of at most N nodes (below the
+                               finest) down run as ONE cooperative launch,
+                               a grid-wide barrier between phases (MG with
+                               two Chebyshev steps, V-cycles; bit-identical
+                               to 0).  0 (default): off, measured no faster
+                               than the graphs' launches; -1:
+                               FISHGPU_COOP_TAIL_POINTS                   */
 } fishgpu_opts;
+
+#define FISHGPU_COOP_TAIL_POINTS 300000
 
 #define FISHGPU_MAX_HIST 512
 #define FISHGPU_MAX_OUTER 32

@@ -90,10 +90,12 @@ static void make_opts(const fishgpu_server_opts &so, int dim, int n, fishgpu_opt
   o->precision = so.precision;
   o->rtol = so.rtol;
   o->norm_type = FISHGPU_NORM_UNPRECONDITIONED;
-  // no persistent solves: one holds a block on every SM for the whole solve,
-  // which serialises the concurrent solves a server overlaps (measured on the
-  // serving stream: 978 against 1156 solves/s with them)
+  // no persistent solves (nor cooperative V-cycle tails): one holds a block
+  // on every SM for the whole solve, which serialises the concurrent solves a
+  // server overlaps (measured on the serving stream: 978 against 1156
+  // solves/s with them)
   o->persist = 0;
+  o->coop_tail = 0;
 }
 
 static void group_opts(const fishgpu_server_opts &so, fishgpu_batch_opts *bo) {

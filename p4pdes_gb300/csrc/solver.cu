@@ -75,6 +75,11 @@ struct Hier {
   size_t psmem = 0;              // dynamic shared memory of the persistent solve (coarse scratch, tail copy)
   size_t pcoarse = 0;            // the coarse solve's scratch (0: its work area in global memory)
   int pcopy = -1;                // offset of block 0's tail copy (-1: none)
+  // the cooperative V-cycle tail (k_vtail_coop): levels 0 .. ctail_top in one launch
+  int ctail_top = 0;  // 0: none
+  int ctail_blocks = 0;
+  size_t ctail_smem = 0;
+  PersistArgs<T> ctail{};  // its level table, coarse solve and barrier (no KSP vectors)
 };
 
 // Threads per block of the slot kernels of a level: 128 on 2D grids (twice
@@ -442,6 +447,84 @@ static int build_persist(fishgpu_solver *S, Hier<T> &H) {
   return FISHGPU_OK;
 }
 
+// The cooperative V-cycle tail of a launch-per-phase solve of a single grid:
+// levels up to coop_tail nodes below the finest (the largest of them and
+// everything under it) as one launch of k_vtail_coop, for V-cycles of two
+// Chebyshev/Jacobi steps.  Below it, levels of at most 1200 (FP32) / 300
+// (FP64) nodes run in block 0, as in the persistent solve.  Only when it
+// reaches above the one-block tail (k_vtail).
+template <typename T>
+static int build_ctail(fishgpu_solver *S, Hier<T> &H) {
+  const fishgpu_opts &o = S->o;
+  H.ctail_top = 0;
+  const int dim = S->fine.dim;
+  if (!o.coop_tail || S->batch || !S->fault || o.pc_type != FISHGPU_PC_MG || o.smooth_type != FISHGPU_SMOOTH_CHEBYSHEV ||
+      o.smooth_its != 2 || o.mg_cycles != 1 || dim < 2 || H.nlev < 3 || H.nlev > kMaxPersistLevels)
+    return FISHGPU_OK;
+  const long long lim = o.coop_tail > 0 ? o.coop_tail : FISHGPU_COOP_TAIL_POINTS;
+  std::vector<long long> pts(H.nlev);
+  for (int l = 0; l < H.nlev; l++) pts[l] = level_points(H.lev[l].g);
+  int top = 0;
+  for (int l = 1; l <= H.nlev - 2; l++)
+    if (pts[l] <= lim) top = l;
+  if (top <= H.tail_top) return FISHGPU_OK;
+  const long long tmax = sizeof(T) == 8 ? 300 : 1200;
+  int btop = 0;
+  for (int l = 1; l < top; l++)
+    if (pts[l] <= tmax) btop = l;
+  int dev = 0, coop = 0, nsm = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || !coop || nsm < 1) {
+    cudaGetLastError();
+    return FISHGPU_OK;
+  }
+  size_t coarse = 0, psmem = 0;
+  int copy_off = -1;
+  tail_smem_plan(dim, H.lev[0].n, sizeof(T), btop, pts.data(), &coarse, &copy_off, &psmem);
+  const void *fn = dim == 2 ? (const void *)k_vtail_coop<2, T> : (const void *)k_vtail_coop<3, T>;
+  if (!allow_smem(fn, psmem)) {
+    copy_off = -1;
+    psmem = coarse;
+  }
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 512, psmem) != cudaSuccess || per_sm < 1) {
+    cudaGetLastError();
+    return FISHGPU_OK;
+  }
+  std::vector<TailLevel<T>> tl(top + 1);
+  for (int l = 0; l <= top; l++) tl[l] = tail_level<T>(H.lev[l], l > 0);
+  TailLevel<T> *dtl = nullptr;
+  int rc;
+  if ((rc = dalloc(S, &dtl, (size_t)(top + 1)))) return rc;
+  if (cudaMemcpyAsync(dtl, tl.data(), sizeof(TailLevel<T>) * (top + 1), cudaMemcpyHostToDevice, S->stream) !=
+      cudaSuccess)
+    return FISHGPU_ERR_CUDA;
+  if (!S->pbar && ((rc = dalloc(S, &S->pbar, 2)) || (rc = dalloc(S, &S->ppart, (size_t)4 * nsm)))) return rc;
+  PersistArgs<T> &a = H.ctail;
+  memset(&a, 0, sizeof(a));
+  a.lv = dtl;
+  a.top = top;
+  a.btop = btop;
+  a.part = S->ppart;
+  a.bar = S->pbar;
+  a.fault = S->fault;
+  const Level<T> &c = H.lev[0];
+  a.S0 = c.S[0];
+  a.S1 = c.S[1];
+  a.S2 = c.S[2];
+  a.ilam = c.ilam;
+  a.work = c.work;
+  a.n0 = c.n[0];
+  a.n1 = c.n[1];
+  a.n2 = c.n[2];
+  a.smem = coarse ? 1 : 0;
+  a.dinv = (T)(1.0 / c.g.scdiag);
+  a.copy_off = copy_off;
+  H.ctail_blocks = (int)std::max<long long>(1, std::min<long long>(nsm, (pts[top] + 511) / 512));
+  H.ctail_smem = psmem;
+  H.ctail_top = top;
+  return FISHGPU_OK;
+}
+
 template <typename T>
 static int build_hier(fishgpu_solver *S, Hier<T> &H) {
   const fishgpu_opts &o = S->o;
@@ -518,6 +601,7 @@ static int build_hier(fishgpu_solver *S, Hier<T> &H) {
     for (int d = c.g.dim; d < 3; d++) c.S[d] = c.S[0];  // unused
   }
   if ((rc = build_tail<T>(S, H))) return rc;
+  if ((rc = build_ctail<T>(S, H))) return rc;
   return build_persist<T>(S, H);
 }
 
@@ -705,6 +789,22 @@ static void enq_vcycle(fishgpu_solver *S, Hier<T> &H, int l, bool from_zero, int
   cudaStream_t s = S->stream;
   KspState *st = S->st;
   if constexpr (DIM >= 2) {
+    if (l > 0 && l == H.ctail_top && from_zero && dots < 0 && !ru) {  // levels l .. 0 in one cooperative launch
+      cudaMemsetAsync(H.ctail.bar, 0, 2 * sizeof(unsigned), s);
+      cudaLaunchConfig_t cfg = {};
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeCooperative;
+      at[0].val.cooperative = 1;
+      cfg.gridDim = dim3(H.ctail_blocks);
+      cfg.blockDim = dim3(512);
+      cfg.dynamicSmemBytes = H.ctail_smem;
+      cfg.stream = s;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      cudaLaunchKernelEx(&cfg, k_vtail_coop<DIM, T>, H.ctail, (const KspState *)st);
+      for (int q = 0; q <= l; q++) H.lev[q].cur = 0;  // every level ends with its iterate in X[0]
+      return;
+    }
     if (l > 0 && l == H.tail_top && from_zero && dots < 0) {  // levels l .. 0 in one block per instance
       const Level<T> &c = H.lev[0];
       k_vtail<DIM, T><<<DIM < 3 && S->batch ? (unsigned)S->nplanes : 1u, H.tail_threads, H.tail_smem, s>>>(

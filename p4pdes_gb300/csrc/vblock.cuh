@@ -856,6 +856,26 @@ __global__ void __launch_bounds__(512, 1) k_ksp_persist(PersistArgs<T> a) {
   }
 }
 
+// ------------------------------------------------------------------ the V-cycle tail in one cooperative launch
+// Levels a.top .. 0 of a launch-per-phase V-cycle from zero (enq_vcycle below
+// the levels that keep a launch per phase): persist_vcycle on level top's
+// stored b, its result in X[0] of every level (as k_vtail leaves it).  The
+// KSP state is read once: it does not change inside a V-cycle, so every block
+// returns, or runs every barrier.  *a.bar must be zero at the launch.
+template <int DIM, typename T>
+__global__ void __launch_bounds__(512, 1) k_vtail_coop(PersistArgs<T> a, const KspState *st) {
+  extern __shared__ __align__(16) unsigned char fg_tail_sm[];
+  __shared__ PersistShared<T> sh;
+  if (ksp_done(st)) return;
+  persist_setup<DIM, T>(a, sh, fg_tail_sm);
+  const T *b = sh.lv[a.top].b;
+  auto bf = [&](long long m) -> T { return b[m]; };
+  auto first = [&](T) -> int { return grid_sync(&sh.gb) ? 1 : 0; };
+  auto last = [](long long, int, int, int, T, T) {};
+  auto end = []() -> bool { return true; };  // the launch's end orders the writes for the next kernel
+  persist_vcycle<DIM, T>(a, sh, fg_tail_sm, bf, first, last, end);
+}
+
 // ------------------------------------------------------------------ the mixed solve in one launch
 // FP64 iterative refinement around the FP32 inner CG (solve_dim's mixed
 // loop), all on the device: the stop tests and inner tolerances in every

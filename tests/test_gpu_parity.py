@@ -554,6 +554,33 @@ def test_vcycle_tail_is_bit_identical(cuda, args):
     assert a.launches <= b.launches  # fewer wherever a level is small enough for the tail
 
 
+@pytest.mark.parametrize("args", [
+    "-fsh_dim 2 -fsh_problem manupoly -da_refine 8 -pc_type mg -mg_levels_ksp_type chebyshev "
+    "-mg_levels_pc_type jacobi -ksp_rtol 1e-10 -fsh_coop_tail -1",
+    "-fsh_dim 2 -fsh_problem manupoly -da_refine 9 -pc_type mg -ksp_rtol 1e-10 -fsh_precision mixed -fsh_coop_tail -1",
+    "-fsh_dim 2 -fsh_problem manupoly -da_grid_x 5 -da_grid_y 3 -da_refine 7 -pc_type mg -ksp_rtol 1e-10 -fsh_cy 3 "
+    "-ksp_norm_type unpreconditioned -fsh_coop_tail 20000",
+    "-fsh_dim 3 -fsh_problem manupoly -da_refine 6 -pc_type mg -ksp_rtol 1e-10 -fsh_coop_tail -1",
+    "-fsh_dim 3 -fsh_problem manuexp -da_refine 6 -pc_type mg -ksp_rtol 1e-10 -fsh_precision mixed -fsh_coop_tail -1",
+    "-fsh_dim 3 -fsh_problem manupoly -da_grid_x 3 -da_grid_y 5 -da_grid_z 9 -da_refine 3 -pc_type mg "
+    "-ksp_rtol 1e-10 -fsh_cz 2 -fsh_precision mixed -fsh_coop_tail 6000",
+])
+def test_cooperative_vcycle_tail_is_bit_identical(cuda, args):
+    """The V-cycle's levels from the largest of at most coop_tail nodes down as
+    one cooperative launch (k_vtail_coop, persist_vcycle's phases with a
+    grid-wide barrier between them; an option, off by default) compute every
+    point with the operations of the per-phase kernels: the launch-per-phase
+    solve is identical, bit for bit, with and without it, in fewer launches."""
+    import torch
+    fg = fgmod()
+    u1, a = fg.solve(fg.options(args + " -fsh_persist 0"))
+    u0, b = fg.solve(fg.options(args + " -fsh_persist 0 -fsh_coop_tail 0"))
+    assert a.reason == b.reason == 2 and a.its == b.its and a.outer_its == b.outer_its
+    assert a.history() == b.history()
+    assert torch.equal(u1, u0)
+    assert a.launches < b.launches
+
+
 PERSIST_CASES = [
     # fish's 2D case (preconditioned norm), FP64 and mixed
     "-fsh_dim 2 -fsh_problem manupoly -da_refine 7 -pc_type mg -mg_levels_ksp_type chebyshev "
