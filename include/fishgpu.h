@@ -226,6 +226,10 @@ typedef struct {
                                to 0).  0 (default): off, measured no faster
                                than the graphs' launches; -1:
                                FISHGPU_COOP_TAIL_POINTS                   */
+  int pair_y;               /* -fsh_pair_y 0|1: the mixed form's accurate
+                               inner CG updates its FP64 correction every
+                               other iteration, two steps at a time
+                               (default 1, bit-identical to 0)            */
 } fishgpu_opts;
 
 #define FISHGPU_COOP_TAIL_POINTS 300000
@@ -301,7 +305,9 @@ int fishgpu_solve_host(const fishgpu_opts *o, const double *f_host, const double
 /* Times `reps` launches of one solver kernel on the finest level with the
    solver's resident data (CUDA events on the solver's stream).  Names:
    "smooth", "smooth_first", "smooth_dots", "smooth_zero", "post2", "cgp_apply",
-   "cgp_apply_acc" (mixed form: the accurate inner form's apply), "cgp_apply_tma" (the same from the
+   "cgp_apply_acc" (mixed form: the accurate inner form's apply), "cgp_apply_acc_pair" (the two
+   launches the solve alternates: y64 left alone, then both owed updates; one rep is the pair),
+   "cgp_apply_tma" (the same from the
    TMA ring, 3D), "cg_update", "resid_restrict" (3D), "grid_sync" (one grid-wide barrier of the
    persistent solve; bytes 0), "demote" (mixed form: an inner solve's set-up from the FP64 residual),
    "resid", "apply", "restrict", "prolong", "residual64".  Reports the mean ms

@@ -76,7 +76,7 @@ class Opts(ctypes.Structure):
                 ("first_floor_scale", c_double), ("inner_accurate", c_int), ("fuse_restrict", c_int),
                 ("tma_apply", c_int), ("vtail", c_int),
                 ("vtail_points", c_int), ("persist", c_int), ("persist_points", c_int),
-                ("persist_tail", c_int), ("fuse_cgr", c_int), ("coop_tail", c_int)]
+                ("persist_tail", c_int), ("fuse_cgr", c_int), ("coop_tail", c_int), ("pair_y", c_int)]
 
     @property
     def dofs(self):

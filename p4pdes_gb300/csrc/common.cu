@@ -196,6 +196,7 @@ extern "C" int fishgpu_opts_default(fishgpu_opts *o) {
   o->persist = -1;
   o->fuse_cgr = 1;
   o->coop_tail = 0;
+  o->pair_y = 1;
   return FISHGPU_OK;
 }
 
@@ -269,6 +270,7 @@ extern "C" int fishgpu_opts_parse(fishgpu_opts *o, int argc, const char *const *
     else if (!strcmp(k, "-fsh_persist_tail")) { NEEDV(); o->persist_tail = atoi(v); }
     else if (!strcmp(k, "-fsh_fuse_cgr")) { NEEDV(); o->fuse_cgr = atoi(v) != 0; }
     else if (!strcmp(k, "-fsh_coop_tail")) { NEEDV(); o->coop_tail = atoi(v); }
+    else if (!strcmp(k, "-fsh_pair_y")) { NEEDV(); o->pair_y = atoi(v) != 0; }
     else if (!strcmp(k, "-fsh_inner_accurate")) { NEEDV(); o->inner_accurate = atoi(v) < 0 ? -1 : atoi(v) != 0; }
     else if (!strcmp(k, "-da_refine")) { NEEDV(); refine = atoi(v); }
     else if (!strcmp(k, "-da_grid_x")) { NEEDV(); base[0] = atoi(v); }

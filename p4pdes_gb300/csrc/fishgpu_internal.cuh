@@ -59,7 +59,9 @@ enum Fin {
   FIN_INIT_ZZZR,      // after B r0: (precond) dp = ||z||, test n=0; beta = z.r
   FIN_PW,             // dpi = p.w, alpha = beta/dpi
   FIN_RR,             // unpreconditioned: dp = ||r||, test n=i+1
-  FIN_ZZZR            // after B r: (precond) dp = ||z||, test; beta = z.r; i++
+  FIN_ZZZR,           // after B r: (precond) dp = ||z||, test; beta = z.r; i++
+  FIN_PW_DEFER        // FIN_PW after a direction update that left y alone: the
+                      // owed update (alpha, pend) moves to (alpha2, pend2)
 };
 
 struct KspState {
@@ -71,9 +73,11 @@ struct KspState {
   int done;    // nonzero: every kernel of the iteration returns at once
   int nhist;
   int pend;    // y += alpha p deferred: 0 none, 1 in p buffer 0, 2 in p buffer 1
+  int pend2;   // an older deferred y += alpha2 p (applied first), in the other buffer
   unsigned int loops;  // bodies run by the device-side solve loop (graph_loop.cuh)
   double dp, rnorm0, ttol, beta, betaold, dpi, dpiold, alpha;
   double bratio;  // beta / betaold for the next direction update (one division, in the finaliser)
+  double alpha2;  // the step of the update owed in pend2
   // Mixed form, solution accumulated in FP64: the inner solve's updates go
   // straight into the outer FP64 solution as y64 += (yscale * alpha) p, with
   // yscale the refinement step's residual norm; yfresh: y64 holds nothing yet
@@ -245,7 +249,14 @@ static __device__ __noinline__ void ksp_finalize(KspState *st, Fin fin, const do
     if (st->beta == 0.0) { st->its = 1; ksp_stop(st, R_CONVERGED_ATOL); }
     break;
   }
-  case FIN_PW: {  // w = A p done: tot = {p.w}; the previous y update was applied
+  case FIN_PW:
+  case FIN_PW_DEFER: {  // w = A p done: tot = {p.w}; the previous y update was applied (FIN_PW) or is still owed
+    if (fin == FIN_PW_DEFER) {
+      st->alpha2 = st->alpha;
+      st->pend2 = st->pend;
+    } else {
+      st->pend2 = 0;
+    }
     double dpi = tot[0];
     st->its = st->i + 1;
     st->betaold = st->beta;

@@ -934,9 +934,19 @@ static void enq_cg_iter(fishgpu_solver *S, Hier<T> &H, KspVecs<T> v, int par) {
   }
   if constexpr (sizeof(T) == 4) {
     if (!planes && v.y64) {  // accurate inner form: difference-form apply, FP64 accumulation
-      if (!(DIM == 3 && S->o.tma_apply && launch_cgp_tma(S, S->fine, st, H.z, pold, pnew, v.w, v.y64, 0)))
-        v_cgp_apply<DIM, T, false, true><<<slot_blocks(S->sfst), S->sfst.chunk, 0, s>>>(
-            S->fine, S->sfst, st, H.z, pold, pnew, v.w, v.y64, S->red, 0);
+      if (!(DIM == 3 && S->o.tma_apply && launch_cgp_tma(S, S->fine, st, H.z, pold, pnew, v.w, v.y64, 0))) {
+        if (S->o.pair_y) {  // y64 updated in pairs (a captured iteration's parity is its own)
+          if (par == 0)
+            v_cgp_apply<DIM, T, false, true, 1><<<slot_blocks(S->sfst), S->sfst.chunk, 0, s>>>(
+                S->fine, S->sfst, st, H.z, pold, pnew, v.w, v.y64, S->red, 0);
+          else
+            v_cgp_apply<DIM, T, false, true, 2><<<slot_blocks(S->sfst), S->sfst.chunk, 0, s>>>(
+                S->fine, S->sfst, st, H.z, pold, pnew, v.w, v.y64, S->red, 0);
+        } else {
+          v_cgp_apply<DIM, T, false, true><<<slot_blocks(S->sfst), S->sfst.chunk, 0, s>>>(
+              S->fine, S->sfst, st, H.z, pold, pnew, v.w, v.y64, S->red, 0);
+        }
+      }
       planes = true;
     }
   }
@@ -1668,6 +1678,14 @@ static int time_kernel_dim(fishgpu_solver *S, const char *name, int reps, double
       v_cgp_apply<DIM, float, false, true><<<gb, sl.chunk, 0, s>>>(g, sl, tst, lf.X[0], S->p32, S->q32, S->w32, S->y64,
                                                                  S->red, 1);
       *bytes = (4.0 + 4.0 + 8.0 + 4.0 + 4.0 + 8.0) * N;
+    } else if (!strcmp(name, "cgp_apply_acc_pair")) {  // the solve's pair of iterations: y left alone, then
+      // both owed updates (reads z, p_old, p_older, y64; writes p, w, y64); one rep is the two launches
+      if (!mixed) return FISHGPU_ERR_UNSUPPORTED;
+      v_cgp_apply<DIM, float, false, true, 1><<<gb, sl.chunk, 0, s>>>(g, sl, tst, lf.X[0], S->p32, S->q32, S->w32,
+                                                                    S->y64, S->red, 1);
+      v_cgp_apply<DIM, float, false, true, 2><<<gb, sl.chunk, 0, s>>>(g, sl, tst, lf.X[0], S->q32, S->p32, S->w32,
+                                                                    S->y64, S->red, 1);
+      *bytes = (4.0 + 4.0 + 4.0 + 4.0) * N + (4.0 + 4.0 + 4.0 + 8.0 + 4.0 + 4.0 + 8.0) * N;
     } else if (!strcmp(name, "cgp_apply_tma")) {  // the accurate form from the TMA ring (3D)
       if (!mixed || !launch_cgp_tma(S, g, tst, lf.X[0], S->p32, S->q32, S->w32, S->y64, 1))
         return FISHGPU_ERR_UNSUPPORTED;

@@ -613,6 +613,14 @@ __global__ void __launch_bounds__(256, MinBlocks<T>::value) v_apply_dot(Geom g, 
 // solution, y64 += (yscale * alpha) p_old (the state's yscale and yfresh), so
 // that neither the apply nor the FP32 storage of the correction limits the
 // true residual an inner solve reaches to ~kappa * 2^-24.
+// YM (the ACC form's y updates in pairs): 1 leaves y alone and keeps the owed
+// update (FIN_PW_DEFER); 2 applies both owed updates, the older one first,
+// y = fma(a, p_old, fma(a2, p_older, y)) -- the values of applying them one
+// per iteration, as the FP64 intermediate is what y would have held.  The
+// older direction is in the buffer this launch overwrites with p_new: each
+// thread reads it at its own points before its store, and no other thread
+// reads it.  Iterations alternate 1, 2 (the graphs' parity), so y moves
+// every other iteration: 16 + 36 instead of 2 x 32 bytes per node.
 // float -> double on the integer pipe (bitconv.cuh: the cast's value)
 template <typename YT, typename T>
 __device__ __forceinline__ YT to_y(T v) {
@@ -629,18 +637,21 @@ struct CgY<T, true> {
   using type = double;
 };
 
-template <int DIM, typename T, bool PL = false, bool ACC = false>
+template <int DIM, typename T, bool PL = false, bool ACC = false, int YM = 0>
 __global__ void __launch_bounds__(256, MinBlocksLean<T>::value) v_cgp_apply(Geom g, Slots s, KspState *st, const T *__restrict__ z,
                                                    const T *__restrict__ pold, T *__restrict__ pnew,
                                                    T *__restrict__ wv, typename CgY<T, ACC>::type *__restrict__ y,
                                                    Reducer red, int slot) {
   using YT = typename CgY<T, ACC>::type;
+  static_assert(YM == 0 || (ACC && !PL), "paired y updates: the accurate form of one grid");
   st = block_state_sel<PL>(st, s);
   if (ksp_done_v(st)) return;
   const SlotPos p = slot_pos_st<DIM>(g, s);
   const Wv<T> w(g);
   const bool first = !st || st->i == 0;  // no state: p = z
-  const bool pend = st && st->pend && y;
+  const bool pend = YM != 1 && st && st->pend && y;
+  const bool pend2 = YM == 2 && pend && st->pend2;
+  const YT a2 = pend2 ? (YT)(st->yscale * st->alpha2) : YT(0);
   // no update has reached y yet (it is not zero-filled); ACC: nor has an
   // earlier refinement step
   const bool yfresh = pend && st->i == 1 && (!ACC || st->yfresh);
@@ -660,21 +671,26 @@ __global__ void __launch_bounds__(256, MinBlocksLean<T>::value) v_cgp_apply(Geom
       }
       set_el(o, e, v);
     }
-    st4(pnew + n, nb.c);
-    st4(wv + n, o);
     if (pend) {  // the first update (iteration 1) starts y from 0 without reading it
       const V4<T> pp = ld4(pold + n);
-      const V4<YT> yy = yfresh ? zero4<YT>() : ld4(y + n);
+      V4<YT> yy = yfresh ? zero4<YT>() : ld4(y + n);
+      if (pend2) {  // the older direction, read before p_new replaces it
+        const V4<T> qq = ld4(pnew + n);
+        yy = V4<YT>{fma(a2, to_y<YT>(qq.x), yy.x), fma(a2, to_y<YT>(qq.y), yy.y), fma(a2, to_y<YT>(qq.z), yy.z),
+                    fma(a2, to_y<YT>(qq.w), yy.w)};
+      }
       st4(y + n, V4<YT>{fma(a, to_y<YT>(pp.x), yy.x), fma(a, to_y<YT>(pp.y), yy.y), fma(a, to_y<YT>(pp.z), yy.z),
                         fma(a, to_y<YT>(pp.w), yy.w)});
     }
+    st4(pnew + n, nb.c);
+    st4(wv + n, o);
   };
   // the first iteration (p = z) and the others (p = z + beta/betaold p_old)
   // march separately, so that no load of the common case tests `first`
   if (first) march_core<DIM, T, ACC>(g, s, p, ArraySrc<T>{z}, op);
   else march_core<DIM, T, ACC>(g, s, p, AxpySrc<T>{z, pold, (T)st->bratio}, op);
   double v1[1] = {(double)acc};
-  reduce_sel<1, PL>(v1, red, slot, st, FIN_PW, nullptr, s);
+  reduce_sel<1, PL>(v1, red, slot, st, YM == 1 ? FIN_PW_DEFER : FIN_PW, nullptr, s);
 }
 
 // The accurate form of v_cgp_apply (3D, FP32, one grid) fed by a TMA ring.
@@ -1463,7 +1479,8 @@ static __global__ void __launch_bounds__(256) v_demote_init(Geom g, Slots s, Ksp
 }
 
 // The end of an inner FP32 solve whose updates accumulate in FP64 (the ACC
-// form of v_cgp_apply): the last deferred update y64 += (yscale * alpha) p.
+// form of v_cgp_apply): the last deferred update y64 += (yscale * alpha) p,
+// after an older one the paired updates still owe (pend2).
 // y64 is read unless nothing has reached it yet (no update in this inner
 // solve and the state's yfresh: the first refinement step), in which case it
 // is written from 0.  Per plane for a batch.
@@ -1473,12 +1490,19 @@ static __global__ void __launch_bounds__(256) v_pend_acc(Geom g, Slots s, const 
   st = block_state(const_cast<KspState *>(st), s);
   if (!st) return;
   const bool keep = ksp_y_written(st) || !st->yfresh;
-  const int pend = st->pend;
-  if (keep && !pend) return;
+  const int pend = st->pend, pend2 = st->pend2;
+  if (keep && !pend && !pend2) return;
   const double a = pend ? st->yscale * st->alpha : 0.0;
+  const double a2 = pend2 ? st->yscale * st->alpha2 : 0.0;
   const float *__restrict__ pv = pend == 1 ? p0 : p1;
+  const float *__restrict__ qv = pend2 == 1 ? p0 : p1;
   FG_PW_BEGIN
   V4<double> yy = keep ? ld4(y + n) : zero4<double>();
+  if (pend2) {  // an older owed update (paired updates): first
+    const V4<float> qq = ld4(qv + n);
+    yy = V4<double>{fma(a2, f2d_bits(qq.x), yy.x), fma(a2, f2d_bits(qq.y), yy.y), fma(a2, f2d_bits(qq.z), yy.z),
+                    fma(a2, f2d_bits(qq.w), yy.w)};
+  }
   if (pend) {
     const V4<float> pp = ld4(pv + n);
     yy = V4<double>{fma(a, f2d_bits(pp.x), yy.x), fma(a, f2d_bits(pp.y), yy.y), fma(a, f2d_bits(pp.z), yy.z),

@@ -581,6 +581,30 @@ def test_cooperative_vcycle_tail_is_bit_identical(cuda, args):
     assert a.launches < b.launches
 
 
+@pytest.mark.parametrize("args", [
+    "-fsh_dim 3 -fsh_problem manupoly -da_refine 6 -pc_type mg -ksp_rtol 1e-10 -fsh_precision mixed",
+    "-fsh_dim 3 -fsh_problem manuexp -da_grid_x 5 -da_grid_y 3 -da_grid_z 9 -da_refine 4 -pc_type mg "
+    "-ksp_rtol 1e-10 -fsh_precision mixed -fsh_inner_accurate 1",
+    "-fsh_dim 2 -fsh_problem manupoly -da_refine 9 -pc_type mg -ksp_rtol 1e-10 -fsh_precision mixed",
+    "-fsh_dim 2 -fsh_problem manupoly -da_refine 8 -pc_type mg -ksp_rtol 1e-10 -fsh_precision mixed "
+    "-fsh_inner_accurate 1 -fsh_graph_iters 4 -fsh_device_loop 0",
+])
+def test_paired_y_updates_are_bit_identical(cuda, args):
+    """The accurate inner form updates its FP64 correction every other CG
+    iteration, two steps at a time, fma(a, p_old, fma(a2, p_older, y)): the
+    values of one update per iteration (the FP64 intermediate is what y would
+    have held), so the solve is identical, bit for bit, to -fsh_pair_y 0 --
+    whatever iteration the inner solves stop at (an update may still be owed
+    from two iterations back)."""
+    import torch
+    fg = fgmod()
+    u1, a = fg.solve(fg.options(args + " -fsh_persist 0"))
+    u0, b = fg.solve(fg.options(args + " -fsh_persist 0 -fsh_pair_y 0"))
+    assert a.reason == b.reason == 2 and a.its == b.its and a.outer_its == b.outer_its
+    assert a.history() == b.history()
+    assert torch.equal(u1, u0)
+
+
 PERSIST_CASES = [
     # fish's 2D case (preconditioned norm), FP64 and mixed
     "-fsh_dim 2 -fsh_problem manupoly -da_refine 7 -pc_type mg -mg_levels_ksp_type chebyshev "
