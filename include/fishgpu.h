@@ -283,6 +283,16 @@ long long fishgpu_solver_bytes(const fishgpu_solver *s);
 int fishgpu_solver_solve_host(fishgpu_solver *s, const double *f_host, const double *g_host,
                               double *u_host, fishgpu_report *rep);
 
+/* n host-array solves in order (FISHGPU_USER), each as fishgpu_solver_solve_host
+   would do it (g_host NULL, or g_host[k] NULL: zero boundary data), pipelined:
+   while problem k is solved, f_host[k+1] is copied in and u_host[k-1] out on
+   two copy streams through device staging buffers (2 more dense arrays,
+   allocated at the first call).  Pinned f_host and u_host let the copies
+   overlap the solves.  reps[k]: problem k's report (solve_ms: its solve). */
+int fishgpu_solver_solve_host_many(fishgpu_solver *s, int n, const double *const *f_host,
+                                   const double *const *g_host, double *const *u_host,
+                                   fishgpu_report *reps);
+
 /* host -> device bytes fishgpu_solver_solve_host moves for f and g (FISHGPU_USER):
    all of f; all of g, or only its boundary nodes when g_host is pinned memory
    (the solver reads g nowhere else) */

@@ -208,6 +208,9 @@ def load():
     lib.fishgpu_solve_host.argtypes = [_P(Opts), c_void_p, c_void_p, c_void_p, _P(Report)]
     lib.fishgpu_solver_solve_host.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, _P(Report)]
     lib.fishgpu_solver_solve_host.restype = c_int
+    lib.fishgpu_solver_solve_host_many.argtypes = [c_void_p, c_int, _P(c_void_p), _P(c_void_p), _P(c_void_p),
+                                                   _P(Report)]
+    lib.fishgpu_solver_solve_host_many.restype = c_int
     lib.fishgpu_batch_opts_default.argtypes = [_P(BatchOpts)]
     lib.fishgpu_batch_create.argtypes = [_P(BatchOpts), c_int, _P(c_int), _P(c_void_p)]
     lib.fishgpu_batch_solve.argtypes = [c_void_p, _P(c_void_p), _P(c_void_p), _P(BatchReport)]
@@ -415,6 +418,24 @@ class Solver:
         if rc not in (0, 4):
             raise FishError(rc, "fishgpu_solver_solve_host")
         return rep
+
+    def solve_host_many(self, fs, gs, us):
+        """Host-array solves of len(fs) problems in order, copies overlapped with the
+        solves (fishgpu_solver_solve_host_many); gs may be None.  Returns the reports."""
+        def addr(a):
+            if a is None:
+                return None
+            return a.data_ptr() if hasattr(a, "data_ptr") else a.ctypes.data
+        n = len(fs)
+        if len(us) != n or (gs is not None and len(gs) != n):
+            raise ValueError("fs, gs and us differ in length")
+        arr = lambda xs: (c_void_p * max(1, n))(*[addr(x) for x in xs])
+        reps = (Report * max(1, n))()
+        rc = load().fishgpu_solver_solve_host_many(self._h, n, arr(fs), None if gs is None else arr(gs), arr(us),
+                                                   reps)
+        if rc not in (0, 4):
+            raise FishError(rc, "fishgpu_solver_solve_host_many")
+        return [reps[k] for k in range(n)]
 
     def barrier_selftest(self, missing):
         """The persistent solve's grid barrier with block 0 absent (missing) or not: the status."""

@@ -173,6 +173,9 @@ struct fishgpu_solver_s {
   int giters = 1;
   int ksp_norm = FISHGPU_NORM_PRECONDITIONED;  // norm of the CG loop the graphs are built for
   double *f_own = nullptr, *g_own = nullptr, *u_own = nullptr;  // FISHGPU_USER, host-array form
+  // fishgpu_solver_solve_host_many: device staging of the next f and the last u, and their copy streams
+  double *f_stage = nullptr, *u_stage = nullptr;
+  cudaStream_t cs_in = nullptr, cs_out = nullptr;
   // batch groups: 2D instances of one size stacked as k-planes
   int batch = 0, nplanes = 1;
   unsigned int *ndone = nullptr;
@@ -1887,6 +1890,8 @@ extern "C" int fishgpu_solver_destroy(fishgpu_solver *S) {
   if (S->mout_h) cudaFreeHost(S->mout_h);
   if (S->ev0) cudaEventDestroy(S->ev0);
   if (S->ev1) cudaEventDestroy(S->ev1);
+  if (S->cs_in) cudaStreamDestroy(S->cs_in);
+  if (S->cs_out) cudaStreamDestroy(S->cs_out);
   if (S->own_stream && S->stream) cudaStreamDestroy(S->stream);
   delete S;
   return FISHGPU_OK;
@@ -2218,6 +2223,28 @@ extern "C" long long fishgpu_solver_host_bytes_in(const fishgpu_solver *S, const
   return b;
 }
 
+// g into the solver's g buffer on its stream: boundary values only, read in
+// place from pinned host memory; all of it from pageable memory; zeros for
+// NULL (the solver reads g nowhere but on the boundary)
+static int stage_g(fishgpu_solver *S, const double *g_host) {
+  cudaStream_t s = S->stream;
+  const size_t N = (size_t)S->dense.plane * S->dense.mz;
+  const double *gdev = g_host ? pinned_device_view(g_host) : nullptr;
+  if (gdev) {
+    const Geom &d = S->dense;
+    const long long nb = fg::bdry_count(d.dim, d.mx, d.my, d.mz);
+    const unsigned blocks = (unsigned)std::min<long long>((nb + 255) / 256, 4LL * sm_count());
+    if (d.dim == 1) fg::k_gather_bdry<1><<<blocks, 256, 0, s>>>(d.mx, d.my, d.mz, gdev, S->g_own);
+    else if (d.dim == 2) fg::k_gather_bdry<2><<<blocks, 256, 0, s>>>(d.mx, d.my, d.mz, gdev, S->g_own);
+    else fg::k_gather_bdry<3><<<blocks, 256, 0, s>>>(d.mx, d.my, d.mz, gdev, S->g_own);
+    return cudaGetLastError() == cudaSuccess ? FISHGPU_OK : FISHGPU_ERR_CUDA;
+  }
+  return (g_host ? cudaMemcpyAsync(S->g_own, g_host, sizeof(double) * N, cudaMemcpyHostToDevice, s)
+                 : cudaMemsetAsync(S->g_own, 0, sizeof(double) * N, s)) == cudaSuccess
+             ? FISHGPU_OK
+             : FISHGPU_ERR_CUDA;
+}
+
 extern "C" int fishgpu_solver_solve_host(fishgpu_solver *S, const double *f_host, const double *g_host,
                                          double *u_host, fishgpu_report *rep) {
   if (!S || !u_host || !rep) return FISHGPU_ERR_ARG;
@@ -2235,21 +2262,7 @@ extern "C" int fishgpu_solver_solve_host(fishgpu_solver *S, const double *f_host
   cudaEventRecord(e0, s);
   if (user && cudaMemcpyAsync(S->f_own, f_host, sizeof(double) * N, cudaMemcpyHostToDevice, s) != cudaSuccess)
     rc = FISHGPU_ERR_CUDA;
-  if (user && !rc) {
-    const double *gdev = g_host ? pinned_device_view(g_host) : nullptr;
-    if (gdev) {  // boundary values only, read in place from pinned host memory
-      const Geom &d = S->dense;
-      const long long nb = fg::bdry_count(d.dim, d.mx, d.my, d.mz);
-      const unsigned blocks = (unsigned)std::min<long long>((nb + 255) / 256, 4LL * sm_count());
-      if (d.dim == 1) fg::k_gather_bdry<1><<<blocks, 256, 0, s>>>(d.mx, d.my, d.mz, gdev, S->g_own);
-      else if (d.dim == 2) fg::k_gather_bdry<2><<<blocks, 256, 0, s>>>(d.mx, d.my, d.mz, gdev, S->g_own);
-      else fg::k_gather_bdry<3><<<blocks, 256, 0, s>>>(d.mx, d.my, d.mz, gdev, S->g_own);
-      if (cudaGetLastError() != cudaSuccess) rc = FISHGPU_ERR_CUDA;
-    } else if ((g_host ? cudaMemcpyAsync(S->g_own, g_host, sizeof(double) * N, cudaMemcpyHostToDevice, s)
-                       : cudaMemsetAsync(S->g_own, 0, sizeof(double) * N, s)) != cudaSuccess) {
-      rc = FISHGPU_ERR_CUDA;
-    }
-  }
+  if (user && !rc) rc = stage_g(S, g_host);
   if (!rc && S->o.initial_type == FISHGPU_INITIAL_GIVEN &&
       cudaMemcpyAsync(S->u_own, u_host, sizeof(double) * N, cudaMemcpyHostToDevice, s) != cudaSuccess)
     rc = FISHGPU_ERR_CUDA;
@@ -2263,6 +2276,78 @@ extern "C" int fishgpu_solver_solve_host(fishgpu_solver *S, const double *f_host
   if (!rc && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess) rep->solve_ms = ms;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  return rc ? rc : src;
+}
+
+// n host-array solves in order, pipelined: while problem k is solved, f of
+// problem k+1 comes in (copy stream cs_in) and u of problem k-1 goes out
+// (cs_out), through device staging buffers -- one device-to-device copy each
+// way per problem on the solver's stream keeps the solver's own f and u
+// buffers, which its captured graphs hold.  Each problem's results are those
+// of fishgpu_solver_solve_host.
+extern "C" int fishgpu_solver_solve_host_many(fishgpu_solver *S, int n, const double *const *f_host,
+                                              const double *const *g_host, double *const *u_host,
+                                              fishgpu_report *reps) {
+  if (!S || n < 0 || (n && (!f_host || !u_host || !reps))) return FISHGPU_ERR_ARG;
+  if (S->o.ctx.problem != FISHGPU_USER || !S->f_own) return FISHGPU_ERR_ARG;
+  for (int k = 0; k < n; k++)
+    if (!f_host[k] || !u_host[k]) return FISHGPU_ERR_ARG;
+  if (!n) return FISHGPU_OK;
+  const size_t N = (size_t)S->dense.plane * S->dense.mz, bytes = sizeof(double) * N;
+  cudaStream_t s = S->stream;
+  int rc = FISHGPU_OK;
+  if (!S->u_own && (rc = dalloc(S, &S->u_own, N))) return rc;
+  if (!S->f_stage && ((rc = dalloc(S, &S->f_stage, N)) || (rc = dalloc(S, &S->u_stage, N)))) return rc;
+  if (!S->cs_in && (cudaStreamCreateWithFlags(&S->cs_in, cudaStreamNonBlocking) != cudaSuccess ||
+                    cudaStreamCreateWithFlags(&S->cs_out, cudaStreamNonBlocking) != cudaSuccess))
+    return FISHGPU_ERR_CUDA;
+  // the staging buffers were zeroed on the solver's stream: the copy streams start after that
+  cudaEvent_t e_in = nullptr, e_fc = nullptr, e_us = nullptr, e_out = nullptr;
+  if (cudaEventCreateWithFlags(&e_in, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&e_fc, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&e_us, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&e_out, cudaEventDisableTiming) != cudaSuccess) {
+    rc = FISHGPU_ERR_CUDA;
+  }
+  int src = FISHGPU_OK;
+  auto ok = [&](cudaError_t e) {
+    if (e != cudaSuccess && !rc) rc = FISHGPU_ERR_CUDA;
+    return !rc;
+  };
+  if (!rc && ok(cudaEventRecord(e_fc, s)) && ok(cudaStreamWaitEvent(S->cs_in, e_fc, 0)) &&
+      ok(cudaMemcpyAsync(S->f_stage, f_host[0], bytes, cudaMemcpyHostToDevice, S->cs_in)))
+    ok(cudaEventRecord(e_in, S->cs_in));
+  for (int k = 0; k < n && !rc; k++) {
+    // f of problem k into the solver's buffer; the staging buffer then takes problem k+1's
+    if (!ok(cudaStreamWaitEvent(s, e_in, 0)) || !ok(cudaMemcpyAsync(S->f_own, S->f_stage, bytes, cudaMemcpyDeviceToDevice, s)) ||
+        !ok(cudaEventRecord(e_fc, s)))
+      break;
+    if (k + 1 < n && (!ok(cudaStreamWaitEvent(S->cs_in, e_fc, 0)) ||
+                      !ok(cudaMemcpyAsync(S->f_stage, f_host[k + 1], bytes, cudaMemcpyHostToDevice, S->cs_in)) ||
+                      !ok(cudaEventRecord(e_in, S->cs_in))))
+      break;
+    if ((rc = stage_g(S, g_host ? g_host[k] : nullptr))) break;
+    if (S->o.initial_type == FISHGPU_INITIAL_GIVEN &&
+        !ok(cudaMemcpyAsync(S->u_own, u_host[k], bytes, cudaMemcpyHostToDevice, s)))
+      break;
+    src = fishgpu_solver_solve(S, S->u_own, &reps[k]);
+    if (src != FISHGPU_OK && src != FISHGPU_ERR_NOT_CONVERGED) {
+      rc = src;
+      break;
+    }
+    // u of problem k out through the staging buffer, once problem k-1's has left it
+    if (k > 0 && !ok(cudaStreamWaitEvent(s, e_out, 0))) break;
+    if (!ok(cudaMemcpyAsync(S->u_stage, S->u_own, bytes, cudaMemcpyDeviceToDevice, s)) || !ok(cudaEventRecord(e_us, s)) ||
+        !ok(cudaStreamWaitEvent(S->cs_out, e_us, 0)) ||
+        !ok(cudaMemcpyAsync(u_host[k], S->u_stage, bytes, cudaMemcpyDeviceToHost, S->cs_out)) ||
+        !ok(cudaEventRecord(e_out, S->cs_out)))
+      break;
+  }
+  if (S->cs_in && cudaStreamSynchronize(S->cs_in) != cudaSuccess && !rc) rc = FISHGPU_ERR_CUDA;
+  if (S->cs_out && cudaStreamSynchronize(S->cs_out) != cudaSuccess && !rc) rc = FISHGPU_ERR_CUDA;
+  if (cudaStreamSynchronize(s) != cudaSuccess && !rc) rc = FISHGPU_ERR_CUDA;
+  for (cudaEvent_t e : {e_in, e_fc, e_us, e_out})
+    if (e) cudaEventDestroy(e);
   return rc ? rc : src;
 }
 

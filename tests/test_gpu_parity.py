@@ -435,6 +435,40 @@ def test_pinned_boundary_gather_equals_full_copy(cuda, dim, refine):
     assert np.array_equal(u1, u2) and r2.reason > 0
 
 
+@pytest.mark.parametrize("args", [
+    "-fsh_dim 3 -da_refine 5 -pc_type mg -ksp_rtol 1e-10 -fsh_precision mixed",
+    "-fsh_dim 2 -da_refine 7 -pc_type mg -ksp_rtol 1e-10",
+    "-fsh_dim 3 -da_refine 4 -pc_type mg -ksp_rtol 1e-10 -fsh_precision mixed -fsh_persist 0",
+])
+def test_pipelined_host_solves_equal_single_calls(cuda, args):
+    """fishgpu_solver_solve_host_many (the next f in and the last u out on
+    copy streams while a problem is solved) gives every problem the solution,
+    bit for bit, and the report of its own fishgpu_solver_solve_host call:
+    different f and g per problem, pinned and pageable arrays, a NULL g."""
+    import torch
+    fg = fgmod()
+    o = fg.options(args)
+    o.ctx.problem = fg.USER
+    rng = np.random.default_rng(21)
+    n = 4
+    fs = [rng.standard_normal(o.shape) for _ in range(n)]
+    gs = [rng.standard_normal(o.shape) for _ in range(n - 1)] + [None]
+    pin = [torch.from_numpy(f).pin_memory() for f in fs[:2]] + fs[2:]
+    us = [torch.empty(o.shape, dtype=torch.float64).pin_memory(), np.empty(o.shape),
+          torch.empty(o.shape, dtype=torch.float64).pin_memory(), np.empty(o.shape)]
+    want = [np.empty(o.shape) for _ in range(n)]
+    with fg.Solver(o) as s:
+        ref = [s.solve_host(fs[k], gs[k], want[k]) for k in range(n)]
+        reps = s.solve_host_many(pin, gs, us)
+        reps2 = s.solve_host_many(pin[:1], None, us[:1])  # again, one problem, zero g
+    for k in range(n):
+        got = us[k].numpy() if hasattr(us[k], "numpy") else us[k]
+        assert np.array_equal(got, want[k])
+        assert reps[k].reason == ref[k].reason > 0 and reps[k].its == ref[k].its
+        assert reps[k].outer_its == ref[k].outer_its
+    assert reps2[0].reason > 0
+
+
 @pytest.mark.parametrize("rec", [r for r in GOLDEN if r["test"] in (1, 7)],
                          ids=lambda r: "fish.test%d" % r["test"])
 def test_fish_driver_replays_golden(cuda, rec):
