@@ -2200,6 +2200,28 @@ __global__ void __launch_bounds__(256) k_gather_bdry(int mx, int my, int mz, con
     dst[n] = src[n];
   }
 }
+
+// dst = src, n doubles, both 16-byte aligned, one side pinned host memory
+// through its device mapping: the pipelined host-array solves move f and u
+// with this kernel instead of the copy engines, on whose queues the solve's
+// own small state copies would otherwise wait behind the 1 GB transfers.
+// Blocks of 128 threads with few registers fit beside a stencil kernel's
+// blocks; four 16-byte loads in flight per thread.
+static __global__ void __launch_bounds__(128) k_copy_mapped(const double2 *__restrict__ src, double2 *__restrict__ dst,
+                                                          long long n) {
+  const long long n2 = n / 2, stride = (long long)gridDim.x * blockDim.x;
+  if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0)  // the odd last element
+    reinterpret_cast<double *>(dst)[n - 1] = reinterpret_cast<const double *>(src)[n - 1];
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  for (; i + 3 * stride < n2; i += 4 * stride) {
+    const double2 a = src[i], b = src[i + stride], c = src[i + 2 * stride], d = src[i + 3 * stride];
+    dst[i] = a;
+    dst[i + stride] = b;
+    dst[i + 2 * stride] = c;
+    dst[i + 3 * stride] = d;
+  }
+  for (; i < n2; i += stride) dst[i] = src[i];
+}
 }  // namespace fg
 
 // A device-usable address of pinned (page-locked, mapped) host memory, or
@@ -2285,6 +2307,24 @@ extern "C" int fishgpu_solver_solve_host(fishgpu_solver *S, const double *f_host
 // way per problem on the solver's stream keeps the solver's own f and u
 // buffers, which its captured graphs hold.  Each problem's results are those
 // of fishgpu_solver_solve_host.
+// dst = src (n doubles) on stream st: by k_copy_mapped when the host side is
+// pinned memory (host is dst for d2h) and both ends are 16-byte aligned, else
+// by the copy engine
+static int copy_host(double *dst, const double *src, size_t n, bool d2h, cudaStream_t st) {
+  const double *hv = pinned_device_view(d2h ? dst : src);
+  const double *s = d2h ? src : hv;
+  double *d = d2h ? const_cast<double *>(hv) : dst;
+  if (hv && ((uintptr_t)s & 15) == 0 && ((uintptr_t)d & 15) == 0) {
+    fg::k_copy_mapped<<<64, 128, 0, st>>>(reinterpret_cast<const double2 *>(s), reinterpret_cast<double2 *>(d),
+                                          (long long)n);
+    return cudaGetLastError() == cudaSuccess ? FISHGPU_OK : FISHGPU_ERR_CUDA;
+  }
+  return cudaMemcpyAsync(dst, src, sizeof(double) * n, d2h ? cudaMemcpyDeviceToHost : cudaMemcpyHostToDevice, st) ==
+                 cudaSuccess
+             ? FISHGPU_OK
+             : FISHGPU_ERR_CUDA;
+}
+
 extern "C" int fishgpu_solver_solve_host_many(fishgpu_solver *S, int n, const double *const *f_host,
                                               const double *const *g_host, double *const *u_host,
                                               fishgpu_report *reps) {
@@ -2315,7 +2355,7 @@ extern "C" int fishgpu_solver_solve_host_many(fishgpu_solver *S, int n, const do
     return !rc;
   };
   if (!rc && ok(cudaEventRecord(e_fc, s)) && ok(cudaStreamWaitEvent(S->cs_in, e_fc, 0)) &&
-      ok(cudaMemcpyAsync(S->f_stage, f_host[0], bytes, cudaMemcpyHostToDevice, S->cs_in)))
+      !(rc = copy_host(S->f_stage, f_host[0], N, false, S->cs_in)))
     ok(cudaEventRecord(e_in, S->cs_in));
   for (int k = 0; k < n && !rc; k++) {
     // f of problem k into the solver's buffer; the staging buffer then takes problem k+1's
@@ -2323,7 +2363,7 @@ extern "C" int fishgpu_solver_solve_host_many(fishgpu_solver *S, int n, const do
         !ok(cudaEventRecord(e_fc, s)))
       break;
     if (k + 1 < n && (!ok(cudaStreamWaitEvent(S->cs_in, e_fc, 0)) ||
-                      !ok(cudaMemcpyAsync(S->f_stage, f_host[k + 1], bytes, cudaMemcpyHostToDevice, S->cs_in)) ||
+                      (rc = copy_host(S->f_stage, f_host[k + 1], N, false, S->cs_in)) ||
                       !ok(cudaEventRecord(e_in, S->cs_in))))
       break;
     if ((rc = stage_g(S, g_host ? g_host[k] : nullptr))) break;
@@ -2338,8 +2378,7 @@ extern "C" int fishgpu_solver_solve_host_many(fishgpu_solver *S, int n, const do
     // u of problem k out through the staging buffer, once problem k-1's has left it
     if (k > 0 && !ok(cudaStreamWaitEvent(s, e_out, 0))) break;
     if (!ok(cudaMemcpyAsync(S->u_stage, S->u_own, bytes, cudaMemcpyDeviceToDevice, s)) || !ok(cudaEventRecord(e_us, s)) ||
-        !ok(cudaStreamWaitEvent(S->cs_out, e_us, 0)) ||
-        !ok(cudaMemcpyAsync(u_host[k], S->u_stage, bytes, cudaMemcpyDeviceToHost, S->cs_out)) ||
+        !ok(cudaStreamWaitEvent(S->cs_out, e_us, 0)) || (rc = copy_host(u_host[k], S->u_stage, N, true, S->cs_out)) ||
         !ok(cudaEventRecord(e_out, S->cs_out)))
       break;
   }

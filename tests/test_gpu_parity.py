@@ -460,7 +460,8 @@ def test_pipelined_host_solves_equal_single_calls(cuda, args):
     with fg.Solver(o) as s:
         ref = [s.solve_host(fs[k], gs[k], want[k]) for k in range(n)]
         reps = s.solve_host_many(pin, gs, us)
-        reps2 = s.solve_host_many(pin[:1], None, us[:1])  # again, one problem, zero g
+        u_zero_g = np.empty(o.shape)
+        reps2 = s.solve_host_many(pin[:1], None, [u_zero_g])  # again, one problem, zero g
     for k in range(n):
         got = us[k].numpy() if hasattr(us[k], "numpy") else us[k]
         assert np.array_equal(got, want[k])
