@@ -93,6 +93,13 @@ def test_minimal_options(built, args, grid, gs, deg):
     o = fg.ms_options(args)
     assert (o.mx, o.my) == grid and o.grid_sequence == gs and o.monitor_degree == deg
     assert o.ctx.q == -0.5 and o.rtol == 1e-8 and o.ksp_rtol == 1e-5 and o.max_it == 50
+    assert o.inner_block == 1 and o.inner_persist == -1 and o.vtail_points == 0
+
+
+def test_minimal_inner_solve_options(built):
+    import p4pdes_gb300 as fg
+    o = fg.ms_options("-ms_inner_persist 0 -ms_vtail_points 4225 -ms_inner_block 0")
+    assert o.inner_persist == 0 and o.vtail_points == 4225 and o.inner_block == 0
 
 
 @pytest.mark.parametrize("args", ["-ms_catenoid_c 0.5", "-ms_problem nosuch", "-ms_quaddegree 4",
@@ -126,11 +133,15 @@ def test_default_options_are_fish_defaults(built):
 
 
 def test_build_options_parse_and_default(built):
-    """Options of this build beside fish's: precision form, inner tolerances,
-    graph shape, device-side loop, fused post-smoother."""
+    """The library's options beside fish's: precision form, inner tolerances,
+    graph shape, device-side loop, fused post-smoother, paired FP64 updates,
+    cooperative V-cycle tail."""
     import p4pdes_gb300 as fg
     o = fg.options([])
     assert o.device_loop == 1 and o.fuse_smooth == 0 and o.precision == fg.FP64
+    assert o.pair_y == 1 and o.coop_tail == 0
+    o2 = fg.options(["-fsh_pair_y", "0", "-fsh_coop_tail", "-1"])
+    assert o2.pair_y == 0 and o2.coop_tail == -1
     o = fg.options("-fsh_precision mixed -fsh_inner_rtol 1e-7 -fsh_inner_max_it 50 -fsh_outer_max_it 9 "
                    "-fsh_graph_iters 6 -fsh_device_loop 0 -fsh_fuse_smooth 1")
     assert o.precision == fg.MIXED and o.inner_rtol == 1e-7 and o.inner_max_it == 50 and o.outer_max_it == 9
