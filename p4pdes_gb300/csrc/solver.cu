@@ -2303,10 +2303,8 @@ extern "C" int fishgpu_solver_solve_host(fishgpu_solver *S, const double *f_host
 
 // n host-array solves in order, pipelined: while problem k is solved, f of
 // problem k+1 comes in (copy stream cs_in) and u of problem k-1 goes out
-// (cs_out), through device staging buffers -- one device-to-device copy each
-// way per problem on the solver's stream keeps the solver's own f and u
-// buffers, which its captured graphs hold.  Each problem's results are those
-// of fishgpu_solver_solve_host.
+// (cs_out), each into or out of the second of two device buffers.  Each
+// problem's results are those of fishgpu_solver_solve_host.
 // dst = src (n doubles) on stream st: by k_copy_mapped when the host side is
 // pinned memory (host is dst for d2h) and both ends are 16-byte aligned, else
 // by the copy engine
@@ -2341,12 +2339,17 @@ extern "C" int fishgpu_solver_solve_host_many(fishgpu_solver *S, int n, const do
   if (!S->cs_in && (cudaStreamCreateWithFlags(&S->cs_in, cudaStreamNonBlocking) != cudaSuccess ||
                     cudaStreamCreateWithFlags(&S->cs_out, cudaStreamNonBlocking) != cudaSuccess))
     return FISHGPU_ERR_CUDA;
-  // the staging buffers were zeroed on the solver's stream: the copy streams start after that
-  cudaEvent_t e_in = nullptr, e_fc = nullptr, e_us = nullptr, e_out = nullptr;
+  // Two f and two u buffers alternate (the solver's own and the staging ones): problem k reads
+  // fb[k & 1] (the solve takes f by value at its start, in S->prob, never from a captured graph) and
+  // writes ub[k & 1] (a launch parameter); f of problem k+1 comes into the other f buffer while
+  // problem k is solved, and u of problem k-1 leaves the other u buffer.
+  double *fb[2] = {S->f_own, S->f_stage}, *ub[2] = {S->u_own, S->u_stage};
+  cudaEvent_t e_in = nullptr, e_z = nullptr, e_us = nullptr, e_out[2] = {nullptr, nullptr};
   if (cudaEventCreateWithFlags(&e_in, cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&e_fc, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&e_z, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&e_us, cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&e_out, cudaEventDisableTiming) != cudaSuccess) {
+      cudaEventCreateWithFlags(&e_out[0], cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&e_out[1], cudaEventDisableTiming) != cudaSuccess) {
     rc = FISHGPU_ERR_CUDA;
   }
   int src = FISHGPU_OK;
@@ -2354,38 +2357,40 @@ extern "C" int fishgpu_solver_solve_host_many(fishgpu_solver *S, int n, const do
     if (e != cudaSuccess && !rc) rc = FISHGPU_ERR_CUDA;
     return !rc;
   };
-  if (!rc && ok(cudaEventRecord(e_fc, s)) && ok(cudaStreamWaitEvent(S->cs_in, e_fc, 0)) &&
-      !(rc = copy_host(S->f_stage, f_host[0], N, false, S->cs_in)))
+  // the staging buffers were zeroed on the solver's stream: the copy streams start after that
+  if (!rc && ok(cudaEventRecord(e_z, s)) && ok(cudaStreamWaitEvent(S->cs_in, e_z, 0)) &&
+      ok(cudaStreamWaitEvent(S->cs_out, e_z, 0)) && !(rc = copy_host(fb[0], f_host[0], N, false, S->cs_in)))
     ok(cudaEventRecord(e_in, S->cs_in));
   for (int k = 0; k < n && !rc; k++) {
-    // f of problem k into the solver's buffer; the staging buffer then takes problem k+1's
-    if (!ok(cudaStreamWaitEvent(s, e_in, 0)) || !ok(cudaMemcpyAsync(S->f_own, S->f_stage, bytes, cudaMemcpyDeviceToDevice, s)) ||
-        !ok(cudaEventRecord(e_fc, s)))
-      break;
-    if (k + 1 < n && (!ok(cudaStreamWaitEvent(S->cs_in, e_fc, 0)) ||
-                      (rc = copy_host(S->f_stage, f_host[k + 1], N, false, S->cs_in)) ||
-                      !ok(cudaEventRecord(e_in, S->cs_in))))
+    double *fk = fb[k & 1], *uk = ub[k & 1];
+    // f of problem k has arrived; problem k+1's goes into the other buffer, which problem k-1 (done:
+    // fishgpu_solver_solve returns after its solve) was the last to read
+    if (!ok(cudaStreamWaitEvent(s, e_in, 0))) break;
+    if (k + 1 < n &&
+        ((rc = copy_host(fb[(k + 1) & 1], f_host[k + 1], N, false, S->cs_in)) || !ok(cudaEventRecord(e_in, S->cs_in))))
       break;
     if ((rc = stage_g(S, g_host ? g_host[k] : nullptr))) break;
+    // uk is free once u of problem k-2 has left it
+    if (k >= 2 && !ok(cudaStreamWaitEvent(s, e_out[k & 1], 0))) break;
     if (S->o.initial_type == FISHGPU_INITIAL_GIVEN &&
-        !ok(cudaMemcpyAsync(S->u_own, u_host[k], bytes, cudaMemcpyHostToDevice, s)))
+        !ok(cudaMemcpyAsync(uk, u_host[k], bytes, cudaMemcpyHostToDevice, s)))
       break;
-    src = fishgpu_solver_solve(S, S->u_own, &reps[k]);
+    S->prob.f = fk;
+    src = fishgpu_solver_solve(S, uk, &reps[k]);
+    S->prob.f = S->f_own;
     if (src != FISHGPU_OK && src != FISHGPU_ERR_NOT_CONVERGED) {
       rc = src;
       break;
     }
-    // u of problem k out through the staging buffer, once problem k-1's has left it
-    if (k > 0 && !ok(cudaStreamWaitEvent(s, e_out, 0))) break;
-    if (!ok(cudaMemcpyAsync(S->u_stage, S->u_own, bytes, cudaMemcpyDeviceToDevice, s)) || !ok(cudaEventRecord(e_us, s)) ||
-        !ok(cudaStreamWaitEvent(S->cs_out, e_us, 0)) || (rc = copy_host(u_host[k], S->u_stage, N, true, S->cs_out)) ||
-        !ok(cudaEventRecord(e_out, S->cs_out)))
+    if (!ok(cudaEventRecord(e_us, s)) || !ok(cudaStreamWaitEvent(S->cs_out, e_us, 0)) ||
+        (rc = copy_host(u_host[k], uk, N, true, S->cs_out)) || !ok(cudaEventRecord(e_out[k & 1], S->cs_out)))
       break;
   }
+  S->prob.f = S->f_own;
   if (S->cs_in && cudaStreamSynchronize(S->cs_in) != cudaSuccess && !rc) rc = FISHGPU_ERR_CUDA;
   if (S->cs_out && cudaStreamSynchronize(S->cs_out) != cudaSuccess && !rc) rc = FISHGPU_ERR_CUDA;
   if (cudaStreamSynchronize(s) != cudaSuccess && !rc) rc = FISHGPU_ERR_CUDA;
-  for (cudaEvent_t e : {e_in, e_fc, e_us, e_out})
+  for (cudaEvent_t e : {e_in, e_z, e_us, e_out[0], e_out[1]})
     if (e) cudaEventDestroy(e);
   return rc ? rc : src;
 }
